@@ -1,0 +1,182 @@
+/*
+ * pfgb.h - C ABI of libpfgb.so, the GB300 (sm_103a) projection step of PyFlow's
+ * 2-D lid-driven cavity solver.
+ *
+ * Every entry point returns an int status: 0 on success, a negative PFGB_E*
+ * code on error (never an exception).  pfgb_last_error() returns the message of
+ * the last error of the calling thread.  Pointers named "device" must point to
+ * device memory of the current CUDA device; `stream` is a cudaStream_t (NULL =
+ * the legacy default stream).  Arrays are row-major with row index = y; `ld` is
+ * the row pitch in elements.
+ *
+ * Reference citations are paths inside the PyFlow-Solver project.
+ */
+#ifndef PFGB_H
+#define PFGB_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define PFGB_API __attribute__((visibility("default")))
+#else
+#define PFGB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PFGB_OK 0
+#define PFGB_EINVAL (-1)   /* invalid argument */
+#define PFGB_ECUDA (-2)    /* a CUDA runtime call failed */
+#define PFGB_ENOMEM (-3)   /* allocation failed */
+#define PFGB_ESTATE (-4)   /* handle used in the wrong state */
+
+/* Advection schemes (config.advection_scheme / disable_advection). */
+#define PFGB_SCHEME_UPWIND 0
+#define PFGB_SCHEME_QUICK 1
+#define PFGB_SCHEME_NONE 2
+
+/* Operators of the pressure solve. */
+#define PFGB_OP_NEG_LAPLACIAN_PINNED 0  /* _NegLaplacianPinned, src/pyflow/solvers/pressure_solver.py:97-105 */
+#define PFGB_OP_LAPLACIAN_DIRICHLET 1   /* _PosLaplacianDirichlet, src/pyflow/solvers/pressure_solver.py:69-77 */
+
+/* Parameters of one cavity instance; the fields are the attributes that
+ * step() reads from its config (src/pyflow/solvers/solver.py:15-99,
+ * src/pyflow/solvers/pressure_solver.py:130-146).  Host code computes the
+ * derived values exactly as the reference rounds them:
+ *   dx = lx / max(nx-1, 1),  nu = 1.0 / Re,
+ *   jacobi_interior = 1.0 / (2.0/dx**2 + 2.0/dy**2). */
+typedef struct pfgb_params {
+  int nx, ny;                /* interior cells */
+  double dx, dy;
+  double nu;                 /* 1/Re */
+  double cfl_target, cfl_growth;
+  double lin_tol;            /* rtol of the CG */
+  int lin_maxiter;
+  int scheme;                /* PFGB_SCHEME_* */
+  int enable_jacobi;         /* enable_jacobi_pc */
+  double jacobi_interior;
+  int has_lid;               /* lid_velocity is not None */
+  double lid_velocity;
+  int precision;             /* 0: binary64 throughout */
+  int reserved[7];
+} pfgb_params;
+
+/* Host-side state.meta carried into a step (solver.py:32,46-50). */
+typedef struct pfgb_step_in {
+  double dt_prev;            /* state.meta['dt_prev'] (default 1e-2) */
+  double hist[5];            /* state.meta['divergence_history'] (at most 5) */
+  int hist_len;
+  int iteration;
+} pfgb_step_in;
+
+/* Raw step results.  Norms are returned squared (exactly rounded sums); the
+ * host applies sqrt and the divisions of the reference. */
+typedef struct pfgb_step_out {
+  double umax, vmax;         /* max|u| + 1e-12, max|v| + 1e-12 */
+  double div_before;         /* ||div_central(u,v;1,1)|| before the step */
+  double dt, cfl;
+  int safeguard;             /* dt halved by the divergence-trend safeguard */
+  int cg_iterations;         /* true number of CG iterations executed */
+  int cg_info;               /* scipy info: 0 converged, maxiter otherwise */
+  int nan_detected;
+  double divstar_sq;         /* ||div_c(u*,v*)||^2 */
+  double bnorm;              /* ||b|| of the pressure system */
+  double res_sq;             /* ||b - A x||^2 */
+  double ru_sq, rv_sq;       /* sum (u-u_old)^2, sum (v-v_old)^2 */
+  double divafter_sq;        /* ||div_c(u,v)||^2 after the correction */
+  double linres_sq;          /* ||A p - b||^2 */
+  double cont_sq;            /* ||div_central(u,v;1,1)||^2 after the step */
+  unsigned reduction_flags;  /* bit 3: a term fell below 2^-1184, bit 4: overflow */
+  unsigned pad;
+} pfgb_step_out;
+
+typedef struct pfgb_solve_out {
+  int info;                  /* scipy info: 0 converged, maxiter otherwise */
+  int iterations;            /* true iteration count */
+  double bnorm;              /* ||b|| */
+  double res_sq;             /* ||b - A x||^2 */
+} pfgb_solve_out;
+
+typedef struct pfgb_handle pfgb_handle;
+
+/* Library version (major*10000 + minor*100 + patch). */
+PFGB_API int pfgb_version(void);
+
+/* Copy the last error message of this thread into buf (NUL terminated). */
+PFGB_API int pfgb_last_error(char* buf, size_t len);
+
+/* ---- one cavity instance ------------------------------------------------ */
+
+/* Replaces the per-step setup of step() (src/pyflow/solvers/solver.py:15-99)
+ * and the Jacobi assembly of solve_pressure_poisson
+ * (src/pyflow/solvers/pressure_solver.py:15-40,139-145).  Allocates the
+ * instance workspace on the current device. */
+PFGB_API int pfgb_create(const pfgb_params* params, pfgb_handle** handle);
+PFGB_API int pfgb_destroy(pfgb_handle* handle);
+/* Bytes of device workspace held by the handle. */
+PFGB_API size_t pfgb_workspace_bytes(const pfgb_handle* handle);
+
+/* One projection step, in place on the ghosted state arrays u, v, p (device,
+ * shape (ny+2, nx+2), ld = nx+2, interior [1:-1,1:-1]).  Replaces step()
+ * (src/pyflow/solvers/solver.py:15-121) including solve_pressure_poisson
+ * (src/pyflow/solvers/pressure_solver.py:95-219) and the CG of
+ * src/pyflow/linear_solvers/interface.py:23-53.  Synchronises `stream`. */
+PFGB_API int pfgb_step(pfgb_handle* handle, double* u, double* v, double* p, long ld,
+              const pfgb_step_in* in, void* stream, pfgb_step_out* out);
+
+/* Stand-alone projection of the state's current u, v with a given dt:
+ * solve_pressure_poisson in normal mode
+ * (src/pyflow/solvers/pressure_solver.py:95-219 with rhs_override None).
+ * u, v are corrected in place and p receives the pinned pressure.  Fills the
+ * projection fields of `out` (divstar_sq, bnorm, res_sq, divafter_sq,
+ * linres_sq, cg_iterations, cg_info, nan_detected).  Synchronises `stream`. */
+PFGB_API int pfgb_project(pfgb_handle* handle, double* u, double* v, double* p, long ld, double dt,
+                          void* stream, pfgb_step_out* out);
+
+/* ---- array operators (device arrays, no synchronisation) --------------- */
+
+/* gradient_coherent, src/pyflow/numerics/core_ops_coherent.py:45-61 */
+PFGB_API int pfgb_gradient_coherent(const double* p, long ldp, double* gx, double* gy, long ldo,
+                           int nx, int ny, double dx, double dy, void* stream);
+/* divergence_coherent, src/pyflow/numerics/core_ops_coherent.py:63-79 */
+PFGB_API int pfgb_divergence_coherent(const double* u, const double* v, long ldi, double* div, long ldo,
+                             int nx, int ny, double dx, double dy, void* stream);
+/* laplacian_coherent, src/pyflow/numerics/core_ops_coherent.py:81-84 */
+PFGB_API int pfgb_laplacian_coherent(const double* p, long ldp, double* lap, long ldo,
+                            int nx, int ny, double dx, double dy, void* stream);
+/* divergence (central), src/pyflow/numerics/fluid_ops.py:8-41 */
+PFGB_API int pfgb_divergence_central(const double* u, const double* v, long ldi, double* div, long ldo,
+                            int nx, int ny, double dx, double dy, void* stream);
+/* advect_upwind / advect_quick, src/pyflow/numerics/operators/advection.py:17-84 */
+PFGB_API int pfgb_advect(int scheme, const double* u, const double* v, const double* f, long ldi,
+                double* conv, long ldo, int nx, int ny, double dx, double dy, void* stream);
+/* y = A x for the pressure operators (PFGB_OP_*); x, y contiguous (ny*nx) */
+PFGB_API int pfgb_apply_operator(int op, const double* x, double* y, int nx, int ny, double dx, double dy,
+                        void* stream);
+
+/* ---- exactly rounded reductions ------------------------------------------ */
+
+/* result = RN(sum a[i]*b[i]) with exact products (order independent); the
+ * twin of np.dot.  Synchronises `stream`; result is a host pointer. */
+PFGB_API int pfgb_xdot(const double* a, const double* b, long n, double* result, void* stream);
+/* result = RN(sum a[i]) (order independent). */
+PFGB_API int pfgb_xsum(const double* a, long n, double* result, void* stream);
+
+/* ---- linear-solver operator interface ------------------------------------ */
+
+/* PCG of scipy.sparse.linalg.cg as called by solve()
+ * (src/pyflow/linear_solvers/interface.py:23-53): x0 = 0, rtol = tol,
+ * M = Jacobi (jacobi_preconditioner, src/pyflow/linear_solvers/preconditioners.py:8-25)
+ * when precond = 1, identity when 0.  b and x are contiguous device vectors of
+ * nx*ny doubles (row-major, k = j*nx + i).  Synchronises `stream`. */
+PFGB_API int pfgb_cg_solve(int op, const double* b, double* x, int nx, int ny, double dx, double dy,
+                  int precond, double jacobi_interior, double tol, int maxiter,
+                  void* stream, pfgb_solve_out* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFGB_H */

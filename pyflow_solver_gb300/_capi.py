@@ -1,0 +1,120 @@
+"""ctypes binding of libpfgb.so (the C ABI declared in include/pfgb.h).
+
+The library is built in-tree by ``pyflow_solver_gb300._build``.  There is no
+CPU fallback: if the library is missing or a CUDA device is absent, the calls
+raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from ._build import LIB
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+        ("nu", ctypes.c_double),
+        ("cfl_target", ctypes.c_double), ("cfl_growth", ctypes.c_double),
+        ("lin_tol", ctypes.c_double), ("lin_maxiter", ctypes.c_int),
+        ("scheme", ctypes.c_int), ("enable_jacobi", ctypes.c_int),
+        ("jacobi_interior", ctypes.c_double),
+        ("has_lid", ctypes.c_int), ("lid_velocity", ctypes.c_double),
+        ("precision", ctypes.c_int), ("reserved", ctypes.c_int * 7),
+    ]
+
+
+class StepIn(ctypes.Structure):
+    _fields_ = [
+        ("dt_prev", ctypes.c_double), ("hist", ctypes.c_double * 5),
+        ("hist_len", ctypes.c_int), ("iteration", ctypes.c_int),
+    ]
+
+
+class StepOut(ctypes.Structure):
+    _fields_ = [
+        ("umax", ctypes.c_double), ("vmax", ctypes.c_double),
+        ("div_before", ctypes.c_double), ("dt", ctypes.c_double), ("cfl", ctypes.c_double),
+        ("safeguard", ctypes.c_int), ("cg_iterations", ctypes.c_int),
+        ("cg_info", ctypes.c_int), ("nan_detected", ctypes.c_int),
+        ("divstar_sq", ctypes.c_double), ("bnorm", ctypes.c_double),
+        ("res_sq", ctypes.c_double), ("ru_sq", ctypes.c_double), ("rv_sq", ctypes.c_double),
+        ("divafter_sq", ctypes.c_double), ("linres_sq", ctypes.c_double),
+        ("cont_sq", ctypes.c_double),
+        ("reduction_flags", ctypes.c_uint), ("pad", ctypes.c_uint),
+    ]
+
+
+class SolveOut(ctypes.Structure):
+    _fields_ = [
+        ("info", ctypes.c_int), ("iterations", ctypes.c_int),
+        ("bnorm", ctypes.c_double), ("res_sq", ctypes.c_double),
+    ]
+
+
+# name -> (restype, argtypes)
+_P = ctypes.c_void_p
+_L = ctypes.c_long
+_I = ctypes.c_int
+_D = ctypes.c_double
+SIGNATURES = {
+    "pfgb_version": (_I, []),
+    "pfgb_last_error": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
+    "pfgb_create": (_I, [ctypes.POINTER(Params), ctypes.POINTER(_P)]),
+    "pfgb_destroy": (_I, [_P]),
+    "pfgb_workspace_bytes": (ctypes.c_size_t, [_P]),
+    "pfgb_step": (_I, [_P, _P, _P, _P, _L, ctypes.POINTER(StepIn), _P, ctypes.POINTER(StepOut)]),
+    "pfgb_project": (_I, [_P, _P, _P, _P, _L, _D, _P, ctypes.POINTER(StepOut)]),
+    "pfgb_gradient_coherent": (_I, [_P, _L, _P, _P, _L, _I, _I, _D, _D, _P]),
+    "pfgb_divergence_coherent": (_I, [_P, _P, _L, _P, _L, _I, _I, _D, _D, _P]),
+    "pfgb_laplacian_coherent": (_I, [_P, _L, _P, _L, _I, _I, _D, _D, _P]),
+    "pfgb_divergence_central": (_I, [_P, _P, _L, _P, _L, _I, _I, _D, _D, _P]),
+    "pfgb_advect": (_I, [_I, _P, _P, _P, _L, _P, _L, _I, _I, _D, _D, _P]),
+    "pfgb_apply_operator": (_I, [_I, _P, _P, _I, _I, _D, _D, _P]),
+    "pfgb_xdot": (_I, [_P, _P, _L, c_double_p, _P]),
+    "pfgb_xsum": (_I, [_P, _L, c_double_p, _P]),
+    "pfgb_cg_solve": (_I, [_I, _P, _P, _I, _I, _D, _D, _I, _D, _D, _I, _P, ctypes.POINTER(SolveOut)]),
+}
+
+SCHEME_UPWIND, SCHEME_QUICK, SCHEME_NONE = 0, 1, 2
+OP_NEG_LAPLACIAN_PINNED, OP_LAPLACIAN_DIRICHLET = 0, 1
+
+_lib = None
+
+
+class PFGBError(RuntimeError):
+    pass
+
+
+def load(path: str | None = None):
+    """Load libpfgb.so (once) and declare its signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB
+    if not os.path.exists(path):
+        raise PFGBError(
+            f"{path} is missing: build it with `python -m pyflow_solver_gb300._build` "
+            "(there is no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    load().pfgb_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int, what: str):
+    if rc != 0:
+        raise PFGBError(f"{what} failed ({rc}): {last_error()}")

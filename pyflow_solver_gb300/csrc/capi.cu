@@ -1,0 +1,88 @@
+// C ABI entry points of libpfgb.so (declared in include/pfgb.h): handles,
+// error reporting, the projection step and the operator-interface CG.
+#include <cstring>
+#include <string>
+
+#include "pfgb_internal.h"
+#include "step64.cuh"
+
+namespace pfgb {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return PFGB_OK;
+  return set_error(PFGB_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace pfgb
+
+struct pfgb_handle {
+  pfgb::Instance64* inst;
+};
+
+using namespace pfgb;
+
+extern "C" int pfgb_version(void) { return 100; }
+
+extern "C" int pfgb_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return PFGB_EINVAL;
+  size_t n = g_last_error.size() < len - 1 ? g_last_error.size() : len - 1;
+  memcpy(buf, g_last_error.data(), n);
+  buf[n] = '\0';
+  return PFGB_OK;
+}
+
+extern "C" int pfgb_create(const pfgb_params* params, pfgb_handle** handle) {
+  if (!params || !handle) return set_error(PFGB_EINVAL, "null argument");
+  if (params->precision != 0) return set_error(PFGB_EINVAL, "precision mode not supported by this entry point");
+  if (params->scheme < 0 || params->scheme > 2) return set_error(PFGB_EINVAL, "unknown advection scheme");
+  if (params->lin_maxiter < 0) return set_error(PFGB_EINVAL, "lin_maxiter must be >= 0");
+  Instance64* inst = nullptr;
+  int rc = instance64_create(params, &inst);
+  if (rc) return rc;
+  pfgb_handle* h = new pfgb_handle;
+  h->inst = inst;
+  *handle = h;
+  return PFGB_OK;
+}
+
+extern "C" int pfgb_destroy(pfgb_handle* handle) {
+  if (!handle) return PFGB_OK;
+  instance64_destroy(handle->inst);
+  delete handle;
+  return PFGB_OK;
+}
+
+extern "C" size_t pfgb_workspace_bytes(const pfgb_handle* handle) {
+  return handle ? instance64_workspace_bytes(handle->inst) : 0;
+}
+
+extern "C" int pfgb_step(pfgb_handle* handle, double* u, double* v, double* p, long ld, const pfgb_step_in* in,
+                         void* stream, pfgb_step_out* out) {
+  if (!handle || !u || !v || !p || !in || !out) return set_error(PFGB_EINVAL, "null argument");
+  if (in->hist_len < 0 || in->hist_len > 5) return set_error(PFGB_EINVAL, "hist_len must be in [0, 5]");
+  StepIn si;
+  si.dt_prev = in->dt_prev;
+  for (int k = 0; k < 5; ++k) si.hist[k] = in->hist[k];
+  si.hist_len = in->hist_len;
+  si.iteration = in->iteration;
+  return instance64_step(handle->inst, u, v, p, ld, si, (cudaStream_t)stream, out);
+}
+
+extern "C" int pfgb_project(pfgb_handle* handle, double* u, double* v, double* p, long ld, double dt, void* stream,
+                            pfgb_step_out* out) {
+  if (!handle || !u || !v || !p || !out) return set_error(PFGB_EINVAL, "null argument");
+  return instance64_project(handle->inst, u, v, p, ld, dt, (cudaStream_t)stream, out);
+}
+
+extern "C" int pfgb_cg_solve(int op, const double* b, double* x, int nx, int ny, double dx, double dy, int precond,
+                             double jacobi_interior, double tol, int maxiter, void* stream, pfgb_solve_out* out) {
+  if (!b || !x || !out) return set_error(PFGB_EINVAL, "null argument");
+  return cg_solve_run(op, b, x, nx, ny, dx, dy, precond, jacobi_interior, tol, maxiter, (cudaStream_t)stream, out);
+}

@@ -1,0 +1,54 @@
+// Shared device helpers for the PyFlow projection step on GB300 (sm_103a).
+//
+// Every binary64 operation that must reproduce the reference's NumPy
+// arithmetic is written with the IEEE round-to-nearest intrinsics
+// (__dadd_rn, __dsub_rn, __dmul_rn, __ddiv_rn), which are never contracted
+// into FMAs, and the translation units are also compiled with -fmad=false.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pfgb {
+
+__device__ __forceinline__ double ADD(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double SUB(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double MUL(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double DIV(double a, double b) { return __ddiv_rn(a, b); }
+
+// Division by a grid spacing.  When the spacing is a power of two the quotient
+// equals the product with its (exact) reciprocal for every operand, so the
+// cheaper multiply is used; otherwise the IEEE division.
+struct Spacing {
+  double h;      // the spacing
+  double rh;     // 1/h, exact when pow2
+  int pow2;
+};
+
+__device__ __forceinline__ double DIVH(double a, const Spacing& s) {
+  return s.pow2 ? __dmul_rn(a, s.rh) : __ddiv_rn(a, s.h);
+}
+
+// A 2-D row-major view: element (j, i) at p[j*ld + i].
+template <typename T>
+struct View2 {
+  T* p;
+  long ld;
+  __device__ __forceinline__ T& operator()(int j, int i) const { return p[(long)j * ld + i]; }
+};
+
+// Ordered bit pattern of a non-negative double (NaN sorts above +inf), for
+// exact max reductions with 64-bit integer atomics.
+__device__ __forceinline__ unsigned long long abs_bits(double a) {
+  return (unsigned long long)__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+__device__ __forceinline__ int isfinite_d(double a) {
+  return ((unsigned long long)__double_as_longlong(a) & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
+}
+
+// Python's min(a, b): returns b only when b < a (NaN-aware exactly like CPython).
+__device__ __forceinline__ double py_min(double a, double b) { return (b < a) ? b : a; }
+// Python's max(a, b): returns b only when b > a.
+__device__ __forceinline__ double py_max(double a, double b) { return (b > a) ? b : a; }
+
+}  // namespace pfgb

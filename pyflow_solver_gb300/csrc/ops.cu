@@ -1,0 +1,223 @@
+// Array operators of the reference as stand-alone device kernels, the pressure
+// operators, and exactly rounded dot products / sums (see xacc.cuh).
+#include <string>
+
+#include "pfgb_internal.h"
+#include "stencil.cuh"
+#include "xacc.cuh"
+
+namespace pfgb {
+
+constexpr int OT = 256;
+
+struct OpGeo {
+  int nx, ny;
+  Grid2 g;
+  double dx, dy;     // raw spacings (central divergence divides by 2*dx etc.)
+};
+
+static Spacing spacing_of(double h) {
+  Spacing s;
+  s.h = h;
+  s.pow2 = 0;
+  s.rh = 0.0;
+  int e;
+  double m = frexp(h, &e);
+  if (h > 0.0 && m == 0.5 && e - 1 >= -1022 && e - 1 <= 1022) {
+    s.pow2 = 1;
+    s.rh = ldexp(1.0, -(e - 1));
+  }
+  return s;
+}
+
+static OpGeo make_geo(int nx, int ny, double dx, double dy) {
+  OpGeo G;
+  G.nx = nx;
+  G.ny = ny;
+  G.g.nx = nx;
+  G.g.ny = ny;
+  G.g.sx = spacing_of(dx);
+  G.g.sy = spacing_of(dy);
+  G.dx = dx;
+  G.dy = dy;
+  return G;
+}
+
+__global__ void k_gradient(OpGeo G, const double* p, long ldp, double* gx, double* gy, long ldo) {
+  int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= G.nx || j >= G.ny) return;
+  View2<const double> P{p, ldp};
+  gx[(long)j * ldo + i] = grad_x(P, j, i, G.g);
+  gy[(long)j * ldo + i] = grad_y(P, j, i, G.g);
+}
+
+__global__ void k_divergence(OpGeo G, const double* u, const double* v, long ldi, double* d, long ldo) {
+  int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= G.nx || j >= G.ny) return;
+  View2<const double> U{u, ldi}, V{v, ldi};
+  d[(long)j * ldo + i] = div_coherent_at(U, V, j, i, G.g);
+}
+
+__global__ void k_laplacian(OpGeo G, const double* p, long ldp, double* l, long ldo) {
+  int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= G.nx || j >= G.ny) return;
+  View2<const double> P{p, ldp};
+  l[(long)j * ldo + i] = lap_coherent_at(P, j, i, G.g);
+}
+
+__global__ void k_div_central(OpGeo G, const double* u, const double* v, long ldi, double* d, long ldo) {
+  int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= G.nx || j >= G.ny) return;
+  View2<const double> U{u, ldi}, V{v, ldi};
+  d[(long)j * ldo + i] = div_central_at(U, V, j, i, G.nx, G.ny, G.dx, G.dy);
+}
+
+__global__ void k_advect(OpGeo G, int scheme, const double* u, const double* v, const double* f, long ldi,
+                         double* c, long ldo) {
+  int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= G.nx || j >= G.ny) return;
+  View2<const double> U{u, ldi}, V{v, ldi}, F{f, ldi};
+  c[(long)j * ldo + i] = (scheme == PFGB_SCHEME_QUICK) ? advect_quick_at(U, V, F, j, i, G.g)
+                                                       : advect_upwind_at(U, V, F, j, i, G.g);
+}
+
+__global__ void k_apply_op(OpGeo G, int op, const double* x, double* y) {
+  int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= G.nx || j >= G.ny) return;
+  View2<const double> X{x, G.nx};
+  double val;
+  if (op == PFGB_OP_NEG_LAPLACIAN_PINNED) {
+    val = (i == 0 && j == 0) ? X(0, 0) : -lap_coherent_at(X, j, i, G.g);
+  } else {
+    bool ring = i == 0 || j == 0 || i == G.nx - 1 || j == G.ny - 1;
+    val = ring ? X(j, i) : lap_coherent_at(X, j, i, G.g);
+  }
+  y[(long)j * G.nx + i] = val;
+}
+
+// ---- exactly rounded dot / sum over a contiguous vector --------------------
+constexpr int XPT = 8;   // elements per thread
+
+__global__ void __launch_bounds__(OT) k_xdot(const double* a, const double* b, long n, int mode, XASlot* slot) {
+  __shared__ long long sacc[XA_DIGITS];
+  __shared__ long long wred[(OT / 32) * XA_WLIMBS];
+  __shared__ int ired[32];
+  for (int k = threadIdx.x; k < XA_DIGITS; k += OT) sacc[k] = 0;
+  long base = (long)blockIdx.x * OT * XPT;
+  XTerm t[XPT];
+  unsigned fl = 0u;
+  int top = INT_MIN;
+#pragma unroll
+  for (int k = 0; k < XPT; ++k) {
+    long idx = base + (long)k * OT + threadIdx.x;
+    xa_zero(t[k]);
+    if (idx < n) {
+      if (mode == 0) xa_term_prod(a[idx], b[idx], t[k], fl);
+      else xa_term_val(a[idx], t[k], fl);
+    }
+    top = max(top, t[k].top);
+  }
+  top = xa_block_max(top, ired);
+  XCtx c;
+  c.clear();
+  c.flags = fl;
+  c.k0 = xa_window_digit(top);
+#pragma unroll
+  for (int k = 0; k < XPT; ++k) c.add(sacc, t[k]);
+  int anyslow = __syncthreads_or(c.slow);
+  xa_cta_commit(slot, c.pos, c.neg, c.k0, sacc, anyslow, c.flags, wred);
+  XASlot* sl[1] = {slot};
+  xa_finish(sl, 1, gridDim.x);
+}
+
+static int xreduce(const double* a, const double* b, long n, int mode, double* result, cudaStream_t s) {
+  if (n < 0) return set_error(PFGB_EINVAL, "negative length");
+  if (n == 0) {
+    *result = 0.0;
+    return PFGB_OK;
+  }
+  long nblocks = (n + (long)OT * XPT - 1) / ((long)OT * XPT);
+  if (nblocks > 0x7fffffffL) return set_error(PFGB_EINVAL, "vector too long");
+  XASlot* slot = nullptr;
+  cudaError_t e = cudaMallocAsync(&slot, sizeof(XASlot), s);
+  if (e != cudaSuccess) return set_error(PFGB_ENOMEM, "cudaMallocAsync of the reduction slot failed");
+  cudaMemsetAsync(slot, 0, sizeof(XASlot), s);
+  k_xdot<<<(unsigned)nblocks, OT, 0, s>>>(a, b, n, mode, slot);
+  e = cudaGetLastError();
+  double r = 0.0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&r, &slot->result, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(slot, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("exact reduction failed: ") + cudaGetErrorString(e));
+  *result = r;
+  return PFGB_OK;
+}
+
+static int check_grid(int nx, int ny) {
+  if (nx < 2 || ny < 2) return set_error(PFGB_EINVAL, "nx and ny must be >= 2");
+  return PFGB_OK;
+}
+
+static int launch_status(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return PFGB_OK;
+}
+
+}  // namespace pfgb
+
+using namespace pfgb;
+
+static dim3 op_grid(int nx, int ny) { return dim3((nx + 31) / 32, (ny + 7) / 8); }
+
+extern "C" int pfgb_gradient_coherent(const double* p, long ldp, double* gx, double* gy, long ldo, int nx, int ny,
+                                      double dx, double dy, void* stream) {
+  if (int rc = check_grid(nx, ny)) return rc;
+  k_gradient<<<op_grid(nx, ny), OT, 0, (cudaStream_t)stream>>>(make_geo(nx, ny, dx, dy), p, ldp, gx, gy, ldo);
+  return launch_status("gradient_coherent");
+}
+
+extern "C" int pfgb_divergence_coherent(const double* u, const double* v, long ldi, double* div, long ldo, int nx,
+                                        int ny, double dx, double dy, void* stream) {
+  if (int rc = check_grid(nx, ny)) return rc;
+  k_divergence<<<op_grid(nx, ny), OT, 0, (cudaStream_t)stream>>>(make_geo(nx, ny, dx, dy), u, v, ldi, div, ldo);
+  return launch_status("divergence_coherent");
+}
+
+extern "C" int pfgb_laplacian_coherent(const double* p, long ldp, double* lap, long ldo, int nx, int ny, double dx,
+                                       double dy, void* stream) {
+  if (int rc = check_grid(nx, ny)) return rc;
+  k_laplacian<<<op_grid(nx, ny), OT, 0, (cudaStream_t)stream>>>(make_geo(nx, ny, dx, dy), p, ldp, lap, ldo);
+  return launch_status("laplacian_coherent");
+}
+
+extern "C" int pfgb_divergence_central(const double* u, const double* v, long ldi, double* div, long ldo, int nx,
+                                       int ny, double dx, double dy, void* stream) {
+  if (int rc = check_grid(nx, ny)) return rc;
+  k_div_central<<<op_grid(nx, ny), OT, 0, (cudaStream_t)stream>>>(make_geo(nx, ny, dx, dy), u, v, ldi, div, ldo);
+  return launch_status("divergence_central");
+}
+
+extern "C" int pfgb_advect(int scheme, const double* u, const double* v, const double* f, long ldi, double* conv,
+                           long ldo, int nx, int ny, double dx, double dy, void* stream) {
+  if (int rc = check_grid(nx, ny)) return rc;
+  if (scheme != PFGB_SCHEME_UPWIND && scheme != PFGB_SCHEME_QUICK) return set_error(PFGB_EINVAL, "unknown scheme");
+  k_advect<<<op_grid(nx, ny), OT, 0, (cudaStream_t)stream>>>(make_geo(nx, ny, dx, dy), scheme, u, v, f, ldi, conv, ldo);
+  return launch_status("advect");
+}
+
+extern "C" int pfgb_apply_operator(int op, const double* x, double* y, int nx, int ny, double dx, double dy,
+                                   void* stream) {
+  if (int rc = check_grid(nx, ny)) return rc;
+  if (op != PFGB_OP_NEG_LAPLACIAN_PINNED && op != PFGB_OP_LAPLACIAN_DIRICHLET) return set_error(PFGB_EINVAL, "unknown operator");
+  k_apply_op<<<op_grid(nx, ny), OT, 0, (cudaStream_t)stream>>>(make_geo(nx, ny, dx, dy), op, x, y);
+  return launch_status("apply_operator");
+}
+
+extern "C" int pfgb_xdot(const double* a, const double* b, long n, double* result, void* stream) {
+  return xreduce(a, b, n, 0, result, (cudaStream_t)stream);
+}
+
+extern "C" int pfgb_xsum(const double* a, long n, double* result, void* stream) {
+  return xreduce(a, a, n, 1, result, (cudaStream_t)stream);
+}

@@ -1,0 +1,27 @@
+// Internal declarations shared by the translation units of libpfgb.so.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/pfgb.h"
+
+namespace pfgb {
+
+// Record the message of the last error of this thread and return `code`.
+int set_error(int code, const std::string& msg);
+int check_cuda(cudaError_t e, const char* what);
+
+struct StepIn;
+struct Instance64;
+int instance64_create(const pfgb_params* prm, Instance64** out);
+void instance64_destroy(Instance64* I);
+size_t instance64_workspace_bytes(const Instance64* I);
+int instance64_project(Instance64* I, double* u, double* v, double* p, long lds, double dt, cudaStream_t s,
+                       pfgb_step_out* out);
+int cg_solve_run(int op, const double* b, double* x, int nx, int ny, double dx, double dy, int precond,
+                 double invd, double tol, int maxiter, cudaStream_t s, pfgb_solve_out* out);
+int instance64_step(Instance64* I, double* u, double* v, double* p, long lds, const StepIn& in,
+                    cudaStream_t s, pfgb_step_out* out);
+
+}  // namespace pfgb

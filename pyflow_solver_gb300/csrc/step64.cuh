@@ -1,0 +1,58 @@
+// Plain binary64 projection step: device structures shared by the kernels and
+// the host driver of one cavity instance.
+#pragma once
+#include "common.cuh"
+#include "xacc.cuh"
+
+namespace pfgb {
+
+// Reduction sites of one step (each an XASlot).
+enum Slot64 {
+  S_DIVC_BEFORE = 0,   // ||div_central(u,v;1,1)||^2 before the step      (solver.py:45)
+  S_DIVSTAR,           // ||div_c(u*,v*)||^2   -> divergence_norm_initial (pressure_solver.py:121)
+  S_BSUM,              // sum of the raw RHS     -> np.mean              (pressure_solver.py:126)
+  S_BB,                // ||b||^2                -> bnrm2 of scipy cg
+  S_RZ0,               // r.z at iteration 0
+  S_PQ,                // p.q                     (one per CG iteration)
+  S_RR,                // r.r                     (one per CG iteration)
+  S_RZ,                // r.z                     (one per CG iteration)
+  S_RES,               // ||b - A x||^2           (interface.py:48-49)
+  S_RU,                // sum (u - u_old)^2       (solver.py:106-109)
+  S_RV,
+  S_DIVAFTER,          // ||div_c(u,v)||^2 after correction (pressure_solver.py:165-170)
+  S_LINRES,            // ||A p - b||^2           (pressure_solver.py:174-178)
+  S_CONT,              // ||div_central(u,v;1,1)||^2 after the step (solver.py:111)
+  S_COUNT
+};
+
+// Host-written inputs of one step.
+struct StepIn {
+  double dt_prev;
+  double hist[5];
+  int hist_len;
+  int iteration;
+};
+
+// Device control block of one instance (written by finalisers / tiny kernels).
+struct Ctrl64 {
+  unsigned long long umax_bits, vmax_bits;  // running maxima (prestep)
+  double umax, vmax;                         // + 1e-12 applied
+  double div_before;
+  double dt, dtm, cfl;
+  int safeguard;
+  // CG
+  int iter, done, info, zero_rhs;
+  double mean, bnrm2, atol, rho, rho_prev, pq, rr;
+  unsigned nan_flag;
+};
+
+// Everything the host reads back after a step (one copy).
+struct StepOut64 {
+  double umax, vmax, div_before, dt, cfl;
+  int safeguard, cg_iters, cg_info, nan_flag;
+  double divstar2, bnrm2, res2, ru2, rv2, divafter2, linres2, cont2;
+  unsigned flags_or;    // OR of the result flags of all slots (inexact / overflow diagnostics)
+  unsigned pad;
+};
+
+}  // namespace pfgb

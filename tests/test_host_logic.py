@@ -1,0 +1,63 @@
+"""Host-side logic of the GPU package that needs no GPU."""
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+from pyflow_solver_gb300 import _capi
+from pyflow_solver_gb300.io import checkpoint as ck
+from pyflow_solver_gb300.linear_solvers.preconditioners import diag_matches_assembled, jacobi_interior
+from pyflow_solver_gb300.solvers.solver import step_params
+
+
+def test_step_params_follow_reference_getattr_defaults():
+    cfg = SimpleNamespace(nx=64, ny=32)
+    P, dx, dy, nu = step_params(cfg, 64, 32)
+    assert dx == 63.0 / 63 and dy == 31.0 / 31           # CLI path: lx = nx - 1 -> dx = 1
+    assert nu == 1.0 / 100.0
+    assert P.lin_maxiter == 400 and P.lin_tol == 1e-10   # pressure_solver.py:133-135 defaults
+    assert P.scheme == _capi.SCHEME_UPWIND                # solver.py:80 fallback
+    assert P.has_lid == 0 and P.enable_jacobi == 1
+    cfg = SimpleNamespace(lx=1.0, ly=1.0, advection_scheme="quick", lid_velocity=1.0, Re=1000.0,
+                          disable_advection=False, enable_jacobi_pc=False)
+    P, dx, dy, nu = step_params(cfg, 512, 512)
+    assert dx == 1.0 / 511 and P.scheme == _capi.SCHEME_QUICK and P.has_lid == 1 and P.enable_jacobi == 0
+    assert P.jacobi_interior == 1.0 / (2.0 / dx**2 + 2.0 / dy**2)
+    P, *_ = step_params(SimpleNamespace(disable_advection=True, advection_scheme="quick"), 8, 8)
+    assert P.scheme == _capi.SCHEME_NONE
+
+
+def test_jacobi_diagonal_equals_assembled():
+    from oracle.ops import jacobi_inv_diag
+    for nx, ny, dx, dy in [(8, 8, 1 / 7, 1 / 7), (5, 9, 1.0, 1.0), (2, 3, 0.5, 0.25)]:
+        inv = jacobi_inv_diag(nx, ny, dx, dy).reshape(ny, nx)
+        if nx > 2 and ny > 2:
+            assert inv[1, 1] == jacobi_interior(dx, dy)
+        D = np.ones((ny, nx))
+        if nx > 2 and ny > 2:
+            D[1:-1, 1:-1] = 2.0 / dx**2 + 2.0 / dy**2
+        assert diag_matches_assembled(D, nx, ny, dx, dy)
+
+
+def test_checkpoint_format_round_trip(tmp_path):
+    from pyflow_solver_gb300.core.ghost_fields import State
+    rng = np.random.default_rng(0)
+    st = State(4, 3, {k: rng.standard_normal((5, 6)) for k in "uvp"})
+    cfg = SimpleNamespace(nx=4, ny=3, seed=7)
+    path = ck.save_checkpoint(str(tmp_path / "c.npz"), st, 12, 0.5, cfg)
+    with np.load(path) as d:
+        assert set(d.files) == {"meta", "field_u", "field_v", "field_p"}
+    st2, meta = ck.load_checkpoint(path, device=None)
+    assert meta["iteration"] == 12 and meta["nx"] == 4 and meta["seed"] == 7 and meta["schema_version"] == 1
+    for k in "uvp":
+        np.testing.assert_array_equal(st2.fields[k], st.fields[k])
+    assert meta["field_hashes"]["u"] == ck._hash_array(st.fields["u"])
+    st3, meta3 = ck.load_checkpoint_bytes(ck.save_checkpoint_bytes(st, 3, 0.0, cfg), device=None)
+    assert meta3["iteration"] == 3
+
+
+def test_driver_requires_state_or_grid():
+    from pyflow_solver_gb300.drivers.simulation_driver import SimulationDriver
+    d = SimulationDriver(SimpleNamespace())
+    with pytest.raises(ValueError):
+        next(d.run(max_steps=1))
