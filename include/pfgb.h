@@ -175,6 +175,18 @@ PFGB_API int pfgb_cg_solve(int op, const double* b, double* x, int nx, int ny, d
                   int precond, double jacobi_interior, double tol, int maxiter,
                   void* stream, pfgb_solve_out* out);
 
+/* ---- measurement ----------------------------------------------------------- */
+
+/* Record CUDA events around every pressure-matvec launch (p = z + beta p;
+ * q = A p; p.q) of the following steps of this handle.  No reference
+ * counterpart: benchmark instrumentation. */
+PFGB_API int pfgb_set_profiling(pfgb_handle* handle, int on);
+/* Total device time (ms) and number of the matvec launches of the last step. */
+PFGB_API int pfgb_profile_result(pfgb_handle* handle, double* ms, int* launches);
+/* Measured FP64 FMA issue rate of the current device, in 1e12 instructions/s.
+ * No reference counterpart: the denominator of the FP64 roofline. */
+PFGB_API int pfgb_probe_fp64(void* stream, double* tops);
+
 #ifdef __cplusplus
 }
 #endif

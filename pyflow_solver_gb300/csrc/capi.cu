@@ -86,3 +86,18 @@ extern "C" int pfgb_cg_solve(int op, const double* b, double* x, int nx, int ny,
   if (!b || !x || !out) return set_error(PFGB_EINVAL, "null argument");
   return cg_solve_run(op, b, x, nx, ny, dx, dy, precond, jacobi_interior, tol, maxiter, (cudaStream_t)stream, out);
 }
+
+extern "C" int pfgb_set_profiling(pfgb_handle* handle, int on) {
+  if (!handle) return set_error(PFGB_EINVAL, "null handle");
+  return instance64_set_profiling(handle->inst, on);
+}
+
+extern "C" int pfgb_profile_result(pfgb_handle* handle, double* ms, int* launches) {
+  if (!handle || !ms || !launches) return set_error(PFGB_EINVAL, "null argument");
+  return instance64_profile_result(handle->inst, ms, launches);
+}
+
+extern "C" int pfgb_probe_fp64(void* stream, double* tops) {
+  if (!tops) return set_error(PFGB_EINVAL, "null argument");
+  return probe_fp64((cudaStream_t)stream, tops);
+}

@@ -579,6 +579,10 @@ struct Instance64 {
   Ctrl64* ctrl;
   StepOut64* out_d;
   StepOut64* out_h = nullptr;
+  // optional per-launch timing of k_cg_matvec (benchmark roofline)
+  int profiling = 0;
+  std::vector<cudaEvent_t> ev;
+  int ev_used = 0;
 };
 
 int instance64_create(const pfgb_params* prm, Instance64** out) {
@@ -643,6 +647,7 @@ int instance64_create(const pfgb_params* prm, Instance64** out) {
 
 void instance64_destroy(Instance64* I) {
   if (!I) return;
+  for (cudaEvent_t e : I->ev) cudaEventDestroy(e);
   if (I->ws) cudaFree(I->ws);
   if (I->out_h) cudaFreeHost(I->out_h);
   delete I;
@@ -663,7 +668,13 @@ static void enqueue_projection(Instance64* I, const Geo64& G, int mode, double* 
   for (int k = 0; k < I->A.maxiter; ++k) {
     const double* pold = I->p[k & 1];
     double* pnew = I->p[(k + 1) & 1];
+    const bool timed = I->profiling && (size_t)(2 * k + 1) < I->ev.size();
+    if (timed) cudaEventRecord(I->ev[2 * k], s);
     k_cg_matvec<0><<<gc, NT, 0, s>>>(G, k, I->r, pold, pnew, I->q, I->slots, I->ctrl);
+    if (timed) {
+      cudaEventRecord(I->ev[2 * k + 1], s);
+      I->ev_used = k + 1;
+    }
     k_cg_update<<<gc, NT, 0, s>>>(G, I->A, k, pnew, I->q, I->x, I->r, I->slots, I->ctrl);
   }
   k_post_resid<0><<<gp, NT, 0, s>>>(G, I->b, I->x, I->slots);
@@ -739,6 +750,75 @@ int instance64_step(Instance64* I, double* u, double* v, double* p, long lds, co
   int rc = instance64_enqueue(I, u, v, p, lds, in, s);
   if (rc) return rc;
   return read_out(I, s, out);
+}
+
+// Per-launch timing of the matvec kernel in the following steps.
+int instance64_set_profiling(Instance64* I, int on) {
+  if (on && I->ev.empty()) {
+    int n = 2 * (I->A.maxiter > 0 ? I->A.maxiter : 1);
+    I->ev.resize(n);
+    for (int k = 0; k < n; ++k)
+      if (cudaEventCreate(&I->ev[k]) != cudaSuccess) return set_error(PFGB_ECUDA, "cudaEventCreate failed");
+  }
+  I->profiling = on;
+  I->ev_used = 0;
+  return PFGB_OK;
+}
+
+// Sum of the matvec launch durations of the last (synchronised) step.  Launches
+// that returned at once because the solve had converged are included.
+int instance64_profile_result(Instance64* I, double* ms, int* launches) {
+  double tot = 0.0;
+  for (int k = 0; k < I->ev_used; ++k) {
+    float t = 0.f;
+    cudaError_t e = cudaEventElapsedTime(&t, I->ev[2 * k], I->ev[2 * k + 1]);
+    if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("event timing: ") + cudaGetErrorString(e));
+    tot += t;
+  }
+  *ms = tot;
+  *launches = I->ev_used;
+  return PFGB_OK;
+}
+
+// FP64 issue-rate probe: independent DFMA chains on every SM.
+__global__ void k_probe_fp64(double* out, double a, double b, int n) {
+  double x0 = a + threadIdx.x, x1 = x0 + 1.0, x2 = x0 + 2.0, x3 = x0 + 3.0;
+#pragma unroll 16
+  for (int i = 0; i < n; ++i) {
+    x0 = fma(x0, b, a); x1 = fma(x1, b, a); x2 = fma(x2, b, a); x3 = fma(x3, b, a);
+  }
+  out[(long)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3;
+}
+
+int probe_fp64(cudaStream_t s, double* tops) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, n = 2048;
+  double* buf = nullptr;
+  if (cudaMallocAsync(&buf, (size_t)blocks * threads * sizeof(double), s) != cudaSuccess)
+    return set_error(PFGB_ENOMEM, "probe buffer allocation failed");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0, s);
+    k_probe_fp64<<<blocks, threads, 0, s>>>(buf, 1.0, 0.9999999, n);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(buf, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("probe failed: ") + cudaGetErrorString(e));
+  // one DFMA = one FP64 instruction (2 flops); report instructions per second
+  *tops = 4.0 * n * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return PFGB_OK;
 }
 
 // ---------------------------------------------------------------------------
