@@ -299,6 +299,8 @@ def e2e_rate(cfg, steps):
     from pyflow_solver_gb300 import ResidualManager
     from pyflow_solver_gb300.core.ghost_fields import State
     from pyflow_solver_gb300.solvers.solver import step
+    if steps <= 0:
+        return None
     host = State(NX, NY, {k: np.zeros((NY + 2, NX + 2)) for k in "uvp"})
     tr = ResidualManager()
     step(cfg, host, tr, 0)
