@@ -175,6 +175,25 @@ PFGB_API int pfgb_cg_solve(int op, const double* b, double* x, int nx, int ny, d
                   int precond, double jacobi_interior, double tol, int maxiter,
                   void* stream, pfgb_solve_out* out);
 
+/* Same solve as pfgb_cg_solve, but it allocates nothing: no cudaMalloc,
+ * cudaMallocAsync, cudaFree or other allocating call.  It has no counterpart in
+ * the reference; it exists for callers that cannot allocate device memory when
+ * they solve -- a thread in the middle of a CUDA graph capture (allocation is
+ * not capturable), a real-time loop that must not wait on the allocator, or a
+ * host application that owns the whole device memory pool.
+ * The CG work vectors live in one fixed device array compiled into the library
+ * (about 8.4 MiB, reserved on every device that loads the library until the
+ * process exits), so nx*ny must not exceed 262,144 cells (512 x 512); larger
+ * grids return PFGB_EINVAL without launching anything.
+ * The first call on a device looks up that array's device address (once per
+ * device, with the device current); make that first call before any stream
+ * capture.  Every call reuses the same array: two calls that overlap on the GPU
+ * (different streams or host threads without ordering) race and corrupt each
+ * other's results, so serialise them.  Synchronises `stream`. */
+PFGB_API int pfgb_cg_solve_noalloc(int op, const double* b, double* x, int nx, int ny, double dx, double dy,
+                                   int precond, double jacobi_interior, double tol, int maxiter,
+                                   void* stream, pfgb_solve_out* out);
+
 /* ---- measurement ----------------------------------------------------------- */
 
 /* Record CUDA events around every pressure-matvec launch (p = z + beta p;

@@ -101,3 +101,11 @@ extern "C" int pfgb_probe_fp64(void* stream, double* tops) {
   if (!tops) return set_error(PFGB_EINVAL, "null argument");
   return probe_fp64((cudaStream_t)stream, tops);
 }
+
+extern "C" int pfgb_cg_solve_noalloc(int op, const double* b, double* x, int nx, int ny, double dx, double dy,
+                                     int precond, double jacobi_interior, double tol, int maxiter, void* stream,
+                                     pfgb_solve_out* out) {
+  if (!b || !x || !out) return set_error(PFGB_EINVAL, "null argument");
+  return cg_solve_noalloc_run(op, b, x, nx, ny, dx, dy, precond, jacobi_interior, tol, maxiter, (cudaStream_t)stream,
+                              out);
+}

@@ -22,6 +22,8 @@ int instance64_project(Instance64* I, double* u, double* v, double* p, long lds,
 int instance64_set_profiling(Instance64* I, int on);
 int instance64_profile_result(Instance64* I, double* ms, int* launches);
 int probe_fp64(cudaStream_t s, double* tops);
+int cg_solve_noalloc_run(int op, const double* b, double* x, int nx, int ny, double dx, double dy, int precond,
+                         double invd, double tol, int maxiter, cudaStream_t s, pfgb_solve_out* out);
 int cg_solve_run(int op, const double* b, double* x, int nx, int ny, double dx, double dy, int precond,
                  double invd, double tol, int maxiter, cudaStream_t s, pfgb_solve_out* out);
 int instance64_step(Instance64* I, double* u, double* v, double* p, long lds, const StepIn& in,

@@ -19,6 +19,7 @@
 // solve is done, so a fixed launch sequence reproduces scipy's early exit.
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -880,6 +881,121 @@ int cg_solve_run(int op, const double* b, double* x, int nx, int ny, double dx, 
   cudaFreeAsync(ws, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("cg solve failed: ") + cudaGetErrorString(e));
+  out->info = hc.info;
+  out->iterations = hc.zero_rhs ? 0 : hc.iter;
+  out->bnorm = hc.bnrm2;
+  out->res_sq = res2;
+  return PFGB_OK;
+}
+
+}  // namespace pfgb
+
+namespace pfgb {
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the operator-interface CG.
+//
+// Some callers cannot allocate device memory at the moment they need a solve:
+// a host thread inside a CUDA graph capture (cudaMalloc is not capturable), a
+// real-time loop that must not block on the allocator, or an embedding
+// application that reserved the whole device for its own pool and forbids
+// third-party allocations.  For them the work vectors, reduction slots and
+// control block of the CG live in one file-scope device array of fixed size,
+// reserved once when the library's module is loaded on a device and held until
+// the process exits.  Its limit is NOALLOC_MAX_CELLS = 262,144 cells
+// (512 x 512), about 8.4 MiB per device.
+namespace noalloc {
+
+constexpr long NOALLOC_MAX_CELLS = 1L << 18;
+
+struct Scratch {
+  double r[NOALLOC_MAX_CELLS];
+  double p0[NOALLOC_MAX_CELLS];
+  double p1[NOALLOC_MAX_CELLS];
+  double q[NOALLOC_MAX_CELLS];
+  XASlot slots[S_COUNT];
+  Ctrl64 ctrl;
+};
+
+static __device__ __align__(256) Scratch g_scratch;
+
+constexpr int MAX_DEVICES = 64;
+static std::mutex g_mu;
+static Scratch* g_addr[MAX_DEVICES] = {};
+
+// Device address of g_scratch on the current device (looked up once per device).
+static int scratch_address(Scratch** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= MAX_DEVICES) return set_error(PFGB_EINVAL, "device index beyond the scratch table");
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess)
+      return set_error(PFGB_ECUDA, std::string("cudaGetSymbolAddress of the CG scratch: ") + cudaGetErrorString(e));
+    g_addr[dev] = static_cast<Scratch*>(p);
+  }
+  *out = g_addr[dev];
+  return PFGB_OK;
+}
+
+}  // namespace noalloc
+
+int cg_solve_noalloc_run(int op, const double* b, double* x, int nx, int ny, double dx, double dy, int precond,
+                         double invd, double tol, int maxiter, cudaStream_t s, pfgb_solve_out* out) {
+  using namespace noalloc;
+  if (nx < 2 || ny < 2) return set_error(PFGB_EINVAL, "nx and ny must be >= 2");
+  if ((long)nx * (long)ny > NOALLOC_MAX_CELLS)
+    return set_error(PFGB_EINVAL, "nx*ny exceeds the 262144-cell limit of the allocation-free CG scratch");
+  if (op != PFGB_OP_NEG_LAPLACIAN_PINNED && op != PFGB_OP_LAPLACIAN_DIRICHLET) return set_error(PFGB_EINVAL, "unknown operator");
+  if (maxiter < 0) return set_error(PFGB_EINVAL, "maxiter must be >= 0");
+  Scratch* S = nullptr;
+  if (int rc = scratch_address(&S)) return rc;
+  Geo64 G;
+  G.nx = nx;
+  G.ny = ny;
+  G.ld = nx;
+  G.lds = nx + 2;
+  G.g.nx = nx;
+  G.g.ny = ny;
+  G.g.sx = make_spacing(dx);
+  G.g.sy = make_spacing(dy);
+  G.invd = invd;
+  G.jacobi = precond;
+  CGArgs A;
+  A.rtol = tol;
+  A.maxiter = maxiter;
+  A.n_cells = (double)nx * (double)ny;
+  // the slots and the control block must start from zero on every call
+  cudaError_t e = cudaMemsetAsync(S->slots, 0, sizeof(S->slots) + sizeof(S->ctrl), s);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("clearing the CG scratch: ") + cudaGetErrorString(e));
+  XASlot* slots = S->slots;
+  Ctrl64* ctrl = &S->ctrl;
+  dim3 gp((nx + TX - 1) / TX, (ny + PB_Y - 1) / PB_Y);
+  dim3 gc((nx + TX - 1) / TX, (ny + TY - 1) / TY);
+  k_cg_init<<<gp, NT, 0, s>>>(G, A, 0, const_cast<double*>(b), S->r, x, slots, ctrl);
+  for (int k = 0; k < maxiter; ++k) {
+    double* pold = (k & 1) ? S->p1 : S->p0;
+    double* pnew = (k & 1) ? S->p0 : S->p1;
+    if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
+      k_cg_matvec<0><<<gc, NT, 0, s>>>(G, k, S->r, pold, pnew, S->q, slots, ctrl);
+    else
+      k_cg_matvec<1><<<gc, NT, 0, s>>>(G, k, S->r, pold, pnew, S->q, slots, ctrl);
+    k_cg_update<<<gc, NT, 0, s>>>(G, A, k, pnew, S->q, x, S->r, slots, ctrl);
+  }
+  if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
+    k_post_resid<0><<<gp, NT, 0, s>>>(G, b, x, slots);
+  else
+    k_post_resid<1><<<gp, NT, 0, s>>>(G, b, x, slots);
+  Ctrl64 hc;
+  double res2 = 0.0;
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hc, ctrl, sizeof(Ctrl64), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&res2, &slots[S_RES].result, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("allocation-free cg solve failed: ") + cudaGetErrorString(e));
   out->info = hc.info;
   out->iterations = hc.zero_rhs ? 0 : hc.iter;
   out->bnorm = hc.bnrm2;
