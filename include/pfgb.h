@@ -178,9 +178,9 @@ PFGB_API int pfgb_cg_solve(int op, const double* b, double* x, int nx, int ny, d
 /* Same solve as pfgb_cg_solve, but it allocates nothing: no cudaMalloc,
  * cudaMallocAsync, cudaFree or other allocating call.  It has no counterpart in
  * the reference; it exists for callers that cannot allocate device memory when
- * they solve -- a thread in the middle of a CUDA graph capture (allocation is
- * not capturable), a real-time loop that must not wait on the allocator, or a
- * host application that owns the whole device memory pool.
+ * they solve: a real-time loop that must not stall on cudaMalloc/cudaFree (they
+ * can synchronise the whole device), or a host application that has reserved
+ * the device memory for its own pool and admits no third-party allocation.
  * The CG work vectors live in one fixed device array compiled into the library
  * (about 8.4 MiB, reserved on every device that loads the library until the
  * process exits), so nx*ny must not exceed 262,144 cells (512 x 512); larger

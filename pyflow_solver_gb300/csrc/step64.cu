@@ -896,10 +896,9 @@ namespace pfgb {
 // Allocation-free variant of the operator-interface CG.
 //
 // Some callers cannot allocate device memory at the moment they need a solve:
-// a host thread inside a CUDA graph capture (cudaMalloc is not capturable), a
-// real-time loop that must not block on the allocator, or an embedding
-// application that reserved the whole device for its own pool and forbids
-// third-party allocations.  For them the work vectors, reduction slots and
+// a real-time loop that must not stall on cudaMalloc/cudaFree (both can
+// synchronise the whole device), or an embedding application that reserved the
+// device memory for its own pool and admits no third-party allocation.  For them the work vectors, reduction slots and
 // control block of the CG live in one file-scope device array of fixed size,
 // reserved once when the library's module is loaded on a device and held until
 // the process exits.  Its limit is NOALLOC_MAX_CELLS = 262,144 cells

@@ -1,9 +1,9 @@
 """The allocation-free CG entry point against the allocating one.
 
 ``pfgb_cg_solve_noalloc`` serves callers that may not allocate device memory
-when they solve (a thread inside a CUDA graph capture, a real-time loop that
-must not wait on the allocator, an application that owns the whole memory
-pool).  It must return exactly what ``pfgb_cg_solve`` returns.  Two calls in a
+when they solve: a real-time loop that must not stall on cudaMalloc/cudaFree
+(both can synchronise the whole device), or an application that reserved the
+device memory for its own pool.  It must return exactly what ``pfgb_cg_solve`` returns.  Two calls in a
 row with different right-hand sides check that the shared scratch array, which
 keeps the previous call's contents, does not leak into the next result.  This
 file is collected last on purpose: it passes alone in a fresh process and after
