@@ -156,6 +156,13 @@ PFGB_API int pfgb_advect(int scheme, const double* u, const double* v, const dou
 PFGB_API int pfgb_apply_operator(int op, const double* x, double* y, int nx, int ny, double dx, double dy,
                         void* stream);
 
+/* out[i] = a[i] / d with the division the stencils use for a grid spacing d > 0
+ * (method 0: exact reciprocal product for powers of two, else the integer-pipe
+ * division by an invariant divisor) or the hardware IEEE division (method 1).
+ * Both return the correctly rounded quotient of NumPy's `a / d`, the form of
+ * every `/ dx`, `/ dy` of src/pyflow/numerics/core_ops_coherent.py:57-77. */
+PFGB_API int pfgb_div_by_constant(const double* a, double* out, long n, double d, int method, void* stream);
+
 /* ---- exactly rounded reductions ------------------------------------------ */
 
 /* result = RN(sum a[i]*b[i]) with exact products (order independent); the

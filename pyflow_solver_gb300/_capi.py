@@ -75,6 +75,7 @@ SIGNATURES = {
     "pfgb_divergence_central": (_I, [_P, _P, _L, _P, _L, _I, _I, _D, _D, _P]),
     "pfgb_advect": (_I, [_I, _P, _P, _P, _L, _P, _L, _I, _I, _D, _D, _P]),
     "pfgb_apply_operator": (_I, [_I, _P, _P, _I, _I, _D, _D, _P]),
+    "pfgb_div_by_constant": (_I, [_P, _P, _L, _D, _I, _P]),
     "pfgb_xdot": (_I, [_P, _P, _L, c_double_p, _P]),
     "pfgb_xsum": (_I, [_P, _L, c_double_p, _P]),
     "pfgb_cg_solve": (_I, [_I, _P, _P, _I, _I, _D, _D, _I, _D, _D, _I, _P, ctypes.POINTER(SolveOut)]),

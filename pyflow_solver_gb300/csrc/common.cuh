@@ -5,8 +5,11 @@
 // (__dadd_rn, __dsub_rn, __dmul_rn, __ddiv_rn), which are never contracted
 // into FMAs, and the translation units are also compiled with -fmad=false.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
+
+#include "idiv.cuh"
 
 namespace pfgb {
 
@@ -17,15 +20,35 @@ __device__ __forceinline__ double DIV(double a, double b) { return __ddiv_rn(a, 
 
 // Division by a grid spacing.  When the spacing is a power of two the quotient
 // equals the product with its (exact) reciprocal for every operand, so the
-// cheaper multiply is used; otherwise the IEEE division.
+// cheaper multiply is used; otherwise the integer-pipe division by an invariant
+// divisor (idiv.cuh), which returns the IEEE quotient.
 struct Spacing {
   double h;      // the spacing
   double rh;     // 1/h, exact when pow2
   int pow2;
+  DivConst dc;   // valid (dc.ok) for positive normal spacings that are not powers of two
 };
 
 __device__ __forceinline__ double DIVH(double a, const Spacing& s) {
-  return s.pow2 ? __dmul_rn(a, s.rh) : __ddiv_rn(a, s.h);
+  if (s.pow2) return __dmul_rn(a, s.rh);
+  if (s.dc.ok) return div_const(a, s.dc);
+  return __ddiv_rn(a, s.h);
+}
+
+// Host-side preparation of a spacing.
+inline Spacing spacing_for(double h) {
+  Spacing s;
+  s.h = h;
+  s.pow2 = 0;
+  s.rh = 0.0;
+  int e;
+  double m = std::frexp(h, &e);
+  if (h > 0.0 && m == 0.5 && e - 1 >= -1022 && e - 1 <= 1022) {   // h = 2^(e-1), 1/h normal
+    s.pow2 = 1;
+    s.rh = std::ldexp(1.0, -(e - 1));
+  }
+  s.dc = make_divconst(h);
+  return s;
 }
 
 // A 2-D row-major view: element (j, i) at p[j*ld + i].

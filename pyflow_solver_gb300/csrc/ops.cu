@@ -16,19 +16,7 @@ struct OpGeo {
   double dx, dy;     // raw spacings (central divergence divides by 2*dx etc.)
 };
 
-static Spacing spacing_of(double h) {
-  Spacing s;
-  s.h = h;
-  s.pow2 = 0;
-  s.rh = 0.0;
-  int e;
-  double m = frexp(h, &e);
-  if (h > 0.0 && m == 0.5 && e - 1 >= -1022 && e - 1 <= 1022) {
-    s.pow2 = 1;
-    s.rh = ldexp(1.0, -(e - 1));
-  }
-  return s;
-}
+static Spacing spacing_of(double h) { return spacing_for(h); }
 
 static OpGeo make_geo(int nx, int ny, double dx, double dy) {
   OpGeo G;
@@ -93,6 +81,14 @@ __global__ void k_apply_op(OpGeo G, int op, const double* x, double* y) {
     val = ring ? X(j, i) : lap_coherent_at(X, j, i, G.g);
   }
   y[(long)j * G.nx + i] = val;
+}
+
+// out[i] = a[i] / d through the spacing division used by the stencils
+// (method 0) or the hardware IEEE division (method 1).
+__global__ void k_div_by(const double* a, double* out, long n, Spacing s, int method) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = method ? __ddiv_rn(a[i], s.h) : DIVH(a[i], s);
 }
 
 // ---- exactly rounded dot / sum over a contiguous vector --------------------
@@ -220,4 +216,13 @@ extern "C" int pfgb_xdot(const double* a, const double* b, long n, double* resul
 
 extern "C" int pfgb_xsum(const double* a, long n, double* result, void* stream) {
   return xreduce(a, a, n, 1, result, (cudaStream_t)stream);
+}
+
+extern "C" int pfgb_div_by_constant(const double* a, double* out, long n, double d, int method, void* stream) {
+  if (n < 0 || !(d > 0.0)) return set_error(PFGB_EINVAL, "n must be >= 0 and d > 0");
+  if (n == 0) return PFGB_OK;
+  long blocks = (n + OT - 1) / OT;
+  if (blocks > 0x7fffffffL) return set_error(PFGB_EINVAL, "vector too long");
+  k_div_by<<<(unsigned)blocks, OT, 0, (cudaStream_t)stream>>>(a, out, n, spacing_for(d), method);
+  return launch_status("div_by_constant");
 }

@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(Geo64 G, int k, const double* 
   __shared__ int ired[32];
   zero_sacc(sacc);
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  const double beta = (k > 0) ? DIV(ctrl->rho, ctrl->rho_prev) : 0.0;
+  const double beta = (k > 0) ? ctrl->beta : 0.0;
   for (int idx = threadIdx.x; idx < (TY + 2) * (TX + 2); idx += NT) {
     int jj = idx / (TX + 2) - 1, ii = idx % (TX + 2) - 1;
     int gj = j0 + jj, gi = i0 + ii;
@@ -343,7 +343,9 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(Geo64 G, int k, const double* 
   reduce_terms(&slots[S_PQ], t, RPT, fl, sacc, wred, ired);
   XASlot* sl[1] = {&slots[S_PQ]};
   if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
-    ctrl->pq = slots[S_PQ].result;
+    const double pq = slots[S_PQ].result;
+    ctrl->pq = pq;
+    ctrl->alpha = DIV(ctrl->rho, pq);
   }
 }
 
@@ -358,7 +360,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(Geo64 G, CGArgs A, int k, cons
   zero_sacc(sacc0);
   zero_sacc(sacc1);
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  const double alpha = DIV(ctrl->rho, ctrl->pq);
+  const double alpha = ctrl->alpha;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   XTerm trr[RPT], trz[RPT];
   unsigned f0 = 0u, f1 = 0u;
@@ -385,6 +387,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(Geo64 G, CGArgs A, int k, cons
     ctrl->rr = rr;
     ctrl->rho_prev = ctrl->rho;
     ctrl->rho = slots[S_RZ].result;
+    ctrl->beta = DIV(ctrl->rho, ctrl->rho_prev);
     int it = k + 1;
     ctrl->iter = it;
     if (it >= A.maxiter) {
@@ -554,19 +557,7 @@ __global__ void k_gather(const XASlot* slots, const Ctrl64* ctrl, StepOut64* out
 
 static long round_up(long a, long m) { return (a + m - 1) / m * m; }
 
-static Spacing make_spacing(double h) {
-  Spacing s;
-  s.h = h;
-  s.pow2 = 0;
-  s.rh = 0.0;
-  int e;
-  double m = frexp(h, &e);
-  if (h > 0.0 && m == 0.5 && e - 1 >= -1022 && e - 1 <= 1022) {   // h = 2^(e-1), 1/h normal
-    s.pow2 = 1;
-    s.rh = ldexp(1.0, -(e - 1));
-  }
-  return s;
-}
+static Spacing make_spacing(double h) { return spacing_for(h); }
 
 struct Instance64 {
   pfgb_params P;

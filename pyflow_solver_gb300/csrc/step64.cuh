@@ -43,6 +43,7 @@ struct Ctrl64 {
   // CG
   int iter, done, info, zero_rhs;
   double mean, bnrm2, atol, rho, rho_prev, pq, rr;
+  double alpha, beta;    // rho/pq and rho/rho_prev, formed once by the finalisers
   unsigned nan_flag;
 };
 

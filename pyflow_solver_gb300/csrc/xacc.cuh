@@ -41,7 +41,9 @@ struct XASlot {                  // one reduction site in global memory (zeroed 
   unsigned int flags;
   double result;                 // value of the last completed reduction
   unsigned int result_flags;     // flags of the last completed reduction
-  unsigned int pad;
+  int lo_inv;                    // XA_DIGITS - lowest digit written (0: none), atomicMax
+  int hi_p1;                     // highest digit written + 1 (0: none), atomicMax
+  int pad;
 };
 
 struct XTerm {                   // value = (-1)^neg * M * 2^e,  M = m3:m2:m1:m0 < 2^106
@@ -287,44 +289,64 @@ __device__ __forceinline__ void xa_cta_commit(XASlot* slot, const XWin& pos, con
     if (flags) atomicOr(&s_flags, flags);
   }
   __syncthreads();
+  int did_atomic = 0;
   if (threadIdx.x < XA_WLIMBS) {
     long long s = 0;
     for (int w = 0; w < nw; ++w) s += wred[w * XA_WLIMBS + threadIdx.x];
     int dig = k0 + threadIdx.x;
     if (s != 0) {
-      if (dig >= 0 && dig < XA_DIGITS) atomicAdd((unsigned long long*)&slot->digit[dig], (unsigned long long)s);
-      else atomicOr(&slot->flags, XA_OVERFLOW);
+      if (dig >= 0 && dig < XA_DIGITS) {
+        atomicAdd((unsigned long long*)&slot->digit[dig], (unsigned long long)s);
+        atomicMax(&slot->lo_inv, XA_DIGITS - dig);
+        atomicMax(&slot->hi_p1, dig + 1);
+      } else {
+        atomicOr(&slot->flags, XA_OVERFLOW);
+      }
+      did_atomic = 1;
     }
   }
   if (any_slow) {
     for (int k = threadIdx.x; k < XA_DIGITS; k += blockDim.x) {
       long long s = sacc[k];
-      if (s != 0) atomicAdd((unsigned long long*)&slot->digit[k], (unsigned long long)s);
+      if (s != 0) {
+        atomicAdd((unsigned long long*)&slot->digit[k], (unsigned long long)s);
+        atomicMax(&slot->lo_inv, XA_DIGITS - k);
+        atomicMax(&slot->hi_p1, k + 1);
+        did_atomic = 1;
+      }
     }
   }
-  if (threadIdx.x == 0 && s_flags) atomicOr(&slot->flags, s_flags);
-  __threadfence();
+  if (threadIdx.x == 0 && s_flags) {
+    atomicOr(&slot->flags, s_flags);
+    did_atomic = 1;
+  }
+  // make this thread's atomics visible before the CTA takes its ticket
+  if (did_atomic) __threadfence();
 }
 
-// Round the normalised superaccumulator to double.  Single thread.
-static __device__ __noinline__ double xa_round(long long* dg, unsigned flags) {
+// Round the superaccumulator to double (round to nearest, ties to even).
+// Only digits [lo, hi] can be non-zero.  Single thread.
+static __device__ __noinline__ double xa_round(const long long* dg, int lo, int hi, unsigned flags) {
   if (flags & XA_NAN) return __longlong_as_double(0x7ff8000000000000ll);
   if ((flags & XA_PINF) && (flags & XA_NINF)) return __longlong_as_double(0x7ff8000000000000ll);
   if (flags & XA_PINF) return __longlong_as_double(0x7ff0000000000000ll);
   if (flags & XA_NINF) return __longlong_as_double((long long)0xfff0000000000000ull);
-  // carry propagation: digits to [0, 2^32), final signed carry
+  if (hi < lo) return 0.0;
+  // normalise digits lo..top into [0, 2^32) with a signed final carry; the
+  // span is widened by three digits so that every carry lands inside it
+  const int top = (hi + 3 < XA_DIGITS) ? hi + 3 : XA_DIGITS - 1;
   uint32_t v[XA_DIGITS];
   long long carry = 0;
-  for (int k = 0; k < XA_DIGITS; ++k) {
-    long long x = dg[k] + carry;   // |dg| < 2^62, |carry| < 2^31: no overflow
+  for (int k = lo; k <= top; ++k) {
+    long long x = (k <= hi ? dg[k] : 0) + carry;   // |dg| < 2^62: no overflow
     v[k] = (uint32_t)x;
-    carry = x >> 32;               // arithmetic shift
+    carry = x >> 32;
   }
   bool neg = carry < 0;
   if (carry != 0 && carry != -1) flags |= XA_OVERFLOW;
-  if (neg) {                        // two's complement negate of the digit array
+  if (neg) {                        // two's complement negate of the span
     uint32_t c = 1;
-    for (int k = 0; k < XA_DIGITS; ++k) {
+    for (int k = lo; k <= top; ++k) {
       uint32_t x = ~v[k] + c;
       c = (c && x == 0u) ? 1u : 0u;
       v[k] = x;
@@ -333,33 +355,28 @@ static __device__ __noinline__ double xa_round(long long* dg, unsigned flags) {
   if (flags & XA_OVERFLOW)
     return __longlong_as_double(neg ? (long long)0xfff0000000000000ull : 0x7ff0000000000000ll);
   int h = -1;
-  for (int k = XA_DIGITS - 1; k >= 0; --k) if (v[k]) { h = k; break; }
+  for (int k = top; k >= lo; --k) if (v[k]) { h = k; break; }
   if (h < 0) return 0.0;
+  auto digit = [&](int k) -> uint64_t { return (k >= lo && k <= top) ? v[k] : 0u; };
   int msb = 32 * h + 31 - __clz(v[h]);          // grid bit index of the leading one
   int E = msb + XA_LSB;                          // value in [2^E, 2^(E+1))
   int lsb = (E >= -1022) ? E - 52 : -1074;       // weight of the double's LSB
   int b0 = lsb - XA_LSB;                         // grid bit index of that LSB (>= 110)
-  // mantissa = bits [b0, msb] (at most 53 bits)
-  auto bit_at = [&](int b) -> uint32_t { return (b < 0 || b >= 32 * XA_DIGITS) ? 0u : (v[b >> 5] >> (b & 31)) & 1u; };
-  uint64_t mant = 0;
+  uint64_t mant;
   {
     int q = b0 >> 5, r = b0 & 31;
-    uint64_t w0 = v[q];
-    uint64_t w1 = (q + 1 < XA_DIGITS) ? v[q + 1] : 0u;
-    uint64_t w2 = (q + 2 < XA_DIGITS) ? v[q + 2] : 0u;
-    // 96 bits starting at digit q; take bits r .. r+52
-    uint64_t lo64 = w0 | (w1 << 32);
-    uint64_t part = (r == 0) ? lo64 : ((lo64 >> r) | (w2 << (64 - r)));
+    uint64_t lo64 = digit(q) | (digit(q + 1) << 32);
+    uint64_t part = (r == 0) ? lo64 : ((lo64 >> r) | (digit(q + 2) << (64 - r)));
     int nb = msb - b0 + 1;
     mant = (nb >= 64) ? part : (part & ((1ull << nb) - 1ull));
   }
-  uint32_t rbit = bit_at(b0 - 1);
+  const int rb = b0 - 1;
+  const uint32_t rbit = (uint32_t)((digit(rb >> 5) >> (rb & 31)) & 1u);
   bool sticky = false;
   {
-    int sb = b0 - 1;                 // bits [0, sb) are sticky
-    int q = sb >> 5, r = sb & 31;
-    for (int k = 0; k < q && !sticky; ++k) sticky = v[k] != 0u;
-    if (!sticky && r) sticky = (v[q] & ((1u << r) - 1u)) != 0u;
+    int q = rb >> 5, r = rb & 31;   // bits [0, rb) are sticky
+    for (int k = lo; k < q && !sticky; ++k) sticky = v[k] != 0u;
+    if (!sticky && r) sticky = (digit(q) & ((1ull << r) - 1ull)) != 0u;
   }
   if (rbit && (sticky || (mant & 1ull))) mant += 1ull;
   uint64_t bits;
@@ -386,13 +403,17 @@ __device__ __forceinline__ bool xa_finish(XASlot* const* slots, int nslots, unsi
   __threadfence();
   if (threadIdx.x < nslots) {
     XASlot* s = slots[threadIdx.x];
+    const int li = *(volatile int*)&s->lo_inv, hp = *(volatile int*)&s->hi_p1;
+    const int lo = li ? XA_DIGITS - li : 0, hi = hp - 1;
     long long dg[XA_DIGITS];
-    for (int k = 0; k < XA_DIGITS; ++k) { dg[k] = *(volatile long long*)&s->digit[k]; }
+    for (int k = lo; k <= hi; ++k) dg[k] = *(volatile long long*)&s->digit[k];
     unsigned fl = *(volatile unsigned*)&s->flags;
-    s->result = xa_round(dg, fl);
+    s->result = xa_round(dg, lo, hi, fl);
     s->result_flags = fl;
-    for (int k = 0; k < XA_DIGITS; ++k) s->digit[k] = 0;
+    for (int k = lo; k <= hi; ++k) s->digit[k] = 0;
     s->flags = 0u;
+    s->lo_inv = 0;
+    s->hi_p1 = 0;
   }
   if (threadIdx.x == 0) slots[0]->ticket = 0u;
   __syncthreads();
