@@ -135,6 +135,12 @@ PFGB_API int pfgb_step(pfgb_handle* handle, double* u, double* v, double* p, lon
 PFGB_API int pfgb_project(pfgb_handle* handle, double* u, double* v, double* p, long ld, double dt,
                           void* stream, pfgb_step_out* out);
 
+/* Run pfgb_step as one CUDA graph (default on) or as individual launches.
+ * The graph is built on the first step and rebuilt when the state arrays
+ * move; the CG loop is a WHILE conditional node, so the device decides when
+ * it stops.  Both modes give identical results.  No reference counterpart. */
+PFGB_API int pfgb_set_graph(pfgb_handle* handle, int on);
+
 /* ---- array operators (device arrays, no synchronisation) --------------- */
 
 /* gradient_coherent, src/pyflow/numerics/core_ops_coherent.py:45-61 */

@@ -109,3 +109,8 @@ extern "C" int pfgb_cg_solve_noalloc(int op, const double* b, double* x, int nx,
   return cg_solve_noalloc_run(op, b, x, nx, ny, dx, dy, precond, jacobi_interior, tol, maxiter, (cudaStream_t)stream,
                               out);
 }
+
+extern "C" int pfgb_set_graph(pfgb_handle* handle, int on) {
+  if (!handle) return set_error(PFGB_EINVAL, "null handle");
+  return instance64_set_graph(handle->inst, on);
+}

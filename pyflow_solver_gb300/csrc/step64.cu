@@ -23,6 +23,7 @@
 #include <string>
 #include <vector>
 
+#include "graph.cuh"
 #include "pfgb_internal.h"
 #include "stencil.cuh"
 #include "step64.cuh"
@@ -31,7 +32,7 @@ namespace pfgb {
 
 constexpr int NT = 256;       // threads per CTA (1-D blocks)
 constexpr int TX = 32;        // tile width (one warp per tile row)
-constexpr int TY = 32;        // tile height of the CG kernels
+constexpr int TY = 16;        // tile height of the CG kernels (2 rows per thread)
 constexpr int RPT = TY / (NT / TX);   // rows per thread in the CG kernels (4)
 constexpr int PB_Y = NT / TX;         // tile height of the per-cell kernels (8)
 
@@ -114,23 +115,23 @@ __global__ void __launch_bounds__(NT) k_prestep(Geo64 G, const double* __restric
 // dt selection, exactly the Python float sequence of solver.py:25-62.
 struct DtArgs {
   double dx, dy, cfl_target, growth, nu;
-  StepIn in;
 };
 
-__global__ void k_dt(DtArgs a, Ctrl64* ctrl) {
+__global__ void k_dt(DtArgs a, const StepIn* __restrict__ in_d, Ctrl64* ctrl) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const StepIn in = *in_d;
   const double umax = ctrl->umax, vmax = ctrl->vmax;
   const double dt_cfl_u = DIV(MUL(a.cfl_target, a.dx), umax);
   const double dt_cfl_v = DIV(MUL(a.cfl_target, a.dy), vmax);
   const double dt_cfl = py_min(dt_cfl_u, dt_cfl_v);
   const double dt_diff = DIV(MUL(0.25, py_min(MUL(a.dx, a.dx), MUL(a.dy, a.dy))), py_max(a.nu, 1e-12));
   const double dt_cand = py_min(dt_cfl, dt_diff);
-  const double lim = MUL(a.in.dt_prev, a.growth);
+  const double lim = MUL(in.dt_prev, a.growth);
   double dt = (dt_cand > lim) ? lim : dt_cand;
   // history: previous entries then the new baseline, keep the last five
   double h[6];
-  int n = a.in.hist_len;
-  for (int k = 0; k < n; ++k) h[k] = a.in.hist[k];
+  int n = in.hist_len;
+  for (int k = 0; k < n; ++k) h[k] = in.hist[k];
   h[n++] = ctrl->div_before;
   int safeguard = 0;
   if (n >= 3) {
@@ -216,7 +217,7 @@ struct CGArgs {
 // ||b||^2; r.(M r).  adjust = 0 (operator interface): b is used as given.
 __global__ void __launch_bounds__(NT) k_cg_init(Geo64 G, CGArgs A, int adjust, double* __restrict__ b,
                                                  double* __restrict__ r, double* __restrict__ x, XASlot* slots,
-                                                 Ctrl64* ctrl) {
+                                                 Ctrl64* ctrl, cudaGraphConditionalHandle cond, int use_cond) {
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
@@ -269,17 +270,22 @@ __global__ void __launch_bounds__(NT) k_cg_init(Geo64 G, CGArgs A, int adjust, d
     } else {
       ctrl->done = 0;
     }
+    if (use_cond) cudaGraphSetConditional(cond, ctrl->done ? 0u : 1u);
   }
 }
 
 // p_new = z + beta*p_old (p_new = z at k = 0); q = A p_new; p_new.q
 // OP 0: A = -lap_c with row 0 = identity (normal projection);
 // OP 1: A = lap_c with identity rows on the boundary ring (manufactured mode).
+// The iteration index k is read from the control block and selects the
+// ping-pong buffers: iteration k reads p[k & 1] and writes p[(k + 1) & 1].
 template <int OP>
-__global__ void __launch_bounds__(NT) k_cg_matvec(Geo64 G, int k, const double* __restrict__ r,
-                                                   const double* __restrict__ pold, double* __restrict__ pnew,
+__global__ void __launch_bounds__(NT) k_cg_matvec(Geo64 G, const double* __restrict__ r, double* p0, double* p1,
                                                    double* __restrict__ q, XASlot* slots, Ctrl64* ctrl) {
   if (*(volatile int*)&ctrl->done) return;
+  const int k = *(volatile int*)&ctrl->iter;
+  const double* __restrict__ pold = (k & 1) ? p1 : p0;
+  double* __restrict__ pnew = (k & 1) ? p0 : p1;
   __shared__ double pn[TY + 2][TX + 2];
   __shared__ double gxs[TY][TX + 1];
   __shared__ double gys[TY + 1][TX];
@@ -350,10 +356,13 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(Geo64 G, int k, const double* 
 }
 
 // x += alpha p; r -= alpha q; r.r; r.(M r)
-__global__ void __launch_bounds__(NT) k_cg_update(Geo64 G, CGArgs A, int k, const double* __restrict__ p,
+__global__ void __launch_bounds__(NT) k_cg_update(Geo64 G, CGArgs A, const double* p0, const double* p1,
                                                    const double* __restrict__ q, double* __restrict__ x,
-                                                   double* __restrict__ r, XASlot* slots, Ctrl64* ctrl) {
+                                                   double* __restrict__ r, XASlot* slots, Ctrl64* ctrl,
+                                                   cudaGraphConditionalHandle cond, int use_cond) {
   if (*(volatile int*)&ctrl->done) return;
+  const int k = *(volatile int*)&ctrl->iter;
+  const double* __restrict__ p = (k & 1) ? p0 : p1;    // the buffer this iteration's matvec wrote
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
@@ -397,6 +406,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(Geo64 G, CGArgs A, int k, cons
       ctrl->done = 1;
       ctrl->info = 0;
     }
+    if (use_cond && ctrl->done) cudaGraphSetConditional(cond, 0u);
   }
 }
 
@@ -569,8 +579,17 @@ struct Instance64 {
   double *us, *vs, *b, *x, *r, *p[2], *q;
   XASlot* slots;
   Ctrl64* ctrl;
+  StepIn* in_d;
+  StepIn* in_h = nullptr;     // pinned staging of the per-step inputs
   StepOut64* out_d;
   StepOut64* out_h = nullptr;
+  // the whole step as one CUDA graph (CG loop = WHILE conditional node)
+  int use_graph = 1;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const double* g_u = nullptr;
+  const double* g_v = nullptr;
+  const double* g_p = nullptr;
   // optional per-launch timing of k_cg_matvec (benchmark roofline)
   int profiling = 0;
   std::vector<cudaEvent_t> ev;
@@ -605,7 +624,7 @@ int instance64_create(const pfgb_params* prm, Instance64** out) {
   I->L.has_lid = prm->has_lid;
   I->L.lid = prm->lid_velocity;
   size_t vec = (size_t)G.ld * G.ny * sizeof(double);
-  size_t bytes = 8 * vec + S_COUNT * sizeof(XASlot) + sizeof(Ctrl64) + sizeof(StepOut64) + 1024;
+  size_t bytes = 8 * vec + S_COUNT * sizeof(XASlot) + sizeof(Ctrl64) + sizeof(StepIn) + sizeof(StepOut64) + 2048;
   if (cudaMalloc(&I->ws, bytes) != cudaSuccess) {
     delete I;
     return set_error(PFGB_ECUDA, "cudaMalloc of the workspace failed");
@@ -627,8 +646,10 @@ int instance64_create(const pfgb_params* prm, Instance64** out) {
   I->q = (double*)take(vec);
   I->slots = (XASlot*)take(S_COUNT * sizeof(XASlot));
   I->ctrl = (Ctrl64*)take(sizeof(Ctrl64));
+  I->in_d = (StepIn*)take(sizeof(StepIn));
   I->out_d = (StepOut64*)take(sizeof(StepOut64));
-  if (cudaMallocHost(&I->out_h, sizeof(StepOut64)) != cudaSuccess) {
+  if (cudaMallocHost(&I->out_h, sizeof(StepOut64)) != cudaSuccess ||
+      cudaMallocHost(&I->in_h, sizeof(StepIn)) != cudaSuccess) {
     cudaFree(I->ws);
     delete I;
     return set_error(PFGB_ECUDA, "cudaMallocHost failed");
@@ -640,14 +661,17 @@ int instance64_create(const pfgb_params* prm, Instance64** out) {
 void instance64_destroy(Instance64* I) {
   if (!I) return;
   for (cudaEvent_t e : I->ev) cudaEventDestroy(e);
+  if (I->exec) cudaGraphExecDestroy(I->exec);
+  if (I->graph) cudaGraphDestroy(I->graph);
   if (I->ws) cudaFree(I->ws);
   if (I->out_h) cudaFreeHost(I->out_h);
+  if (I->in_h) cudaFreeHost(I->in_h);
   delete I;
 }
 
 size_t instance64_workspace_bytes(const Instance64* I) {
   size_t vec = (size_t)I->G.ld * I->G.ny * sizeof(double);
-  return 8 * vec + S_COUNT * sizeof(XASlot) + sizeof(Ctrl64) + sizeof(StepOut64) + 1024;
+  return 8 * vec + S_COUNT * sizeof(XASlot) + sizeof(Ctrl64) + sizeof(StepIn) + sizeof(StepOut64) + 2048;
 }
 
 // Projection stage on u*, v* (pitch usld): RHS, CG, pin, correction, diagnostics.
@@ -656,18 +680,16 @@ static void enqueue_projection(Instance64* I, const Geo64& G, int mode, double* 
   dim3 gp((G.nx + TX - 1) / TX, (G.ny + PB_Y - 1) / PB_Y);
   dim3 gc((G.nx + TX - 1) / TX, (G.ny + TY - 1) / TY);
   k_rhs<<<gp, NT, 0, s>>>(G, us, vs, usld, I->b, I->slots, I->ctrl);
-  k_cg_init<<<gp, NT, 0, s>>>(G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl);
+  k_cg_init<<<gp, NT, 0, s>>>(G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, 0ull, 0);
   for (int k = 0; k < I->A.maxiter; ++k) {
-    const double* pold = I->p[k & 1];
-    double* pnew = I->p[(k + 1) & 1];
     const bool timed = I->profiling && (size_t)(2 * k + 1) < I->ev.size();
     if (timed) cudaEventRecord(I->ev[2 * k], s);
-    k_cg_matvec<0><<<gc, NT, 0, s>>>(G, k, I->r, pold, pnew, I->q, I->slots, I->ctrl);
+    k_cg_matvec<0><<<gc, NT, 0, s>>>(G, I->r, I->p[0], I->p[1], I->q, I->slots, I->ctrl);
     if (timed) {
       cudaEventRecord(I->ev[2 * k + 1], s);
       I->ev_used = k + 1;
     }
-    k_cg_update<<<gc, NT, 0, s>>>(G, I->A, k, pnew, I->q, I->x, I->r, I->slots, I->ctrl);
+    k_cg_update<<<gc, NT, 0, s>>>(G, I->A, I->p[0], I->p[1], I->q, I->x, I->r, I->slots, I->ctrl, 0ull, 0);
   }
   k_post_resid<0><<<gp, NT, 0, s>>>(G, I->b, I->x, I->slots);
   k_pin_correct<<<gp, NT, 0, s>>>(G, I->L, mode, I->x, us, vs, usld, ui, vi, pi, I->slots, I->ctrl);
@@ -683,13 +705,64 @@ int instance64_enqueue(Instance64* I, double* u, double* v, double* p, long lds,
   double* vi = v + lds + 1;
   double* pi = p + lds + 1;
   dim3 gp((G.nx + TX - 1) / TX, (G.ny + PB_Y - 1) / PB_Y);
-  I->D.in = in;
+  *I->in_h = in;
+  cudaMemcpyAsync(I->in_d, I->in_h, sizeof(StepIn), cudaMemcpyHostToDevice, s);
   k_prestep<<<gp, NT, 0, s>>>(G, ui, vi, I->slots, I->ctrl);
-  k_dt<<<1, 32, 0, s>>>(I->D, I->ctrl);
+  k_dt<<<1, 32, 0, s>>>(I->D, I->in_d, I->ctrl);
   k_predict<<<gp, NT, 0, s>>>(G, ui, vi, I->us, I->vs, I->P.scheme, I->ctrl);
   enqueue_projection(I, G, 0, I->us, I->vs, G.ld, ui, vi, pi, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+  return PFGB_OK;
+}
+
+// Build the step graph for the given state arrays.
+static int build_step_graph(Instance64* I, double* ui, double* vi, double* pi) {
+  if (I->exec) {
+    cudaGraphExecDestroy(I->exec);
+    I->exec = nullptr;
+  }
+  if (I->graph) {
+    cudaGraphDestroy(I->graph);
+    I->graph = nullptr;
+  }
+  cudaError_t e = cudaGraphCreate(&I->graph, 0);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("cudaGraphCreate: ") + cudaGetErrorString(e));
+  const Geo64& G = I->G;
+  dim3 gp((G.nx + TX - 1) / TX, (G.ny + PB_Y - 1) / PB_Y);
+  dim3 gc((G.nx + TX - 1) / TX, (G.ny + TY - 1) / TY);
+  GraphChain c(I->graph);
+  c.kernel(k_prestep, gp, dim3(NT), G, (const double*)ui, (const double*)vi, I->slots, I->ctrl);
+  c.kernel(k_dt, dim3(1), dim3(32), I->D, (const StepIn*)I->in_d, I->ctrl);
+  c.kernel(k_predict, gp, dim3(NT), G, (const double*)ui, (const double*)vi, I->us, I->vs, I->P.scheme,
+           (const Ctrl64*)I->ctrl);
+  c.kernel(k_rhs, gp, dim3(NT), G, (const double*)I->us, (const double*)I->vs, G.ld, I->b, I->slots,
+           (const Ctrl64*)I->ctrl);
+  cudaGraphConditionalHandle cond = 0;
+  // the handle is created by while_loop; k_cg_init sets it, so create the loop first on a
+  // detached chain is not possible: create the handle now and pass it to init
+  e = cudaGraphConditionalHandleCreate(&cond, I->graph, 1u, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("conditional handle: ") + cudaGetErrorString(e));
+  c.kernel(k_cg_init, gp, dim3(NT), G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, cond, 1);
+  GraphChain body = c.while_loop_with(cond);
+  body.kernel(k_cg_matvec<0>, gc, dim3(NT), G, (const double*)I->r, I->p[0], I->p[1], I->q, I->slots, I->ctrl);
+  body.kernel(k_cg_update, gc, dim3(NT), G, I->A, (const double*)I->p[0], (const double*)I->p[1],
+              (const double*)I->q, I->x, I->r, I->slots, I->ctrl, cond, 1);
+  c.kernel(k_post_resid<0>, gp, dim3(NT), G, (const double*)I->b, (const double*)I->x, I->slots);
+  c.kernel(k_pin_correct, gp, dim3(NT), G, I->L, 0, (const double*)I->x, I->us, I->vs, G.ld, ui, vi, pi, I->slots,
+           I->ctrl);
+  c.kernel(k_post_diag, gp, dim3(NT), G, (const double*)I->us, (const double*)I->vs, G.ld, (const double*)I->b,
+           (const double*)ui, (const double*)vi, (const double*)pi, I->slots);
+  c.kernel(k_gather, dim3(1), dim3(32), (const XASlot*)I->slots, (const Ctrl64*)I->ctrl, I->out_d);
+  if (c.status() != cudaSuccess || body.status() != cudaSuccess) {
+    cudaError_t be = c.status() != cudaSuccess ? c.status() : body.status();
+    return set_error(PFGB_ECUDA, std::string("building the step graph: ") + cudaGetErrorString(be));
+  }
+  e = cudaGraphInstantiate(&I->exec, I->graph, 0);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  I->g_u = ui;
+  I->g_v = vi;
+  I->g_p = pi;
   return PFGB_OK;
 }
 
@@ -739,9 +812,28 @@ int instance64_project(Instance64* I, double* u, double* v, double* p, long lds,
 
 int instance64_step(Instance64* I, double* u, double* v, double* p, long lds, const StepIn& in, cudaStream_t s,
                     pfgb_step_out* out) {
+  if (I->use_graph && !I->profiling) {
+    if (lds != I->G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
+    double* ui = u + lds + 1;
+    double* vi = v + lds + 1;
+    double* pi = p + lds + 1;
+    if (!I->exec || I->g_u != ui || I->g_v != vi || I->g_p != pi) {
+      if (int rc = build_step_graph(I, ui, vi, pi)) return rc;
+    }
+    *I->in_h = in;
+    cudaError_t e = cudaMemcpyAsync(I->in_d, I->in_h, sizeof(StepIn), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaGraphLaunch(I->exec, s);
+    if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+    return read_out(I, s, out);
+  }
   int rc = instance64_enqueue(I, u, v, p, lds, in, s);
   if (rc) return rc;
   return read_out(I, s, out);
+}
+
+int instance64_set_graph(Instance64* I, int on) {
+  I->use_graph = on ? 1 : 0;
+  return PFGB_OK;
 }
 
 // Per-launch timing of the matvec kernel in the following steps.
@@ -850,15 +942,13 @@ int cg_solve_run(int op, const double* b, double* x, int nx, int ny, double dx, 
   Ctrl64* ctrl = (Ctrl64*)(ws + 4 * vecr + ((S_COUNT * sizeof(XASlot) + 255) / 256 * 256));
   dim3 gp((nx + TX - 1) / TX, (ny + PB_Y - 1) / PB_Y);
   dim3 gc((nx + TX - 1) / TX, (ny + TY - 1) / TY);
-  k_cg_init<<<gp, NT, 0, s>>>(G, A, 0, const_cast<double*>(b), r, x, slots, ctrl);
+  k_cg_init<<<gp, NT, 0, s>>>(G, A, 0, const_cast<double*>(b), r, x, slots, ctrl, 0ull, 0);
   for (int k = 0; k < maxiter; ++k) {
-    double* pold = (k & 1) ? p1 : p0;
-    double* pnew = (k & 1) ? p0 : p1;
     if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
-      k_cg_matvec<0><<<gc, NT, 0, s>>>(G, k, r, pold, pnew, q, slots, ctrl);
+      k_cg_matvec<0><<<gc, NT, 0, s>>>(G, r, p0, p1, q, slots, ctrl);
     else
-      k_cg_matvec<1><<<gc, NT, 0, s>>>(G, k, r, pold, pnew, q, slots, ctrl);
-    k_cg_update<<<gc, NT, 0, s>>>(G, A, k, pnew, q, x, r, slots, ctrl);
+      k_cg_matvec<1><<<gc, NT, 0, s>>>(G, r, p0, p1, q, slots, ctrl);
+    k_cg_update<<<gc, NT, 0, s>>>(G, A, p0, p1, q, x, r, slots, ctrl, 0ull, 0);
   }
   if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
     k_post_resid<0><<<gp, NT, 0, s>>>(G, b, x, slots);
@@ -965,15 +1055,13 @@ int cg_solve_noalloc_run(int op, const double* b, double* x, int nx, int ny, dou
   Ctrl64* ctrl = &S->ctrl;
   dim3 gp((nx + TX - 1) / TX, (ny + PB_Y - 1) / PB_Y);
   dim3 gc((nx + TX - 1) / TX, (ny + TY - 1) / TY);
-  k_cg_init<<<gp, NT, 0, s>>>(G, A, 0, const_cast<double*>(b), S->r, x, slots, ctrl);
+  k_cg_init<<<gp, NT, 0, s>>>(G, A, 0, const_cast<double*>(b), S->r, x, slots, ctrl, 0ull, 0);
   for (int k = 0; k < maxiter; ++k) {
-    double* pold = (k & 1) ? S->p1 : S->p0;
-    double* pnew = (k & 1) ? S->p0 : S->p1;
     if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
-      k_cg_matvec<0><<<gc, NT, 0, s>>>(G, k, S->r, pold, pnew, S->q, slots, ctrl);
+      k_cg_matvec<0><<<gc, NT, 0, s>>>(G, S->r, S->p0, S->p1, S->q, slots, ctrl);
     else
-      k_cg_matvec<1><<<gc, NT, 0, s>>>(G, k, S->r, pold, pnew, S->q, slots, ctrl);
-    k_cg_update<<<gc, NT, 0, s>>>(G, A, k, pnew, S->q, x, S->r, slots, ctrl);
+      k_cg_matvec<1><<<gc, NT, 0, s>>>(G, S->r, S->p0, S->p1, S->q, slots, ctrl);
+    k_cg_update<<<gc, NT, 0, s>>>(G, A, S->p0, S->p1, S->q, x, S->r, slots, ctrl, 0ull, 0);
   }
   if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
     k_post_resid<0><<<gp, NT, 0, s>>>(G, b, x, slots);

@@ -6,6 +6,10 @@ import ctypes
 from .. import _capi
 
 
+# Run each step as one CUDA graph (True) or as individual kernel launches.
+GRAPH_MODE = True
+
+
 class Instance:
     """Owns one ``pfgb_handle`` (device workspace of one cavity)."""
 
@@ -15,6 +19,7 @@ class Instance:
         _capi.check(lib.pfgb_create(ctypes.byref(params), ctypes.byref(h)), "pfgb_create")
         self._h = h
         self.params = params
+        _capi.check(lib.pfgb_set_graph(h, 1 if GRAPH_MODE else 0), "pfgb_set_graph")
 
     @property
     def handle(self):

@@ -53,6 +53,20 @@ def test_p1_cavity64_unit_square_50_steps_bitwise():
     assert all(r["cg_iterations"] == 300 for r in got[1:])   # the reference never converges at maxiter 300
 
 
+def test_direct_launches_equal_graph_replay():
+    """The step as individual launches and as one CUDA graph give the same bits."""
+    from pyflow_solver_gb300.solvers import _handle
+    g = G.load("s16x12_quick")
+    cfg = G.config_of(g)
+    graph = gpu_trajectory(cfg, cfg.nx, cfg.ny, 12)
+    _handle.GRAPH_MODE = False
+    try:
+        direct = gpu_trajectory(cfg, cfg.nx, cfg.ny, 12)
+    finally:
+        _handle.GRAPH_MODE = True
+    check_bitwise(direct, graph, "graph vs direct")
+
+
 def test_p1_cavity64_cli_spacing_bitwise():
     g = G.load("cavity64_cli")
     cfg = G.config_of(g)
