@@ -59,8 +59,16 @@ typedef struct pfgb_params {
   double jacobi_interior;
   int has_lid;               /* lid_velocity is not None */
   double lid_velocity;
-  int precision;             /* 0: binary64 throughout */
-  int reserved[7];
+  int precision;             /* 0: binary64 throughout (the reference's CG); 1: mixed */
+  /* precision 1 only: FP64 iterative refinement of the pressure solve to
+   * ||b - A x|| <= mixed_tol_outer*||b|| (lin_tol when 0) around a binary32
+   * multigrid-preconditioned CG with relative tolerance mixed_tol_inner (1e-5
+   * when 0); at most mixed_max_outer passes (8 when 0) of mixed_max_inner
+   * inner iterations (50 when 0).  nx and ny must halve down to at most 1024
+   * cells on the coarsest multigrid level. */
+  double mixed_tol_outer, mixed_tol_inner;
+  int mixed_max_outer, mixed_max_inner;
+  int reserved[4];
 } pfgb_params;
 
 /* Host-side state.meta carried into a step (solver.py:32,46-50). */

@@ -60,8 +60,49 @@ def _red(red):
     return red if isinstance(red, Reductions) else Reductions(red)
 
 
+def neg_laplacian_matrix(nx, ny, dx, dy):
+    """Sparse -lap_c (Neumann, coherent 5-point): the matrix of the reference's operator rows k != 0."""
+    import scipy.sparse as sp
+    N = nx * ny
+    idx = np.arange(N).reshape(ny, nx)
+    cx, cy = 1.0 / dx**2, 1.0 / dy**2
+    rows, cols, vals = [], [], []
+    diag = np.zeros((ny, nx))
+    for (a, b, c) in ((idx[:, :-1], idx[:, 1:], cx), (idx[:-1, :], idx[1:, :], cy)):
+        a, b = a.ravel(), b.ravel()
+        rows += [a, b]
+        cols += [b, a]
+        vals += [np.full(a.size, -c), np.full(a.size, -c)]
+        np.add.at(diag.reshape(-1), a, c)
+        np.add.at(diag.reshape(-1), b, c)
+    rows.append(idx.ravel())
+    cols.append(idx.ravel())
+    vals.append(diag.reshape(-1))
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(N, N))
+
+
+def converged_pressure(b, nx, ny, dx, dy):
+    """The exact solution of the reference's pinned system A x = b (x[0] = b[0] = 0).
+
+    Rows k != 0 of A restricted to the unknowns k != 0 are SPD; a sparse direct
+    solve gives x to binary64 accuracy.  This is the converged FP64 oracle of the
+    mixed-precision path (the reference's own CG stops at lin_maxiter unconverged).
+    """
+    import scipy.sparse.linalg as spla
+    L = neg_laplacian_matrix(nx, ny, dx, dy).tocsc()
+    x = np.zeros(nx * ny)
+    x[0] = b[0]
+    rhs = b[1:] - L[1:, :1].toarray().ravel() * x[0]
+    x[1:] = spla.spsolve(L[1:, 1:], rhs)
+    return x
+
+
 def solve_pressure_poisson(state, dt, dx, dy, cfg, red="exact", rhs_override=None, extra=None):
-    """Restatement of pressure_solver.py:42-219 (normal and manufactured modes)."""
+    """Restatement of pressure_solver.py:42-219 (normal and manufactured modes).
+
+    ``cfg.oracle_pressure == "converged"`` replaces the CG by the exact solution
+    of the same system (the converged FP64 oracle of the mixed-precision path).
+    """
     red = _red(red)
     ui = interior(state.fields["u"])
     vi = interior(state.fields["v"])
@@ -108,7 +149,11 @@ def solve_pressure_poisson(state, dt, dx, dy, cfg, red="exact", rhs_override=Non
             psolve = lambda r: invd * r  # noqa: E731
         else:
             psolve = lambda r: r  # noqa: E731
-        res = pcg(matvec, psolve, rhs, lin_tol, lin_maxiter, red.dot, red.norm)
+        if getattr(cfg, "oracle_pressure", "cg") == "converged":
+            from .cg import CGResult
+            res = CGResult(converged_pressure(rhs, nx, ny, dx, dy), 0, 0, [])
+        else:
+            res = pcg(matvec, psolve, rhs, lin_tol, lin_maxiter, red.dot, red.norm)
         info, x = res.info, res.x
         r = rhs - matvec(x)
         rnorm = red.norm(r)

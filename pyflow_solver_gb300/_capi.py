@@ -24,7 +24,10 @@ class Params(ctypes.Structure):
         ("scheme", ctypes.c_int), ("enable_jacobi", ctypes.c_int),
         ("jacobi_interior", ctypes.c_double),
         ("has_lid", ctypes.c_int), ("lid_velocity", ctypes.c_double),
-        ("precision", ctypes.c_int), ("reserved", ctypes.c_int * 7),
+        ("precision", ctypes.c_int),
+        ("mixed_tol_outer", ctypes.c_double), ("mixed_tol_inner", ctypes.c_double),
+        ("mixed_max_outer", ctypes.c_int), ("mixed_max_inner", ctypes.c_int),
+        ("reserved", ctypes.c_int * 4),
     ]
 
 

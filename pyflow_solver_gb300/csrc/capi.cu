@@ -40,7 +40,7 @@ extern "C" int pfgb_last_error(char* buf, size_t len) {
 
 extern "C" int pfgb_create(const pfgb_params* params, pfgb_handle** handle) {
   if (!params || !handle) return set_error(PFGB_EINVAL, "null argument");
-  if (params->precision != 0) return set_error(PFGB_EINVAL, "precision mode not supported by this entry point");
+  if (params->precision != 0 && params->precision != 1) return set_error(PFGB_EINVAL, "precision must be 0 or 1");
   if (params->scheme < 0 || params->scheme > 2) return set_error(PFGB_EINVAL, "unknown advection scheme");
   if (params->lin_maxiter < 0) return set_error(PFGB_EINVAL, "lin_maxiter must be >= 0");
   Instance64* inst = nullptr;

@@ -1,0 +1,548 @@
+// Mixed-precision pressure solve: FP64 iterative refinement around an FP32
+// multigrid-preconditioned CG.
+//
+// The reference's system A x = b (A = -lap_c with row 0 replaced by the
+// identity, b mean-free with b[0] = 0; src/pyflow/solvers/pressure_solver.py:97-128)
+// has x[0] = 0, and its rows k != 0 form the SPD matrix -lap_c without row and
+// column 0.  The refinement keeps x and the residual r = b - A x in binary64
+// (the reference stencil, exactly rounded norms); each correction e solves the
+// equivalent singular Neumann system -lap_c e = r~ in binary32, where r~ equals
+// r except r~_0 = -sum_{k != 0} r_k (which makes it consistent), and is shifted
+// by -e[0] so that x[0] stays 0.  The inner solve is CG preconditioned by a
+// geometric multigrid V-cycle: Galerkin coarse operators for piecewise-constant
+// prolongation P and restriction R = P^T (face coefficients double per level),
+// two damped-Jacobi sweeps before and after, one CTA for the coarsest grid.
+// All dot products are exact (binary32 products are exact integers, summed in
+// the same superaccumulator as the binary64 path); alpha and beta are binary64.
+//
+// Both loops are WHILE conditional nodes of the step graph: the inner loop
+// stops at ||r_in|| <= tol_in ||r~|| or max_inner iterations, the outer loop
+// at ||b - A x|| <= tol_out ||b|| or max_outer passes.
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "graph.cuh"
+#include "mixed.cuh"
+#include "pfgb_internal.h"
+#include "stencil.cuh"
+#include "step64.cuh"
+
+namespace pfgb {
+namespace mixed {
+
+constexpr int MT = 256;
+constexpr int BX = 32, BY = 8;
+
+__device__ __forceinline__ float mg_diag(const Lvl& L, int j, int i) {
+  float d = 0.f;
+  if (i > 0) d += L.cx;
+  if (i < L.nx - 1) d += L.cx;
+  if (j > 0) d += L.cy;
+  if (j < L.ny - 1) d += L.cy;
+  return d;
+}
+
+// sum of c * u over the existing neighbours of (j, i), reading u(jj, ii) via `at`
+template <typename F>
+__device__ __forceinline__ float mg_nsum(const Lvl& L, int j, int i, F at) {
+  float s = 0.f;
+  if (i > 0) s = fmaf(L.cx, at(j, i - 1), s);
+  if (i < L.nx - 1) s = fmaf(L.cx, at(j, i + 1), s);
+  if (j > 0) s = fmaf(L.cy, at(j - 1, i), s);
+  if (j < L.ny - 1) s = fmaf(L.cy, at(j + 1, i), s);
+  return s;
+}
+
+// ---- V-cycle kernels -------------------------------------------------------
+
+// two damped-Jacobi sweeps from u = 0: t = S(S(0)) for A u = f
+__global__ void __launch_bounds__(MT) k_mg_pre(Lvl L, float omega) {
+  __shared__ float s1[BY + 2][BX + 2];
+  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+  for (int idx = threadIdx.x; idx < (BY + 2) * (BX + 2); idx += MT) {
+    int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
+    int gj = j0 + jj, gi = i0 + ii;
+    float v = 0.f;
+    if (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx) v = omega * L.f[(long)gj * L.ld + gi] / mg_diag(L, gj, gi);
+    s1[jj + 1][ii + 1] = v;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int gi = i0 + tx, gj = j0 + ty;
+  if (gi < L.nx && gj < L.ny) {
+    auto at = [&](int j, int i) { return s1[j - j0 + 1][i - i0 + 1]; };
+    const float d = mg_diag(L, gj, gi);
+    const float u1 = s1[ty + 1][tx + 1];
+    const float f = L.f[(long)gj * L.ld + gi];
+    const float u2 = (1.f - omega) * u1 + omega * (f + mg_nsum(L, gj, gi, at)) / d;
+    L.t[(long)gj * L.ld + gi] = u2;
+  }
+}
+
+// f_C(J, I) = sum over the 2x2 children of (f - A t) on the fine level
+__global__ void __launch_bounds__(MT) k_mg_restrict(Lvl F, Lvl C) {
+  const int I = blockIdx.x * BX + (threadIdx.x & 31), J = blockIdx.y * BY + (threadIdx.x >> 5);
+  if (I >= C.nx || J >= C.ny) return;
+  auto at = [&](int j, int i) { return F.t[(long)j * F.ld + i]; };
+  float s = 0.f;
+#pragma unroll
+  for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+    for (int di = 0; di < 2; ++di) {
+      const int j = 2 * J + dj, i = 2 * I + di;
+      const float au = mg_diag(F, j, i) * at(j, i) - mg_nsum(F, j, i, at);
+      s += F.f[(long)j * F.ld + i] - au;
+    }
+  C.f[(long)J * C.ld + I] = s;
+}
+
+// u = S(S(t + P u_C))
+__global__ void __launch_bounds__(MT) k_mg_post(Lvl F, Lvl C, float omega) {
+  __shared__ float w0[BY + 4][BX + 4];
+  __shared__ float w1[BY + 2][BX + 2];
+  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+  for (int idx = threadIdx.x; idx < (BY + 4) * (BX + 4); idx += MT) {
+    int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
+    int gj = j0 + jj, gi = i0 + ii;
+    float v = 0.f;
+    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx)
+      v = F.t[(long)gj * F.ld + gi] + C.u[(long)(gj >> 1) * C.ld + (gi >> 1)];
+    w0[jj + 2][ii + 2] = v;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < (BY + 2) * (BX + 2); idx += MT) {
+    int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
+    int gj = j0 + jj, gi = i0 + ii;
+    float v = 0.f;
+    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) {
+      auto at = [&](int j, int i) { return w0[j - j0 + 2][i - i0 + 2]; };
+      const float d = mg_diag(F, gj, gi);
+      v = (1.f - omega) * w0[jj + 2][ii + 2] + omega * (F.f[(long)gj * F.ld + gi] + mg_nsum(F, gj, gi, at)) / d;
+    }
+    w1[jj + 1][ii + 1] = v;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int gi = i0 + tx, gj = j0 + ty;
+  if (gi < F.nx && gj < F.ny) {
+    auto at = [&](int j, int i) { return w1[j - j0 + 1][i - i0 + 1]; };
+    const float d = mg_diag(F, gj, gi);
+    const float v = (1.f - omega) * w1[ty + 1][tx + 1] + omega * (F.f[(long)gj * F.ld + gi] + mg_nsum(F, gj, gi, at)) / d;
+    F.u[(long)gj * F.ld + gi] = v;
+  }
+}
+
+// coarsest grid: `sweeps` damped-Jacobi sweeps from zero in one CTA
+__global__ void __launch_bounds__(1024) k_mg_coarse(Lvl C, int sweeps, float omega) {
+  __shared__ float ua[1024], ub[1024], fs[1024];
+  const int n = C.nx * C.ny;
+  const int c = threadIdx.x;
+  const int j = c / C.nx, i = c % C.nx;
+  const bool in = c < n;
+  float d = 1.f;
+  if (in) {
+    fs[c] = C.f[(long)j * C.ld + i];
+    d = mg_diag(C, j, i);
+    ua[c] = 0.f;
+  }
+  __syncthreads();
+  float* src = ua;
+  float* dst = ub;
+  for (int s = 0; s < sweeps; ++s) {
+    if (in) {
+      auto at = [&](int jj, int ii) { return src[jj * C.nx + ii]; };
+      dst[c] = (1.f - omega) * src[c] + omega * (fs[c] + mg_nsum(C, j, i, at)) / d;
+    }
+    __syncthreads();
+    float* tmp = src;
+    src = dst;
+    dst = tmp;
+  }
+  if (in) C.u[(long)j * C.ld + i] = src[c];
+}
+
+// ---- PCG and refinement kernels -------------------------------------------
+
+__device__ __forceinline__ void mx_reduce(XASlot* slot, const XTerm* t, int nt, unsigned fl, long long* sacc,
+                                          long long* wred, int* ired) {
+  int top = INT_MIN;
+  for (int k = 0; k < nt; ++k) top = max(top, t[k].top);
+  top = xa_block_max(top, ired);
+  XCtx c;
+  c.clear();
+  c.flags = fl;
+  c.k0 = xa_window_digit(top);
+  for (int k = 0; k < nt; ++k) c.add(sacc, t[k]);
+  int anyslow = __syncthreads_or(c.slow);
+  xa_cta_commit(slot, c.pos, c.neg, c.k0, sacc, anyslow, c.flags, wred);
+}
+
+#define MX_SMEM_SLOT(name)                      \
+  __shared__ long long name[XA_DIGITS];         \
+  for (int k_ = threadIdx.x; k_ < XA_DIGITS; k_ += blockDim.x) name[k_] = 0;
+
+// x = 0, r64 = b; ||b||^2 and sum(b)
+__global__ void __launch_bounds__(MT) k_mx_init(Geo G, const double* __restrict__ b, double* __restrict__ x,
+                                                 double* __restrict__ r64, XASlot* slots, MixCtrl* ctrl,
+                                                 cudaGraphConditionalHandle cond_outer) {
+  MX_SMEM_SLOT(sa0);
+  MX_SMEM_SLOT(sa1);
+  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
+  __shared__ int ired[32];
+  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  XTerm t0, t1;
+  xa_zero(t0);
+  xa_zero(t1);
+  unsigned f0 = 0u, f1 = 0u;
+  if (i < G.nx && j < G.ny) {
+    const long o = (long)j * G.ld + i;
+    const double bv = b[o];
+    x[o] = 0.0;
+    r64[o] = bv;
+    xa_term_prod(bv, bv, t0, f0);
+    xa_term_val(bv, t1, f1);
+  }
+  mx_reduce(&slots[M_RR64], &t0, 1, f0, sa0, wred, ired);
+  mx_reduce(&slots[M_SUM64], &t1, 1, f1, sa1, wred, ired);
+  XASlot* sl[2] = {&slots[M_RR64], &slots[M_SUM64]};
+  if (xa_finish(sl, 2, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+    const double bb = slots[M_RR64].result;
+    ctrl->bnorm = __dsqrt_rn(bb);
+    ctrl->tol_abs_out = __dmul_rn(ctrl->tol_out, ctrl->bnorm);
+    ctrl->rr64 = bb;
+    ctrl->sum64 = slots[M_SUM64].result;
+    ctrl->outer = 0;
+    ctrl->inner_total = 0;
+    ctrl->converged = (bb == 0.0) ? 1 : 0;
+    cudaGraphSetConditional(cond_outer, bb == 0.0 ? 0u : 1u);
+  }
+}
+
+// r~ = float(r64) with r~_0 = -sum_{k != 0} r64_k; e = 0; ||r~||^2; starts an inner solve
+__global__ void __launch_bounds__(MT) k_mx_prep(Geo G, Lvl L0, const double* __restrict__ r64, float* __restrict__ e,
+                                                 XASlot* slots, MixCtrl* ctrl, cudaGraphConditionalHandle cond_inner) {
+  MX_SMEM_SLOT(sa0);
+  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
+  __shared__ int ired[32];
+  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  XTerm t0;
+  xa_zero(t0);
+  unsigned f0 = 0u;
+  if (i < G.nx && j < G.ny) {
+    const double rv = (i == 0 && j == 0) ? -__dsub_rn(ctrl->sum64, r64[0]) : r64[(long)j * G.ld + i];
+    const float rf = __double2float_rn(rv);
+    L0.f[(long)j * L0.ld + i] = rf;
+    e[(long)j * L0.ld + i] = 0.f;
+    xa_term_prod_f32(rf, rf, t0, f0);
+  }
+  mx_reduce(&slots[M_RT], &t0, 1, f0, sa0, wred, ired);
+  XASlot* sl[1] = {&slots[M_RT]};
+  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+    const double rt = __dsqrt_rn(slots[M_RT].result);
+    ctrl->rt_norm = rt;
+    ctrl->tol_abs_in = __dmul_rn(ctrl->tol_in, rt);
+    ctrl->inner = 0;
+    cudaGraphSetConditional(cond_inner, rt > 0.0 ? 1u : 0u);
+  }
+}
+
+// rho = r.z (exact); beta = rho / rho_prev after the first inner iteration
+__global__ void __launch_bounds__(MT) k_mx_rz(Lvl L0, const float* __restrict__ z, XASlot* slots, MixCtrl* ctrl) {
+  MX_SMEM_SLOT(sa0);
+  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
+  __shared__ int ired[32];
+  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  XTerm t0;
+  xa_zero(t0);
+  unsigned f0 = 0u;
+  if (i < L0.nx && j < L0.ny) {
+    const long o = (long)j * L0.ld + i;
+    xa_term_prod_f32(L0.f[o], z[o], t0, f0);
+  }
+  mx_reduce(&slots[M_RZ], &t0, 1, f0, sa0, wred, ired);
+  XASlot* sl[1] = {&slots[M_RZ]};
+  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+    const double rz = slots[M_RZ].result;
+    if (ctrl->inner > 0) ctrl->beta = __ddiv_rn(rz, ctrl->rho);
+    ctrl->rho = rz;
+  }
+}
+
+// p_new = z (first) or z + beta p_old; q = A p_new (binary32 Neumann operator); p.q
+__global__ void __launch_bounds__(MT) k_mx_matvec(Lvl L0, const float* __restrict__ z, float* p0, float* p1,
+                                                   float* __restrict__ q, XASlot* slots, MixCtrl* ctrl) {
+  __shared__ float pn[BY + 2][BX + 2];
+  MX_SMEM_SLOT(sa0);
+  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
+  __shared__ int ired[32];
+  const int k = *(volatile int*)&ctrl->inner;
+  const float* __restrict__ pold = (k & 1) ? p1 : p0;
+  float* __restrict__ pnew = (k & 1) ? p0 : p1;
+  const float beta = (float)ctrl->beta;
+  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+  for (int idx = threadIdx.x; idx < (BY + 2) * (BX + 2); idx += MT) {
+    int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
+    int gj = j0 + jj, gi = i0 + ii;
+    float v = 0.f;
+    if (gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx) {
+      const long o = (long)gj * L0.ld + gi;
+      v = (k == 0) ? z[o] : fmaf(beta, pold[o], z[o]);
+    }
+    pn[jj + 1][ii + 1] = v;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int gi = i0 + tx, gj = j0 + ty;
+  XTerm t0;
+  xa_zero(t0);
+  unsigned f0 = 0u;
+  if (gi < L0.nx && gj < L0.ny) {
+    auto at = [&](int j, int i) { return pn[j - j0 + 1][i - i0 + 1]; };
+    const float pv = pn[ty + 1][tx + 1];
+    const float qv = mg_diag(L0, gj, gi) * pv - mg_nsum(L0, gj, gi, at);
+    const long o = (long)gj * L0.ld + gi;
+    pnew[o] = pv;
+    q[o] = qv;
+    xa_term_prod_f32(pv, qv, t0, f0);
+  }
+  mx_reduce(&slots[M_PQ], &t0, 1, f0, sa0, wred, ired);
+  XASlot* sl[1] = {&slots[M_PQ]};
+  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+    const double pq = slots[M_PQ].result;
+    ctrl->pq = pq;
+    ctrl->alpha = __ddiv_rn(ctrl->rho, pq);
+  }
+}
+
+// e += alpha p; r -= alpha q; ||r||^2 and the inner stopping test
+__global__ void __launch_bounds__(MT) k_mx_update(Lvl L0, const float* p0, const float* p1, const float* __restrict__ q,
+                                                   float* __restrict__ e, XASlot* slots, MixCtrl* ctrl,
+                                                   cudaGraphConditionalHandle cond_inner) {
+  MX_SMEM_SLOT(sa0);
+  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
+  __shared__ int ired[32];
+  const int k = *(volatile int*)&ctrl->inner;
+  const float* __restrict__ p = (k & 1) ? p0 : p1;
+  const float alpha = (float)ctrl->alpha;
+  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  XTerm t0;
+  xa_zero(t0);
+  unsigned f0 = 0u;
+  if (i < L0.nx && j < L0.ny) {
+    const long o = (long)j * L0.ld + i;
+    e[o] = fmaf(alpha, p[o], e[o]);
+    const float rv = fmaf(-alpha, q[o], L0.f[o]);
+    L0.f[o] = rv;
+    xa_term_prod_f32(rv, rv, t0, f0);
+  }
+  mx_reduce(&slots[M_RR], &t0, 1, f0, sa0, wred, ired);
+  XASlot* sl[1] = {&slots[M_RR]};
+  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+    const double rr = slots[M_RR].result;
+    const int it = k + 1;
+    ctrl->inner = it;
+    ctrl->inner_total += 1;
+    ctrl->rr_in = rr;
+    if (!(__dsqrt_rn(rr) > ctrl->tol_abs_in) || it >= ctrl->max_inner) cudaGraphSetConditional(cond_inner, 0u);
+  }
+}
+
+// x += e - e[0] (binary64)
+__global__ void __launch_bounds__(MT) k_mx_correct(Geo G, long lde, const float* __restrict__ e, double* __restrict__ x) {
+  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  if (i >= G.nx || j >= G.ny) return;
+  const double e0 = (double)e[0];
+  const long o = (long)j * G.ld + i;
+  x[o] = __dadd_rn(x[o], __dsub_rn((double)e[(long)j * lde + i], e0));
+}
+
+// r64 = b - A x with the reference's pinned operator; ||r64||^2, sum(r64); outer test
+__global__ void __launch_bounds__(MT) k_mx_resid(Geo G, const double* __restrict__ b, const double* __restrict__ x,
+                                                  double* __restrict__ r64, XASlot* slots, MixCtrl* ctrl,
+                                                  cudaGraphConditionalHandle cond_outer) {
+  MX_SMEM_SLOT(sa0);
+  MX_SMEM_SLOT(sa1);
+  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
+  __shared__ int ired[32];
+  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  XTerm t0, t1;
+  xa_zero(t0);
+  xa_zero(t1);
+  unsigned f0 = 0u, f1 = 0u;
+  if (i < G.nx && j < G.ny) {
+    View2<const double> X{x, G.ld};
+    const double ax = (i == 0 && j == 0) ? X(0, 0) : -lap_coherent_at(X, j, i, G.g);
+    const long o = (long)j * G.ld + i;
+    const double rv = __dsub_rn(b[o], ax);
+    r64[o] = rv;
+    xa_term_prod(rv, rv, t0, f0);
+    xa_term_val(rv, t1, f1);
+  }
+  mx_reduce(&slots[M_RR64], &t0, 1, f0, sa0, wred, ired);
+  mx_reduce(&slots[M_SUM64], &t1, 1, f1, sa1, wred, ired);
+  XASlot* sl[2] = {&slots[M_RR64], &slots[M_SUM64]};
+  if (xa_finish(sl, 2, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+    const double rr = slots[M_RR64].result;
+    ctrl->rr64 = rr;
+    ctrl->sum64 = slots[M_SUM64].result;
+    ctrl->outer += 1;
+    const bool conv = !(__dsqrt_rn(rr) > ctrl->tol_abs_out);
+    ctrl->converged = conv ? 1 : 0;
+    if (conv || ctrl->outer >= ctrl->max_outer) cudaGraphSetConditional(cond_outer, 0u);
+  }
+}
+
+// summary of the mixed solve for the step record
+__global__ void k_mx_finish(const MixCtrl* __restrict__ m, Ctrl64* c, int maxiter_report) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  c->iter = m->inner_total;
+  c->info = m->converged ? 0 : maxiter_report;
+  c->zero_rhs = (m->bnorm == 0.0) ? 1 : 0;
+  c->bnrm2 = m->bnorm;
+}
+
+// ---- host side --------------------------------------------------------------
+
+static long round_up(long a, long m) { return (a + m - 1) / m * m; }
+
+int solver_create(int nx, int ny, double dx, double dy, long ld64, double tol_out, double tol_in, int max_outer,
+                  int max_inner, Solver** out) {
+  Solver* S = new Solver();
+  S->G.nx = nx;
+  S->G.ny = ny;
+  S->G.ld = ld64;
+  S->G.g.nx = nx;
+  S->G.g.ny = ny;
+  S->G.g.sx = spacing_for(dx);
+  S->G.g.sy = spacing_for(dy);
+  S->tol_out = tol_out;
+  S->tol_in = tol_in;
+  S->max_outer = max_outer;
+  S->max_inner = max_inner;
+  // levels: halve while both sides are even and the coarse grid keeps >= 8 cells a side
+  int L = 0;
+  int lx = nx, ly = ny;
+  std::vector<std::pair<int, int>> dims;
+  dims.push_back({lx, ly});
+  while (L + 1 < MAX_LEVELS && lx % 2 == 0 && ly % 2 == 0 && lx / 2 >= 8 && ly / 2 >= 8 && (long)lx * ly > 1024) {
+    lx /= 2;
+    ly /= 2;
+    dims.push_back({lx, ly});
+    ++L;
+  }
+  if ((long)lx * ly > 1024) {
+    delete S;
+    return set_error(PFGB_EINVAL, "mixed solver: the coarsest multigrid level would exceed 1024 cells "
+                                  "(nx and ny need enough factors of two)");
+  }
+  S->nlev = L + 1;
+  size_t bytes = 0;
+  std::vector<long> lds(S->nlev);
+  for (int l = 0; l < S->nlev; ++l) {
+    lds[l] = round_up(dims[l].first, 32);
+    bytes += 3 * (size_t)lds[l] * dims[l].second * sizeof(float) + 3 * 256;
+  }
+  const long ld0 = lds[0];
+  const size_t v0 = (size_t)ld0 * ny * sizeof(float);
+  bytes += 4 * (v0 + 256);                                   // e, p0, p1, q
+  bytes += (size_t)ld64 * ny * sizeof(double) + 256;         // r64
+  bytes += M_COUNT * sizeof(XASlot) + sizeof(MixCtrl) + 1024;
+  if (cudaMalloc(&S->ws, bytes) != cudaSuccess) {
+    delete S;
+    return set_error(PFGB_ENOMEM, "cudaMalloc of the mixed-solver workspace failed");
+  }
+  cudaMemset(S->ws, 0, bytes);
+  S->ws_bytes = bytes;
+  char* c = S->ws;
+  auto take = [&](size_t n) { char* r = c; c += (n + 255) / 256 * 256; return r; };
+  const double dx2 = dx * dx, dy2 = dy * dy;
+  float cx = (float)(1.0 / dx2), cy = (float)(1.0 / dy2);
+  for (int l = 0; l < S->nlev; ++l) {
+    Lvl& v = S->lev[l];
+    v.nx = dims[l].first;
+    v.ny = dims[l].second;
+    v.ld = lds[l];
+    v.cx = cx;
+    v.cy = cy;
+    size_t n = (size_t)v.ld * v.ny * sizeof(float);
+    v.u = (float*)take(n);
+    v.t = (float*)take(n);
+    v.f = (float*)take(n);
+    cx *= 2.f;
+    cy *= 2.f;
+  }
+  S->e = (float*)take(v0);
+  S->p0 = (float*)take(v0);
+  S->p1 = (float*)take(v0);
+  S->q = (float*)take(v0);
+  S->r64 = (double*)take((size_t)ld64 * ny * sizeof(double));
+  S->slots = (XASlot*)take(M_COUNT * sizeof(XASlot));
+  S->ctrl = (MixCtrl*)take(sizeof(MixCtrl));
+  MixCtrl hc = {};
+  hc.tol_out = tol_out;
+  hc.tol_in = tol_in;
+  hc.max_outer = max_outer;
+  hc.max_inner = max_inner;
+  cudaMemcpy(S->ctrl, &hc, sizeof(MixCtrl), cudaMemcpyHostToDevice);
+  *out = S;
+  return PFGB_OK;
+}
+
+void solver_destroy(Solver* S) {
+  if (!S) return;
+  if (S->ws) cudaFree(S->ws);
+  delete S;
+}
+
+static void add_vcycle(GraphChain& c, Solver* S, const float omega) {
+  const int L = S->nlev - 1;
+  for (int l = 0; l < L; ++l) {
+    const Lvl& F = S->lev[l];
+    const Lvl& C = S->lev[l + 1];
+    c.kernel(k_mg_pre, dim3((F.nx + BX - 1) / BX, (F.ny + BY - 1) / BY), dim3(MT), F, omega);
+    c.kernel(k_mg_restrict, dim3((C.nx + BX - 1) / BX, (C.ny + BY - 1) / BY), dim3(MT), F, C);
+  }
+  const Lvl& Cc = S->lev[L];
+  c.kernel(k_mg_coarse, dim3(1), dim3(1024), Cc, 4 * (Cc.nx + Cc.ny), omega);
+  for (int l = L - 1; l >= 0; --l) {
+    const Lvl& F = S->lev[l];
+    const Lvl& C = S->lev[l + 1];
+    c.kernel(k_mg_post, dim3((F.nx + BX - 1) / BX, (F.ny + BY - 1) / BY), dim3(MT), F, C, omega);
+  }
+}
+
+// Append the refinement loop (x, given b) to a graph chain.  b and x are the
+// binary64 vectors of the step (pitch ld64).
+int append_solve(GraphChain& c, Solver* S, const double* b, double* x, Ctrl64* ctrl64, int maxiter_report) {
+  const float omega = 0.8f;
+  const Lvl& L0 = S->lev[0];
+  dim3 g64((S->G.nx + BX - 1) / BX, (S->G.ny + BY - 1) / BY);
+  dim3 g0((L0.nx + BX - 1) / BX, (L0.ny + BY - 1) / BY);
+  cudaGraphConditionalHandle cond_outer = 0, cond_inner = 0;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&cond_outer, c.graph(), 1u, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("outer conditional: ") + cudaGetErrorString(e));
+  c.kernel(k_mx_init, g64, dim3(MT), S->G, b, x, S->r64, S->slots, S->ctrl, cond_outer);
+  GraphChain outer = c.while_loop_with(cond_outer);
+  if (outer.status() != cudaSuccess) return set_error(PFGB_ECUDA, "outer loop node");
+  e = cudaGraphConditionalHandleCreate(&cond_inner, outer.graph(), 1u, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("inner conditional: ") + cudaGetErrorString(e));
+  outer.kernel(k_mx_prep, g64, dim3(MT), S->G, L0, (const double*)S->r64, S->e, S->slots, S->ctrl, cond_inner);
+  add_vcycle(outer, S, omega);
+  outer.kernel(k_mx_rz, g0, dim3(MT), L0, (const float*)L0.u, S->slots, S->ctrl);
+  GraphChain inner = outer.while_loop_with(cond_inner);
+  inner.kernel(k_mx_matvec, g0, dim3(MT), L0, (const float*)L0.u, S->p0, S->p1, S->q, S->slots, S->ctrl);
+  inner.kernel(k_mx_update, g0, dim3(MT), L0, (const float*)S->p0, (const float*)S->p1, (const float*)S->q, S->e,
+               S->slots, S->ctrl, cond_inner);
+  add_vcycle(inner, S, omega);
+  inner.kernel(k_mx_rz, g0, dim3(MT), L0, (const float*)L0.u, S->slots, S->ctrl);
+  outer.kernel(k_mx_correct, g64, dim3(MT), S->G, L0.ld, (const float*)S->e, x);
+  outer.kernel(k_mx_resid, g64, dim3(MT), S->G, b, (const double*)x, S->r64, S->slots, S->ctrl, cond_outer);
+  c.kernel(k_mx_finish, dim3(1), dim3(32), (const MixCtrl*)S->ctrl, ctrl64, maxiter_report);
+  cudaError_t st = c.status() != cudaSuccess ? c.status() : (outer.status() != cudaSuccess ? outer.status() : inner.status());
+  if (st != cudaSuccess) return set_error(PFGB_ECUDA, std::string("building the mixed solve: ") + cudaGetErrorString(st));
+  return PFGB_OK;
+}
+
+}  // namespace mixed
+}  // namespace pfgb

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "graph.cuh"
+#include "mixed.cuh"
 #include "pfgb_internal.h"
 #include "stencil.cuh"
 #include "step64.cuh"
@@ -583,6 +584,8 @@ struct Instance64 {
   StepIn* in_h = nullptr;     // pinned staging of the per-step inputs
   StepOut64* out_d;
   StepOut64* out_h = nullptr;
+  // mixed-precision pressure solve (precision 1)
+  mixed::Solver* mix = nullptr;
   // the whole step as one CUDA graph (CG loop = WHILE conditional node)
   int use_graph = 1;
   cudaGraph_t graph = nullptr;
@@ -654,12 +657,24 @@ int instance64_create(const pfgb_params* prm, Instance64** out) {
     delete I;
     return set_error(PFGB_ECUDA, "cudaMallocHost failed");
   }
+  if (prm->precision == 1) {
+    const double tol_out = prm->mixed_tol_outer > 0.0 ? prm->mixed_tol_outer : prm->lin_tol;
+    const double tol_in = prm->mixed_tol_inner > 0.0 ? prm->mixed_tol_inner : 1e-5;
+    const int mo = prm->mixed_max_outer > 0 ? prm->mixed_max_outer : 8;
+    const int mi = prm->mixed_max_inner > 0 ? prm->mixed_max_inner : 50;
+    int rc = mixed::solver_create(prm->nx, prm->ny, prm->dx, prm->dy, G.ld, tol_out, tol_in, mo, mi, &I->mix);
+    if (rc) {
+      instance64_destroy(I);
+      return rc;
+    }
+  }
   *out = I;
   return PFGB_OK;
 }
 
 void instance64_destroy(Instance64* I) {
   if (!I) return;
+  if (I->mix) mixed::solver_destroy(I->mix);
   for (cudaEvent_t e : I->ev) cudaEventDestroy(e);
   if (I->exec) cudaGraphExecDestroy(I->exec);
   if (I->graph) cudaGraphDestroy(I->graph);
@@ -743,18 +758,25 @@ static int build_step_graph(Instance64* I, double* ui, double* vi, double* pi) {
   // detached chain is not possible: create the handle now and pass it to init
   e = cudaGraphConditionalHandleCreate(&cond, I->graph, 1u, cudaGraphCondAssignDefault);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("conditional handle: ") + cudaGetErrorString(e));
-  c.kernel(k_cg_init, gp, dim3(NT), G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, cond, 1);
-  GraphChain body = c.while_loop_with(cond);
-  body.kernel(k_cg_matvec<0>, gc, dim3(NT), G, (const double*)I->r, I->p[0], I->p[1], I->q, I->slots, I->ctrl);
-  body.kernel(k_cg_update, gc, dim3(NT), G, I->A, (const double*)I->p[0], (const double*)I->p[1],
-              (const double*)I->q, I->x, I->r, I->slots, I->ctrl, cond, 1);
+  GraphChain body(nullptr);
+  if (I->mix) {
+    // b is finished (mean removed, b[0] = 0) by the CG init; the refinement solves A x = b
+    c.kernel(k_cg_init, gp, dim3(NT), G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, cond, 0);
+    if (int rc = mixed::append_solve(c, I->mix, I->b, I->x, I->ctrl, I->A.maxiter)) return rc;
+  } else {
+    c.kernel(k_cg_init, gp, dim3(NT), G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, cond, 1);
+    body = c.while_loop_with(cond);
+    body.kernel(k_cg_matvec<0>, gc, dim3(NT), G, (const double*)I->r, I->p[0], I->p[1], I->q, I->slots, I->ctrl);
+    body.kernel(k_cg_update, gc, dim3(NT), G, I->A, (const double*)I->p[0], (const double*)I->p[1],
+                (const double*)I->q, I->x, I->r, I->slots, I->ctrl, cond, 1);
+  }
   c.kernel(k_post_resid<0>, gp, dim3(NT), G, (const double*)I->b, (const double*)I->x, I->slots);
   c.kernel(k_pin_correct, gp, dim3(NT), G, I->L, 0, (const double*)I->x, I->us, I->vs, G.ld, ui, vi, pi, I->slots,
            I->ctrl);
   c.kernel(k_post_diag, gp, dim3(NT), G, (const double*)I->us, (const double*)I->vs, G.ld, (const double*)I->b,
            (const double*)ui, (const double*)vi, (const double*)pi, I->slots);
   c.kernel(k_gather, dim3(1), dim3(32), (const XASlot*)I->slots, (const Ctrl64*)I->ctrl, I->out_d);
-  if (c.status() != cudaSuccess || body.status() != cudaSuccess) {
+  if (c.status() != cudaSuccess || (!I->mix && body.status() != cudaSuccess)) {
     cudaError_t be = c.status() != cudaSuccess ? c.status() : body.status();
     return set_error(PFGB_ECUDA, std::string("building the step graph: ") + cudaGetErrorString(be));
   }
@@ -798,6 +820,7 @@ static int read_out(Instance64* I, cudaStream_t s, pfgb_step_out* out) {
 // Stand-alone projection (solve_pressure_poisson, normal mode) on the state.
 int instance64_project(Instance64* I, double* u, double* v, double* p, long lds, double dt, cudaStream_t s,
                        pfgb_step_out* out) {
+  if (I->mix) return set_error(PFGB_ESTATE, "pfgb_project runs the binary64 path only");
   const Geo64& G = I->G;
   if (lds != G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
   double* ui = u + lds + 1;
@@ -812,6 +835,8 @@ int instance64_project(Instance64* I, double* u, double* v, double* p, long lds,
 
 int instance64_step(Instance64* I, double* u, double* v, double* p, long lds, const StepIn& in, cudaStream_t s,
                     pfgb_step_out* out) {
+  if (I->mix && (!I->use_graph || I->profiling))
+    return set_error(PFGB_ESTATE, "the mixed-precision step runs only as a CUDA graph (no profiling mode)");
   if (I->use_graph && !I->profiling) {
     if (lds != I->G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
     double* ui = u + lds + 1;

@@ -103,6 +103,32 @@ __device__ __forceinline__ void xa_term_prod(double a, double b, XTerm& t, unsig
   t.top = t.e + bl - 1;
 }
 
+// Exact term for the product of two binary32 values (48-bit significand product).
+__device__ __forceinline__ void xa_term_prod_f32(float a, float b, XTerm& t, unsigned& flags) {
+  const uint32_t ba = __float_as_uint(a), bb = __float_as_uint(b);
+  const int efa = (int)((ba >> 23) & 0xff), efb = (int)((bb >> 23) & 0xff);
+  uint32_t ma = ba & 0x7fffffu, mb = bb & 0x7fffffu;
+  const bool sa = (ba >> 31) != 0, sb = (bb >> 31) != 0;
+  xa_zero(t);
+  if (efa == 0xff || efb == 0xff) {
+    if ((efa == 0xff && ma) || (efb == 0xff && mb)) { flags |= XA_NAN; return; }
+    const bool zero_other = (efa == 0xff) ? (efb == 0 && mb == 0) : (efa == 0 && ma == 0);
+    if (zero_other) { flags |= XA_NAN; return; }
+    flags |= (sa != sb) ? XA_NINF : XA_PINF;
+    return;
+  }
+  int ea, eb;
+  if (efa == 0) { ea = 1 - 150; } else { ma |= 0x800000u; ea = efa - 150; }
+  if (efb == 0) { eb = 1 - 150; } else { mb |= 0x800000u; eb = efb - 150; }
+  if (ma == 0u || mb == 0u) return;
+  const uint64_t prod = (uint64_t)ma * (uint64_t)mb;
+  t.m[0] = (uint32_t)prod;
+  t.m[1] = (uint32_t)(prod >> 32);
+  t.e = ea + eb;
+  t.neg = sa != sb;
+  t.top = t.e + xa_bitlen64(prod) - 1;
+}
+
 // Exact term for a single double (used for sums of rounded values).
 __device__ __forceinline__ void xa_term_val(double a, XTerm& t, unsigned& flags) {
   uint64_t ma; int ea; bool sa;

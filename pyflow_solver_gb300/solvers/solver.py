@@ -10,6 +10,11 @@ Jacobi-PCG pressure solve, the pinned correction, the lid and the residual
 reductions -- runs in one enqueued kernel sequence of libpfgb.so; the host
 receives one record of scalars and forms the dicts exactly as the reference.
 
+``config.precision = "mixed"`` selects the mixed-precision form: the pressure
+system is solved to ``||b - A x|| <= lin_tol ||b||`` by binary64 iterative
+refinement around a binary32 multigrid-preconditioned CG (``mixed_tol_inner``,
+``mixed_max_outer``, ``mixed_max_inner``); everything else stays binary64.
+
 Not restated (host side effects outside the array path): the ``print`` output
 of the diagnostic mode is limited to its scalar lines, and JSONL logging /
 emergency checkpoints are left to the caller.
@@ -48,7 +53,15 @@ def step_params(config, nx: int, ny: int):
     lid = getattr(config, "lid_velocity", None)
     P.has_lid = 0 if lid is None else 1
     P.lid_velocity = 0.0 if lid is None else float(lid)
-    P.precision = 0
+    prec = getattr(config, "precision", "fp64")
+    if prec not in ("fp64", "mixed"):
+        raise ValueError(f"precision must be 'fp64' or 'mixed', not {prec!r}")
+    P.precision = 1 if prec == "mixed" else 0
+    if P.precision == 1:
+        P.mixed_tol_outer = float(getattr(config, "mixed_tol_outer", 0.0))
+        P.mixed_tol_inner = float(getattr(config, "mixed_tol_inner", 1e-5))
+        P.mixed_max_outer = int(getattr(config, "mixed_max_outer", 8))
+        P.mixed_max_inner = int(getattr(config, "mixed_max_inner", 50))
     return P, dx, dy, nu
 
 

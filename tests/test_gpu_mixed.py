@@ -1,0 +1,91 @@
+"""Mixed-precision step (P3): binary32 multigrid-PCG inside binary64 refinement.
+
+The reference's own CG stops at lin_maxiter far from the solution of its
+pressure system (relative residual ~0.3 at 512x512 after 300 iterations), so
+the mixed form is checked against the *converged* binary64 solution of the same
+system: the oracle step with the CG replaced by a sparse direct solve.  The
+bar is 1e-6 relative error (max |gpu - oracle| / max |oracle|) in u, v and p,
+step by step from the same state and along short trajectories.
+"""
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+from oracle import step as ost
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+
+
+def cavity(nx, ny, Re, lid, **kw):
+    c = SimpleNamespace(nx=nx, ny=ny, lx=1.0, ly=1.0, Re=Re, lid_velocity=lid, advection_scheme="quick",
+                        cfl_target=0.5, cfl_growth=1.05, lin_tol=1e-8, lin_maxiter=300, diagnostics=False)
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def run_pair(cfg, steps):
+    import torch
+
+    from pyflow_solver_gb300 import ResidualManager, allocate_state, interior_view, step
+    gcfg = SimpleNamespace(**vars(cfg), precision="mixed")
+    ocfg = SimpleNamespace(**vars(cfg), oracle_pressure="converged")
+    st = allocate_state(cfg.nx, cfg.ny)
+    tw = ost.allocate_state(cfg.nx, cfg.ny)
+    tr, otr = ResidualManager(), ost.ResidualManager()
+    worst = {"u": 0.0, "v": 0.0, "p": 0.0}
+    diags = []
+    for it in range(steps):
+        # per-step parity: start the GPU step from the oracle's state
+        for k in "uvp":
+            interior_view(st.fields[k]).copy_(torch.from_numpy(ost.interior(tw.fields[k])))
+        st.meta = {"dt_prev": tw.meta.get("dt_prev", 1e-2), "divergence_history": list(tw.meta.get("divergence_history", []))}
+        _, res, diag = step(gcfg, st, tr, it)
+        _, ores, odiag = ost.step(ocfg, tw, otr, it, red="exact")
+        assert diag["dt"] == odiag["dt"]
+        for k in "uvp":
+            got = interior_view(st.fields[k]).cpu().numpy()
+            ref = ost.interior(tw.fields[k])
+            if np.max(np.abs(ref)) > 0:
+                worst[k] = max(worst[k], rel(got, ref))
+        diags.append(diag)
+    return worst, diags
+
+
+@pytest.mark.parametrize("nx,ny,Re,lid,steps", [(64, 64, 100.0, 1.0, 12), (96, 48, 800.0, 1.5, 6),
+                                               (128, 128, 1000.0, 1.0, 4)])
+def test_mixed_step_matches_converged_fp64(nx, ny, Re, lid, steps):
+    worst, diags = run_pair(cavity(nx, ny, Re, lid), steps)
+    assert max(worst.values()) <= TOL, worst
+    for d in diags[1:]:
+        assert d["Rp_converged"], d
+        assert d["cg_iterations"] > 0
+
+
+@pytest.mark.slow
+def test_mixed_step_512_matches_converged_fp64():
+    worst, diags = run_pair(cavity(512, 512, 1000.0, 1.0), 3)
+    assert max(worst.values()) <= TOL, worst
+
+
+def test_mixed_trajectory_stays_close():
+    """Free-running trajectories (no resynchronisation) of GPU mixed and converged oracle."""
+    from pyflow_solver_gb300 import ResidualManager, SimulationDriver, allocate_state, interior_view
+    cfg = cavity(64, 64, 100.0, 1.0)
+    gcfg = SimpleNamespace(**vars(cfg), precision="mixed")
+    ocfg = SimpleNamespace(**vars(cfg), oracle_pressure="converged")
+    st = allocate_state(64, 64)
+    for _ in SimulationDriver(gcfg, st, ResidualManager()).run(max_steps=20):
+        pass
+    tw = ost.allocate_state(64, 64)
+    for _ in ost.run(ocfg, tw, max_steps=20, red="exact"):
+        pass
+    for k in "uv":
+        assert rel(interior_view(st.fields[k]).cpu().numpy(), ost.interior(tw.fields[k])) <= 1e-5, k
