@@ -754,16 +754,15 @@ static int build_step_graph(Instance64* I, double* ui, double* vi, double* pi) {
   c.kernel(k_rhs, gp, dim3(NT), G, (const double*)I->us, (const double*)I->vs, G.ld, I->b, I->slots,
            (const Ctrl64*)I->ctrl);
   cudaGraphConditionalHandle cond = 0;
-  // the handle is created by while_loop; k_cg_init sets it, so create the loop first on a
-  // detached chain is not possible: create the handle now and pass it to init
-  e = cudaGraphConditionalHandleCreate(&cond, I->graph, 1u, cudaGraphCondAssignDefault);
-  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("conditional handle: ") + cudaGetErrorString(e));
   GraphChain body(nullptr);
   if (I->mix) {
     // b is finished (mean removed, b[0] = 0) by the CG init; the refinement solves A x = b
     c.kernel(k_cg_init, gp, dim3(NT), G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, cond, 0);
     if (int rc = mixed::append_solve(c, I->mix, I->b, I->x, I->ctrl, I->A.maxiter)) return rc;
   } else {
+    // every conditional handle must belong to a conditional node: create it only here
+    e = cudaGraphConditionalHandleCreate(&cond, I->graph, 1u, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("conditional handle: ") + cudaGetErrorString(e));
     c.kernel(k_cg_init, gp, dim3(NT), G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, cond, 1);
     body = c.while_loop_with(cond);
     body.kernel(k_cg_matvec<0>, gc, dim3(NT), G, (const double*)I->r, I->p[0], I->p[1], I->q, I->slots, I->ctrl);
