@@ -46,11 +46,11 @@ MAXITER = 300
 WORKLOAD = "lid-driven cavity 512x512, Re=1000, lid 1.0, unit square, QUICK, CG rtol 1e-8 maxiter 300, Jacobi"
 
 
-def make_cfg():
+def make_cfg(precision="fp64"):
     from types import SimpleNamespace
     return SimpleNamespace(nx=NX, ny=NY, lx=1.0, ly=1.0, Re=RE, lid_velocity=1.0, advection_scheme="quick",
                            cfl_target=0.5, cfl_growth=1.05, lin_tol=1e-8, lin_maxiter=MAXITER,
-                           enable_jacobi_pc=True, diagnostics=False)
+                           enable_jacobi_pc=True, diagnostics=False, precision=precision)
 
 
 def dist_env():
@@ -162,6 +162,8 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-roofline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -181,7 +183,7 @@ def main():
     from pyflow_solver_gb300 import _capi
     lib = _capi.load()
 
-    cfg = make_cfg()
+    cfg = make_cfg(args.precision)
     st = allocate_state(NX, NY)
     tr = ResidualManager()
     stream = torch.cuda.current_stream()
@@ -220,11 +222,11 @@ def main():
     value = cells / (total_ms / 1e3)
 
     # roofline of the dominant kernel: per-launch CUDA-event timing of k_cg_matvec
-    roof = kernel_roofline(lib, st, cfg, it, tr)
+    roof = None if (args.no_roofline or args.precision == "mixed") else kernel_roofline(lib, st, cfg, it, tr)
     it += 1
 
     # end to end through the public API with host buffers
-    e2e = e2e_rate(cfg, args.e2e_steps)
+    e2e = e2e_rate(cfg, args.e2e_steps) if args.e2e_steps > 0 else None
 
     if rank == 0:
         cpu = None

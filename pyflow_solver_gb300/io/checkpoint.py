@@ -45,7 +45,8 @@ def _meta(state, iteration, sim_time, cfg, arrays, structured=True):
         "config_hash": _hash_config(cfg),
     }
     if structured:
-        m["structured_config_hash"] = getattr(cfg, "config_hash", None) if not callable(getattr(cfg, "config_hash", None)) else None
+        h = getattr(cfg, "config_hash", None)
+        m["structured_config_hash"] = h if isinstance(h, str) else None
     m.update({"field_hashes": {k: _hash_array(v) for k, v in arrays.items()},
               "seed": getattr(cfg, "seed", None), "schema_version": 1})
     return m
