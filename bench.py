@@ -164,6 +164,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-roofline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true", help="individual launches instead of one graph per step")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -181,6 +182,8 @@ def main():
 
     from pyflow_solver_gb300 import ResidualManager, allocate_state, step
     from pyflow_solver_gb300 import _capi
+    from pyflow_solver_gb300.solvers import _handle
+    _handle.GRAPH_MODE = not args.no_graph
     lib = _capi.load()
 
     cfg = make_cfg(args.precision)
@@ -195,6 +198,7 @@ def main():
     # timed steps: events around each step, L2 flushed in between (outside the intervals)
     step_ms = []
     cg_iters = []
+    passes = []
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -209,6 +213,7 @@ def main():
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
             cg_iters.append(diag["cg_iterations"])
+            passes.append(diag.get("refine_passes"))
             it += 1
         torch.cuda.synchronize()
     if dist is not None:
@@ -245,7 +250,7 @@ def main():
                        "precision": "binary64 plain path (exactly rounded reductions)",
                        "l2": "flushed between timed steps (256 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "cg_iterations_per_step": cg_iters},
+                       "cg_iterations_per_step": cg_iters, "refine_passes_per_step": passes},
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,

@@ -97,7 +97,7 @@ typedef struct pfgb_step_out {
   double linres_sq;          /* ||A p - b||^2 */
   double cont_sq;            /* ||div_central(u,v;1,1)||^2 after the step */
   unsigned reduction_flags;  /* bit 3: a term fell below 2^-1184, bit 4: overflow */
-  unsigned pad;
+  int refine_passes;         /* precision 1: FP64 refinement passes of the pressure solve */
 } pfgb_step_out;
 
 typedef struct pfgb_solve_out {

@@ -48,7 +48,7 @@ class StepOut(ctypes.Structure):
         ("res_sq", ctypes.c_double), ("ru_sq", ctypes.c_double), ("rv_sq", ctypes.c_double),
         ("divafter_sq", ctypes.c_double), ("linres_sq", ctypes.c_double),
         ("cont_sq", ctypes.c_double),
-        ("reduction_flags", ctypes.c_uint), ("pad", ctypes.c_uint),
+        ("reduction_flags", ctypes.c_uint), ("refine_passes", ctypes.c_int),
     ]
 
 

@@ -27,6 +27,16 @@ class GraphChain {
     add_kernel(reinterpret_cast<void*>(f), grid, block, vals, std::index_sequence_for<P...>{});
   }
 
+  // Same, with dynamic shared memory.
+  template <typename... P, typename... A>
+  void kernel_smem(void (*f)(P...), dim3 grid, dim3 block, size_t smem, A&&... args) {
+    if (err_ != cudaSuccess) return;
+    std::tuple<P...> vals(std::forward<A>(args)...);
+    smem_ = smem;
+    add_kernel(reinterpret_cast<void*>(f), grid, block, vals, std::index_sequence_for<P...>{});
+    smem_ = 0;
+  }
+
   // Append a WHILE node on an existing conditional handle (created on this
   // graph with cudaGraphConditionalHandleCreate; kernels upstream of the node
   // or in its body set it with cudaGraphSetConditional).  The body runs while
@@ -56,7 +66,7 @@ class GraphChain {
     kp.func = f;
     kp.gridDim = grid;
     kp.blockDim = block;
-    kp.sharedMemBytes = 0;
+    kp.sharedMemBytes = (unsigned)smem_;
     kp.kernelParams = argp;
     kp.extra = nullptr;
     cudaGraphNode_t node;
@@ -71,6 +81,7 @@ class GraphChain {
   cudaGraphNode_t last_ = nullptr;
   bool has_last_ = false;
   cudaError_t err_ = cudaSuccess;
+  size_t smem_ = 0;
 };
 
 }  // namespace pfgb

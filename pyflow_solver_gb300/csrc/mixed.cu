@@ -162,6 +162,159 @@ __global__ void __launch_bounds__(1024) k_mg_coarse(Lvl C, int sweeps, float ome
   if (in) C.u[(long)j * C.ld + i] = src[c];
 }
 
+// Levels of at most 64 x 64 cells run inside one CTA: all of them live in
+// shared memory and two V-cycles (the same smoother, restriction and
+// prolongation as the global levels, Jacobi sweeps on the bottom level) form
+// the coarse "solve" -- a fixed linear, symmetric operator, as PCG requires.
+constexpr int CT = 1024;                     // threads of the coarse CTA
+constexpr int CMAX = 4096;                   // cells of its finest level
+
+struct CLvl {                                // a shared-memory level
+  int nx, ny, off;                           // off: offset into the level arrays
+  float cx, cy;
+};
+
+__device__ __forceinline__ float c_diag(const CLvl& L, int j, int i) {
+  float d = 0.f;
+  if (i > 0) d += L.cx;
+  if (i < L.nx - 1) d += L.cx;
+  if (j > 0) d += L.cy;
+  if (j < L.ny - 1) d += L.cy;
+  return d;
+}
+
+__device__ __forceinline__ float c_nsum(const CLvl& L, const float* a, int j, int i) {
+  const float* b = a + L.off;
+  float s = 0.f;
+  if (i > 0) s = fmaf(L.cx, b[j * L.nx + i - 1], s);
+  if (i < L.nx - 1) s = fmaf(L.cx, b[j * L.nx + i + 1], s);
+  if (j > 0) s = fmaf(L.cy, b[(j - 1) * L.nx + i], s);
+  if (j < L.ny - 1) s = fmaf(L.cy, b[(j + 1) * L.nx + i], s);
+  return s;
+}
+
+// one damped-Jacobi sweep src -> dst on level L (all threads; ends with a barrier)
+__device__ __forceinline__ void c_sweep(const CLvl& L, const float* f, const float* src, float* dst, float omega) {
+  const int n = L.nx * L.ny;
+  for (int c = threadIdx.x; c < n; c += CT) {
+    const int j = c / L.nx, i = c - j * L.nx;
+    dst[L.off + c] = (1.f - omega) * src[L.off + c] + omega * (f[L.off + c] + c_nsum(L, src, j, i)) / c_diag(L, j, i);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(CT) k_mg_coarse_cycles(Lvl C, int nl, int cycles, int bottom_sweeps, float omega) {
+  extern __shared__ float sm[];
+  // level table (nl <= 8), arrays f, u, t of total `tot` cells each
+  CLvl L[8];
+  int tot = 0;
+  {
+    int nx = C.nx, ny = C.ny;
+    float cx = C.cx, cy = C.cy;
+    for (int l = 0; l < nl; ++l) {
+      L[l].nx = nx;
+      L[l].ny = ny;
+      L[l].off = tot;
+      L[l].cx = cx;
+      L[l].cy = cy;
+      tot += nx * ny;
+      nx /= 2;
+      ny /= 2;
+      cx *= 2.f;
+      cy *= 2.f;
+    }
+  }
+  float* f = sm;
+  float* u = sm + tot;
+  float* t = sm + 2 * tot;
+  const int n0 = C.nx * C.ny;
+  for (int c = threadIdx.x; c < n0; c += CT) {
+    const int j = c / C.nx, i = c - j * C.nx;
+    f[c] = C.f[(long)j * C.ld + i];
+    u[c] = 0.f;
+  }
+  __syncthreads();
+  // x_{k+1} = x_k + V(f - A x_k): the first cycle starts from zero
+  for (int cyc = 0; cyc < cycles; ++cyc) {
+    // residual of the current iterate on level 0 goes into t[level 0]
+    {
+      const CLvl& L0 = L[0];
+      for (int c = threadIdx.x; c < n0; c += CT) {
+        const int j = c / L0.nx, i = c - j * L0.nx;
+        t[c] = f[c] - (c_diag(L0, j, i) * u[c] - c_nsum(L0, u, j, i));
+      }
+      __syncthreads();
+    }
+    // V-cycle on the correction, with right-hand side t[level 0]; the level
+    // RHS array of the cycle is `f` for coarser levels and t for level 0, so
+    // copy the level-0 residual into a scratch slot: reuse f of level 0 after
+    // saving it in u?  Keep it simple: the cycle works on arrays rh (RHS),
+    // e (correction) and w (work) laid over t, and over u's coarse slots.
+    float* rh = t;     // level 0 RHS = residual; coarser RHS written below
+    // the correction of every level lives in the spare shared arrays after tot*3
+    float* e = sm + 3 * tot;
+    float* w = sm + 4 * tot;
+    for (int l = 0; l < nl; ++l) {
+      const CLvl& Lv = L[l];
+      const int n = Lv.nx * Lv.ny;
+      if (l == nl - 1) {
+        for (int c = threadIdx.x; c < n; c += CT) e[Lv.off + c] = 0.f;
+        __syncthreads();
+        for (int s = 0; s < bottom_sweeps; ++s) {
+          c_sweep(Lv, rh, (s & 1) ? w : e, (s & 1) ? e : w, omega);
+        }
+        if (bottom_sweeps & 1) {
+          for (int c = threadIdx.x; c < n; c += CT) e[Lv.off + c] = w[Lv.off + c];
+          __syncthreads();
+        }
+        break;
+      }
+      // two sweeps from zero: e = S(S(0))
+      for (int c = threadIdx.x; c < n; c += CT) {
+        const int j = c / Lv.nx, i = c - j * Lv.nx;
+        w[Lv.off + c] = omega * rh[Lv.off + c] / c_diag(Lv, j, i);
+      }
+      __syncthreads();
+      c_sweep(Lv, rh, w, e, omega);
+      // restrict the residual rh - A e into the next level's rh
+      const CLvl& Cv = L[l + 1];
+      const int nc = Cv.nx * Cv.ny;
+      for (int c = threadIdx.x; c < nc; c += CT) {
+        const int J = c / Cv.nx, I = c - J * Cv.nx;
+        float sres = 0.f;
+        for (int dj = 0; dj < 2; ++dj)
+          for (int di = 0; di < 2; ++di) {
+            const int j = 2 * J + dj, i = 2 * I + di;
+            const int fc = j * Lv.nx + i;
+            sres += rh[Lv.off + fc] - (c_diag(Lv, j, i) * e[Lv.off + fc] - c_nsum(Lv, e, j, i));
+          }
+        rh[Cv.off + c] = sres;
+      }
+      __syncthreads();
+    }
+    for (int l = nl - 2; l >= 0; --l) {
+      const CLvl& Lv = L[l];
+      const CLvl& Cv = L[l + 1];
+      const int n = Lv.nx * Lv.ny;
+      for (int c = threadIdx.x; c < n; c += CT) {
+        const int j = c / Lv.nx, i = c - j * Lv.nx;
+        w[Lv.off + c] = e[Lv.off + c] + e[Cv.off + (j >> 1) * Cv.nx + (i >> 1)];
+      }
+      __syncthreads();
+      c_sweep(Lv, rh, w, e, omega);
+      c_sweep(Lv, rh, e, w, omega);
+      for (int c = threadIdx.x; c < n; c += CT) e[Lv.off + c] = w[Lv.off + c];
+      __syncthreads();
+    }
+    for (int c = threadIdx.x; c < n0; c += CT) u[c] += e[c];
+    __syncthreads();
+  }
+  for (int c = threadIdx.x; c < n0; c += CT) {
+    const int j = c / C.nx, i = c - j * C.nx;
+    C.u[(long)j * C.ld + i] = u[c];
+  }
+}
+
 // ---- PCG and refinement kernels -------------------------------------------
 
 __device__ __forceinline__ void mx_reduce(XASlot* slot, const XTerm* t, int nt, unsigned fl, long long* sacc,
@@ -185,7 +338,7 @@ __device__ __forceinline__ void mx_reduce(XASlot* slot, const XTerm* t, int nt, 
 // x = 0, r64 = b; ||b||^2 and sum(b)
 __global__ void __launch_bounds__(MT) k_mx_init(Geo G, const double* __restrict__ b, double* __restrict__ x,
                                                  double* __restrict__ r64, XASlot* slots, MixCtrl* ctrl,
-                                                 cudaGraphConditionalHandle cond_outer) {
+                                                 cudaGraphConditionalHandle cond_outer, int use_cond) {
   MX_SMEM_SLOT(sa0);
   MX_SMEM_SLOT(sa1);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
@@ -215,13 +368,15 @@ __global__ void __launch_bounds__(MT) k_mx_init(Geo G, const double* __restrict_
     ctrl->outer = 0;
     ctrl->inner_total = 0;
     ctrl->converged = (bb == 0.0) ? 1 : 0;
-    cudaGraphSetConditional(cond_outer, bb == 0.0 ? 0u : 1u);
+    ctrl->outer_done = (bb == 0.0) ? 1 : 0;
+    if (use_cond) cudaGraphSetConditional(cond_outer, bb == 0.0 ? 0u : 1u);
   }
 }
 
 // r~ = float(r64) with r~_0 = -sum_{k != 0} r64_k; e = 0; ||r~||^2; starts an inner solve
 __global__ void __launch_bounds__(MT) k_mx_prep(Geo G, Lvl L0, const double* __restrict__ r64, float* __restrict__ e,
-                                                 XASlot* slots, MixCtrl* ctrl, cudaGraphConditionalHandle cond_inner) {
+                                                 XASlot* slots, MixCtrl* ctrl, cudaGraphConditionalHandle cond_inner,
+                                                 int use_cond) {
   MX_SMEM_SLOT(sa0);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
@@ -243,7 +398,8 @@ __global__ void __launch_bounds__(MT) k_mx_prep(Geo G, Lvl L0, const double* __r
     ctrl->rt_norm = rt;
     ctrl->tol_abs_in = __dmul_rn(ctrl->tol_in, rt);
     ctrl->inner = 0;
-    cudaGraphSetConditional(cond_inner, rt > 0.0 ? 1u : 0u);
+    ctrl->inner_done = rt > 0.0 ? 0 : 1;
+    if (use_cond) cudaGraphSetConditional(cond_inner, rt > 0.0 ? 1u : 0u);
   }
 }
 
@@ -318,7 +474,7 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(Lvl L0, const float* __restric
 // e += alpha p; r -= alpha q; ||r||^2 and the inner stopping test
 __global__ void __launch_bounds__(MT) k_mx_update(Lvl L0, const float* p0, const float* p1, const float* __restrict__ q,
                                                    float* __restrict__ e, XASlot* slots, MixCtrl* ctrl,
-                                                   cudaGraphConditionalHandle cond_inner) {
+                                                   cudaGraphConditionalHandle cond_inner, int use_cond) {
   MX_SMEM_SLOT(sa0);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
@@ -344,7 +500,10 @@ __global__ void __launch_bounds__(MT) k_mx_update(Lvl L0, const float* p0, const
     ctrl->inner = it;
     ctrl->inner_total += 1;
     ctrl->rr_in = rr;
-    if (!(__dsqrt_rn(rr) > ctrl->tol_abs_in) || it >= ctrl->max_inner) cudaGraphSetConditional(cond_inner, 0u);
+    if (!(__dsqrt_rn(rr) > ctrl->tol_abs_in) || it >= ctrl->max_inner) {
+      ctrl->inner_done = 1;
+      if (use_cond) cudaGraphSetConditional(cond_inner, 0u);
+    }
   }
 }
 
@@ -360,7 +519,7 @@ __global__ void __launch_bounds__(MT) k_mx_correct(Geo G, long lde, const float*
 // r64 = b - A x with the reference's pinned operator; ||r64||^2, sum(r64); outer test
 __global__ void __launch_bounds__(MT) k_mx_resid(Geo G, const double* __restrict__ b, const double* __restrict__ x,
                                                   double* __restrict__ r64, XASlot* slots, MixCtrl* ctrl,
-                                                  cudaGraphConditionalHandle cond_outer) {
+                                                  cudaGraphConditionalHandle cond_outer, int use_cond) {
   MX_SMEM_SLOT(sa0);
   MX_SMEM_SLOT(sa1);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
@@ -389,7 +548,10 @@ __global__ void __launch_bounds__(MT) k_mx_resid(Geo G, const double* __restrict
     ctrl->outer += 1;
     const bool conv = !(__dsqrt_rn(rr) > ctrl->tol_abs_out);
     ctrl->converged = conv ? 1 : 0;
-    if (conv || ctrl->outer >= ctrl->max_outer) cudaGraphSetConditional(cond_outer, 0u);
+    if (conv || ctrl->outer >= ctrl->max_outer) {
+      ctrl->outer_done = 1;
+      if (use_cond) cudaGraphSetConditional(cond_outer, 0u);
+    }
   }
 }
 
@@ -397,6 +559,7 @@ __global__ void __launch_bounds__(MT) k_mx_resid(Geo G, const double* __restrict
 __global__ void k_mx_finish(const MixCtrl* __restrict__ m, Ctrl64* c, int maxiter_report) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   c->iter = m->inner_total;
+  c->refine_passes = m->outer;
   c->info = m->converged ? 0 : maxiter_report;
   c->zero_rhs = (m->bnorm == 0.0) ? 1 : 0;
   c->bnrm2 = m->bnorm;
@@ -425,16 +588,35 @@ int solver_create(int nx, int ny, double dx, double dy, long ld64, double tol_ou
   int lx = nx, ly = ny;
   std::vector<std::pair<int, int>> dims;
   dims.push_back({lx, ly});
-  while (L + 1 < MAX_LEVELS && lx % 2 == 0 && ly % 2 == 0 && lx / 2 >= 8 && ly / 2 >= 8 && (long)lx * ly > 1024) {
+  while (L + 1 < MAX_LEVELS && lx % 2 == 0 && ly % 2 == 0 && lx / 2 >= 8 && ly / 2 >= 8 && (long)lx * ly > CMAX) {
     lx /= 2;
     ly /= 2;
     dims.push_back({lx, ly});
     ++L;
   }
-  if ((long)lx * ly > 1024) {
+  if ((long)lx * ly > CMAX) {
     delete S;
-    return set_error(PFGB_EINVAL, "mixed solver: the coarsest multigrid level would exceed 1024 cells "
+    return set_error(PFGB_EINVAL, "mixed solver: the coarse multigrid level would exceed 4096 cells "
                                   "(nx and ny need enough factors of two)");
+  }
+  // levels resolved inside the coarse CTA: halve while even and at least 2 a side
+  {
+    int cn = 1, cx = lx, cy = ly;
+    while (cn < 8 && cx % 2 == 0 && cy % 2 == 0 && cx / 2 >= 2 && cy / 2 >= 2) {
+      cx /= 2;
+      cy /= 2;
+      ++cn;
+    }
+    S->coarse_levels = cn;
+    int tot = 0;
+    int ax = lx, ay = ly;
+    for (int l = 0; l < cn; ++l) {
+      tot += ax * ay;
+      ax /= 2;
+      ay /= 2;
+    }
+    S->coarse_smem = (size_t)5 * tot * sizeof(float);
+    cudaFuncSetAttribute(k_mg_coarse_cycles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->coarse_smem);
   }
   S->nlev = L + 1;
   size_t bytes = 0;
@@ -504,7 +686,7 @@ static void add_vcycle(GraphChain& c, Solver* S, const float omega) {
     c.kernel(k_mg_restrict, dim3((C.nx + BX - 1) / BX, (C.ny + BY - 1) / BY), dim3(MT), F, C);
   }
   const Lvl& Cc = S->lev[L];
-  c.kernel(k_mg_coarse, dim3(1), dim3(1024), Cc, 4 * (Cc.nx + Cc.ny), omega);
+  c.kernel_smem(k_mg_coarse_cycles, dim3(1), dim3(CT), S->coarse_smem, Cc, S->coarse_levels, 2, 32, omega);
   for (int l = L - 1; l >= 0; --l) {
     const Lvl& F = S->lev[l];
     const Lvl& C = S->lev[l + 1];
@@ -522,25 +704,78 @@ int append_solve(GraphChain& c, Solver* S, const double* b, double* x, Ctrl64* c
   cudaGraphConditionalHandle cond_outer = 0, cond_inner = 0;
   cudaError_t e = cudaGraphConditionalHandleCreate(&cond_outer, c.graph(), 1u, cudaGraphCondAssignDefault);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("outer conditional: ") + cudaGetErrorString(e));
-  c.kernel(k_mx_init, g64, dim3(MT), S->G, b, x, S->r64, S->slots, S->ctrl, cond_outer);
+  c.kernel(k_mx_init, g64, dim3(MT), S->G, b, x, S->r64, S->slots, S->ctrl, cond_outer, 1);
   GraphChain outer = c.while_loop_with(cond_outer);
   if (outer.status() != cudaSuccess) return set_error(PFGB_ECUDA, "outer loop node");
   e = cudaGraphConditionalHandleCreate(&cond_inner, outer.graph(), 1u, cudaGraphCondAssignDefault);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("inner conditional: ") + cudaGetErrorString(e));
-  outer.kernel(k_mx_prep, g64, dim3(MT), S->G, L0, (const double*)S->r64, S->e, S->slots, S->ctrl, cond_inner);
+  outer.kernel(k_mx_prep, g64, dim3(MT), S->G, L0, (const double*)S->r64, S->e, S->slots, S->ctrl, cond_inner, 1);
   add_vcycle(outer, S, omega);
   outer.kernel(k_mx_rz, g0, dim3(MT), L0, (const float*)L0.u, S->slots, S->ctrl);
   GraphChain inner = outer.while_loop_with(cond_inner);
   inner.kernel(k_mx_matvec, g0, dim3(MT), L0, (const float*)L0.u, S->p0, S->p1, S->q, S->slots, S->ctrl);
   inner.kernel(k_mx_update, g0, dim3(MT), L0, (const float*)S->p0, (const float*)S->p1, (const float*)S->q, S->e,
-               S->slots, S->ctrl, cond_inner);
+               S->slots, S->ctrl, cond_inner, 1);
   add_vcycle(inner, S, omega);
   inner.kernel(k_mx_rz, g0, dim3(MT), L0, (const float*)L0.u, S->slots, S->ctrl);
   outer.kernel(k_mx_correct, g64, dim3(MT), S->G, L0.ld, (const float*)S->e, x);
-  outer.kernel(k_mx_resid, g64, dim3(MT), S->G, b, (const double*)x, S->r64, S->slots, S->ctrl, cond_outer);
+  outer.kernel(k_mx_resid, g64, dim3(MT), S->G, b, (const double*)x, S->r64, S->slots, S->ctrl, cond_outer, 1);
   c.kernel(k_mx_finish, dim3(1), dim3(32), (const MixCtrl*)S->ctrl, ctrl64, maxiter_report);
   cudaError_t st = c.status() != cudaSuccess ? c.status() : (outer.status() != cudaSuccess ? outer.status() : inner.status());
   if (st != cudaSuccess) return set_error(PFGB_ECUDA, std::string("building the mixed solve: ") + cudaGetErrorString(st));
+  return PFGB_OK;
+}
+
+// Host-driven form of append_solve with direct launches: the loop decisions
+// are read back from the control block after each stopping test.  Used for
+// profiling (ncu does not profile kernels of graphs with conditional nodes).
+static void launch_vcycle(Solver* S, float omega, cudaStream_t s) {
+  const int L = S->nlev - 1;
+  for (int l = 0; l < L; ++l) {
+    const Lvl& F = S->lev[l];
+    const Lvl& C = S->lev[l + 1];
+    k_mg_pre<<<dim3((F.nx + BX - 1) / BX, (F.ny + BY - 1) / BY), MT, 0, s>>>(F, omega);
+    k_mg_restrict<<<dim3((C.nx + BX - 1) / BX, (C.ny + BY - 1) / BY), MT, 0, s>>>(F, C);
+  }
+  k_mg_coarse_cycles<<<1, CT, S->coarse_smem, s>>>(S->lev[L], S->coarse_levels, 2, 32, omega);
+  for (int l = L - 1; l >= 0; --l) {
+    const Lvl& F = S->lev[l];
+    const Lvl& C = S->lev[l + 1];
+    k_mg_post<<<dim3((F.nx + BX - 1) / BX, (F.ny + BY - 1) / BY), MT, 0, s>>>(F, C, omega);
+  }
+}
+
+int run_direct(Solver* S, const double* b, double* x, Ctrl64* ctrl64, int maxiter_report, cudaStream_t s) {
+  const float omega = 0.8f;
+  const Lvl& L0 = S->lev[0];
+  dim3 g64((S->G.nx + BX - 1) / BX, (S->G.ny + BY - 1) / BY);
+  dim3 g0((L0.nx + BX - 1) / BX, (L0.ny + BY - 1) / BY);
+  MixCtrl h;
+  auto read = [&]() -> bool {
+    return cudaMemcpyAsync(&h, S->ctrl, sizeof(MixCtrl), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+           cudaStreamSynchronize(s) == cudaSuccess;
+  };
+  k_mx_init<<<g64, MT, 0, s>>>(S->G, b, x, S->r64, S->slots, S->ctrl, 0ull, 0);
+  if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
+  while (!h.outer_done) {
+    k_mx_prep<<<g64, MT, 0, s>>>(S->G, L0, S->r64, S->e, S->slots, S->ctrl, 0ull, 0);
+    launch_vcycle(S, omega, s);
+    k_mx_rz<<<g0, MT, 0, s>>>(L0, L0.u, S->slots, S->ctrl);
+    if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
+    while (!h.inner_done) {
+      k_mx_matvec<<<g0, MT, 0, s>>>(L0, L0.u, S->p0, S->p1, S->q, S->slots, S->ctrl);
+      k_mx_update<<<g0, MT, 0, s>>>(L0, S->p0, S->p1, S->q, S->e, S->slots, S->ctrl, 0ull, 0);
+      launch_vcycle(S, omega, s);
+      k_mx_rz<<<g0, MT, 0, s>>>(L0, L0.u, S->slots, S->ctrl);
+      if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
+    }
+    k_mx_correct<<<g64, MT, 0, s>>>(S->G, L0.ld, S->e, x);
+    k_mx_resid<<<g64, MT, 0, s>>>(S->G, b, x, S->r64, S->slots, S->ctrl, 0ull, 0);
+    if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
+  }
+  k_mx_finish<<<1, 32, 0, s>>>(S->ctrl, ctrl64, maxiter_report);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("mixed solve launch: ") + cudaGetErrorString(e));
   return PFGB_OK;
 }
 

@@ -41,6 +41,7 @@ struct MixCtrl {
   double rt_norm, tol_abs_in;
   double rho, beta, pq, alpha, rr_in;
   int outer, inner, inner_total, converged;
+  int inner_done, outer_done;
 };
 
 struct Solver {
@@ -49,6 +50,8 @@ struct Solver {
   int max_outer, max_inner;
   int nlev = 0;
   Lvl lev[MAX_LEVELS];
+  int coarse_levels = 1;       // levels resolved inside the coarse CTA
+  size_t coarse_smem = 0;      // its dynamic shared memory
   char* ws = nullptr;
   size_t ws_bytes = 0;
   float *e, *p0, *p1, *q;
@@ -63,6 +66,8 @@ void solver_destroy(Solver* S);
 // Append x = A^{-1} b (refinement loop) to a graph chain, then record the
 // total inner iterations / convergence in the step's control block.
 int append_solve(GraphChain& c, Solver* S, const double* b, double* x, Ctrl64* ctrl64, int maxiter_report);
+// The same solve with direct launches and host loop control (for profiling).
+int run_direct(Solver* S, const double* b, double* x, Ctrl64* ctrl64, int maxiter_report, cudaStream_t s);
 
 }  // namespace mixed
 }  // namespace pfgb

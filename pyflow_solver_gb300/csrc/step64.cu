@@ -561,6 +561,7 @@ __global__ void k_gather(const XASlot* slots, const Ctrl64* ctrl, StepOut64* out
   unsigned f = 0u;
   for (int s = 0; s < S_COUNT; ++s) f |= slots[s].result_flags;
   out->flags_or = f;
+  out->refine_passes = ctrl->refine_passes;
 }
 
 // ---------------------------------------------------------------------------
@@ -806,6 +807,7 @@ static void copy_out(const StepOut64& o, pfgb_step_out* out) {
   out->linres_sq = o.linres2;
   out->cont_sq = o.cont2;
   out->reduction_flags = o.flags_or;
+  out->refine_passes = o.refine_passes;
 }
 
 static int read_out(Instance64* I, cudaStream_t s, pfgb_step_out* out) {
@@ -832,10 +834,35 @@ int instance64_project(Instance64* I, double* u, double* v, double* p, long lds,
   return read_out(I, s, out);
 }
 
+// Mixed-precision step with direct launches (host loop control).
+static int mixed_step_direct(Instance64* I, double* u, double* v, double* p, long lds, const StepIn& in,
+                             cudaStream_t s, pfgb_step_out* out) {
+  const Geo64& G = I->G;
+  if (lds != G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
+  double* ui = u + lds + 1;
+  double* vi = v + lds + 1;
+  double* pi = p + lds + 1;
+  dim3 gp((G.nx + TX - 1) / TX, (G.ny + PB_Y - 1) / PB_Y);
+  *I->in_h = in;
+  cudaMemcpyAsync(I->in_d, I->in_h, sizeof(StepIn), cudaMemcpyHostToDevice, s);
+  k_prestep<<<gp, NT, 0, s>>>(G, ui, vi, I->slots, I->ctrl);
+  k_dt<<<1, 32, 0, s>>>(I->D, I->in_d, I->ctrl);
+  k_predict<<<gp, NT, 0, s>>>(G, ui, vi, I->us, I->vs, I->P.scheme, I->ctrl);
+  k_rhs<<<gp, NT, 0, s>>>(G, I->us, I->vs, G.ld, I->b, I->slots, I->ctrl);
+  k_cg_init<<<gp, NT, 0, s>>>(G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, 0ull, 0);
+  if (int rc = mixed::run_direct(I->mix, I->b, I->x, I->ctrl, I->A.maxiter, s)) return rc;
+  k_post_resid<0><<<gp, NT, 0, s>>>(G, I->b, I->x, I->slots);
+  k_pin_correct<<<gp, NT, 0, s>>>(G, I->L, 0, I->x, I->us, I->vs, G.ld, ui, vi, pi, I->slots, I->ctrl);
+  k_post_diag<<<gp, NT, 0, s>>>(G, I->us, I->vs, G.ld, I->b, ui, vi, pi, I->slots);
+  k_gather<<<1, 32, 0, s>>>(I->slots, I->ctrl, I->out_d);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+  return read_out(I, s, out);
+}
+
 int instance64_step(Instance64* I, double* u, double* v, double* p, long lds, const StepIn& in, cudaStream_t s,
                     pfgb_step_out* out) {
-  if (I->mix && (!I->use_graph || I->profiling))
-    return set_error(PFGB_ESTATE, "the mixed-precision step runs only as a CUDA graph (no profiling mode)");
+  if (I->mix && (!I->use_graph || I->profiling)) return mixed_step_direct(I, u, v, p, lds, in, s, out);
   if (I->use_graph && !I->profiling) {
     if (lds != I->G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
     double* ui = u + lds + 1;

@@ -45,6 +45,7 @@ struct Ctrl64 {
   double mean, bnrm2, atol, rho, rho_prev, pq, rr;
   double alpha, beta;    // rho/pq and rho/rho_prev, formed once by the finalisers
   unsigned nan_flag;
+  int refine_passes;     // mixed precision: outer refinement passes
 };
 
 // Everything the host reads back after a step (one copy).
@@ -53,7 +54,7 @@ struct StepOut64 {
   int safeguard, cg_iters, cg_info, nan_flag;
   double divstar2, bnrm2, res2, ru2, rv2, divafter2, linres2, cont2;
   unsigned flags_or;    // OR of the result flags of all slots (inexact / overflow diagnostics)
-  unsigned pad;
+  int refine_passes;
 };
 
 }  // namespace pfgb

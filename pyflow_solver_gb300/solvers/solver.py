@@ -148,6 +148,8 @@ def step(config, state, tracker, iteration: int) -> tuple[Any, dict[str, float],
         "nan_detected": nan_detected,
         "cg_iterations": int(out.cg_iterations),
     }
+    if P.precision == 1:
+        diagnostics["refine_passes"] = int(out.refine_passes)
     if getattr(config, "seed", None) is not None:
         diagnostics["seed"] = config.seed
     if getattr(config, "assert_invariants", False):

@@ -272,6 +272,16 @@ def main():
         cfg = cavity_cfg(512, 512, 1000.0, 1.0, True)
         arr = run_trajectory(R, cfg, 512, 512, 4, {1, 3})
         save("cavity512", arr, cfg)
+    if want("config_hashes"):
+        from pyflow.config.model import SimulationConfig
+        cases = [dict(nx=64, ny=64), dict(nx=32, ny=32, Re=400.0, lid_velocity=1.5, advection_scheme="quick",
+                                          lin_tol=1e-8, lin_maxiter=300, diagnostics=False, seed=7),
+                 dict(nx=512, ny=512, Re=1000.0, cfl_growth=1.1, checkpoint_interval=10, disable_advection=True)]
+        out = [{"kwargs": c, "hash": SimulationConfig(**c).config_hash} for c in cases]
+        path = os.path.join(HERE, "config_hashes.json")
+        with open(path, "w") as f:
+            json.dump({"meta": json.loads(meta), "cases": out}, f, indent=1)
+        print(f"wrote {path}")
     if want("batched16"):
         inst = batched_instances()
         pick = list(range(0, 256, 16))
@@ -279,7 +289,8 @@ def main():
         for i in pick:
             nx, ny, Re, U = inst[i]
             cfg = cavity_cfg(nx, ny, Re, U, True)
-            arr = run_trajectory(R, cfg, nx, ny, 5, {4})
+            # fields only for the smaller instances (fixture size); scalars for all
+            arr = run_trajectory(R, cfg, nx, ny, 5, {4} if nx * ny <= 64 * 64 else set())
             for k, v in arr.items():
                 out[f"i{i}_{k}"] = v
         save("batched16", out)

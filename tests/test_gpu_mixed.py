@@ -89,3 +89,23 @@ def test_mixed_trajectory_stays_close():
         pass
     for k in "uv":
         assert rel(interior_view(st.fields[k]).cpu().numpy(), ost.interior(tw.fields[k])) <= 1e-5, k
+
+
+def test_mixed_graph_and_direct_launches_agree():
+    """The graph (device-side loop control) and the host-driven direct form give the same bits."""
+    from pyflow_solver_gb300 import ResidualManager, SimulationDriver, allocate_state, interior_view
+    from pyflow_solver_gb300.solvers import _handle
+    cfg = SimpleNamespace(**vars(cavity(64, 48, 400.0, 1.0)), precision="mixed")
+    out = []
+    for mode in (True, False):
+        _handle.GRAPH_MODE = mode
+        try:
+            st = allocate_state(64, 48)
+            diags = [d for _, _, d in SimulationDriver(cfg, st, ResidualManager()).run(max_steps=4)]
+        finally:
+            _handle.GRAPH_MODE = True
+        out.append(([interior_view(st.fields[k]).cpu().numpy() for k in "uvp"],
+                    [(d["cg_iterations"], d["refine_passes"], d["dt"]) for d in diags]))
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    assert out[0][1] == out[1][1]
