@@ -9,9 +9,12 @@
 // equivalent singular Neumann system -lap_c e = r~ in binary32, where r~ equals
 // r except r~_0 = -sum_{k != 0} r_k (which makes it consistent), and is shifted
 // by -e[0] so that x[0] stays 0.  The inner solve is CG preconditioned by a
-// geometric multigrid V-cycle: Galerkin coarse operators for piecewise-constant
-// prolongation P and restriction R = P^T (face coefficients double per level),
-// two damped-Jacobi sweeps before and after, one CTA for the coarsest grid.
+// cell-centred geometric multigrid V-cycle: bilinear prolongation P (weights
+// 3/4, 1/4 per axis, reflected at the Neumann walls), restriction R = P^T,
+// coarse operators rediscretised with the same face coefficients (consistent
+// with R = P^T, which sums four children), two damped-Jacobi sweeps before and
+// after, and every level of at most 64 x 64 cells inside one CTA.  The cycle is
+// symmetric (R = P^T, adjoint smoothing), as PCG requires.
 // All dot products are exact (binary32 products are exact integers, summed in
 // the same superaccumulator as the binary64 path); alpha and beta are binary64.
 //
@@ -54,50 +57,93 @@ __device__ __forceinline__ float mg_nsum(const Lvl& L, int j, int i, F at) {
   return s;
 }
 
+// Bilinear prolongation (3/4 parent + 1/4 neighbour per axis, all of the
+// parent at a wall) and its transpose.
+// value of P e at fine cell (j, i), e the coarse correction
+__device__ __forceinline__ float prolong_at(const Lvl& C, int j, int i) {
+  const int I = i >> 1, J = j >> 1;
+  const int I2 = (i & 1) ? I + 1 : I - 1;
+  const int J2 = (j & 1) ? J + 1 : J - 1;
+  const bool hx = I2 >= 0 && I2 < C.nx, hy = J2 >= 0 && J2 < C.ny;
+  const float wx = hx ? 0.75f : 1.f, wy = hy ? 0.75f : 1.f;
+  const float* e = C.u;
+  float v = wx * wy * e[(long)J * C.ld + I];
+  if (hx) v = fmaf(0.25f * wy, e[(long)J * C.ld + I2], v);
+  if (hy) v = fmaf(wx * 0.25f, e[(long)J2 * C.ld + I], v);
+  if (hx && hy) v = fmaf(0.0625f, e[(long)J2 * C.ld + I2], v);
+  return v;
+}
+
+// weight with which fine index i (offset d = i - 2I in {-1, 0, 1, 2}) enters coarse I (R = P^T)
+__device__ __forceinline__ float rweight(int d, int I, int nc) {
+  if (d == -1) return (I - 1 >= 0) ? 0.25f : 0.f;
+  if (d == 2) return (I + 1 < nc) ? 0.25f : 0.f;
+  if (d == 0) return (I == 0) ? 1.f : 0.75f;
+  return (I == nc - 1) ? 1.f : 0.75f;          // d == 1
+}
+
 // ---- V-cycle kernels -------------------------------------------------------
 
-// two damped-Jacobi sweeps from u = 0: t = S(S(0)) for A u = f
+// two damped-Jacobi sweeps from u = 0: t = S(S(0)) for A u = f, and the
+// residual r = f - A t of the tile
 __global__ void __launch_bounds__(MT) k_mg_pre(Lvl L, float omega) {
-  __shared__ float s1[BY + 2][BX + 2];
+  __shared__ float s1[BY + 4][BX + 4];
+  __shared__ float s2[BY + 2][BX + 2];
   const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+  for (int idx = threadIdx.x; idx < (BY + 4) * (BX + 4); idx += MT) {
+    int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
+    int gj = j0 + jj, gi = i0 + ii;
+    float v = 0.f;
+    if (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx) v = omega * L.f[(long)gj * L.ld + gi] / mg_diag(L, gj, gi);
+    s1[jj + 2][ii + 2] = v;
+  }
+  __syncthreads();
   for (int idx = threadIdx.x; idx < (BY + 2) * (BX + 2); idx += MT) {
     int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
     int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx) v = omega * L.f[(long)gj * L.ld + gi] / mg_diag(L, gj, gi);
-    s1[jj + 1][ii + 1] = v;
+    if (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx) {
+      auto at = [&](int j, int i) { return s1[j - j0 + 2][i - i0 + 2]; };
+      const float d = mg_diag(L, gj, gi);
+      v = (1.f - omega) * s1[jj + 2][ii + 2] + omega * (L.f[(long)gj * L.ld + gi] + mg_nsum(L, gj, gi, at)) / d;
+    }
+    s2[jj + 1][ii + 1] = v;
   }
   __syncthreads();
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int gi = i0 + tx, gj = j0 + ty;
   if (gi < L.nx && gj < L.ny) {
-    auto at = [&](int j, int i) { return s1[j - j0 + 1][i - i0 + 1]; };
-    const float d = mg_diag(L, gj, gi);
-    const float u1 = s1[ty + 1][tx + 1];
-    const float f = L.f[(long)gj * L.ld + gi];
-    const float u2 = (1.f - omega) * u1 + omega * (f + mg_nsum(L, gj, gi, at)) / d;
-    L.t[(long)gj * L.ld + gi] = u2;
+    auto at = [&](int j, int i) { return s2[j - j0 + 1][i - i0 + 1]; };
+    const float t = s2[ty + 1][tx + 1];
+    const long o = (long)gj * L.ld + gi;
+    L.t[o] = t;
+    L.r[o] = L.f[o] - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
   }
 }
 
-// f_C(J, I) = sum over the 2x2 children of (f - A t) on the fine level
+// f_C = P^T r: each coarse cell gathers the residual of a 4 x 4 fine patch
 __global__ void __launch_bounds__(MT) k_mg_restrict(Lvl F, Lvl C) {
   const int I = blockIdx.x * BX + (threadIdx.x & 31), J = blockIdx.y * BY + (threadIdx.x >> 5);
   if (I >= C.nx || J >= C.ny) return;
-  auto at = [&](int j, int i) { return F.t[(long)j * F.ld + i]; };
   float s = 0.f;
 #pragma unroll
-  for (int dj = 0; dj < 2; ++dj)
+  for (int dj = -1; dj <= 2; ++dj) {
+    const float wy = rweight(dj, J, C.ny);
+    if (wy == 0.f) continue;
+    const int j = 2 * J + dj;
+    float row = 0.f;
 #pragma unroll
-    for (int di = 0; di < 2; ++di) {
-      const int j = 2 * J + dj, i = 2 * I + di;
-      const float au = mg_diag(F, j, i) * at(j, i) - mg_nsum(F, j, i, at);
-      s += F.f[(long)j * F.ld + i] - au;
+    for (int di = -1; di <= 2; ++di) {
+      const float wx = rweight(di, I, C.nx);
+      if (wx == 0.f) continue;
+      row = fmaf(wx, F.r[(long)j * F.ld + (2 * I + di)], row);
     }
+    s = fmaf(wy, row, s);
+  }
   C.f[(long)J * C.ld + I] = s;
 }
 
-// u = S(S(t + P u_C))
+// u = S(S(t + P u_C)) with the bilinear P
 __global__ void __launch_bounds__(MT) k_mg_post(Lvl F, Lvl C, float omega) {
   __shared__ float w0[BY + 4][BX + 4];
   __shared__ float w1[BY + 2][BX + 2];
@@ -106,8 +152,7 @@ __global__ void __launch_bounds__(MT) k_mg_post(Lvl F, Lvl C, float omega) {
     int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
     int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx)
-      v = F.t[(long)gj * F.ld + gi] + C.u[(long)(gj >> 1) * C.ld + (gi >> 1)];
+    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) v = F.t[(long)gj * F.ld + gi] + prolong_at(C, gj, gi);
     w0[jj + 2][ii + 2] = v;
   }
   __syncthreads();
@@ -220,8 +265,6 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(Lvl C, int nl, int cycl
       tot += nx * ny;
       nx /= 2;
       ny /= 2;
-      cx *= 2.f;
-      cy *= 2.f;
     }
   }
   float* f = sm;
@@ -276,18 +319,28 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(Lvl C, int nl, int cycl
       }
       __syncthreads();
       c_sweep(Lv, rh, w, e, omega);
-      // restrict the residual rh - A e into the next level's rh
+      // residual rh - A e of this level into w, then rh_{l+1} = P^T w
+      for (int c = threadIdx.x; c < n; c += CT) {
+        const int j = c / Lv.nx, i = c - j * Lv.nx;
+        w[Lv.off + c] = rh[Lv.off + c] - (c_diag(Lv, j, i) * e[Lv.off + c] - c_nsum(Lv, e, j, i));
+      }
+      __syncthreads();
       const CLvl& Cv = L[l + 1];
       const int nc = Cv.nx * Cv.ny;
       for (int c = threadIdx.x; c < nc; c += CT) {
         const int J = c / Cv.nx, I = c - J * Cv.nx;
         float sres = 0.f;
-        for (int dj = 0; dj < 2; ++dj)
-          for (int di = 0; di < 2; ++di) {
-            const int j = 2 * J + dj, i = 2 * I + di;
-            const int fc = j * Lv.nx + i;
-            sres += rh[Lv.off + fc] - (c_diag(Lv, j, i) * e[Lv.off + fc] - c_nsum(Lv, e, j, i));
+        for (int dj = -1; dj <= 2; ++dj) {
+          const float wy = rweight(dj, J, Cv.ny);
+          if (wy == 0.f) continue;
+          float row = 0.f;
+          for (int di = -1; di <= 2; ++di) {
+            const float wx = rweight(di, I, Cv.nx);
+            if (wx == 0.f) continue;
+            row = fmaf(wx, w[Lv.off + (2 * J + dj) * Lv.nx + (2 * I + di)], row);
           }
+          sres = fmaf(wy, row, sres);
+        }
         rh[Cv.off + c] = sres;
       }
       __syncthreads();
@@ -298,7 +351,16 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(Lvl C, int nl, int cycl
       const int n = Lv.nx * Lv.ny;
       for (int c = threadIdx.x; c < n; c += CT) {
         const int j = c / Lv.nx, i = c - j * Lv.nx;
-        w[Lv.off + c] = e[Lv.off + c] + e[Cv.off + (j >> 1) * Cv.nx + (i >> 1)];
+        const int I = i >> 1, J = j >> 1;
+        const int I2 = (i & 1) ? I + 1 : I - 1, J2 = (j & 1) ? J + 1 : J - 1;
+        const bool hx = I2 >= 0 && I2 < Cv.nx, hy = J2 >= 0 && J2 < Cv.ny;
+        const float wx = hx ? 0.75f : 1.f, wy = hy ? 0.75f : 1.f;
+        const float* ec = e + Cv.off;
+        float pv = wx * wy * ec[J * Cv.nx + I];
+        if (hx) pv = fmaf(0.25f * wy, ec[J * Cv.nx + I2], pv);
+        if (hy) pv = fmaf(wx * 0.25f, ec[J2 * Cv.nx + I], pv);
+        if (hx && hy) pv = fmaf(0.0625f, ec[J2 * Cv.nx + I2], pv);
+        w[Lv.off + c] = e[Lv.off + c] + pv;
       }
       __syncthreads();
       c_sweep(Lv, rh, w, e, omega);
@@ -623,7 +685,7 @@ int solver_create(int nx, int ny, double dx, double dy, long ld64, double tol_ou
   std::vector<long> lds(S->nlev);
   for (int l = 0; l < S->nlev; ++l) {
     lds[l] = round_up(dims[l].first, 32);
-    bytes += 3 * (size_t)lds[l] * dims[l].second * sizeof(float) + 3 * 256;
+    bytes += 4 * (size_t)lds[l] * dims[l].second * sizeof(float) + 4 * 256;
   }
   const long ld0 = lds[0];
   const size_t v0 = (size_t)ld0 * ny * sizeof(float);
@@ -651,8 +713,7 @@ int solver_create(int nx, int ny, double dx, double dy, long ld64, double tol_ou
     v.u = (float*)take(n);
     v.t = (float*)take(n);
     v.f = (float*)take(n);
-    cx *= 2.f;
-    cy *= 2.f;
+    v.r = (float*)take(n);
   }
   S->e = (float*)take(v0);
   S->p0 = (float*)take(v0);

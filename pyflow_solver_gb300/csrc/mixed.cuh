@@ -14,8 +14,8 @@ namespace mixed {
 constexpr int MAX_LEVELS = 16;
 
 // One multigrid level: binary32 arrays of (ny, ld); cx, cy are the face
-// coefficients of the Galerkin operator (1/dx^2, 1/dy^2 on the finest level,
-// doubled on each coarser one).
+// coefficients (1/dx^2, 1/dy^2 on every level: with R = P^T summing about four
+// children, the rediscretised coarse operator keeps the fine coefficients).
 struct Lvl {
   int nx, ny;
   long ld;
@@ -23,6 +23,7 @@ struct Lvl {
   float* u;   // V-cycle result
   float* t;   // pre-smoothed iterate
   float* f;   // right-hand side (on level 0: the PCG residual)
+  float* r;   // residual f - A t after pre-smoothing
 };
 
 // binary64 geometry of the refinement
