@@ -134,6 +134,21 @@ PFGB_API size_t pfgb_workspace_bytes(const pfgb_handle* handle);
 PFGB_API int pfgb_step(pfgb_handle* handle, double* u, double* v, double* p, long ld,
               const pfgb_step_in* in, void* stream, pfgb_step_out* out);
 
+/* ---- batches of independent cavities ----------------------------------- */
+
+/* n instances (params[k] each, binary64: precision 0) advanced together: every
+ * kernel of a step covers the tiles of all instances (one CUDA graph launch
+ * per step, CG loop as one WHILE node with per-instance convergence masks).
+ * Same per-instance semantics as pfgb_step (src/pyflow/solvers/solver.py:15-121
+ * for each cavity). */
+PFGB_API int pfgb_batch_create(const pfgb_params* params, int n, pfgb_handle** handle);
+/* One step of every instance k with u[k], v[k], p[k] non-null (the others sit
+ * the step out): state arrays as in pfgb_step, in[k] / out[k] per instance.
+ * Synchronises `stream`. */
+PFGB_API int pfgb_batch_step(pfgb_handle* handle, double* const* u, double* const* v, double* const* p,
+                             const pfgb_step_in* in, void* stream, pfgb_step_out* out);
+PFGB_API int pfgb_batch_size(const pfgb_handle* handle);
+
 /* Stand-alone projection of the state's current u, v with a given dt:
  * solve_pressure_poisson in normal mode
  * (src/pyflow/solvers/pressure_solver.py:95-219 with rhs_override None).

@@ -72,6 +72,10 @@ SIGNATURES = {
     "pfgb_workspace_bytes": (ctypes.c_size_t, [_P]),
     "pfgb_step": (_I, [_P, _P, _P, _P, _L, ctypes.POINTER(StepIn), _P, ctypes.POINTER(StepOut)]),
     "pfgb_project": (_I, [_P, _P, _P, _P, _L, _D, _P, ctypes.POINTER(StepOut)]),
+    "pfgb_batch_create": (_I, [ctypes.POINTER(Params), _I, ctypes.POINTER(_P)]),
+    "pfgb_batch_step": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(StepIn), _P,
+                             ctypes.POINTER(StepOut)]),
+    "pfgb_batch_size": (_I, [_P]),
     "pfgb_gradient_coherent": (_I, [_P, _L, _P, _P, _L, _I, _I, _D, _D, _P]),
     "pfgb_divergence_coherent": (_I, [_P, _P, _L, _P, _L, _I, _I, _D, _D, _P]),
     "pfgb_laplacian_coherent": (_I, [_P, _L, _P, _L, _I, _I, _D, _D, _P]),

@@ -2,6 +2,7 @@
 // error reporting, the projection step and the operator-interface CG.
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "pfgb_internal.h"
 #include "step64.cuh"
@@ -114,3 +115,35 @@ extern "C" int pfgb_set_graph(pfgb_handle* handle, int on) {
   if (!handle) return set_error(PFGB_EINVAL, "null handle");
   return instance64_set_graph(handle->inst, on);
 }
+
+extern "C" int pfgb_batch_create(const pfgb_params* params, int n, pfgb_handle** handle) {
+  if (!params || !handle || n < 1) return set_error(PFGB_EINVAL, "invalid batch arguments");
+  for (int k = 0; k < n; ++k) {
+    if (params[k].precision != 0 && params[k].precision != 1) return set_error(PFGB_EINVAL, "precision must be 0 or 1");
+    if (params[k].scheme < 0 || params[k].scheme > 2) return set_error(PFGB_EINVAL, "unknown advection scheme");
+  }
+  Instance64* inst = nullptr;
+  int rc = instance64_create_batch(params, n, &inst);
+  if (rc) return rc;
+  pfgb_handle* h = new pfgb_handle;
+  h->inst = inst;
+  *handle = h;
+  return PFGB_OK;
+}
+
+extern "C" int pfgb_batch_step(pfgb_handle* handle, double* const* u, double* const* v, double* const* p,
+                               const pfgb_step_in* in, void* stream, pfgb_step_out* out) {
+  if (!handle || !u || !v || !p || !in || !out) return set_error(PFGB_EINVAL, "null argument");
+  const int n = instance64_count(handle->inst);
+  std::vector<StepIn> si(n);
+  for (int k = 0; k < n; ++k) {
+    if (in[k].hist_len < 0 || in[k].hist_len > 5) return set_error(PFGB_EINVAL, "hist_len must be in [0, 5]");
+    si[k].dt_prev = in[k].dt_prev;
+    for (int q = 0; q < 5; ++q) si[k].hist[q] = in[k].hist[q];
+    si[k].hist_len = in[k].hist_len;
+    si[k].iteration = in[k].iteration;
+  }
+  return instance64_batch_step(handle->inst, u, v, p, si.data(), (cudaStream_t)stream, out);
+}
+
+extern "C" int pfgb_batch_size(const pfgb_handle* handle) { return handle ? instance64_count(handle->inst) : 0; }

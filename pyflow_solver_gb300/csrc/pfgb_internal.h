@@ -15,6 +15,10 @@ int check_cuda(cudaError_t e, const char* what);
 struct StepIn;
 struct Instance64;
 int instance64_create(const pfgb_params* prm, Instance64** out);
+int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out);
+int instance64_count(const Instance64* I);
+int instance64_batch_step(Instance64* I, double* const* u, double* const* v, double* const* p, const StepIn* in,
+                          cudaStream_t s, pfgb_step_out* out);
 void instance64_destroy(Instance64* I);
 size_t instance64_workspace_bytes(const Instance64* I);
 int instance64_project(Instance64* I, double* u, double* v, double* p, long lds, double dt, cudaStream_t s,

@@ -34,17 +34,8 @@ namespace pfgb {
 constexpr int NT = 256;       // threads per CTA (1-D blocks)
 constexpr int TX = 32;        // tile width (one warp per tile row)
 constexpr int TY = 16;        // tile height of the CG kernels (2 rows per thread)
-constexpr int RPT = TY / (NT / TX);   // rows per thread in the CG kernels (4)
+constexpr int RPT = TY / (NT / TX);   // rows per thread in the CG kernels (2)
 constexpr int PB_Y = NT / TX;         // tile height of the per-cell kernels (8)
-
-struct Geo64 {
-  int nx, ny;
-  long ld;            // pitch of the work vectors (doubles)
-  long lds;           // pitch of the state arrays (nx + 2)
-  Grid2 g;
-  double invd;        // interior Jacobi entry 1/(2/dx^2 + 2/dy^2)
-  int jacobi;
-};
 
 __device__ __forceinline__ double jacobi_apply(const Geo64& G, int j, int i, double r) {
   if (!G.jacobi) return r;
@@ -72,16 +63,25 @@ __device__ __forceinline__ void zero_sacc(long long* sacc) {
   for (int k = threadIdx.x; k < XA_DIGITS; k += blockDim.x) sacc[k] = 0;
 }
 
+// The CTA's tile and instance.  Every CTA of an inactive instance returns.
+#define TILE_PROLOGUE                                             \
+  const Tile tl = TL[blockIdx.x];                                 \
+  const InstDesc& D = ID[tl.inst];                                \
+  if (!D.active) return;                                          \
+  const Geo64 G = D.G;
+
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NT) k_prestep(Geo64 G, const double* __restrict__ u, const double* __restrict__ v,
-                                                 XASlot* slots, Ctrl64* ctrl) {
+__global__ void __launch_bounds__(NT) k_prestep(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
   __shared__ long long sacc[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
   zero_sacc(sacc);
-  const int i = blockIdx.x * TX + (threadIdx.x & 31);
-  const int j = blockIdx.y * PB_Y + (threadIdx.x >> 5);
-  View2<const double> U{u, G.lds}, V{v, G.lds};
+  XASlot* slots = D.slots;
+  Ctrl64* ctrl = D.ctrl;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
+  View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds};
   XTerm t;
   xa_zero(t);
   unsigned fl = 0u;
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(NT) k_prestep(Geo64 G, const double* __restric
   }
   reduce_terms(&slots[S_DIVC_BEFORE], &t, 1, fl, sacc, wred, ired);
   XASlot* sl[1] = {&slots[S_DIVC_BEFORE]};
-  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 1, D.nt_pc) && threadIdx.x == 0) {
     double um = __longlong_as_double((long long)*(volatile unsigned long long*)&ctrl->umax_bits);
     double vm = __longlong_as_double((long long)*(volatile unsigned long long*)&ctrl->vmax_bits);
     ctrl->umax = ADD(um, 1e-12);
@@ -113,14 +113,15 @@ __global__ void __launch_bounds__(NT) k_prestep(Geo64 G, const double* __restric
   }
 }
 
-// dt selection, exactly the Python float sequence of solver.py:25-62.
-struct DtArgs {
-  double dx, dy, cfl_target, growth, nu;
-};
-
-__global__ void k_dt(DtArgs a, const StepIn* __restrict__ in_d, Ctrl64* ctrl) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const StepIn in = *in_d;
+// dt selection, exactly the Python float sequence of solver.py:25-62 (one thread per instance)
+__global__ void k_dt(const InstDesc* __restrict__ ID, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const InstDesc& Dd = ID[k];
+  if (!Dd.active) return;
+  const DtArgs a = Dd.D;
+  const StepIn in = *Dd.in;
+  Ctrl64* ctrl = Dd.ctrl;
   const double umax = ctrl->umax, vmax = ctrl->vmax;
   const double dt_cfl_u = DIV(MUL(a.cfl_target, a.dx), umax);
   const double dt_cfl_v = DIV(MUL(a.cfl_target, a.dy), vmax);
@@ -131,12 +132,12 @@ __global__ void k_dt(DtArgs a, const StepIn* __restrict__ in_d, Ctrl64* ctrl) {
   double dt = (dt_cand > lim) ? lim : dt_cand;
   // history: previous entries then the new baseline, keep the last five
   double h[6];
-  int n = in.hist_len;
-  for (int k = 0; k < n; ++k) h[k] = in.hist[k];
-  h[n++] = ctrl->div_before;
+  int nh = in.hist_len;
+  for (int q = 0; q < nh; ++q) h[q] = in.hist[q];
+  h[nh++] = ctrl->div_before;
   int safeguard = 0;
-  if (n >= 3) {
-    double x = h[n - 3], y = h[n - 2], z = h[n - 1];
+  if (nh >= 3) {
+    double x = h[nh - 3], y = h[nh - 2], z = h[nh - 1];
     if (x > 0.0 && y > MUL(x, 1.01) && z > MUL(y, 1.01)) {
       dt = MUL(dt, 0.5);
       safeguard = 1;
@@ -148,106 +149,104 @@ __global__ void k_dt(DtArgs a, const StepIn* __restrict__ in_d, Ctrl64* ctrl) {
   ctrl->dtm = py_max(dt, 1e-14);
 }
 
-// dt given by the caller of a stand-alone projection
-__global__ void k_set_dt(double dt, Ctrl64* ctrl) {
+// dt given by the caller of a stand-alone projection (instance 0)
+__global__ void k_set_dt(const InstDesc* __restrict__ ID, double dt) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Ctrl64* ctrl = ID[0].ctrl;
   ctrl->dt = dt;
   ctrl->dtm = py_max(dt, 1e-14);
   ctrl->safeguard = 0;
 }
 
 // predictor: u* = u - dt*conv_u(u,v), v* likewise (solver.py:73-95)
-__global__ void __launch_bounds__(NT) k_predict(Geo64 G, const double* __restrict__ u, const double* __restrict__ v,
-                                                 double* __restrict__ us, double* __restrict__ vs, int scheme,
-                                                 const Ctrl64* __restrict__ ctrl) {
-  const int i = blockIdx.x * TX + (threadIdx.x & 31);
-  const int j = blockIdx.y * PB_Y + (threadIdx.x >> 5);
+__global__ void __launch_bounds__(NT) k_predict(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
   if (i >= G.nx || j >= G.ny) return;
-  View2<const double> U{u, G.lds}, V{v, G.lds};
-  const double dt = ctrl->dt;
+  View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds};
+  const double dt = D.ctrl->dt;
   double u0 = U(j, i), v0 = V(j, i), un, vn;
-  if (scheme == 2) {            // advection disabled: u* = u_old
+  if (D.scheme == 2) {            // advection disabled: u* = u_old
     un = u0; vn = v0;
-  } else if (scheme == 1) {     // QUICK
+  } else if (D.scheme == 1) {     // QUICK
     un = SUB(u0, MUL(dt, advect_quick_at(U, V, U, j, i, G.g)));
     vn = SUB(v0, MUL(dt, advect_quick_at(U, V, V, j, i, G.g)));
-  } else {                      // upwind
+  } else {                        // upwind
     un = SUB(u0, MUL(dt, advect_upwind_at(U, V, U, j, i, G.g)));
     vn = SUB(v0, MUL(dt, advect_upwind_at(U, V, V, j, i, G.g)));
   }
-  us[(long)j * G.ld + i] = un;
-  vs[(long)j * G.ld + i] = vn;
+  D.us[(long)j * D.usld + i] = un;
+  D.vs[(long)j * D.usld + i] = vn;
 }
 
 // RHS: b = -div_c(u*,v*)/max(dt,1e-14); sum(b); ||div_c(u*,v*)||^2
-__global__ void __launch_bounds__(NT) k_rhs(Geo64 G, const double* __restrict__ us, const double* __restrict__ vs,
-                                             long usld, double* __restrict__ b, XASlot* slots,
-                                             const Ctrl64* __restrict__ ctrl) {
+__global__ void __launch_bounds__(NT) k_rhs(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
-  const int i = blockIdx.x * TX + (threadIdx.x & 31);
-  const int j = blockIdx.y * PB_Y + (threadIdx.x >> 5);
+  XASlot* slots = D.slots;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
   XTerm t0, t1;
   xa_zero(t0);
   xa_zero(t1);
   unsigned f0 = 0u, f1 = 0u;
   if (i < G.nx && j < G.ny) {
-    View2<const double> US{us, usld}, VS{vs, usld};
+    View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
     double d = div_coherent_at(US, VS, j, i, G.g);
-    double bv = DIV(-d, ctrl->dtm);
-    b[(long)j * G.ld + i] = bv;
+    double bv = DIV(-d, D.ctrl->dtm);
+    D.b[(long)j * G.ld + i] = bv;
     xa_term_val(bv, t0, f0);
     xa_term_prod(d, d, t1, f1);
   }
   reduce_terms(&slots[S_BSUM], &t0, 1, f0, sacc0, wred, ired);
   reduce_terms(&slots[S_DIVSTAR], &t1, 1, f1, sacc1, wred, ired);
   XASlot* sl[2] = {&slots[S_BSUM], &slots[S_DIVSTAR]};
-  xa_finish(sl, 2, gridDim.x * gridDim.y);
+  xa_finish(sl, 2, D.nt_pc);
 }
-
-struct CGArgs {
-  double rtol;
-  int maxiter;
-  double n_cells;     // N as a double (exact)
-};
 
 // adjust = 1 (projection): b -= mean(b); b[0] = 0.  Then r = b; x = 0;
 // ||b||^2; r.(M r).  adjust = 0 (operator interface): b is used as given.
-__global__ void __launch_bounds__(NT) k_cg_init(Geo64 G, CGArgs A, int adjust, double* __restrict__ b,
-                                                 double* __restrict__ r, double* __restrict__ x, XASlot* slots,
-                                                 Ctrl64* ctrl, cudaGraphConditionalHandle cond, int use_cond) {
+// Instances that start iterating are counted in the loop control.
+__global__ void __launch_bounds__(NT) k_cg_init(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
+                                                 LoopCtl* lc) {
+  TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
-  const int i = blockIdx.x * TX + (threadIdx.x & 31);
-  const int j = blockIdx.y * PB_Y + (threadIdx.x >> 5);
-  const double mean = adjust ? DIV(slots[S_BSUM].result, A.n_cells) : 0.0;
+  XASlot* slots = D.slots;
+  Ctrl64* ctrl = D.ctrl;
+  const CGArgs A = D.A;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
+  const double mean = D.adjust ? DIV(slots[S_BSUM].result, A.n_cells) : 0.0;
   XTerm t0, t1;
   xa_zero(t0);
   xa_zero(t1);
   unsigned f0 = 0u, f1 = 0u;
   if (i < G.nx && j < G.ny) {
     long o = (long)j * G.ld + i;
-    double bv = b[o];
-    if (adjust) {
+    double bv = D.b[o];
+    if (D.adjust) {
       bv = SUB(bv, mean);
       if (i == 0 && j == 0) bv = 0.0;
-      b[o] = bv;
+      D.b[o] = bv;
     }
-    r[o] = bv;
-    x[o] = 0.0;
+    D.r[o] = bv;
+    D.x[o] = 0.0;
     xa_term_prod(bv, bv, t0, f0);
     xa_term_prod(bv, jacobi_apply(G, j, i, bv), t1, f1);
   }
   reduce_terms(&slots[S_BB], &t0, 1, f0, sacc0, wred, ired);
   reduce_terms(&slots[S_RZ0], &t1, 1, f1, sacc1, wred, ired);
   XASlot* sl[2] = {&slots[S_BB], &slots[S_RZ0]};
-  if (xa_finish(sl, 2, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 2, D.nt_pc) && threadIdx.x == 0) {
     double bb = slots[S_BB].result;
     double bnrm2 = __dsqrt_rn(bb);
     ctrl->mean = mean;
@@ -257,6 +256,7 @@ __global__ void __launch_bounds__(NT) k_cg_init(Geo64 G, CGArgs A, int adjust, d
     ctrl->info = 0;
     ctrl->zero_rhs = 0;
     ctrl->nan_flag = 0u;
+    ctrl->refine_passes = 0;
     ctrl->rr = bb;
     ctrl->rho = slots[S_RZ0].result;
     ctrl->rho_prev = 0.0;
@@ -270,8 +270,26 @@ __global__ void __launch_bounds__(NT) k_cg_init(Geo64 G, CGArgs A, int adjust, d
       ctrl->done = 1;
     } else {
       ctrl->done = 0;
+      if (lc) atomicAdd(&lc->active, 1);
     }
-    if (use_cond) cudaGraphSetConditional(cond, ctrl->done ? 0u : 1u);
+  }
+}
+
+// Arms a WHILE loop: its condition is "some instance still iterates".
+__global__ void k_loop_arm(LoopCtl* lc, cudaGraphConditionalHandle cond, int use_cond) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  lc->guard = 0;
+  lc->tripped = 0;
+  if (use_cond) cudaGraphSetConditional(cond, lc->active > 0 ? 1u : 0u);
+}
+
+// Last node of a WHILE body: stops the loop after guard_max trips in any case.
+__global__ void k_loop_guard(LoopCtl* lc, cudaGraphConditionalHandle cond, int use_cond) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int g = ++lc->guard;
+  if (g >= lc->guard_max && lc->active > 0) {
+    lc->tripped = 1;
+    if (use_cond) cudaGraphSetConditional(cond, 0u);
   }
 }
 
@@ -281,12 +299,10 @@ __global__ void __launch_bounds__(NT) k_cg_init(Geo64 G, CGArgs A, int adjust, d
 // The iteration index k is read from the control block and selects the
 // ping-pong buffers: iteration k reads p[k & 1] and writes p[(k + 1) & 1].
 template <int OP>
-__global__ void __launch_bounds__(NT) k_cg_matvec(Geo64 G, const double* __restrict__ r, double* p0, double* p1,
-                                                   double* __restrict__ q, XASlot* slots, Ctrl64* ctrl) {
+__global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
+  Ctrl64* ctrl = D.ctrl;
   if (*(volatile int*)&ctrl->done) return;
-  const int k = *(volatile int*)&ctrl->iter;
-  const double* __restrict__ pold = (k & 1) ? p1 : p0;
-  double* __restrict__ pnew = (k & 1) ? p0 : p1;
   __shared__ double pn[TY + 2][TX + 2];
   __shared__ double gxs[TY][TX + 1];
   __shared__ double gys[TY + 1][TX];
@@ -294,7 +310,12 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(Geo64 G, const double* __restr
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
   zero_sacc(sacc);
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  XASlot* slots = D.slots;
+  const int k = *(volatile int*)&ctrl->iter;
+  const double* __restrict__ pold = (k & 1) ? D.p1 : D.p0;
+  double* __restrict__ pnew = (k & 1) ? D.p0 : D.p1;
+  const double* __restrict__ r = D.r;
+  const int i0 = tl.i0, j0 = tl.j0;
   const double beta = (k > 0) ? ctrl->beta : 0.0;
   for (int idx = threadIdx.x; idx < (TY + 2) * (TX + 2); idx += NT) {
     int jj = idx / (TX + 2) - 1, ii = idx % (TX + 2) - 1;
@@ -342,34 +363,37 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(Geo64 G, const double* __restr
       if (OP == 0) qv = (gi == 0 && gj == 0) ? pv : -ADD(xp, yp);
       else qv = (gi == 0 || gj == 0 || gi == G.nx - 1 || gj == G.ny - 1) ? pv : ADD(xp, yp);
       long o = (long)gj * G.ld + gi;
-      q[o] = qv;
+      D.q[o] = qv;
       pnew[o] = pv;
       xa_term_prod(pv, qv, t[rr], fl);
     }
   }
   reduce_terms(&slots[S_PQ], t, RPT, fl, sacc, wred, ired);
   XASlot* sl[1] = {&slots[S_PQ]};
-  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 1, D.nt_cg) && threadIdx.x == 0) {
     const double pq = slots[S_PQ].result;
     ctrl->pq = pq;
     ctrl->alpha = DIV(ctrl->rho, pq);
   }
 }
 
-// x += alpha p; r -= alpha q; r.r; r.(M r)
-__global__ void __launch_bounds__(NT) k_cg_update(Geo64 G, CGArgs A, const double* p0, const double* p1,
-                                                   const double* __restrict__ q, double* __restrict__ x,
-                                                   double* __restrict__ r, XASlot* slots, Ctrl64* ctrl,
-                                                   cudaGraphConditionalHandle cond, int use_cond) {
+// x += alpha p; r -= alpha q; r.r; r.(M r).  An instance that finishes
+// leaves the loop control's active count; the last one stops the loop.
+__global__ void __launch_bounds__(NT) k_cg_update(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
+                                                   LoopCtl* lc, cudaGraphConditionalHandle cond, int use_cond) {
+  TILE_PROLOGUE
+  Ctrl64* ctrl = D.ctrl;
   if (*(volatile int*)&ctrl->done) return;
-  const int k = *(volatile int*)&ctrl->iter;
-  const double* __restrict__ p = (k & 1) ? p0 : p1;    // the buffer this iteration's matvec wrote
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  XASlot* slots = D.slots;
+  const CGArgs A = D.A;
+  const int k = *(volatile int*)&ctrl->iter;
+  const double* __restrict__ p = (k & 1) ? D.p0 : D.p1;    // the buffer this iteration's matvec wrote
+  const int i0 = tl.i0, j0 = tl.j0;
   const double alpha = ctrl->alpha;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   XTerm trr[RPT], trz[RPT];
@@ -381,10 +405,10 @@ __global__ void __launch_bounds__(NT) k_cg_update(Geo64 G, CGArgs A, const doubl
     int gj = j0 + ty + rr * PB_Y, gi = i0 + tx;
     if (gj < G.ny && gi < G.nx) {
       long o = (long)gj * G.ld + gi;
-      double xv = ADD(x[o], MUL(alpha, p[o]));
-      double rv = SUB(r[o], MUL(alpha, q[o]));
-      x[o] = xv;
-      r[o] = rv;
+      double xv = ADD(D.x[o], MUL(alpha, p[o]));
+      double rv = SUB(D.r[o], MUL(alpha, D.q[o]));
+      D.x[o] = xv;
+      D.r[o] = rv;
       xa_term_prod(rv, rv, trr[rr], f0);
       xa_term_prod(rv, jacobi_apply(G, gj, gi, rv), trz[rr], f1);
     }
@@ -392,7 +416,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(Geo64 G, CGArgs A, const doubl
   reduce_terms(&slots[S_RR], trr, RPT, f0, sacc0, wred, ired);
   reduce_terms(&slots[S_RZ], trz, RPT, f1, sacc1, wred, ired);
   XASlot* sl[2] = {&slots[S_RR], &slots[S_RZ]};
-  if (xa_finish(sl, 2, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 2, D.nt_cg) && threadIdx.x == 0) {
     double rr = slots[S_RR].result;
     ctrl->rr = rr;
     ctrl->rho_prev = ctrl->rho;
@@ -407,7 +431,9 @@ __global__ void __launch_bounds__(NT) k_cg_update(Geo64 G, CGArgs A, const doubl
       ctrl->done = 1;
       ctrl->info = 0;
     }
-    if (use_cond && ctrl->done) cudaGraphSetConditional(cond, 0u);
+    if (ctrl->done && lc) {
+      if (atomicSub(&lc->active, 1) == 1 && use_cond) cudaGraphSetConditional(cond, 0u);
+    }
   }
 }
 
@@ -424,47 +450,45 @@ __device__ __forceinline__ double apply_A(View2<const double> X, int j, int i, c
 
 // ||b - A x||^2 (the true residual of interface.solve)
 template <int OP>
-__global__ void __launch_bounds__(NT) k_post_resid(Geo64 G, const double* __restrict__ b, const double* __restrict__ x,
-                                                    XASlot* slots) {
+__global__ void __launch_bounds__(NT) k_post_resid(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
   __shared__ long long sacc[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
   zero_sacc(sacc);
-  const int i = blockIdx.x * TX + (threadIdx.x & 31);
-  const int j = blockIdx.y * PB_Y + (threadIdx.x >> 5);
+  XASlot* slots = D.slots;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
   XTerm t;
   xa_zero(t);
   unsigned fl = 0u;
   if (i < G.nx && j < G.ny) {
-    View2<const double> X{x, G.ld};
-    double rv = SUB(b[(long)j * G.ld + i], apply_A<OP>(X, j, i, G.g));
+    View2<const double> X{D.x, G.ld};
+    double rv = SUB(D.b[(long)j * G.ld + i], apply_A<OP>(X, j, i, G.g));
     xa_term_prod(rv, rv, t, fl);
   }
   reduce_terms(&slots[S_RES], &t, 1, fl, sacc, wred, ired);
   XASlot* sl[1] = {&slots[S_RES]};
-  xa_finish(sl, 1, gridDim.x * gridDim.y);
+  xa_finish(sl, 1, D.nt_pc);
 }
 
-struct LidArgs {
-  int has_lid;
-  double lid;
-};
-
 // p = x - x[0] into the state; u = u* - dt*gx(p).
-// mode 0 (full step): u* lives in us/vs (pitch usld) and keeps the pre-lid
-//   corrected velocity for the divergence diagnostic; the state gets the lid
-//   on its top interior row and the sums of (u-u_old)^2 are formed.
+// mode 0 (full step): u* lives in us/vs and keeps the pre-lid corrected
+//   velocity for the divergence diagnostic; the state gets the lid on its top
+//   interior row and the sums of (u-u_old)^2 are formed.
 // mode 1 (projection only): us/vs are the state's own u/v, corrected in place.
-__global__ void __launch_bounds__(NT) k_pin_correct(Geo64 G, LidArgs L, int mode, const double* __restrict__ x,
-                                                     double* us, double* vs, long usld, double* u, double* v,
-                                                     double* __restrict__ p, XASlot* slots, Ctrl64* ctrl) {
+__global__ void __launch_bounds__(NT) k_pin_correct(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
-  const int i = blockIdx.x * TX + (threadIdx.x & 31);
-  const int j = blockIdx.y * PB_Y + (threadIdx.x >> 5);
+  XASlot* slots = D.slots;
+  Ctrl64* ctrl = D.ctrl;
+  const LidArgs L = D.L;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
   XTerm t0, t1;
   xa_zero(t0);
   xa_zero(t1);
@@ -472,24 +496,25 @@ __global__ void __launch_bounds__(NT) k_pin_correct(Geo64 G, LidArgs L, int mode
   int bad = 0;
   if (i < G.nx && j < G.ny) {
     const double dt = ctrl->dt;
+    const double* __restrict__ x = D.x;
     const double x0 = x[0];
     View2<const double> X{x, G.ld};
     const double pv = SUB(X(j, i), x0);
     const double gx = (i < G.nx - 1) ? DIVH(SUB(SUB(X(j, i + 1), x0), pv), G.g.sx) : 0.0;
     const double gy = (j < G.ny - 1) ? DIVH(SUB(SUB(X(j + 1, i), x0), pv), G.g.sy) : 0.0;
-    long o = (long)j * usld + i;
+    long o = (long)j * D.usld + i;
     long os = (long)j * G.lds + i;
-    const double uc = SUB(us[o], MUL(dt, gx));
-    const double vc = SUB(vs[o], MUL(dt, gy));
-    us[o] = uc;
-    vs[o] = vc;
-    p[os] = pv;
-    if (mode == 0) {
+    const double uc = SUB(D.us[o], MUL(dt, gx));
+    const double vc = SUB(D.vs[o], MUL(dt, gy));
+    D.us[o] = uc;
+    D.vs[o] = vc;
+    D.pi[os] = pv;
+    if (D.mode == 0) {
       const double uf = (L.has_lid && j == G.ny - 1) ? L.lid : uc;
-      const double du = SUB(uf, u[os]);
-      const double dv = SUB(vc, v[os]);
-      u[os] = uf;
-      v[os] = vc;
+      const double du = SUB(uf, D.ui[os]);
+      const double dv = SUB(vc, D.vi[os]);
+      D.ui[os] = uf;
+      D.vi[os] = vc;
       xa_term_val(MUL(du, du), t0, f0);
       xa_term_val(MUL(dv, dv), t1, f1);
       bad = !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
@@ -501,33 +526,32 @@ __global__ void __launch_bounds__(NT) k_pin_correct(Geo64 G, LidArgs L, int mode
   reduce_terms(&slots[S_RU], &t0, 1, f0, sacc0, wred, ired);
   reduce_terms(&slots[S_RV], &t1, 1, f1, sacc1, wred, ired);
   XASlot* sl[2] = {&slots[S_RU], &slots[S_RV]};
-  xa_finish(sl, 2, gridDim.x * gridDim.y);
+  xa_finish(sl, 2, D.nt_pc);
 }
 
 // ||div_c(u_corr)||^2, ||A p - b||^2, ||div_central(u,v;1,1)||^2
-__global__ void __launch_bounds__(NT) k_post_diag(Geo64 G, const double* __restrict__ us, const double* __restrict__ vs,
-                                                   long usld, const double* __restrict__ b, const double* __restrict__ u,
-                                                   const double* __restrict__ v, const double* __restrict__ p,
-                                                   XASlot* slots) {
+__global__ void __launch_bounds__(NT) k_post_diag(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS], sacc2[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
   zero_sacc(sacc2);
-  const int i = blockIdx.x * TX + (threadIdx.x & 31);
-  const int j = blockIdx.y * PB_Y + (threadIdx.x >> 5);
+  XASlot* slots = D.slots;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
   XTerm t0, t1, t2;
   xa_zero(t0);
   xa_zero(t1);
   xa_zero(t2);
   unsigned f0 = 0u, f1 = 0u, f2 = 0u;
   if (i < G.nx && j < G.ny) {
-    View2<const double> US{us, usld}, VS{vs, usld};
-    View2<const double> U{u, G.lds}, V{v, G.lds}, P{p, G.lds};
+    View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
+    View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds}, P{D.pi, G.lds};
     double d = div_coherent_at(US, VS, j, i, G.g);
     xa_term_prod(d, d, t0, f0);
-    double lr = SUB(apply_A<0>(P, j, i, G.g), b[(long)j * G.ld + i]);
+    double lr = SUB(apply_A<0>(P, j, i, G.g), D.b[(long)j * G.ld + i]);
     xa_term_prod(lr, lr, t1, f1);
     double c = div_central_at(U, V, j, i, G.nx, G.ny, 1.0, 1.0);
     xa_term_prod(c, c, t2, f2);
@@ -536,11 +560,18 @@ __global__ void __launch_bounds__(NT) k_post_diag(Geo64 G, const double* __restr
   reduce_terms(&slots[S_LINRES], &t1, 1, f1, sacc1, wred, ired);
   reduce_terms(&slots[S_CONT], &t2, 1, f2, sacc2, wred, ired);
   XASlot* sl[3] = {&slots[S_DIVAFTER], &slots[S_LINRES], &slots[S_CONT]};
-  xa_finish(sl, 3, gridDim.x * gridDim.y);
+  xa_finish(sl, 3, D.nt_pc);
 }
 
-__global__ void k_gather(const XASlot* slots, const Ctrl64* ctrl, StepOut64* out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// one StepOut64 record per instance
+__global__ void k_gather(const InstDesc* __restrict__ ID, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const InstDesc& Dd = ID[k];
+  if (!Dd.active) return;
+  const XASlot* slots = Dd.slots;
+  const Ctrl64* ctrl = Dd.ctrl;
+  StepOut64* out = Dd.out;
   out->umax = ctrl->umax;
   out->vmax = ctrl->vmax;
   out->div_before = ctrl->div_before;
@@ -571,99 +602,168 @@ static long round_up(long a, long m) { return (a + m - 1) / m * m; }
 
 static Spacing make_spacing(double h) { return spacing_for(h); }
 
-struct Instance64 {
-  pfgb_params P;
+// tiles of height th covering an nx x ny grid of instance k
+static void add_tiles(std::vector<Tile>& v, int k, int nx, int ny, int th) {
+  for (int j0 = 0; j0 < ny; j0 += th)
+    for (int i0 = 0; i0 < nx; i0 += TX) v.push_back(Tile{k, i0, j0, 0});
+}
+
+static int count_tiles(int nx, int ny, int th) { return ((nx + TX - 1) / TX) * ((ny + th - 1) / th); }
+
+static Geo64 make_geo(int nx, int ny, long ld, double dx, double dy, double invd, int jacobi) {
   Geo64 G;
-  CGArgs A;
-  DtArgs D;
-  LidArgs L;
+  G.nx = nx;
+  G.ny = ny;
+  G.ld = ld;
+  G.lds = nx + 2;
+  G.g.nx = nx;
+  G.g.ny = ny;
+  G.g.sx = make_spacing(dx);
+  G.g.sy = make_spacing(dy);
+  G.invd = invd;
+  G.jacobi = jacobi;
+  return G;
+}
+
+// A batch of n independent cavity instances (n = 1 for a single cavity).
+struct Instance64 {
+  int n = 0;
+  std::vector<pfgb_params> P;
+  std::vector<InstDesc> hd;          // host copy of the descriptors
+  InstDesc* dd = nullptr;            // device descriptors
+  Tile* tpc = nullptr;               // per-cell tiles (32 x 8)
+  Tile* tcg = nullptr;               // CG tiles (32 x 16)
+  int ntpc = 0, ntcg = 0;
+  LoopCtl* lc = nullptr;
+  int maxiter_max = 0;
   char* ws = nullptr;
-  double *us, *vs, *b, *x, *r, *p[2], *q;
-  XASlot* slots;
-  Ctrl64* ctrl;
-  StepIn* in_d;
-  StepIn* in_h = nullptr;     // pinned staging of the per-step inputs
-  StepOut64* out_d;
+  size_t ws_bytes = 0;
+  StepIn* in_d = nullptr;
+  StepIn* in_h = nullptr;            // pinned staging of the per-step inputs
+  StepOut64* out_d = nullptr;
   StepOut64* out_h = nullptr;
-  // mixed-precision pressure solve (precision 1)
+  bool desc_dirty = true;
+  // mixed-precision pressure solve (precision 1, single instance)
   mixed::Solver* mix = nullptr;
   // the whole step as one CUDA graph (CG loop = WHILE conditional node)
   int use_graph = 1;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  const double* g_u = nullptr;
-  const double* g_v = nullptr;
-  const double* g_p = nullptr;
-  // optional per-launch timing of k_cg_matvec (benchmark roofline)
+  int graph_mode = -1;               // 0 step, 1 projection
+  // optional per-launch timing of k_cg_matvec (benchmark roofline, single instance)
   int profiling = 0;
   std::vector<cudaEvent_t> ev;
   int ev_used = 0;
 };
 
-int instance64_create(const pfgb_params* prm, Instance64** out) {
+static int validate_params(const pfgb_params* prm) {
   if (prm->nx < 2 || prm->ny < 2) return set_error(PFGB_EINVAL, "nx and ny must be >= 2 (the reference's central divergence indexes two columns and rows)");
   if (prm->nx > (1 << 20) || prm->ny > (1 << 20)) return set_error(PFGB_EINVAL, "grid side above 2^20");
   if (!(prm->dx > 0.0) || !(prm->dy > 0.0)) return set_error(PFGB_EINVAL, "dx and dy must be positive");
+  if (prm->lin_maxiter < 0) return set_error(PFGB_EINVAL, "lin_maxiter must be >= 0");
+  return PFGB_OK;
+}
+
+int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
+  if (n < 1) return set_error(PFGB_EINVAL, "batch size must be >= 1");
+  for (int k = 0; k < n; ++k)
+    if (int rc = validate_params(&prms[k])) return rc;
+  for (int k = 0; k < n; ++k)
+    if (prms[k].precision == 1 && n > 1) return set_error(PFGB_EINVAL, "mixed precision runs one instance per handle");
   Instance64* I = new Instance64();
-  I->P = *prm;
-  Geo64& G = I->G;
-  G.nx = prm->nx;
-  G.ny = prm->ny;
-  G.ld = round_up(prm->nx, 32);
-  G.lds = prm->nx + 2;
-  G.g.nx = prm->nx;
-  G.g.ny = prm->ny;
-  G.g.sx = make_spacing(prm->dx);
-  G.g.sy = make_spacing(prm->dy);
-  G.invd = prm->jacobi_interior;
-  G.jacobi = prm->enable_jacobi;
-  I->A.rtol = prm->lin_tol;
-  I->A.maxiter = prm->lin_maxiter;
-  I->A.n_cells = (double)prm->nx * (double)prm->ny;
-  I->D.dx = prm->dx;
-  I->D.dy = prm->dy;
-  I->D.cfl_target = prm->cfl_target;
-  I->D.growth = prm->cfl_growth;
-  I->D.nu = prm->nu;
-  I->L.has_lid = prm->has_lid;
-  I->L.lid = prm->lid_velocity;
-  size_t vec = (size_t)G.ld * G.ny * sizeof(double);
-  size_t bytes = 8 * vec + S_COUNT * sizeof(XASlot) + sizeof(Ctrl64) + sizeof(StepIn) + sizeof(StepOut64) + 2048;
+  I->n = n;
+  I->P.assign(prms, prms + n);
+  I->hd.resize(n);
+  // workspace layout: per instance 8 vectors + slots + ctrl; then descriptors, tiles, loop control, in/out
+  std::vector<size_t> vec(n);
+  size_t bytes = 0;
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  std::vector<Tile> tpc, tcg;
+  for (int k = 0; k < n; ++k) {
+    const long ld = round_up(prms[k].nx, 32);
+    vec[k] = up((size_t)ld * prms[k].ny * sizeof(double));
+    bytes += 8 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64));
+    add_tiles(tpc, k, prms[k].nx, prms[k].ny, PB_Y);
+    add_tiles(tcg, k, prms[k].nx, prms[k].ny, TY);
+    I->maxiter_max = std::max(I->maxiter_max, prms[k].lin_maxiter);
+  }
+  I->ntpc = (int)tpc.size();
+  I->ntcg = (int)tcg.size();
+  bytes += up(n * sizeof(InstDesc)) + up(tpc.size() * sizeof(Tile)) + up(tcg.size() * sizeof(Tile)) +
+           up(sizeof(LoopCtl)) + up(n * sizeof(StepIn)) + up(n * sizeof(StepOut64));
   if (cudaMalloc(&I->ws, bytes) != cudaSuccess) {
     delete I;
-    return set_error(PFGB_ECUDA, "cudaMalloc of the workspace failed");
+    return set_error(PFGB_ENOMEM, "cudaMalloc of the workspace failed");
   }
+  I->ws_bytes = bytes;
   if (cudaMemset(I->ws, 0, bytes) != cudaSuccess) {
     cudaFree(I->ws);
     delete I;
     return set_error(PFGB_ECUDA, "cudaMemset of the workspace failed");
   }
   char* c = I->ws;
-  auto take = [&](size_t n) { char* r = c; c += (n + 255) / 256 * 256; return r; };
-  I->us = (double*)take(vec);
-  I->vs = (double*)take(vec);
-  I->b = (double*)take(vec);
-  I->x = (double*)take(vec);
-  I->r = (double*)take(vec);
-  I->p[0] = (double*)take(vec);
-  I->p[1] = (double*)take(vec);
-  I->q = (double*)take(vec);
-  I->slots = (XASlot*)take(S_COUNT * sizeof(XASlot));
-  I->ctrl = (Ctrl64*)take(sizeof(Ctrl64));
-  I->in_d = (StepIn*)take(sizeof(StepIn));
-  I->out_d = (StepOut64*)take(sizeof(StepOut64));
-  if (cudaMallocHost(&I->out_h, sizeof(StepOut64)) != cudaSuccess ||
-      cudaMallocHost(&I->in_h, sizeof(StepIn)) != cudaSuccess) {
-    cudaFree(I->ws);
-    delete I;
-    return set_error(PFGB_ECUDA, "cudaMallocHost failed");
+  auto take = [&](size_t b) { char* r = c; c += up(b); return r; };
+  for (int k = 0; k < n; ++k) {
+    const pfgb_params& prm = prms[k];
+    InstDesc& D = I->hd[k];
+    const long ld = round_up(prm.nx, 32);
+    D.G = make_geo(prm.nx, prm.ny, ld, prm.dx, prm.dy, prm.jacobi_interior, prm.enable_jacobi);
+    D.A.rtol = prm.lin_tol;
+    D.A.maxiter = prm.lin_maxiter;
+    D.A.n_cells = (double)prm.nx * (double)prm.ny;
+    D.D.dx = prm.dx;
+    D.D.dy = prm.dy;
+    D.D.cfl_target = prm.cfl_target;
+    D.D.growth = prm.cfl_growth;
+    D.D.nu = prm.nu;
+    D.L.has_lid = prm.has_lid;
+    D.L.lid = prm.lid_velocity;
+    D.scheme = prm.scheme;
+    D.adjust = 1;
+    D.mode = 0;
+    D.active = 1;
+    D.ui = D.vi = D.pi = nullptr;
+    D.us = (double*)take(vec[k]);
+    D.vs = (double*)take(vec[k]);
+    D.usld = ld;
+    D.b = (double*)take(vec[k]);
+    D.x = (double*)take(vec[k]);
+    D.r = (double*)take(vec[k]);
+    D.p0 = (double*)take(vec[k]);
+    D.p1 = (double*)take(vec[k]);
+    D.q = (double*)take(vec[k]);
+    D.slots = (XASlot*)take(S_COUNT * sizeof(XASlot));
+    D.ctrl = (Ctrl64*)take(sizeof(Ctrl64));
+    D.nt_pc = count_tiles(prm.nx, prm.ny, PB_Y);
+    D.nt_cg = count_tiles(prm.nx, prm.ny, TY);
   }
-  if (prm->precision == 1) {
-    const double tol_out = prm->mixed_tol_outer > 0.0 ? prm->mixed_tol_outer : prm->lin_tol;
-    const double tol_in = prm->mixed_tol_inner > 0.0 ? prm->mixed_tol_inner : 1e-5;
-    const int mo = prm->mixed_max_outer > 0 ? prm->mixed_max_outer : 8;
-    const int mi = prm->mixed_max_inner > 0 ? prm->mixed_max_inner : 50;
-    int rc = mixed::solver_create(prm->nx, prm->ny, prm->dx, prm->dy, G.ld, tol_out, tol_in, mo, mi, &I->mix);
+  I->dd = (InstDesc*)take(n * sizeof(InstDesc));
+  I->tpc = (Tile*)take(tpc.size() * sizeof(Tile));
+  I->tcg = (Tile*)take(tcg.size() * sizeof(Tile));
+  I->lc = (LoopCtl*)take(sizeof(LoopCtl));
+  I->in_d = (StepIn*)take(n * sizeof(StepIn));
+  I->out_d = (StepOut64*)take(n * sizeof(StepOut64));
+  for (int k = 0; k < n; ++k) {
+    I->hd[k].in = I->in_d + k;
+    I->hd[k].out = I->out_d + k;
+  }
+  cudaError_t e = cudaMemcpy(I->tpc, tpc.data(), tpc.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(I->tcg, tcg.data(), tcg.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+  LoopCtl lc0 = {0, 0, I->maxiter_max + 1, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(I->lc, &lc0, sizeof(LoopCtl), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMallocHost(&I->out_h, n * sizeof(StepOut64));
+  if (e == cudaSuccess) e = cudaMallocHost(&I->in_h, n * sizeof(StepIn));
+  if (e != cudaSuccess) {
+    instance64_destroy(I);
+    return set_error(PFGB_ECUDA, std::string("batch set-up: ") + cudaGetErrorString(e));
+  }
+  if (prms[0].precision == 1) {
+    const pfgb_params& prm = prms[0];
+    const double tol_out = prm.mixed_tol_outer > 0.0 ? prm.mixed_tol_outer : prm.lin_tol;
+    const double tol_in = prm.mixed_tol_inner > 0.0 ? prm.mixed_tol_inner : 1e-5;
+    const int mo = prm.mixed_max_outer > 0 ? prm.mixed_max_outer : 8;
+    const int mi = prm.mixed_max_inner > 0 ? prm.mixed_max_inner : 50;
+    int rc = mixed::solver_create(prm.nx, prm.ny, prm.dx, prm.dy, I->hd[0].G.ld, tol_out, tol_in, mo, mi, &I->mix);
     if (rc) {
       instance64_destroy(I);
       return rc;
@@ -672,6 +772,8 @@ int instance64_create(const pfgb_params* prm, Instance64** out) {
   *out = I;
   return PFGB_OK;
 }
+
+int instance64_create(const pfgb_params* prm, Instance64** out) { return instance64_create_batch(prm, 1, out); }
 
 void instance64_destroy(Instance64* I) {
   if (!I) return;
@@ -686,54 +788,85 @@ void instance64_destroy(Instance64* I) {
 }
 
 size_t instance64_workspace_bytes(const Instance64* I) {
-  size_t vec = (size_t)I->G.ld * I->G.ny * sizeof(double);
-  return 8 * vec + S_COUNT * sizeof(XASlot) + sizeof(Ctrl64) + sizeof(StepIn) + sizeof(StepOut64) + 2048;
+  return I->ws_bytes + (I->mix ? I->mix->ws_bytes : 0);
 }
 
-// Projection stage on u*, v* (pitch usld): RHS, CG, pin, correction, diagnostics.
-static void enqueue_projection(Instance64* I, const Geo64& G, int mode, double* us, double* vs, long usld,
-                               double* ui, double* vi, double* pi, cudaStream_t s) {
-  dim3 gp((G.nx + TX - 1) / TX, (G.ny + PB_Y - 1) / PB_Y);
-  dim3 gc((G.nx + TX - 1) / TX, (G.ny + TY - 1) / TY);
-  k_rhs<<<gp, NT, 0, s>>>(G, us, vs, usld, I->b, I->slots, I->ctrl);
-  k_cg_init<<<gp, NT, 0, s>>>(G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, 0ull, 0);
-  for (int k = 0; k < I->A.maxiter; ++k) {
+int instance64_count(const Instance64* I) { return I->n; }
+
+// Point instance k at its state arrays and mark the descriptors for upload.
+static int bind_state(Instance64* I, int k, double* u, double* v, double* p, long lds, int mode, int active) {
+  InstDesc& D = I->hd[k];
+  if (active && lds != D.G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
+  double* ui = active ? u + lds + 1 : nullptr;   // interior pointers of the ghosted state arrays
+  double* vi = active ? v + lds + 1 : nullptr;
+  double* pi = active ? p + lds + 1 : nullptr;
+  double* us = mode == 0 ? D.us : ui;            // projection only: correct the state in place
+  double* vs = mode == 0 ? D.vs : vi;
+  const long usld = mode == 0 ? D.G.ld : lds;
+  if (D.ui != ui || D.vi != vi || D.pi != pi || D.mode != mode || D.active != active || D.usld != usld ||
+      (mode == 1 && (D.us != us || D.vs != vs))) {
+    D.ui = ui;
+    D.vi = vi;
+    D.pi = pi;
+    D.mode = mode;
+    D.active = active;
+    if (mode == 1) {
+      D.us = us;
+      D.vs = vs;
+    }
+    D.usld = usld;
+    I->desc_dirty = true;
+  }
+  return PFGB_OK;
+}
+
+static int upload_desc(Instance64* I, cudaStream_t s) {
+  if (!I->desc_dirty) return PFGB_OK;
+  cudaError_t e = cudaMemcpyAsync(I->dd, I->hd.data(), I->n * sizeof(InstDesc), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("descriptor upload: ") + cudaGetErrorString(e));
+  // the host array may change before the copy runs: wait for it
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("descriptor upload: ") + cudaGetErrorString(e));
+  I->desc_dirty = false;
+  return PFGB_OK;
+}
+
+__global__ void k_loop_reset(LoopCtl* lc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    lc->active = 0;
+    lc->guard = 0;
+    lc->tripped = 0;
+  }
+}
+
+// Direct launches of the projection stage (host loop bound = largest maxiter).
+static void enqueue_projection(Instance64* I, cudaStream_t s) {
+  k_rhs<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  k_cg_init<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc, nullptr);
+  for (int k = 0; k < I->maxiter_max; ++k) {
     const bool timed = I->profiling && (size_t)(2 * k + 1) < I->ev.size();
     if (timed) cudaEventRecord(I->ev[2 * k], s);
-    k_cg_matvec<0><<<gc, NT, 0, s>>>(G, I->r, I->p[0], I->p[1], I->q, I->slots, I->ctrl);
+    k_cg_matvec<0><<<I->ntcg, NT, 0, s>>>(I->dd, I->tcg);
     if (timed) {
       cudaEventRecord(I->ev[2 * k + 1], s);
       I->ev_used = k + 1;
     }
-    k_cg_update<<<gc, NT, 0, s>>>(G, I->A, I->p[0], I->p[1], I->q, I->x, I->r, I->slots, I->ctrl, 0ull, 0);
+    k_cg_update<<<I->ntcg, NT, 0, s>>>(I->dd, I->tcg, nullptr, 0ull, 0);
   }
-  k_post_resid<0><<<gp, NT, 0, s>>>(G, I->b, I->x, I->slots);
-  k_pin_correct<<<gp, NT, 0, s>>>(G, I->L, mode, I->x, us, vs, usld, ui, vi, pi, I->slots, I->ctrl);
-  k_post_diag<<<gp, NT, 0, s>>>(G, us, vs, usld, I->b, ui, vi, pi, I->slots);
-  k_gather<<<1, 32, 0, s>>>(I->slots, I->ctrl, I->out_d);
+  k_post_resid<0><<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  k_pin_correct<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  k_post_diag<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
 }
 
-// Enqueue the whole step on `s` (no host synchronisation).
-int instance64_enqueue(Instance64* I, double* u, double* v, double* p, long lds, const StepIn& in, cudaStream_t s) {
-  const Geo64& G = I->G;
-  if (lds != G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
-  double* ui = u + lds + 1;   // interior pointers of the ghosted state arrays
-  double* vi = v + lds + 1;
-  double* pi = p + lds + 1;
-  dim3 gp((G.nx + TX - 1) / TX, (G.ny + PB_Y - 1) / PB_Y);
-  *I->in_h = in;
-  cudaMemcpyAsync(I->in_d, I->in_h, sizeof(StepIn), cudaMemcpyHostToDevice, s);
-  k_prestep<<<gp, NT, 0, s>>>(G, ui, vi, I->slots, I->ctrl);
-  k_dt<<<1, 32, 0, s>>>(I->D, I->in_d, I->ctrl);
-  k_predict<<<gp, NT, 0, s>>>(G, ui, vi, I->us, I->vs, I->P.scheme, I->ctrl);
-  enqueue_projection(I, G, 0, I->us, I->vs, G.ld, ui, vi, pi, s);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
-  return PFGB_OK;
+static void enqueue_prologue(Instance64* I, cudaStream_t s) {
+  k_prestep<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  k_dt<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
+  k_predict<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
 }
 
-// Build the step graph for the given state arrays.
-static int build_step_graph(Instance64* I, double* ui, double* vi, double* pi) {
+// Build the step graph (mode 0: full step; mode 1: stand-alone projection).
+static int build_graph(Instance64* I, int mode) {
   if (I->exec) {
     cudaGraphExecDestroy(I->exec);
     I->exec = nullptr;
@@ -744,47 +877,44 @@ static int build_step_graph(Instance64* I, double* ui, double* vi, double* pi) {
   }
   cudaError_t e = cudaGraphCreate(&I->graph, 0);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("cudaGraphCreate: ") + cudaGetErrorString(e));
-  const Geo64& G = I->G;
-  dim3 gp((G.nx + TX - 1) / TX, (G.ny + PB_Y - 1) / PB_Y);
-  dim3 gc((G.nx + TX - 1) / TX, (G.ny + TY - 1) / TY);
+  const dim3 gp(I->ntpc), gc(I->ntcg), g1((I->n + 31) / 32);
   GraphChain c(I->graph);
-  c.kernel(k_prestep, gp, dim3(NT), G, (const double*)ui, (const double*)vi, I->slots, I->ctrl);
-  c.kernel(k_dt, dim3(1), dim3(32), I->D, (const StepIn*)I->in_d, I->ctrl);
-  c.kernel(k_predict, gp, dim3(NT), G, (const double*)ui, (const double*)vi, I->us, I->vs, I->P.scheme,
-           (const Ctrl64*)I->ctrl);
-  c.kernel(k_rhs, gp, dim3(NT), G, (const double*)I->us, (const double*)I->vs, G.ld, I->b, I->slots,
-           (const Ctrl64*)I->ctrl);
-  cudaGraphConditionalHandle cond = 0;
+  if (mode == 0) {
+    c.kernel(k_prestep, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+    c.kernel(k_dt, g1, dim3(32), (const InstDesc*)I->dd, I->n);
+    c.kernel(k_predict, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  }
+  c.kernel(k_rhs, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   GraphChain body(nullptr);
   if (I->mix) {
     // b is finished (mean removed, b[0] = 0) by the CG init; the refinement solves A x = b
-    c.kernel(k_cg_init, gp, dim3(NT), G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, cond, 0);
-    if (int rc = mixed::append_solve(c, I->mix, I->b, I->x, I->ctrl, I->A.maxiter)) return rc;
+    c.kernel(k_cg_init, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc, (LoopCtl*)nullptr);
+    const InstDesc& D0 = I->hd[0];
+    if (int rc = mixed::append_solve(c, I->mix, D0.b, D0.x, D0.ctrl, D0.A.maxiter)) return rc;
   } else {
+    cudaGraphConditionalHandle cond = 0;
     // every conditional handle must belong to a conditional node: create it only here
-    e = cudaGraphConditionalHandleCreate(&cond, I->graph, 1u, cudaGraphCondAssignDefault);
+    e = cudaGraphConditionalHandleCreate(&cond, I->graph, 0u, cudaGraphCondAssignDefault);
     if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("conditional handle: ") + cudaGetErrorString(e));
-    c.kernel(k_cg_init, gp, dim3(NT), G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, cond, 1);
+    c.kernel(k_loop_reset, dim3(1), dim3(32), I->lc);
+    c.kernel(k_cg_init, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc, I->lc);
+    c.kernel(k_loop_arm, dim3(1), dim3(32), I->lc, cond, 1);
     body = c.while_loop_with(cond);
-    body.kernel(k_cg_matvec<0>, gc, dim3(NT), G, (const double*)I->r, I->p[0], I->p[1], I->q, I->slots, I->ctrl);
-    body.kernel(k_cg_update, gc, dim3(NT), G, I->A, (const double*)I->p[0], (const double*)I->p[1],
-                (const double*)I->q, I->x, I->r, I->slots, I->ctrl, cond, 1);
+    body.kernel(k_cg_matvec<0>, gc, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tcg);
+    body.kernel(k_cg_update, gc, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tcg, I->lc, cond, 1);
+    body.kernel(k_loop_guard, dim3(1), dim3(32), I->lc, cond, 1);
   }
-  c.kernel(k_post_resid<0>, gp, dim3(NT), G, (const double*)I->b, (const double*)I->x, I->slots);
-  c.kernel(k_pin_correct, gp, dim3(NT), G, I->L, 0, (const double*)I->x, I->us, I->vs, G.ld, ui, vi, pi, I->slots,
-           I->ctrl);
-  c.kernel(k_post_diag, gp, dim3(NT), G, (const double*)I->us, (const double*)I->vs, G.ld, (const double*)I->b,
-           (const double*)ui, (const double*)vi, (const double*)pi, I->slots);
-  c.kernel(k_gather, dim3(1), dim3(32), (const XASlot*)I->slots, (const Ctrl64*)I->ctrl, I->out_d);
+  c.kernel(k_post_resid<0>, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  c.kernel(k_pin_correct, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  c.kernel(k_post_diag, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  c.kernel(k_gather, g1, dim3(32), (const InstDesc*)I->dd, I->n);
   if (c.status() != cudaSuccess || (!I->mix && body.status() != cudaSuccess)) {
     cudaError_t be = c.status() != cudaSuccess ? c.status() : body.status();
     return set_error(PFGB_ECUDA, std::string("building the step graph: ") + cudaGetErrorString(be));
   }
   e = cudaGraphInstantiate(&I->exec, I->graph, 0);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-  I->g_u = ui;
-  I->g_v = vi;
-  I->g_p = pi;
+  I->graph_mode = mode;
   return PFGB_OK;
 }
 
@@ -811,75 +941,77 @@ static void copy_out(const StepOut64& o, pfgb_step_out* out) {
 }
 
 static int read_out(Instance64* I, cudaStream_t s, pfgb_step_out* out) {
-  cudaError_t e = cudaMemcpyAsync(I->out_h, I->out_d, sizeof(StepOut64), cudaMemcpyDeviceToHost, s);
+  cudaError_t e = cudaMemcpyAsync(I->out_h, I->out_d, I->n * sizeof(StepOut64), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("step failed: ") + cudaGetErrorString(e));
-  copy_out(*I->out_h, out);
+  LoopCtl lc;
+  if (!I->mix && I->use_graph && !I->profiling) {
+    e = cudaMemcpy(&lc, I->lc, sizeof(LoopCtl), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && lc.tripped)
+      return set_error(PFGB_ESTATE, "the CG loop guard stopped the step (an instance did not report completion)");
+  }
+  for (int k = 0; k < I->n; ++k)
+    if (I->hd[k].active) copy_out(I->out_h[k], &out[k]);
   return PFGB_OK;
 }
 
-// Stand-alone projection (solve_pressure_poisson, normal mode) on the state.
-int instance64_project(Instance64* I, double* u, double* v, double* p, long lds, double dt, cudaStream_t s,
-                       pfgb_step_out* out) {
-  if (I->mix) return set_error(PFGB_ESTATE, "pfgb_project runs the binary64 path only");
-  const Geo64& G = I->G;
-  if (lds != G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
-  double* ui = u + lds + 1;
-  double* vi = v + lds + 1;
-  double* pi = p + lds + 1;
-  k_set_dt<<<1, 32, 0, s>>>(dt, I->ctrl);
-  enqueue_projection(I, G, 1, ui, vi, lds, ui, vi, pi, s);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
-  return read_out(I, s, out);
-}
-
-// Mixed-precision step with direct launches (host loop control).
-static int mixed_step_direct(Instance64* I, double* u, double* v, double* p, long lds, const StepIn& in,
-                             cudaStream_t s, pfgb_step_out* out) {
-  const Geo64& G = I->G;
-  if (lds != G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
-  double* ui = u + lds + 1;
-  double* vi = v + lds + 1;
-  double* pi = p + lds + 1;
-  dim3 gp((G.nx + TX - 1) / TX, (G.ny + PB_Y - 1) / PB_Y);
-  *I->in_h = in;
-  cudaMemcpyAsync(I->in_d, I->in_h, sizeof(StepIn), cudaMemcpyHostToDevice, s);
-  k_prestep<<<gp, NT, 0, s>>>(G, ui, vi, I->slots, I->ctrl);
-  k_dt<<<1, 32, 0, s>>>(I->D, I->in_d, I->ctrl);
-  k_predict<<<gp, NT, 0, s>>>(G, ui, vi, I->us, I->vs, I->P.scheme, I->ctrl);
-  k_rhs<<<gp, NT, 0, s>>>(G, I->us, I->vs, G.ld, I->b, I->slots, I->ctrl);
-  k_cg_init<<<gp, NT, 0, s>>>(G, I->A, 1, I->b, I->r, I->x, I->slots, I->ctrl, 0ull, 0);
-  if (int rc = mixed::run_direct(I->mix, I->b, I->x, I->ctrl, I->A.maxiter, s)) return rc;
-  k_post_resid<0><<<gp, NT, 0, s>>>(G, I->b, I->x, I->slots);
-  k_pin_correct<<<gp, NT, 0, s>>>(G, I->L, 0, I->x, I->us, I->vs, G.ld, ui, vi, pi, I->slots, I->ctrl);
-  k_post_diag<<<gp, NT, 0, s>>>(G, I->us, I->vs, G.ld, I->b, ui, vi, pi, I->slots);
-  k_gather<<<1, 32, 0, s>>>(I->slots, I->ctrl, I->out_d);
-  cudaError_t e = cudaGetLastError();
+// Run one step (mode 0) or projection (mode 1) for the bound instances.
+static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
+  if (int rc = upload_desc(I, s)) return rc;
+  cudaError_t e = cudaMemcpyAsync(I->in_d, I->in_h, I->n * sizeof(StepIn), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("step input upload: ") + cudaGetErrorString(e));
+  if (I->use_graph && !I->profiling) {
+    if (!I->exec || I->graph_mode != mode)
+      if (int rc = build_graph(I, mode)) return rc;
+    e = cudaGraphLaunch(I->exec, s);
+    if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+    return read_out(I, s, out);
+  }
+  if (mode == 0) enqueue_prologue(I, s);
+  if (I->mix) {
+    const InstDesc& D0 = I->hd[0];
+    k_rhs<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_cg_init<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc, nullptr);
+    if (int rc = mixed::run_direct(I->mix, D0.b, D0.x, D0.ctrl, D0.A.maxiter, s)) return rc;
+    k_post_resid<0><<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_pin_correct<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_post_diag<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
+  } else {
+    enqueue_projection(I, s);
+  }
+  e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
   return read_out(I, s, out);
 }
 
 int instance64_step(Instance64* I, double* u, double* v, double* p, long lds, const StepIn& in, cudaStream_t s,
                     pfgb_step_out* out) {
-  if (I->mix && (!I->use_graph || I->profiling)) return mixed_step_direct(I, u, v, p, lds, in, s, out);
-  if (I->use_graph && !I->profiling) {
-    if (lds != I->G.lds) return set_error(PFGB_EINVAL, "state pitch must be nx + 2");
-    double* ui = u + lds + 1;
-    double* vi = v + lds + 1;
-    double* pi = p + lds + 1;
-    if (!I->exec || I->g_u != ui || I->g_v != vi || I->g_p != pi) {
-      if (int rc = build_step_graph(I, ui, vi, pi)) return rc;
-    }
-    *I->in_h = in;
-    cudaError_t e = cudaMemcpyAsync(I->in_d, I->in_h, sizeof(StepIn), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaGraphLaunch(I->exec, s);
-    if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("graph launch: ") + cudaGetErrorString(e));
-    return read_out(I, s, out);
+  if (int rc = bind_state(I, 0, u, v, p, lds, 0, 1)) return rc;
+  I->in_h[0] = in;
+  return run(I, 0, s, out);
+}
+
+// Batch step: instance k uses us[k]... (null u[k] leaves instance k out of this step).
+int instance64_batch_step(Instance64* I, double* const* u, double* const* v, double* const* p, const StepIn* in,
+                          cudaStream_t s, pfgb_step_out* out) {
+  for (int k = 0; k < I->n; ++k) {
+    const int act = (u[k] && v[k] && p[k]) ? 1 : 0;
+    if (int rc = bind_state(I, k, u[k], v[k], p[k], I->hd[k].G.lds, 0, act)) return rc;
+    I->in_h[k] = in[k];
   }
-  int rc = instance64_enqueue(I, u, v, p, lds, in, s);
-  if (rc) return rc;
-  return read_out(I, s, out);
+  return run(I, 0, s, out);
+}
+
+// Stand-alone projection (solve_pressure_poisson, normal mode) on the state.
+int instance64_project(Instance64* I, double* u, double* v, double* p, long lds, double dt, cudaStream_t s,
+                       pfgb_step_out* out) {
+  if (I->mix) return set_error(PFGB_ESTATE, "pfgb_project runs the binary64 path only");
+  if (I->n != 1) return set_error(PFGB_ESTATE, "pfgb_project takes a single-instance handle");
+  if (int rc = bind_state(I, 0, u, v, p, lds, 1, 1)) return rc;
+  if (int rc = upload_desc(I, s)) return rc;
+  k_set_dt<<<1, 32, 0, s>>>(I->dd, dt);
+  return run(I, 1, s, out);
 }
 
 int instance64_set_graph(Instance64* I, int on) {
@@ -887,10 +1019,10 @@ int instance64_set_graph(Instance64* I, int on) {
   return PFGB_OK;
 }
 
-// Per-launch timing of the matvec kernel in the following steps.
+// Per-launch timing of the matvec kernel in the following steps (single instance).
 int instance64_set_profiling(Instance64* I, int on) {
   if (on && I->ev.empty()) {
-    int n = 2 * (I->A.maxiter > 0 ? I->A.maxiter : 1);
+    int n = 2 * (I->maxiter_max > 0 ? I->maxiter_max : 1);
     I->ev.resize(n);
     for (int k = 0; k < n; ++k)
       if (cudaEventCreate(&I->ev[k]) != cudaSuccess) return set_error(PFGB_ECUDA, "cudaEventCreate failed");
@@ -958,53 +1090,81 @@ int probe_fp64(cudaStream_t s, double* tops) {
 
 // ---------------------------------------------------------------------------
 // Operator-interface CG (x0 = 0) on contiguous vectors of nx*ny doubles.
+// tiles of one instance written on the device (no host allocation)
+__global__ void k_fill_tiles(Tile* t, int nx, int ny, int th) {
+  const int ntx = (nx + TX - 1) / TX, nty = (ny + th - 1) / th;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ntx * nty; k += gridDim.x * blockDim.x)
+    t[k] = Tile{0, (k % ntx) * TX, (k / ntx) * th, 0};
+}
+
+// Descriptor of the one-instance operator-interface solve (b and x contiguous).
+static InstDesc op_solve_desc(const double* b, double* x, int nx, int ny, double dx, double dy, int precond,
+                              double invd, double tol, int maxiter, double* r, double* p0, double* p1, double* q,
+                              XASlot* slots, Ctrl64* ctrl) {
+  InstDesc D = {};
+  D.G = make_geo(nx, ny, nx, dx, dy, invd, precond);
+  D.A.rtol = tol;
+  D.A.maxiter = maxiter;
+  D.A.n_cells = (double)nx * (double)ny;
+  D.adjust = 0;
+  D.mode = 1;
+  D.active = 1;
+  D.b = const_cast<double*>(b);
+  D.x = x;
+  D.r = r;
+  D.p0 = p0;
+  D.p1 = p1;
+  D.q = q;
+  D.slots = slots;
+  D.ctrl = ctrl;
+  D.nt_pc = count_tiles(nx, ny, PB_Y);
+  D.nt_cg = count_tiles(nx, ny, TY);
+  return D;
+}
+
+static void op_solve_launch(int op, const InstDesc* dd, const Tile* tpc, int ntpc, const Tile* tcg, int ntcg,
+                            int maxiter, cudaStream_t s) {
+  k_cg_init<<<ntpc, NT, 0, s>>>(dd, tpc, nullptr);
+  for (int k = 0; k < maxiter; ++k) {
+    if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
+      k_cg_matvec<0><<<ntcg, NT, 0, s>>>(dd, tcg);
+    else
+      k_cg_matvec<1><<<ntcg, NT, 0, s>>>(dd, tcg);
+    k_cg_update<<<ntcg, NT, 0, s>>>(dd, tcg, nullptr, 0ull, 0);
+  }
+  if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
+    k_post_resid<0><<<ntpc, NT, 0, s>>>(dd, tpc);
+  else
+    k_post_resid<1><<<ntpc, NT, 0, s>>>(dd, tpc);
+}
+
 int cg_solve_run(int op, const double* b, double* x, int nx, int ny, double dx, double dy, int precond,
                  double invd, double tol, int maxiter, cudaStream_t s, pfgb_solve_out* out) {
   if (nx < 2 || ny < 2) return set_error(PFGB_EINVAL, "nx and ny must be >= 2");
   if (op != PFGB_OP_NEG_LAPLACIAN_PINNED && op != PFGB_OP_LAPLACIAN_DIRICHLET) return set_error(PFGB_EINVAL, "unknown operator");
   if (maxiter < 0) return set_error(PFGB_EINVAL, "maxiter must be >= 0");
-  Geo64 G;
-  G.nx = nx;
-  G.ny = ny;
-  G.ld = nx;
-  G.lds = nx + 2;
-  G.g.nx = nx;
-  G.g.ny = ny;
-  G.g.sx = make_spacing(dx);
-  G.g.sy = make_spacing(dy);
-  G.invd = invd;
-  G.jacobi = precond;
-  CGArgs A;
-  A.rtol = tol;
-  A.maxiter = maxiter;
-  A.n_cells = (double)nx * (double)ny;
-  size_t vec = (size_t)nx * ny * sizeof(double);
-  size_t vecr = (vec + 255) / 256 * 256;
-  size_t bytes = 4 * vecr + S_COUNT * sizeof(XASlot) + 256 + sizeof(Ctrl64) + 256;
+  const int ntpc = count_tiles(nx, ny, PB_Y), ntcg = count_tiles(nx, ny, TY);
+  auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+  const size_t vecr = up((size_t)nx * ny * sizeof(double));
+  const size_t o_slots = 4 * vecr, o_ctrl = o_slots + up(S_COUNT * sizeof(XASlot));
+  const size_t o_desc = o_ctrl + up(sizeof(Ctrl64)), o_tpc = o_desc + up(sizeof(InstDesc));
+  const size_t o_tcg = o_tpc + up(ntpc * sizeof(Tile)), bytes = o_tcg + up(ntcg * sizeof(Tile));
   char* ws = nullptr;
   cudaError_t e = cudaMallocAsync(&ws, bytes, s);
   if (e != cudaSuccess) return set_error(PFGB_ENOMEM, "cudaMallocAsync of the CG workspace failed");
-  cudaMemsetAsync(ws, 0, bytes, s);
-  double* r = (double*)ws;
-  double* p0 = (double*)(ws + vecr);
-  double* p1 = (double*)(ws + 2 * vecr);
-  double* q = (double*)(ws + 3 * vecr);
-  XASlot* slots = (XASlot*)(ws + 4 * vecr);
-  Ctrl64* ctrl = (Ctrl64*)(ws + 4 * vecr + ((S_COUNT * sizeof(XASlot) + 255) / 256 * 256));
-  dim3 gp((nx + TX - 1) / TX, (ny + PB_Y - 1) / PB_Y);
-  dim3 gc((nx + TX - 1) / TX, (ny + TY - 1) / TY);
-  k_cg_init<<<gp, NT, 0, s>>>(G, A, 0, const_cast<double*>(b), r, x, slots, ctrl, 0ull, 0);
-  for (int k = 0; k < maxiter; ++k) {
-    if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
-      k_cg_matvec<0><<<gc, NT, 0, s>>>(G, r, p0, p1, q, slots, ctrl);
-    else
-      k_cg_matvec<1><<<gc, NT, 0, s>>>(G, r, p0, p1, q, slots, ctrl);
-    k_cg_update<<<gc, NT, 0, s>>>(G, A, p0, p1, q, x, r, slots, ctrl, 0ull, 0);
-  }
-  if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
-    k_post_resid<0><<<gp, NT, 0, s>>>(G, b, x, slots);
-  else
-    k_post_resid<1><<<gp, NT, 0, s>>>(G, b, x, slots);
+  cudaMemsetAsync(ws, 0, o_desc, s);
+  XASlot* slots = (XASlot*)(ws + o_slots);
+  Ctrl64* ctrl = (Ctrl64*)(ws + o_ctrl);
+  InstDesc* dd = (InstDesc*)(ws + o_desc);
+  Tile* tpc = (Tile*)(ws + o_tpc);
+  Tile* tcg = (Tile*)(ws + o_tcg);
+  const InstDesc hd = op_solve_desc(b, x, nx, ny, dx, dy, precond, invd, tol, maxiter, (double*)ws,
+                                    (double*)(ws + vecr), (double*)(ws + 2 * vecr), (double*)(ws + 3 * vecr), slots,
+                                    ctrl);
+  cudaMemcpyAsync(dd, &hd, sizeof(InstDesc), cudaMemcpyHostToDevice, s);
+  k_fill_tiles<<<64, 256, 0, s>>>(tpc, nx, ny, PB_Y);
+  k_fill_tiles<<<64, 256, 0, s>>>(tcg, nx, ny, TY);
+  op_solve_launch(op, dd, tpc, ntpc, tcg, ntcg, maxiter, s);
   Ctrl64 hc;
   double res2 = 0.0;
   e = cudaGetLastError();
@@ -1034,10 +1194,12 @@ namespace pfgb {
 // control block of the CG live in one file-scope device array of fixed size,
 // reserved once when the library's module is loaded on a device and held until
 // the process exits.  Its limit is NOALLOC_MAX_CELLS = 262,144 cells
-// (512 x 512), about 8.4 MiB per device.
+// (512 x 512), about 9 MiB per device.
 namespace noalloc {
 
 constexpr long NOALLOC_MAX_CELLS = 1L << 18;
+
+constexpr int NOALLOC_MAX_TILES = 32768;   // per-cell plus CG tiles of one grid
 
 struct Scratch {
   double r[NOALLOC_MAX_CELLS];
@@ -1046,6 +1208,8 @@ struct Scratch {
   double q[NOALLOC_MAX_CELLS];
   XASlot slots[S_COUNT];
   Ctrl64 ctrl;
+  InstDesc desc;
+  Tile tiles[NOALLOC_MAX_TILES];
 };
 
 static __device__ __align__(256) Scratch g_scratch;
@@ -1082,42 +1246,23 @@ int cg_solve_noalloc_run(int op, const double* b, double* x, int nx, int ny, dou
     return set_error(PFGB_EINVAL, "nx*ny exceeds the 262144-cell limit of the allocation-free CG scratch");
   if (op != PFGB_OP_NEG_LAPLACIAN_PINNED && op != PFGB_OP_LAPLACIAN_DIRICHLET) return set_error(PFGB_EINVAL, "unknown operator");
   if (maxiter < 0) return set_error(PFGB_EINVAL, "maxiter must be >= 0");
+  const int ntpc = count_tiles(nx, ny, PB_Y), ntcg = count_tiles(nx, ny, TY);
+  if (ntpc + ntcg > NOALLOC_MAX_TILES)
+    return set_error(PFGB_EINVAL, "grid shape needs more tiles than the allocation-free CG scratch holds");
   Scratch* S = nullptr;
   if (int rc = scratch_address(&S)) return rc;
-  Geo64 G;
-  G.nx = nx;
-  G.ny = ny;
-  G.ld = nx;
-  G.lds = nx + 2;
-  G.g.nx = nx;
-  G.g.ny = ny;
-  G.g.sx = make_spacing(dx);
-  G.g.sy = make_spacing(dy);
-  G.invd = invd;
-  G.jacobi = precond;
-  CGArgs A;
-  A.rtol = tol;
-  A.maxiter = maxiter;
-  A.n_cells = (double)nx * (double)ny;
   // the slots and the control block must start from zero on every call
   cudaError_t e = cudaMemsetAsync(S->slots, 0, sizeof(S->slots) + sizeof(S->ctrl), s);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("clearing the CG scratch: ") + cudaGetErrorString(e));
   XASlot* slots = S->slots;
   Ctrl64* ctrl = &S->ctrl;
-  dim3 gp((nx + TX - 1) / TX, (ny + PB_Y - 1) / PB_Y);
-  dim3 gc((nx + TX - 1) / TX, (ny + TY - 1) / TY);
-  k_cg_init<<<gp, NT, 0, s>>>(G, A, 0, const_cast<double*>(b), S->r, x, slots, ctrl, 0ull, 0);
-  for (int k = 0; k < maxiter; ++k) {
-    if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
-      k_cg_matvec<0><<<gc, NT, 0, s>>>(G, S->r, S->p0, S->p1, S->q, slots, ctrl);
-    else
-      k_cg_matvec<1><<<gc, NT, 0, s>>>(G, S->r, S->p0, S->p1, S->q, slots, ctrl);
-    k_cg_update<<<gc, NT, 0, s>>>(G, A, S->p0, S->p1, S->q, x, S->r, slots, ctrl, 0ull, 0);
-  }
-  if (op == PFGB_OP_NEG_LAPLACIAN_PINNED)
-    k_post_resid<0><<<gp, NT, 0, s>>>(G, b, x, slots);
-  else
-    k_post_resid<1><<<gp, NT, 0, s>>>(G, b, x, slots);
+  const InstDesc hd = op_solve_desc(b, x, nx, ny, dx, dy, precond, invd, tol, maxiter, S->r, S->p0, S->p1, S->q,
+                                    slots, ctrl);
+  // the descriptor goes through a host stack copy: no allocation
+  cudaMemcpyAsync(&S->desc, &hd, sizeof(InstDesc), cudaMemcpyHostToDevice, s);
+  k_fill_tiles<<<64, 256, 0, s>>>(S->tiles, nx, ny, PB_Y);
+  k_fill_tiles<<<64, 256, 0, s>>>(S->tiles + ntpc, nx, ny, TY);
+  op_solve_launch(op, &S->desc, S->tiles, ntpc, S->tiles + ntpc, ntcg, maxiter, s);
   Ctrl64 hc;
   double res2 = 0.0;
   e = cudaGetLastError();

@@ -1,7 +1,11 @@
-// Plain binary64 projection step: device structures shared by the kernels and
-// the host driver of one cavity instance.
+// Binary64 projection step: device structures shared by the kernels and the
+// host driver.  Kernels work on a *batch* of independent cavity instances:
+// every CTA reads its tile (instance, origin) from a tile table and that
+// instance's descriptor from an instance table; a single cavity is a batch of
+// one.
 #pragma once
 #include "common.cuh"
+#include "stencil.cuh"
 #include "xacc.cuh"
 
 namespace pfgb {
@@ -55,6 +59,66 @@ struct StepOut64 {
   double divstar2, bnrm2, res2, ru2, rv2, divafter2, linres2, cont2;
   unsigned flags_or;    // OR of the result flags of all slots (inexact / overflow diagnostics)
   int refine_passes;
+};
+
+struct Geo64 {
+  int nx, ny;
+  long ld;            // pitch of the work vectors (doubles)
+  long lds;           // pitch of the state arrays (nx + 2)
+  Grid2 g;
+  double invd;        // interior Jacobi entry 1/(2/dx^2 + 2/dy^2)
+  int jacobi;
+};
+
+struct CGArgs {
+  double rtol;
+  int maxiter;
+  double n_cells;     // N as a double (exact)
+};
+
+struct DtArgs {
+  double dx, dy, cfl_target, growth, nu;
+};
+
+struct LidArgs {
+  int has_lid;
+  double lid;
+};
+
+// One tile of work: instance index and the tile's first cell.
+struct Tile {
+  int inst, i0, j0, pad;
+};
+
+// Everything the kernels need about one instance.
+struct InstDesc {
+  Geo64 G;
+  CGArgs A;
+  DtArgs D;
+  LidArgs L;
+  int scheme;          // advection scheme of the predictor
+  int adjust;          // 1: projection RHS (mean removal, b[0] = 0); 0: b as given
+  int mode;            // correction: 0 full step (lid, residuals), 1 projection only
+  int active;          // 0: the instance sits out this launch (all its kernels return)
+  double *ui, *vi, *pi;        // state interiors (pitch G.lds)
+  double *us, *vs;             // u*, v* (pitch usld)
+  long usld;
+  double *b, *x, *r, *p0, *p1, *q;
+  XASlot* slots;
+  Ctrl64* ctrl;
+  const StepIn* in;
+  StepOut64* out;
+  int nt_pc, nt_cg;            // this instance's tiles in the per-cell / CG tile tables
+};
+
+// Batch-wide loop control of a WHILE node: the number of instances still
+// iterating, and a guard that stops the loop after guard_max trips whatever
+// the instances report.
+struct LoopCtl {
+  int active;
+  int guard;
+  int guard_max;
+  int tripped;
 };
 
 }  // namespace pfgb
