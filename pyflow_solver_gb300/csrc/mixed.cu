@@ -208,9 +208,10 @@ __global__ void __launch_bounds__(1024) k_mg_coarse(Lvl C, int sweeps, float ome
 }
 
 // Levels of at most 64 x 64 cells run inside one CTA: all of them live in
-// shared memory and two V-cycles (the same smoother, restriction and
-// prolongation as the global levels, Jacobi sweeps on the bottom level) form
-// the coarse "solve" -- a fixed linear, symmetric operator, as PCG requires.
+// shared memory and one V-cycle (the same smoother, restriction and
+// prolongation as the global levels, eight Jacobi sweeps on the bottom level)
+// forms the coarse "solve" -- a fixed linear, symmetric operator, as PCG
+// requires.  More cycles or sweeps do not lower the PCG iteration count.
 constexpr int CT = 1024;                     // threads of the coarse CTA
 constexpr int CMAX = 4096;                   // cells of its finest level
 
@@ -747,7 +748,7 @@ static void add_vcycle(GraphChain& c, Solver* S, const float omega) {
     c.kernel(k_mg_restrict, dim3((C.nx + BX - 1) / BX, (C.ny + BY - 1) / BY), dim3(MT), F, C);
   }
   const Lvl& Cc = S->lev[L];
-  c.kernel_smem(k_mg_coarse_cycles, dim3(1), dim3(CT), S->coarse_smem, Cc, S->coarse_levels, 2, 32, omega);
+  c.kernel_smem(k_mg_coarse_cycles, dim3(1), dim3(CT), S->coarse_smem, Cc, S->coarse_levels, 1, 8, omega);
   for (int l = L - 1; l >= 0; --l) {
     const Lvl& F = S->lev[l];
     const Lvl& C = S->lev[l + 1];
@@ -798,7 +799,7 @@ static void launch_vcycle(Solver* S, float omega, cudaStream_t s) {
     k_mg_pre<<<dim3((F.nx + BX - 1) / BX, (F.ny + BY - 1) / BY), MT, 0, s>>>(F, omega);
     k_mg_restrict<<<dim3((C.nx + BX - 1) / BX, (C.ny + BY - 1) / BY), MT, 0, s>>>(F, C);
   }
-  k_mg_coarse_cycles<<<1, CT, S->coarse_smem, s>>>(S->lev[L], S->coarse_levels, 2, 32, omega);
+  k_mg_coarse_cycles<<<1, CT, S->coarse_smem, s>>>(S->lev[L], S->coarse_levels, 1, 8, omega);
   for (int l = L - 1; l >= 0; --l) {
     const Lvl& F = S->lev[l];
     const Lvl& C = S->lev[l + 1];

@@ -65,28 +65,27 @@ def step_params(config, nx: int, ny: int):
     return P, dx, dy, nu
 
 
-def step(config, state, tracker, iteration: int) -> tuple[Any, dict[str, float], dict[str, Any]]:
-    require_cuda()
-    diagnostics_enabled = getattr(config, "diagnostics", True)
+def prepare(config, state, iteration: int):
+    """Parameters and per-step inputs of one instance (reads state.meta, not modified)."""
     nx, ny = int(state.nx), int(state.ny)
     P, dx, dy, nu = step_params(config, nx, ny)
-    if diagnostics_enabled:
-        print(f"[Step {iteration}] Grid: nx={nx}, ny={ny}, dx={dx:.4g}, dy={dy:.4g}, Re={getattr(config, 'Re', 100.0)}")
-    dt_prev = float(state.meta.get("dt_prev", 1e-2))
-    hist = state.meta.get("divergence_history", [])
     sin = _capi.StepIn()
-    sin.dt_prev = dt_prev
-    tail = [float(h) for h in hist[-5:]]
+    sin.dt_prev = float(state.meta.get("dt_prev", 1e-2))
+    tail = [float(h) for h in state.meta.get("divergence_history", [])[-5:]]
     for k, h in enumerate(tail):
         sin.hist[k] = h
     sin.hist_len = len(tail)
     sin.iteration = int(iteration)
-    inst = instance_for(state, P)
-    out = _capi.StepOut()
-    with device_fields(state) as (u, v, p):
-        _capi.check(_capi.load().pfgb_step(inst.handle, ptr(u), ptr(v), ptr(p), nx + 2, sin, stream_handle(), out),
-                    "pfgb_step")
+    return P, sin, (dx, dy, nu)
+
+
+def finish(config, state, tracker, iteration: int, P, geo, out):
+    """Form the reference's residual / diagnostic dicts and state.meta from a step record."""
+    dx, dy, nu = geo
+    nx, ny = int(state.nx), int(state.ny)
+    diagnostics_enabled = getattr(config, "diagnostics", True)
     dt = out.dt
+    hist = state.meta.get("divergence_history", [])
     hist.append(out.div_before)
     hist = hist[-5:]
     state.meta["divergence_history"] = hist
@@ -156,4 +155,20 @@ def step(config, state, tracker, iteration: int) -> tuple[Any, dict[str, float],
         assert continuity <= max(1e3, divergence_norm * 10)
         p0 = float(state.fields["p"][1, 1])
         assert abs(p0) < 1e-10, "Invariant failed: reference pressure cell not ~0"
+    return residuals, diagnostics
+
+
+def step(config, state, tracker, iteration: int) -> tuple[Any, dict[str, float], dict[str, Any]]:
+    require_cuda()
+    nx, ny = int(state.nx), int(state.ny)
+    P, sin, geo = prepare(config, state, iteration)
+    if getattr(config, "diagnostics", True):
+        print(f"[Step {iteration}] Grid: nx={nx}, ny={ny}, dx={geo[0]:.4g}, dy={geo[1]:.4g}, "
+              f"Re={getattr(config, 'Re', 100.0)}")
+    inst = instance_for(state, P)
+    out = _capi.StepOut()
+    with device_fields(state) as (u, v, p):
+        _capi.check(_capi.load().pfgb_step(inst.handle, ptr(u), ptr(v), ptr(p), nx + 2, sin, stream_handle(), out),
+                    "pfgb_step")
+    residuals, diagnostics = finish(config, state, tracker, iteration, P, geo, out)
     return state, residuals, diagnostics
