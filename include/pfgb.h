@@ -136,7 +136,7 @@ PFGB_API int pfgb_step(pfgb_handle* handle, double* u, double* v, double* p, lon
 
 /* ---- batches of independent cavities ----------------------------------- */
 
-/* n instances (params[k] each, binary64: precision 0) advanced together: every
+/* n instances (params[k] each; all with the same precision) advanced together: every
  * kernel of a step covers the tiles of all instances (one CUDA graph launch
  * per step, CG loop as one WHILE node with per-instance convergence masks).
  * Same per-instance semantics as pfgb_step (src/pyflow/solvers/solver.py:15-121

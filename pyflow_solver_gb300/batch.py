@@ -34,9 +34,9 @@ class BatchedCavities:
         self._geo = []
         for k, (cfg, st) in enumerate(zip(self.configs, self.states)):
             P, _, geo = prepare(cfg, st, 0)
-            if P.precision != 0:
-                raise ValueError("batches run the binary64 path (precision 'fp64')")
             params[k] = P
+            if P.precision != params[0].precision:
+                raise ValueError("all instances of a batch share one precision")
             self._geo.append(geo)
         self._params = params
         h = ctypes.c_void_p()

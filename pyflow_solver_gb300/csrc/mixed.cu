@@ -83,13 +83,32 @@ __device__ __forceinline__ float rweight(int d, int I, int nc) {
 }
 
 // ---- V-cycle kernels -------------------------------------------------------
+//
+// Every kernel takes the instance table and a tile table; a CTA returns when
+// its instance sits the step out or has left the loop the kernel belongs to
+// (gate 0: the refinement loop, gate 1: the inner PCG loop).
+
+__device__ __forceinline__ bool mx_live(const MixDesc& M, int gate) {
+  if (!*M.active) return false;
+  const MixCtrl* c = M.ctrl;
+  if (*(volatile const int*)&c->outer_done) return false;
+  return gate == 0 || !*(volatile const int*)&c->inner_done;
+}
+
+#define MX_TILE(gate)                                      \
+  const MTile tl = TL[blockIdx.x];                         \
+  const MixDesc& M = MD[tl.inst];                          \
+  if (!mx_live(M, gate)) return;
 
 // two damped-Jacobi sweeps from u = 0: t = S(S(0)) for A u = f, and the
 // residual r = f - A t of the tile
-__global__ void __launch_bounds__(MT) k_mg_pre(Lvl L, float omega) {
+__global__ void __launch_bounds__(MT) k_mg_pre(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
+                                                int gate, float omega) {
+  MX_TILE(gate)
+  const Lvl L = M.lev[l];
   __shared__ float s1[BY + 4][BX + 4];
   __shared__ float s2[BY + 2][BX + 2];
-  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+  const int i0 = tl.i0, j0 = tl.j0;
   for (int idx = threadIdx.x; idx < (BY + 4) * (BX + 4); idx += MT) {
     int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
     int gj = j0 + jj, gi = i0 + ii;
@@ -121,9 +140,12 @@ __global__ void __launch_bounds__(MT) k_mg_pre(Lvl L, float omega) {
   }
 }
 
-// f_C = P^T r: each coarse cell gathers the residual of a 4 x 4 fine patch
-__global__ void __launch_bounds__(MT) k_mg_restrict(Lvl F, Lvl C) {
-  const int I = blockIdx.x * BX + (threadIdx.x & 31), J = blockIdx.y * BY + (threadIdx.x >> 5);
+// f_{l+1} = P^T r_l: each coarse cell gathers the residual of a 4 x 4 fine patch
+__global__ void __launch_bounds__(MT) k_mg_restrict(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
+                                                     int l, int gate) {
+  MX_TILE(gate)
+  const Lvl F = M.lev[l], C = M.lev[l + 1];
+  const int I = tl.i0 + (threadIdx.x & 31), J = tl.j0 + (threadIdx.x >> 5);
   if (I >= C.nx || J >= C.ny) return;
   float s = 0.f;
 #pragma unroll
@@ -143,11 +165,14 @@ __global__ void __launch_bounds__(MT) k_mg_restrict(Lvl F, Lvl C) {
   C.f[(long)J * C.ld + I] = s;
 }
 
-// u = S(S(t + P u_C)) with the bilinear P
-__global__ void __launch_bounds__(MT) k_mg_post(Lvl F, Lvl C, float omega) {
+// u_l = S(S(t_l + P u_{l+1})) with the bilinear P
+__global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
+                                                 int gate, float omega) {
+  MX_TILE(gate)
+  const Lvl F = M.lev[l], C = M.lev[l + 1];
   __shared__ float w0[BY + 4][BX + 4];
   __shared__ float w1[BY + 2][BX + 2];
-  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+  const int i0 = tl.i0, j0 = tl.j0;
   for (int idx = threadIdx.x; idx < (BY + 4) * (BX + 4); idx += MT) {
     int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
     int gj = j0 + jj, gi = i0 + ii;
@@ -178,37 +203,8 @@ __global__ void __launch_bounds__(MT) k_mg_post(Lvl F, Lvl C, float omega) {
   }
 }
 
-// coarsest grid: `sweeps` damped-Jacobi sweeps from zero in one CTA
-__global__ void __launch_bounds__(1024) k_mg_coarse(Lvl C, int sweeps, float omega) {
-  __shared__ float ua[1024], ub[1024], fs[1024];
-  const int n = C.nx * C.ny;
-  const int c = threadIdx.x;
-  const int j = c / C.nx, i = c % C.nx;
-  const bool in = c < n;
-  float d = 1.f;
-  if (in) {
-    fs[c] = C.f[(long)j * C.ld + i];
-    d = mg_diag(C, j, i);
-    ua[c] = 0.f;
-  }
-  __syncthreads();
-  float* src = ua;
-  float* dst = ub;
-  for (int s = 0; s < sweeps; ++s) {
-    if (in) {
-      auto at = [&](int jj, int ii) { return src[jj * C.nx + ii]; };
-      dst[c] = (1.f - omega) * src[c] + omega * (fs[c] + mg_nsum(C, j, i, at)) / d;
-    }
-    __syncthreads();
-    float* tmp = src;
-    src = dst;
-    dst = tmp;
-  }
-  if (in) C.u[(long)j * C.ld + i] = src[c];
-}
-
-// Levels of at most 64 x 64 cells run inside one CTA: all of them live in
-// shared memory and one V-cycle (the same smoother, restriction and
+// Levels of at most 64 x 64 cells run inside one CTA per instance: all of them
+// live in shared memory and one V-cycle (the same smoother, restriction and
 // prolongation as the global levels, eight Jacobi sweeps on the bottom level)
 // forms the coarse "solve" -- a fixed linear, symmetric operator, as PCG
 // requires.  More cycles or sweeps do not lower the PCG iteration count.
@@ -249,20 +245,23 @@ __device__ __forceinline__ void c_sweep(const CLvl& L, const float* f, const flo
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(CT) k_mg_coarse_cycles(Lvl C, int nl, int cycles, int bottom_sweeps, float omega) {
+__global__ void __launch_bounds__(CT) k_mg_coarse_cycles(const MixDesc* __restrict__ MD, int gate, int cycles,
+                                                          int bottom_sweeps, float omega) {
+  const MixDesc& M = MD[blockIdx.x];
+  if (!mx_live(M, gate)) return;
+  const Lvl C = M.lev[M.nlev - 1];
+  const int nl = M.coarse_levels;
   extern __shared__ float sm[];
-  // level table (nl <= 8), arrays f, u, t of total `tot` cells each
   CLvl L[8];
   int tot = 0;
   {
     int nx = C.nx, ny = C.ny;
-    float cx = C.cx, cy = C.cy;
     for (int l = 0; l < nl; ++l) {
       L[l].nx = nx;
       L[l].ny = ny;
       L[l].off = tot;
-      L[l].cx = cx;
-      L[l].cy = cy;
+      L[l].cx = C.cx;
+      L[l].cy = C.cy;
       tot += nx * ny;
       nx /= 2;
       ny /= 2;
@@ -271,6 +270,8 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(Lvl C, int nl, int cycl
   float* f = sm;
   float* u = sm + tot;
   float* t = sm + 2 * tot;
+  float* e = sm + 3 * tot;
+  float* w = sm + 4 * tot;
   const int n0 = C.nx * C.ny;
   for (int c = threadIdx.x; c < n0; c += CT) {
     const int j = c / C.nx, i = c - j * C.nx;
@@ -280,7 +281,6 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(Lvl C, int nl, int cycl
   __syncthreads();
   // x_{k+1} = x_k + V(f - A x_k): the first cycle starts from zero
   for (int cyc = 0; cyc < cycles; ++cyc) {
-    // residual of the current iterate on level 0 goes into t[level 0]
     {
       const CLvl& L0 = L[0];
       for (int c = threadIdx.x; c < n0; c += CT) {
@@ -289,24 +289,14 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(Lvl C, int nl, int cycl
       }
       __syncthreads();
     }
-    // V-cycle on the correction, with right-hand side t[level 0]; the level
-    // RHS array of the cycle is `f` for coarser levels and t for level 0, so
-    // copy the level-0 residual into a scratch slot: reuse f of level 0 after
-    // saving it in u?  Keep it simple: the cycle works on arrays rh (RHS),
-    // e (correction) and w (work) laid over t, and over u's coarse slots.
-    float* rh = t;     // level 0 RHS = residual; coarser RHS written below
-    // the correction of every level lives in the spare shared arrays after tot*3
-    float* e = sm + 3 * tot;
-    float* w = sm + 4 * tot;
+    float* rh = t;     // right-hand side of every level (level 0: the residual)
     for (int l = 0; l < nl; ++l) {
       const CLvl& Lv = L[l];
       const int n = Lv.nx * Lv.ny;
       if (l == nl - 1) {
         for (int c = threadIdx.x; c < n; c += CT) e[Lv.off + c] = 0.f;
         __syncthreads();
-        for (int s = 0; s < bottom_sweeps; ++s) {
-          c_sweep(Lv, rh, (s & 1) ? w : e, (s & 1) ? e : w, omega);
-        }
+        for (int s = 0; s < bottom_sweeps; ++s) c_sweep(Lv, rh, (s & 1) ? w : e, (s & 1) ? e : w, omega);
         if (bottom_sweeps & 1) {
           for (int c = threadIdx.x; c < n; c += CT) e[Lv.off + c] = w[Lv.off + c];
           __syncthreads();
@@ -398,90 +388,136 @@ __device__ __forceinline__ void mx_reduce(XASlot* slot, const XTerm* t, int nt, 
   __shared__ long long name[XA_DIGITS];         \
   for (int k_ = threadIdx.x; k_ < XA_DIGITS; k_ += blockDim.x) name[k_] = 0;
 
-// x = 0, r64 = b; ||b||^2 and sum(b)
-__global__ void __launch_bounds__(MT) k_mx_init(Geo G, const double* __restrict__ b, double* __restrict__ x,
-                                                 double* __restrict__ r64, XASlot* slots, MixCtrl* ctrl,
-                                                 cudaGraphConditionalHandle cond_outer, int use_cond) {
+// x = 0, r64 = b; ||b||^2 and sum(b); counts the instances that refine
+__global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
+                                                 MixLoop* ml) {
+  const MTile tl = TL[blockIdx.x];
+  const MixDesc& M = MD[tl.inst];
+  if (!*M.active) return;
   MX_SMEM_SLOT(sa0);
   MX_SMEM_SLOT(sa1);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
-  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  const Geo G = M.G;
+  XASlot* slots = M.slots;
+  MixCtrl* ctrl = M.ctrl;
+  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
   XTerm t0, t1;
   xa_zero(t0);
   xa_zero(t1);
   unsigned f0 = 0u, f1 = 0u;
   if (i < G.nx && j < G.ny) {
     const long o = (long)j * G.ld + i;
-    const double bv = b[o];
-    x[o] = 0.0;
-    r64[o] = bv;
+    const double bv = M.b[o];
+    M.x[o] = 0.0;
+    M.r64[o] = bv;
     xa_term_prod(bv, bv, t0, f0);
     xa_term_val(bv, t1, f1);
   }
   mx_reduce(&slots[M_RR64], &t0, 1, f0, sa0, wred, ired);
   mx_reduce(&slots[M_SUM64], &t1, 1, f1, sa1, wred, ired);
   XASlot* sl[2] = {&slots[M_RR64], &slots[M_SUM64]};
-  if (xa_finish(sl, 2, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 2, M.nt0) && threadIdx.x == 0) {
     const double bb = slots[M_RR64].result;
     ctrl->bnorm = __dsqrt_rn(bb);
     ctrl->tol_abs_out = __dmul_rn(ctrl->tol_out, ctrl->bnorm);
     ctrl->rr64 = bb;
     ctrl->sum64 = slots[M_SUM64].result;
     ctrl->outer = 0;
+    ctrl->inner = 0;
     ctrl->inner_total = 0;
+    ctrl->inner_done = 1;
     ctrl->converged = (bb == 0.0) ? 1 : 0;
     ctrl->outer_done = (bb == 0.0) ? 1 : 0;
-    if (use_cond) cudaGraphSetConditional(cond_outer, bb == 0.0 ? 0u : 1u);
+    if (bb != 0.0) atomicAdd(&ml->outer_active, 1);
+  }
+}
+
+__global__ void k_ml_reset(MixLoop* ml, int which) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (which == 0) {
+    ml->outer_active = 0;
+    ml->guard_o = 0;
+    ml->tripped = 0;
+  } else {
+    ml->inner_active = 0;
+    ml->guard_i = 0;
+  }
+}
+
+// condition of a loop = some instance still in it
+__global__ void k_ml_arm(MixLoop* ml, int which, cudaGraphConditionalHandle cond, int use_cond) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int a = which == 0 ? ml->outer_active : ml->inner_active;
+  if (use_cond) cudaGraphSetConditional(cond, a > 0 ? 1u : 0u);
+}
+
+// last node of a loop body: stops the loop after its trip bound whatever the instances report
+__global__ void k_ml_guard(MixLoop* ml, int which, cudaGraphConditionalHandle cond, int use_cond) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int g = which == 0 ? ++ml->guard_o : ++ml->guard_i;
+  const int gmax = which == 0 ? ml->gmax_o : ml->gmax_i;
+  const int a = which == 0 ? ml->outer_active : ml->inner_active;
+  if (g >= gmax && a > 0) {
+    ml->tripped = 1;
+    if (use_cond) cudaGraphSetConditional(cond, 0u);
   }
 }
 
 // r~ = float(r64) with r~_0 = -sum_{k != 0} r64_k; e = 0; ||r~||^2; starts an inner solve
-__global__ void __launch_bounds__(MT) k_mx_prep(Geo G, Lvl L0, const double* __restrict__ r64, float* __restrict__ e,
-                                                 XASlot* slots, MixCtrl* ctrl, cudaGraphConditionalHandle cond_inner,
-                                                 int use_cond) {
+__global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
+                                                 MixLoop* ml) {
+  MX_TILE(0)
   MX_SMEM_SLOT(sa0);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
-  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  const Geo G = M.G;
+  const Lvl L0 = M.lev[0];
+  XASlot* slots = M.slots;
+  MixCtrl* ctrl = M.ctrl;
+  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
   XTerm t0;
   xa_zero(t0);
   unsigned f0 = 0u;
   if (i < G.nx && j < G.ny) {
-    const double rv = (i == 0 && j == 0) ? -__dsub_rn(ctrl->sum64, r64[0]) : r64[(long)j * G.ld + i];
+    const double rv = (i == 0 && j == 0) ? -__dsub_rn(ctrl->sum64, M.r64[0]) : M.r64[(long)j * G.ld + i];
     const float rf = __double2float_rn(rv);
     L0.f[(long)j * L0.ld + i] = rf;
-    e[(long)j * L0.ld + i] = 0.f;
+    M.e[(long)j * L0.ld + i] = 0.f;
     xa_term_prod_f32(rf, rf, t0, f0);
   }
   mx_reduce(&slots[M_RT], &t0, 1, f0, sa0, wred, ired);
   XASlot* sl[1] = {&slots[M_RT]};
-  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 1, M.nt0) && threadIdx.x == 0) {
     const double rt = __dsqrt_rn(slots[M_RT].result);
     ctrl->rt_norm = rt;
     ctrl->tol_abs_in = __dmul_rn(ctrl->tol_in, rt);
     ctrl->inner = 0;
     ctrl->inner_done = rt > 0.0 ? 0 : 1;
-    if (use_cond) cudaGraphSetConditional(cond_inner, rt > 0.0 ? 1u : 0u);
+    if (rt > 0.0) atomicAdd(&ml->inner_active, 1);
   }
 }
 
 // rho = r.z (exact); beta = rho / rho_prev after the first inner iteration
-__global__ void __launch_bounds__(MT) k_mx_rz(Lvl L0, const float* __restrict__ z, XASlot* slots, MixCtrl* ctrl) {
+__global__ void __launch_bounds__(MT) k_mx_rz(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
+  MX_TILE(1)
   MX_SMEM_SLOT(sa0);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
-  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  const Lvl L0 = M.lev[0];
+  XASlot* slots = M.slots;
+  MixCtrl* ctrl = M.ctrl;
+  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
   XTerm t0;
   xa_zero(t0);
   unsigned f0 = 0u;
   if (i < L0.nx && j < L0.ny) {
     const long o = (long)j * L0.ld + i;
-    xa_term_prod_f32(L0.f[o], z[o], t0, f0);
+    xa_term_prod_f32(L0.f[o], L0.u[o], t0, f0);
   }
   mx_reduce(&slots[M_RZ], &t0, 1, f0, sa0, wred, ired);
   XASlot* sl[1] = {&slots[M_RZ]};
-  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 1, M.nt0) && threadIdx.x == 0) {
     const double rz = slots[M_RZ].result;
     if (ctrl->inner > 0) ctrl->beta = __ddiv_rn(rz, ctrl->rho);
     ctrl->rho = rz;
@@ -489,17 +525,21 @@ __global__ void __launch_bounds__(MT) k_mx_rz(Lvl L0, const float* __restrict__ 
 }
 
 // p_new = z (first) or z + beta p_old; q = A p_new (binary32 Neumann operator); p.q
-__global__ void __launch_bounds__(MT) k_mx_matvec(Lvl L0, const float* __restrict__ z, float* p0, float* p1,
-                                                   float* __restrict__ q, XASlot* slots, MixCtrl* ctrl) {
+__global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
+  MX_TILE(1)
   __shared__ float pn[BY + 2][BX + 2];
   MX_SMEM_SLOT(sa0);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
+  const Lvl L0 = M.lev[0];
+  XASlot* slots = M.slots;
+  MixCtrl* ctrl = M.ctrl;
+  const float* __restrict__ z = L0.u;
   const int k = *(volatile int*)&ctrl->inner;
-  const float* __restrict__ pold = (k & 1) ? p1 : p0;
-  float* __restrict__ pnew = (k & 1) ? p0 : p1;
+  const float* __restrict__ pold = (k & 1) ? M.p1 : M.p0;
+  float* __restrict__ pnew = (k & 1) ? M.p0 : M.p1;
   const float beta = (float)ctrl->beta;
-  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+  const int i0 = tl.i0, j0 = tl.j0;
   for (int idx = threadIdx.x; idx < (BY + 2) * (BX + 2); idx += MT) {
     int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
     int gj = j0 + jj, gi = i0 + ii;
@@ -522,12 +562,12 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(Lvl L0, const float* __restric
     const float qv = mg_diag(L0, gj, gi) * pv - mg_nsum(L0, gj, gi, at);
     const long o = (long)gj * L0.ld + gi;
     pnew[o] = pv;
-    q[o] = qv;
+    M.q[o] = qv;
     xa_term_prod_f32(pv, qv, t0, f0);
   }
   mx_reduce(&slots[M_PQ], &t0, 1, f0, sa0, wred, ired);
   XASlot* sl[1] = {&slots[M_PQ]};
-  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 1, M.nt0) && threadIdx.x == 0) {
     const double pq = slots[M_PQ].result;
     ctrl->pq = pq;
     ctrl->alpha = __ddiv_rn(ctrl->rho, pq);
@@ -535,29 +575,32 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(Lvl L0, const float* __restric
 }
 
 // e += alpha p; r -= alpha q; ||r||^2 and the inner stopping test
-__global__ void __launch_bounds__(MT) k_mx_update(Lvl L0, const float* p0, const float* p1, const float* __restrict__ q,
-                                                   float* __restrict__ e, XASlot* slots, MixCtrl* ctrl,
-                                                   cudaGraphConditionalHandle cond_inner, int use_cond) {
+__global__ void __launch_bounds__(MT) k_mx_update(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
+                                                   MixLoop* ml, cudaGraphConditionalHandle cond_inner, int use_cond) {
+  MX_TILE(1)
   MX_SMEM_SLOT(sa0);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
+  const Lvl L0 = M.lev[0];
+  XASlot* slots = M.slots;
+  MixCtrl* ctrl = M.ctrl;
   const int k = *(volatile int*)&ctrl->inner;
-  const float* __restrict__ p = (k & 1) ? p0 : p1;
+  const float* __restrict__ p = (k & 1) ? M.p0 : M.p1;
   const float alpha = (float)ctrl->alpha;
-  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
   XTerm t0;
   xa_zero(t0);
   unsigned f0 = 0u;
   if (i < L0.nx && j < L0.ny) {
     const long o = (long)j * L0.ld + i;
-    e[o] = fmaf(alpha, p[o], e[o]);
-    const float rv = fmaf(-alpha, q[o], L0.f[o]);
+    M.e[o] = fmaf(alpha, p[o], M.e[o]);
+    const float rv = fmaf(-alpha, M.q[o], L0.f[o]);
     L0.f[o] = rv;
     xa_term_prod_f32(rv, rv, t0, f0);
   }
   mx_reduce(&slots[M_RR], &t0, 1, f0, sa0, wred, ired);
   XASlot* sl[1] = {&slots[M_RR]};
-  if (xa_finish(sl, 1, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 1, M.nt0) && threadIdx.x == 0) {
     const double rr = slots[M_RR].result;
     const int it = k + 1;
     ctrl->inner = it;
@@ -565,46 +608,52 @@ __global__ void __launch_bounds__(MT) k_mx_update(Lvl L0, const float* p0, const
     ctrl->rr_in = rr;
     if (!(__dsqrt_rn(rr) > ctrl->tol_abs_in) || it >= ctrl->max_inner) {
       ctrl->inner_done = 1;
-      if (use_cond) cudaGraphSetConditional(cond_inner, 0u);
+      if (atomicSub(&ml->inner_active, 1) == 1 && use_cond) cudaGraphSetConditional(cond_inner, 0u);
     }
   }
 }
 
 // x += e - e[0] (binary64)
-__global__ void __launch_bounds__(MT) k_mx_correct(Geo G, long lde, const float* __restrict__ e, double* __restrict__ x) {
-  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+__global__ void __launch_bounds__(MT) k_mx_correct(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
+  MX_TILE(0)
+  const Geo G = M.G;
+  const long lde = M.lev[0].ld;
+  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
   if (i >= G.nx || j >= G.ny) return;
-  const double e0 = (double)e[0];
+  const double e0 = (double)M.e[0];
   const long o = (long)j * G.ld + i;
-  x[o] = __dadd_rn(x[o], __dsub_rn((double)e[(long)j * lde + i], e0));
+  M.x[o] = __dadd_rn(M.x[o], __dsub_rn((double)M.e[(long)j * lde + i], e0));
 }
 
 // r64 = b - A x with the reference's pinned operator; ||r64||^2, sum(r64); outer test
-__global__ void __launch_bounds__(MT) k_mx_resid(Geo G, const double* __restrict__ b, const double* __restrict__ x,
-                                                  double* __restrict__ r64, XASlot* slots, MixCtrl* ctrl,
-                                                  cudaGraphConditionalHandle cond_outer, int use_cond) {
+__global__ void __launch_bounds__(MT) k_mx_resid(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
+                                                  MixLoop* ml, cudaGraphConditionalHandle cond_outer, int use_cond) {
+  MX_TILE(0)
   MX_SMEM_SLOT(sa0);
   MX_SMEM_SLOT(sa1);
   __shared__ long long wred[(MT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
-  const int i = blockIdx.x * BX + (threadIdx.x & 31), j = blockIdx.y * BY + (threadIdx.x >> 5);
+  const Geo G = M.G;
+  XASlot* slots = M.slots;
+  MixCtrl* ctrl = M.ctrl;
+  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
   XTerm t0, t1;
   xa_zero(t0);
   xa_zero(t1);
   unsigned f0 = 0u, f1 = 0u;
   if (i < G.nx && j < G.ny) {
-    View2<const double> X{x, G.ld};
+    View2<const double> X{M.x, G.ld};
     const double ax = (i == 0 && j == 0) ? X(0, 0) : -lap_coherent_at(X, j, i, G.g);
     const long o = (long)j * G.ld + i;
-    const double rv = __dsub_rn(b[o], ax);
-    r64[o] = rv;
+    const double rv = __dsub_rn(M.b[o], ax);
+    M.r64[o] = rv;
     xa_term_prod(rv, rv, t0, f0);
     xa_term_val(rv, t1, f1);
   }
   mx_reduce(&slots[M_RR64], &t0, 1, f0, sa0, wred, ired);
   mx_reduce(&slots[M_SUM64], &t1, 1, f1, sa1, wred, ired);
   XASlot* sl[2] = {&slots[M_RR64], &slots[M_SUM64]};
-  if (xa_finish(sl, 2, gridDim.x * gridDim.y) && threadIdx.x == 0) {
+  if (xa_finish(sl, 2, M.nt0) && threadIdx.x == 0) {
     const double rr = slots[M_RR64].result;
     ctrl->rr64 = rr;
     ctrl->sum64 = slots[M_SUM64].result;
@@ -613,17 +662,22 @@ __global__ void __launch_bounds__(MT) k_mx_resid(Geo G, const double* __restrict
     ctrl->converged = conv ? 1 : 0;
     if (conv || ctrl->outer >= ctrl->max_outer) {
       ctrl->outer_done = 1;
-      if (use_cond) cudaGraphSetConditional(cond_outer, 0u);
+      if (atomicSub(&ml->outer_active, 1) == 1 && use_cond) cudaGraphSetConditional(cond_outer, 0u);
     }
   }
 }
 
 // summary of the mixed solve for the step record
-__global__ void k_mx_finish(const MixCtrl* __restrict__ m, Ctrl64* c, int maxiter_report) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void k_mx_finish(const MixDesc* __restrict__ MD, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const MixDesc& M = MD[k];
+  if (!*M.active) return;
+  const MixCtrl* m = M.ctrl;
+  Ctrl64* c = M.ctrl64;
   c->iter = m->inner_total;
   c->refine_passes = m->outer;
-  c->info = m->converged ? 0 : maxiter_report;
+  c->info = m->converged ? 0 : M.maxiter_report;
   c->zero_rhs = (m->bnorm == 0.0) ? 1 : 0;
   c->bnrm2 = m->bnorm;
 }
@@ -632,210 +686,254 @@ __global__ void k_mx_finish(const MixCtrl* __restrict__ m, Ctrl64* c, int maxite
 
 static long round_up(long a, long m) { return (a + m - 1) / m * m; }
 
-int solver_create(int nx, int ny, double dx, double dy, long ld64, double tol_out, double tol_in, int max_outer,
-                  int max_inner, Solver** out) {
-  Solver* S = new Solver();
-  S->G.nx = nx;
-  S->G.ny = ny;
-  S->G.ld = ld64;
-  S->G.g.nx = nx;
-  S->G.g.ny = ny;
-  S->G.g.sx = spacing_for(dx);
-  S->G.g.sy = spacing_for(dy);
-  S->tol_out = tol_out;
-  S->tol_in = tol_in;
-  S->max_outer = max_outer;
-  S->max_inner = max_inner;
-  // levels: halve while both sides are even and the coarse grid keeps >= 8 cells a side
-  int L = 0;
+static void level_dims(int nx, int ny, std::vector<std::pair<int, int>>& dims, int& coarse_levels, int& coarse_tot) {
+  dims.clear();
   int lx = nx, ly = ny;
-  std::vector<std::pair<int, int>> dims;
   dims.push_back({lx, ly});
-  while (L + 1 < MAX_LEVELS && lx % 2 == 0 && ly % 2 == 0 && lx / 2 >= 8 && ly / 2 >= 8 && (long)lx * ly > CMAX) {
+  while ((int)dims.size() < MAX_LEVELS && lx % 2 == 0 && ly % 2 == 0 && lx / 2 >= 8 && ly / 2 >= 8 &&
+         (long)lx * ly > CMAX) {
     lx /= 2;
     ly /= 2;
     dims.push_back({lx, ly});
-    ++L;
   }
-  if ((long)lx * ly > CMAX) {
-    delete S;
-    return set_error(PFGB_EINVAL, "mixed solver: the coarse multigrid level would exceed 4096 cells "
-                                  "(nx and ny need enough factors of two)");
+  int cn = 1, cx = lx, cy = ly;
+  while (cn < 8 && cx % 2 == 0 && cy % 2 == 0 && cx / 2 >= 2 && cy / 2 >= 2) {
+    cx /= 2;
+    cy /= 2;
+    ++cn;
   }
-  // levels resolved inside the coarse CTA: halve while even and at least 2 a side
-  {
-    int cn = 1, cx = lx, cy = ly;
-    while (cn < 8 && cx % 2 == 0 && cy % 2 == 0 && cx / 2 >= 2 && cy / 2 >= 2) {
-      cx /= 2;
-      cy /= 2;
-      ++cn;
-    }
-    S->coarse_levels = cn;
-    int tot = 0;
-    int ax = lx, ay = ly;
-    for (int l = 0; l < cn; ++l) {
-      tot += ax * ay;
-      ax /= 2;
-      ay /= 2;
-    }
-    S->coarse_smem = (size_t)5 * tot * sizeof(float);
-    cudaFuncSetAttribute(k_mg_coarse_cycles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->coarse_smem);
+  coarse_levels = cn;
+  coarse_tot = 0;
+  int ax = lx, ay = ly;
+  for (int l = 0; l < cn; ++l) {
+    coarse_tot += ax * ay;
+    ax /= 2;
+    ay /= 2;
   }
-  S->nlev = L + 1;
+}
+
+static void add_mtiles(std::vector<MTile>& v, int k, int nx, int ny) {
+  for (int j0 = 0; j0 < ny; j0 += BY)
+    for (int i0 = 0; i0 < nx; i0 += BX) v.push_back(MTile{k, i0, j0, 0});
+}
+
+int batch_create(const MixParams* prm, int n, Batch** out) {
+  Batch* B = new Batch();
+  B->n = n;
+  B->hd.resize(n);
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   size_t bytes = 0;
-  std::vector<long> lds(S->nlev);
-  for (int l = 0; l < S->nlev; ++l) {
-    lds[l] = round_up(dims[l].first, 32);
-    bytes += 4 * (size_t)lds[l] * dims[l].second * sizeof(float) + 4 * 256;
+  std::vector<std::vector<std::pair<int, int>>> dims(n);
+  std::vector<int> cls(n), ctot(n);
+  size_t smem = 0;
+  for (int k = 0; k < n; ++k) {
+    level_dims(prm[k].nx, prm[k].ny, dims[k], cls[k], ctot[k]);
+    const auto& last = dims[k].back();
+    if ((long)last.first * last.second > CMAX) {
+      delete B;
+      return set_error(PFGB_EINVAL, "mixed solver: the coarse multigrid level would exceed 4096 cells "
+                                    "(nx and ny need enough factors of two)");
+    }
+    smem = std::max(smem, (size_t)5 * ctot[k] * sizeof(float));
+    B->maxlev = std::max(B->maxlev, (int)dims[k].size());
+    for (auto& d : dims[k]) bytes += 4 * up((size_t)round_up(d.first, 32) * d.second * sizeof(float));
+    const size_t v0 = up((size_t)round_up(prm[k].nx, 32) * prm[k].ny * sizeof(float));
+    bytes += 4 * v0 + up((size_t)prm[k].ld64 * prm[k].ny * sizeof(double)) + up(M_COUNT * sizeof(XASlot)) +
+             up(sizeof(MixCtrl));
   }
-  const long ld0 = lds[0];
-  const size_t v0 = (size_t)ld0 * ny * sizeof(float);
-  bytes += 4 * (v0 + 256);                                   // e, p0, p1, q
-  bytes += (size_t)ld64 * ny * sizeof(double) + 256;         // r64
-  bytes += M_COUNT * sizeof(XASlot) + sizeof(MixCtrl) + 1024;
-  if (cudaMalloc(&S->ws, bytes) != cudaSuccess) {
-    delete S;
+  // tile tables
+  std::vector<MTile> tl[MAX_LEVELS], tlr[MAX_LEVELS], tpre[MAX_LEVELS];
+  for (int k = 0; k < n; ++k) {
+    const int nl = (int)dims[k].size();
+    for (int l = 0; l < nl; ++l) {
+      add_mtiles(tl[l], k, dims[k][l].first, dims[k][l].second);
+      if (l + 1 < nl) {
+        add_mtiles(tpre[l], k, dims[k][l].first, dims[k][l].second);
+        add_mtiles(tlr[l], k, dims[k][l + 1].first, dims[k][l + 1].second);
+      }
+    }
+  }
+  for (int l = 0; l < B->maxlev; ++l)
+    bytes += up(tl[l].size() * sizeof(MTile)) + up(tlr[l].size() * sizeof(MTile)) + up(tpre[l].size() * sizeof(MTile));
+  bytes += up(n * sizeof(MixDesc)) + up(sizeof(MixLoop));
+  if (cudaMalloc(&B->ws, bytes) != cudaSuccess) {
+    delete B;
     return set_error(PFGB_ENOMEM, "cudaMalloc of the mixed-solver workspace failed");
   }
-  cudaMemset(S->ws, 0, bytes);
-  S->ws_bytes = bytes;
-  char* c = S->ws;
-  auto take = [&](size_t n) { char* r = c; c += (n + 255) / 256 * 256; return r; };
-  const double dx2 = dx * dx, dy2 = dy * dy;
-  float cx = (float)(1.0 / dx2), cy = (float)(1.0 / dy2);
-  for (int l = 0; l < S->nlev; ++l) {
-    Lvl& v = S->lev[l];
-    v.nx = dims[l].first;
-    v.ny = dims[l].second;
-    v.ld = lds[l];
-    v.cx = cx;
-    v.cy = cy;
-    size_t n = (size_t)v.ld * v.ny * sizeof(float);
-    v.u = (float*)take(n);
-    v.t = (float*)take(n);
-    v.f = (float*)take(n);
-    v.r = (float*)take(n);
+  cudaMemset(B->ws, 0, bytes);
+  B->ws_bytes = bytes;
+  char* c = B->ws;
+  auto take = [&](size_t b) { char* r = c; c += up(b); return r; };
+  int gmax_i = 1, gmax_o = 1;
+  for (int k = 0; k < n; ++k) {
+    MixDesc& M = B->hd[k];
+    M.G.nx = prm[k].nx;
+    M.G.ny = prm[k].ny;
+    M.G.ld = prm[k].ld64;
+    M.G.g.nx = prm[k].nx;
+    M.G.g.ny = prm[k].ny;
+    M.G.g.sx = spacing_for(prm[k].dx);
+    M.G.g.sy = spacing_for(prm[k].dy);
+    M.nlev = (int)dims[k].size();
+    M.coarse_levels = cls[k];
+    const float cx = (float)(1.0 / (prm[k].dx * prm[k].dx)), cy = (float)(1.0 / (prm[k].dy * prm[k].dy));
+    for (int l = 0; l < M.nlev; ++l) {
+      Lvl& v = M.lev[l];
+      v.nx = dims[k][l].first;
+      v.ny = dims[k][l].second;
+      v.ld = round_up(v.nx, 32);
+      v.cx = cx;
+      v.cy = cy;
+      const size_t nb = (size_t)v.ld * v.ny * sizeof(float);
+      v.u = (float*)take(nb);
+      v.t = (float*)take(nb);
+      v.f = (float*)take(nb);
+      v.r = (float*)take(nb);
+    }
+    const size_t v0 = (size_t)M.lev[0].ld * prm[k].ny * sizeof(float);
+    M.e = (float*)take(v0);
+    M.p0 = (float*)take(v0);
+    M.p1 = (float*)take(v0);
+    M.q = (float*)take(v0);
+    M.r64 = (double*)take((size_t)prm[k].ld64 * prm[k].ny * sizeof(double));
+    M.slots = (XASlot*)take(M_COUNT * sizeof(XASlot));
+    M.ctrl = (MixCtrl*)take(sizeof(MixCtrl));
+    M.b = prm[k].b;
+    M.x = prm[k].x;
+    M.ctrl64 = prm[k].ctrl64;
+    M.active = prm[k].active;
+    M.maxiter_report = prm[k].maxiter_report;
+    M.nt0 = ((prm[k].nx + BX - 1) / BX) * ((prm[k].ny + BY - 1) / BY);
+    MixCtrl hc = {};
+    hc.tol_out = prm[k].tol_out;
+    hc.tol_in = prm[k].tol_in;
+    hc.max_outer = prm[k].max_outer;
+    hc.max_inner = prm[k].max_inner;
+    hc.inner_done = 1;
+    hc.outer_done = 1;
+    cudaMemcpy(M.ctrl, &hc, sizeof(MixCtrl), cudaMemcpyHostToDevice);
+    gmax_i = std::max(gmax_i, prm[k].max_inner + 1);
+    gmax_o = std::max(gmax_o, prm[k].max_outer + 1);
   }
-  S->e = (float*)take(v0);
-  S->p0 = (float*)take(v0);
-  S->p1 = (float*)take(v0);
-  S->q = (float*)take(v0);
-  S->r64 = (double*)take((size_t)ld64 * ny * sizeof(double));
-  S->slots = (XASlot*)take(M_COUNT * sizeof(XASlot));
-  S->ctrl = (MixCtrl*)take(sizeof(MixCtrl));
-  MixCtrl hc = {};
-  hc.tol_out = tol_out;
-  hc.tol_in = tol_in;
-  hc.max_outer = max_outer;
-  hc.max_inner = max_inner;
-  cudaMemcpy(S->ctrl, &hc, sizeof(MixCtrl), cudaMemcpyHostToDevice);
-  *out = S;
+  for (int l = 0; l < B->maxlev; ++l) {
+    auto put = [&](std::vector<MTile>& v, MTile*& dst, int& cnt) {
+      cnt = (int)v.size();
+      dst = (MTile*)take(v.size() * sizeof(MTile));
+      if (cnt) cudaMemcpy(dst, v.data(), v.size() * sizeof(MTile), cudaMemcpyHostToDevice);
+    };
+    put(tl[l], B->tl[l], B->ntl[l]);
+    put(tlr[l], B->tlr[l], B->ntlr[l]);
+    put(tpre[l], B->tpre[l], B->ntpre[l]);
+  }
+  B->dd = (MixDesc*)take(n * sizeof(MixDesc));
+  B->loop = (MixLoop*)take(sizeof(MixLoop));
+  MixLoop ml0 = {0, 0, 0, 0, gmax_o, gmax_i, 0};
+  cudaMemcpy(B->loop, &ml0, sizeof(MixLoop), cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMemcpy(B->dd, B->hd.data(), n * sizeof(MixDesc), cudaMemcpyHostToDevice);
+  B->coarse_smem = smem;
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mg_coarse_cycles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) {
+    batch_destroy(B);
+    return set_error(PFGB_ECUDA, std::string("mixed batch set-up: ") + cudaGetErrorString(e));
+  }
+  *out = B;
   return PFGB_OK;
 }
 
-void solver_destroy(Solver* S) {
-  if (!S) return;
-  if (S->ws) cudaFree(S->ws);
-  delete S;
+void batch_destroy(Batch* B) {
+  if (!B) return;
+  if (B->ws) cudaFree(B->ws);
+  delete B;
 }
 
-static void add_vcycle(GraphChain& c, Solver* S, const float omega) {
-  const int L = S->nlev - 1;
-  for (int l = 0; l < L; ++l) {
-    const Lvl& F = S->lev[l];
-    const Lvl& C = S->lev[l + 1];
-    c.kernel(k_mg_pre, dim3((F.nx + BX - 1) / BX, (F.ny + BY - 1) / BY), dim3(MT), F, omega);
-    c.kernel(k_mg_restrict, dim3((C.nx + BX - 1) / BX, (C.ny + BY - 1) / BY), dim3(MT), F, C);
+static void add_vcycle(GraphChain& c, Batch* B, int gate, float omega) {
+  const MixDesc* dd = B->dd;
+  for (int l = 0; l + 1 < B->maxlev; ++l) {
+    if (B->ntpre[l]) c.kernel(k_mg_pre, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, omega);
+    if (B->ntlr[l]) c.kernel(k_mg_restrict, dim3(B->ntlr[l]), dim3(MT), dd, (const MTile*)B->tlr[l], l, gate);
   }
-  const Lvl& Cc = S->lev[L];
-  c.kernel_smem(k_mg_coarse_cycles, dim3(1), dim3(CT), S->coarse_smem, Cc, S->coarse_levels, 1, 8, omega);
-  for (int l = L - 1; l >= 0; --l) {
-    const Lvl& F = S->lev[l];
-    const Lvl& C = S->lev[l + 1];
-    c.kernel(k_mg_post, dim3((F.nx + BX - 1) / BX, (F.ny + BY - 1) / BY), dim3(MT), F, C, omega);
-  }
+  c.kernel_smem(k_mg_coarse_cycles, dim3(B->n), dim3(CT), B->coarse_smem, dd, gate, 1, 8, omega);
+  for (int l = B->maxlev - 2; l >= 0; --l)
+    if (B->ntpre[l]) c.kernel(k_mg_post, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, omega);
 }
 
-// Append the refinement loop (x, given b) to a graph chain.  b and x are the
-// binary64 vectors of the step (pitch ld64).
-int append_solve(GraphChain& c, Solver* S, const double* b, double* x, Ctrl64* ctrl64, int maxiter_report) {
+int append_solve(GraphChain& c, Batch* B) {
   const float omega = 0.8f;
-  const Lvl& L0 = S->lev[0];
-  dim3 g64((S->G.nx + BX - 1) / BX, (S->G.ny + BY - 1) / BY);
-  dim3 g0((L0.nx + BX - 1) / BX, (L0.ny + BY - 1) / BY);
+  const MixDesc* dd = B->dd;
+  const dim3 g0(B->ntl[0]);
   cudaGraphConditionalHandle cond_outer = 0, cond_inner = 0;
-  cudaError_t e = cudaGraphConditionalHandleCreate(&cond_outer, c.graph(), 1u, cudaGraphCondAssignDefault);
+  cudaError_t e = cudaGraphConditionalHandleCreate(&cond_outer, c.graph(), 0u, cudaGraphCondAssignDefault);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("outer conditional: ") + cudaGetErrorString(e));
-  c.kernel(k_mx_init, g64, dim3(MT), S->G, b, x, S->r64, S->slots, S->ctrl, cond_outer, 1);
+  c.kernel(k_ml_reset, dim3(1), dim3(32), B->loop, 0);
+  c.kernel(k_mx_init, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop);
+  c.kernel(k_ml_arm, dim3(1), dim3(32), B->loop, 0, cond_outer, 1);
   GraphChain outer = c.while_loop_with(cond_outer);
   if (outer.status() != cudaSuccess) return set_error(PFGB_ECUDA, "outer loop node");
-  e = cudaGraphConditionalHandleCreate(&cond_inner, outer.graph(), 1u, cudaGraphCondAssignDefault);
+  e = cudaGraphConditionalHandleCreate(&cond_inner, outer.graph(), 0u, cudaGraphCondAssignDefault);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("inner conditional: ") + cudaGetErrorString(e));
-  outer.kernel(k_mx_prep, g64, dim3(MT), S->G, L0, (const double*)S->r64, S->e, S->slots, S->ctrl, cond_inner, 1);
-  add_vcycle(outer, S, omega);
-  outer.kernel(k_mx_rz, g0, dim3(MT), L0, (const float*)L0.u, S->slots, S->ctrl);
+  outer.kernel(k_ml_reset, dim3(1), dim3(32), B->loop, 1);
+  outer.kernel(k_mx_prep, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop);
+  add_vcycle(outer, B, 1, omega);
+  outer.kernel(k_mx_rz, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
+  outer.kernel(k_ml_arm, dim3(1), dim3(32), B->loop, 1, cond_inner, 1);
   GraphChain inner = outer.while_loop_with(cond_inner);
-  inner.kernel(k_mx_matvec, g0, dim3(MT), L0, (const float*)L0.u, S->p0, S->p1, S->q, S->slots, S->ctrl);
-  inner.kernel(k_mx_update, g0, dim3(MT), L0, (const float*)S->p0, (const float*)S->p1, (const float*)S->q, S->e,
-               S->slots, S->ctrl, cond_inner, 1);
-  add_vcycle(inner, S, omega);
-  inner.kernel(k_mx_rz, g0, dim3(MT), L0, (const float*)L0.u, S->slots, S->ctrl);
-  outer.kernel(k_mx_correct, g64, dim3(MT), S->G, L0.ld, (const float*)S->e, x);
-  outer.kernel(k_mx_resid, g64, dim3(MT), S->G, b, (const double*)x, S->r64, S->slots, S->ctrl, cond_outer, 1);
-  c.kernel(k_mx_finish, dim3(1), dim3(32), (const MixCtrl*)S->ctrl, ctrl64, maxiter_report);
+  inner.kernel(k_mx_matvec, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
+  inner.kernel(k_mx_update, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_inner, 1);
+  add_vcycle(inner, B, 1, omega);
+  inner.kernel(k_mx_rz, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
+  inner.kernel(k_ml_guard, dim3(1), dim3(32), B->loop, 1, cond_inner, 1);
+  outer.kernel(k_mx_correct, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
+  outer.kernel(k_mx_resid, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_outer, 1);
+  outer.kernel(k_ml_guard, dim3(1), dim3(32), B->loop, 0, cond_outer, 1);
+  c.kernel(k_mx_finish, dim3((B->n + 31) / 32), dim3(32), dd, B->n);
   cudaError_t st = c.status() != cudaSuccess ? c.status() : (outer.status() != cudaSuccess ? outer.status() : inner.status());
   if (st != cudaSuccess) return set_error(PFGB_ECUDA, std::string("building the mixed solve: ") + cudaGetErrorString(st));
   return PFGB_OK;
 }
 
 // Host-driven form of append_solve with direct launches: the loop decisions
-// are read back from the control block after each stopping test.  Used for
+// are read back from the loop control after each stopping test.  Used for
 // profiling (ncu does not profile kernels of graphs with conditional nodes).
-static void launch_vcycle(Solver* S, float omega, cudaStream_t s) {
-  const int L = S->nlev - 1;
-  for (int l = 0; l < L; ++l) {
-    const Lvl& F = S->lev[l];
-    const Lvl& C = S->lev[l + 1];
-    k_mg_pre<<<dim3((F.nx + BX - 1) / BX, (F.ny + BY - 1) / BY), MT, 0, s>>>(F, omega);
-    k_mg_restrict<<<dim3((C.nx + BX - 1) / BX, (C.ny + BY - 1) / BY), MT, 0, s>>>(F, C);
+static void launch_vcycle(Batch* B, int gate, float omega, cudaStream_t s) {
+  for (int l = 0; l + 1 < B->maxlev; ++l) {
+    if (B->ntpre[l]) k_mg_pre<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, omega);
+    if (B->ntlr[l]) k_mg_restrict<<<B->ntlr[l], MT, 0, s>>>(B->dd, B->tlr[l], l, gate);
   }
-  k_mg_coarse_cycles<<<1, CT, S->coarse_smem, s>>>(S->lev[L], S->coarse_levels, 1, 8, omega);
-  for (int l = L - 1; l >= 0; --l) {
-    const Lvl& F = S->lev[l];
-    const Lvl& C = S->lev[l + 1];
-    k_mg_post<<<dim3((F.nx + BX - 1) / BX, (F.ny + BY - 1) / BY), MT, 0, s>>>(F, C, omega);
-  }
+  k_mg_coarse_cycles<<<B->n, CT, B->coarse_smem, s>>>(B->dd, gate, 1, 8, omega);
+  for (int l = B->maxlev - 2; l >= 0; --l)
+    if (B->ntpre[l]) k_mg_post<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, omega);
 }
 
-int run_direct(Solver* S, const double* b, double* x, Ctrl64* ctrl64, int maxiter_report, cudaStream_t s) {
+int run_direct(Batch* B, cudaStream_t s) {
   const float omega = 0.8f;
-  const Lvl& L0 = S->lev[0];
-  dim3 g64((S->G.nx + BX - 1) / BX, (S->G.ny + BY - 1) / BY);
-  dim3 g0((L0.nx + BX - 1) / BX, (L0.ny + BY - 1) / BY);
-  MixCtrl h;
+  const int g0 = B->ntl[0];
+  MixLoop h;
   auto read = [&]() -> bool {
-    return cudaMemcpyAsync(&h, S->ctrl, sizeof(MixCtrl), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+    return cudaMemcpyAsync(&h, B->loop, sizeof(MixLoop), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
            cudaStreamSynchronize(s) == cudaSuccess;
   };
-  k_mx_init<<<g64, MT, 0, s>>>(S->G, b, x, S->r64, S->slots, S->ctrl, 0ull, 0);
+  k_ml_reset<<<1, 32, 0, s>>>(B->loop, 0);
+  k_mx_init<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop);
   if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
-  while (!h.outer_done) {
-    k_mx_prep<<<g64, MT, 0, s>>>(S->G, L0, S->r64, S->e, S->slots, S->ctrl, 0ull, 0);
-    launch_vcycle(S, omega, s);
-    k_mx_rz<<<g0, MT, 0, s>>>(L0, L0.u, S->slots, S->ctrl);
+  for (int po = 0; h.outer_active > 0 && po < h.gmax_o; ++po) {
+    k_ml_reset<<<1, 32, 0, s>>>(B->loop, 1);
+    k_mx_prep<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop);
+    launch_vcycle(B, 1, omega, s);
+    k_mx_rz<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
     if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
-    while (!h.inner_done) {
-      k_mx_matvec<<<g0, MT, 0, s>>>(L0, L0.u, S->p0, S->p1, S->q, S->slots, S->ctrl);
-      k_mx_update<<<g0, MT, 0, s>>>(L0, S->p0, S->p1, S->q, S->e, S->slots, S->ctrl, 0ull, 0);
-      launch_vcycle(S, omega, s);
-      k_mx_rz<<<g0, MT, 0, s>>>(L0, L0.u, S->slots, S->ctrl);
+    for (int pi = 0; h.inner_active > 0 && pi < h.gmax_i; ++pi) {
+      k_mx_matvec<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
+      k_mx_update<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0);
+      launch_vcycle(B, 1, omega, s);
+      k_mx_rz<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
       if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
     }
-    k_mx_correct<<<g64, MT, 0, s>>>(S->G, L0.ld, S->e, x);
-    k_mx_resid<<<g64, MT, 0, s>>>(S->G, b, x, S->r64, S->slots, S->ctrl, 0ull, 0);
+    k_mx_correct<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
+    k_mx_resid<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0);
     if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
   }
-  k_mx_finish<<<1, 32, 0, s>>>(S->ctrl, ctrl64, maxiter_report);
+  k_mx_finish<<<(B->n + 31) / 32, 32, 0, s>>>(B->dd, B->n);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("mixed solve launch: ") + cudaGetErrorString(e));
   return PFGB_OK;

@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "graph.cuh"
 #include "stencil.cuh"
 #include "step64.cuh"
@@ -45,30 +47,73 @@ struct MixCtrl {
   int inner_done, outer_done;
 };
 
-struct Solver {
-  Geo G;
-  double tol_out, tol_in;
-  int max_outer, max_inner;
-  int nlev = 0;
-  Lvl lev[MAX_LEVELS];
-  int coarse_levels = 1;       // levels resolved inside the coarse CTA
-  size_t coarse_smem = 0;      // its dynamic shared memory
-  char* ws = nullptr;
-  size_t ws_bytes = 0;
-  float *e, *p0, *p1, *q;
-  double* r64;
-  XASlot* slots;
-  MixCtrl* ctrl;
+// One tile of work of a mixed batch: instance and the tile's first cell.
+struct MTile {
+  int inst, i0, j0, pad;
 };
 
-int solver_create(int nx, int ny, double dx, double dy, long ld64, double tol_out, double tol_in, int max_outer,
-                  int max_inner, Solver** out);
-void solver_destroy(Solver* S);
-// Append x = A^{-1} b (refinement loop) to a graph chain, then record the
-// total inner iterations / convergence in the step's control block.
-int append_solve(GraphChain& c, Solver* S, const double* b, double* x, Ctrl64* ctrl64, int maxiter_report);
-// The same solve with direct launches and host loop control (for profiling).
-int run_direct(Solver* S, const double* b, double* x, Ctrl64* ctrl64, int maxiter_report, cudaStream_t s);
+// Everything the mixed-precision kernels need about one instance.
+struct MixDesc {
+  Geo G;                       // binary64 geometry of the refinement
+  int nlev;                    // global levels; the last one is solved by the coarse CTA
+  int coarse_levels;           // levels resolved inside the coarse CTA
+  Lvl lev[MAX_LEVELS];
+  float *e, *p0, *p1, *q;      // binary32 PCG vectors (pitch lev[0].ld)
+  double* r64;                 // binary64 refinement residual (pitch G.ld)
+  const double* b;             // the step's right-hand side (binary64, pitch G.ld)
+  double* x;                   // the step's pressure solution
+  XASlot* slots;
+  MixCtrl* ctrl;
+  Ctrl64* ctrl64;              // the step's control block (iteration summary)
+  const int* active;           // the step's per-instance activity flag
+  int maxiter_report;
+  int nt0;                     // tiles of level 0 (= tiles of the binary64 grid)
+};
+
+// Batch-wide control of the two WHILE loops.
+struct MixLoop {
+  int outer_active, inner_active;
+  int guard_o, guard_i;
+  int gmax_o, gmax_i;
+  int tripped;
+};
+
+struct Batch {
+  int n = 0;
+  std::vector<MixDesc> hd;
+  MixDesc* dd = nullptr;
+  int maxlev = 0;                              // most global levels of any instance
+  MTile* tl[MAX_LEVELS] = {};                  // tiles of level l of the instances that have it
+  int ntl[MAX_LEVELS] = {};
+  MTile* tlr[MAX_LEVELS] = {};                 // tiles of level l+1 of the instances that restrict into it
+  int ntlr[MAX_LEVELS] = {};
+  MTile* tpre[MAX_LEVELS] = {};                // tiles of level l of the instances that smooth on it (l < nlev-1)
+  int ntpre[MAX_LEVELS] = {};
+  size_t coarse_smem = 0;                      // dynamic shared memory of the coarse CTA (largest instance)
+  MixLoop* loop = nullptr;
+  char* ws = nullptr;
+  size_t ws_bytes = 0;
+};
+
+struct MixParams {
+  int nx, ny;
+  double dx, dy;
+  long ld64;
+  double tol_out, tol_in;
+  int max_outer, max_inner;
+  const double* b;
+  double* x;
+  Ctrl64* ctrl64;
+  const int* active;
+  int maxiter_report;
+};
+
+int batch_create(const MixParams* prm, int n, Batch** out);
+void batch_destroy(Batch* B);
+// Append the refinement of every instance (x = A^{-1} b) to a graph chain.
+int append_solve(GraphChain& c, Batch* B);
+// The same with direct launches and host loop control (for profiling).
+int run_direct(Batch* B, cudaStream_t s);
 
 }  // namespace mixed
 }  // namespace pfgb

@@ -17,10 +17,12 @@
 //
 // Every CG kernel returns at once when the device control block says the
 // solve is done, so a fixed launch sequence reproduces scipy's early exit.
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "graph.cuh"
@@ -643,8 +645,8 @@ struct Instance64 {
   StepOut64* out_d = nullptr;
   StepOut64* out_h = nullptr;
   bool desc_dirty = true;
-  // mixed-precision pressure solve (precision 1, single instance)
-  mixed::Solver* mix = nullptr;
+  // mixed-precision pressure solve of every instance (precision 1)
+  mixed::Batch* mix = nullptr;
   // the whole step as one CUDA graph (CG loop = WHILE conditional node)
   int use_graph = 1;
   cudaGraph_t graph = nullptr;
@@ -668,8 +670,8 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
   if (n < 1) return set_error(PFGB_EINVAL, "batch size must be >= 1");
   for (int k = 0; k < n; ++k)
     if (int rc = validate_params(&prms[k])) return rc;
-  for (int k = 0; k < n; ++k)
-    if (prms[k].precision == 1 && n > 1) return set_error(PFGB_EINVAL, "mixed precision runs one instance per handle");
+  for (int k = 1; k < n; ++k)
+    if (prms[k].precision != prms[0].precision) return set_error(PFGB_EINVAL, "all instances of a batch share one precision");
   Instance64* I = new Instance64();
   I->n = n;
   I->P.assign(prms, prms + n);
@@ -758,12 +760,27 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     return set_error(PFGB_ECUDA, std::string("batch set-up: ") + cudaGetErrorString(e));
   }
   if (prms[0].precision == 1) {
-    const pfgb_params& prm = prms[0];
-    const double tol_out = prm.mixed_tol_outer > 0.0 ? prm.mixed_tol_outer : prm.lin_tol;
-    const double tol_in = prm.mixed_tol_inner > 0.0 ? prm.mixed_tol_inner : 1e-5;
-    const int mo = prm.mixed_max_outer > 0 ? prm.mixed_max_outer : 8;
-    const int mi = prm.mixed_max_inner > 0 ? prm.mixed_max_inner : 50;
-    int rc = mixed::solver_create(prm.nx, prm.ny, prm.dx, prm.dy, I->hd[0].G.ld, tol_out, tol_in, mo, mi, &I->mix);
+    std::vector<mixed::MixParams> mp(n);
+    for (int k = 0; k < n; ++k) {
+      const pfgb_params& prm = prms[k];
+      mixed::MixParams& m = mp[k];
+      m.nx = prm.nx;
+      m.ny = prm.ny;
+      m.dx = prm.dx;
+      m.dy = prm.dy;
+      m.ld64 = I->hd[k].G.ld;
+      m.tol_out = prm.mixed_tol_outer > 0.0 ? prm.mixed_tol_outer : prm.lin_tol;
+      m.tol_in = prm.mixed_tol_inner > 0.0 ? prm.mixed_tol_inner : 1e-5;
+      m.max_outer = prm.mixed_max_outer > 0 ? prm.mixed_max_outer : 8;
+      m.max_inner = prm.mixed_max_inner > 0 ? prm.mixed_max_inner : 50;
+      m.b = I->hd[k].b;
+      m.x = I->hd[k].x;
+      m.ctrl64 = I->hd[k].ctrl;
+      // the instance's activity flag inside the device descriptor table
+      m.active = reinterpret_cast<const int*>(reinterpret_cast<const char*>(I->dd + k) + offsetof(InstDesc, active));
+      m.maxiter_report = prm.lin_maxiter;
+    }
+    int rc = mixed::batch_create(mp.data(), n, &I->mix);
     if (rc) {
       instance64_destroy(I);
       return rc;
@@ -777,7 +794,7 @@ int instance64_create(const pfgb_params* prm, Instance64** out) { return instanc
 
 void instance64_destroy(Instance64* I) {
   if (!I) return;
-  if (I->mix) mixed::solver_destroy(I->mix);
+  if (I->mix) mixed::batch_destroy(I->mix);
   for (cudaEvent_t e : I->ev) cudaEventDestroy(e);
   if (I->exec) cudaGraphExecDestroy(I->exec);
   if (I->graph) cudaGraphDestroy(I->graph);
@@ -889,8 +906,7 @@ static int build_graph(Instance64* I, int mode) {
   if (I->mix) {
     // b is finished (mean removed, b[0] = 0) by the CG init; the refinement solves A x = b
     c.kernel(k_cg_init, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc, (LoopCtl*)nullptr);
-    const InstDesc& D0 = I->hd[0];
-    if (int rc = mixed::append_solve(c, I->mix, D0.b, D0.x, D0.ctrl, D0.A.maxiter)) return rc;
+    if (int rc = mixed::append_solve(c, I->mix)) return rc;
   } else {
     cudaGraphConditionalHandle cond = 0;
     // every conditional handle must belong to a conditional node: create it only here
@@ -944,11 +960,18 @@ static int read_out(Instance64* I, cudaStream_t s, pfgb_step_out* out) {
   cudaError_t e = cudaMemcpyAsync(I->out_h, I->out_d, I->n * sizeof(StepOut64), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("step failed: ") + cudaGetErrorString(e));
-  LoopCtl lc;
-  if (!I->mix && I->use_graph && !I->profiling) {
-    e = cudaMemcpy(&lc, I->lc, sizeof(LoopCtl), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && lc.tripped)
-      return set_error(PFGB_ESTATE, "the CG loop guard stopped the step (an instance did not report completion)");
+  if (I->use_graph && !I->profiling) {
+    int tripped = 0;
+    if (I->mix) {
+      mixed::MixLoop ml;
+      e = cudaMemcpy(&ml, I->mix->loop, sizeof(ml), cudaMemcpyDeviceToHost);
+      tripped = (e == cudaSuccess) ? ml.tripped : 0;
+    } else {
+      LoopCtl lc;
+      e = cudaMemcpy(&lc, I->lc, sizeof(LoopCtl), cudaMemcpyDeviceToHost);
+      tripped = (e == cudaSuccess) ? lc.tripped : 0;
+    }
+    if (tripped) return set_error(PFGB_ESTATE, "a loop guard stopped the step (an instance did not report completion)");
   }
   for (int k = 0; k < I->n; ++k)
     if (I->hd[k].active) copy_out(I->out_h[k], &out[k]);
@@ -969,10 +992,9 @@ static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
   }
   if (mode == 0) enqueue_prologue(I, s);
   if (I->mix) {
-    const InstDesc& D0 = I->hd[0];
     k_rhs<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
     k_cg_init<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc, nullptr);
-    if (int rc = mixed::run_direct(I->mix, D0.b, D0.x, D0.ctrl, D0.A.maxiter, s)) return rc;
+    if (int rc = mixed::run_direct(I->mix, s)) return rc;
     k_post_resid<0><<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
     k_pin_correct<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
     k_post_diag<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
