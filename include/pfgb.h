@@ -148,6 +148,10 @@ PFGB_API int pfgb_batch_create(const pfgb_params* params, int n, pfgb_handle** h
 PFGB_API int pfgb_batch_step(pfgb_handle* handle, double* const* u, double* const* v, double* const* p,
                              const pfgb_step_in* in, void* stream, pfgb_step_out* out);
 PFGB_API int pfgb_batch_size(const pfgb_handle* handle);
+/* New physical parameters (Re, lid velocity, CFL, tolerance, scheme, ...) for
+ * instance k, e.g. when a serving slot takes a new request.  Grid, spacing,
+ * precision and preconditioner stay those of the slot. */
+PFGB_API int pfgb_batch_set_params(pfgb_handle* handle, int k, const pfgb_params* params);
 
 /* Stand-alone projection of the state's current u, v with a given dt:
  * solve_pressure_poisson in normal mode

@@ -76,6 +76,7 @@ SIGNATURES = {
     "pfgb_batch_step": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(StepIn), _P,
                              ctypes.POINTER(StepOut)]),
     "pfgb_batch_size": (_I, [_P]),
+    "pfgb_batch_set_params": (_I, [_P, _I, ctypes.POINTER(Params)]),
     "pfgb_gradient_coherent": (_I, [_P, _L, _P, _P, _L, _I, _I, _D, _D, _P]),
     "pfgb_divergence_coherent": (_I, [_P, _P, _L, _P, _L, _I, _I, _D, _D, _P]),
     "pfgb_laplacian_coherent": (_I, [_P, _L, _P, _L, _I, _I, _D, _D, _P]),

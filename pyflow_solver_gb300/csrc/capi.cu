@@ -147,3 +147,8 @@ extern "C" int pfgb_batch_step(pfgb_handle* handle, double* const* u, double* co
 }
 
 extern "C" int pfgb_batch_size(const pfgb_handle* handle) { return handle ? instance64_count(handle->inst) : 0; }
+
+extern "C" int pfgb_batch_set_params(pfgb_handle* handle, int k, const pfgb_params* params) {
+  if (!handle || !params) return set_error(PFGB_EINVAL, "null argument");
+  return instance64_set_params(handle->inst, k, params);
+}

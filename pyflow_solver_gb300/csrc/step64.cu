@@ -1036,6 +1036,32 @@ int instance64_project(Instance64* I, double* u, double* v, double* p, long lds,
   return run(I, 1, s, out);
 }
 
+// New physical parameters for instance k of a batch (a new request in a slot).
+// The grid (nx, ny, dx, dy), the precision and the preconditioner stay; the
+// iteration limit may not exceed the batch's largest one (the loop guard).
+int instance64_set_params(Instance64* I, int k, const pfgb_params* prm) {
+  if (k < 0 || k >= I->n) return set_error(PFGB_EINVAL, "instance index out of range");
+  const pfgb_params& o = I->P[k];
+  if (prm->nx != o.nx || prm->ny != o.ny || prm->dx != o.dx || prm->dy != o.dy || prm->precision != o.precision ||
+      prm->enable_jacobi != o.enable_jacobi || prm->jacobi_interior != o.jacobi_interior)
+    return set_error(PFGB_EINVAL, "a slot keeps its grid, spacing, precision and preconditioner");
+  if (prm->lin_maxiter < 0 || prm->lin_maxiter > I->maxiter_max)
+    return set_error(PFGB_EINVAL, "lin_maxiter above the batch's largest");
+  if (prm->scheme < 0 || prm->scheme > 2) return set_error(PFGB_EINVAL, "unknown advection scheme");
+  InstDesc& D = I->hd[k];
+  D.A.rtol = prm->lin_tol;
+  D.A.maxiter = prm->lin_maxiter;
+  D.D.cfl_target = prm->cfl_target;
+  D.D.growth = prm->cfl_growth;
+  D.D.nu = prm->nu;
+  D.L.has_lid = prm->has_lid;
+  D.L.lid = prm->lid_velocity;
+  D.scheme = prm->scheme;
+  I->P[k] = *prm;
+  I->desc_dirty = true;
+  return PFGB_OK;
+}
+
 int instance64_set_graph(Instance64* I, int on) {
   I->use_graph = on ? 1 : 0;
   return PFGB_OK;

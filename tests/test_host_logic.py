@@ -61,3 +61,14 @@ def test_driver_requires_state_or_grid():
     d = SimulationDriver(SimpleNamespace())
     with pytest.raises(ValueError):
         next(d.run(max_steps=1))
+
+
+def test_batched_workload_matches_fixture_draws():
+    from pyflow_solver_gb300.workloads import batched_instances, serving_trace
+    from tests import _golden as G
+    g = G.load("batched16")
+    inst = batched_instances()
+    np.testing.assert_array_equal(np.asarray(inst), g["instances"])
+    tr = serving_trace(duration=2.0)
+    assert 300 < len(tr) < 500 and all(a.arrival < b.arrival for a, b in zip(tr, tr[1:]))
+    assert {r.side for r in tr} <= {32, 64, 128, 256, 512, 1024}
