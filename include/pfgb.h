@@ -237,8 +237,10 @@ PFGB_API int pfgb_cg_solve_noalloc(int op, const double* b, double* x, int nx, i
 /* ---- measurement ----------------------------------------------------------- */
 
 /* Record CUDA events around every pressure-matvec launch (p = z + beta p;
- * q = A p; p.q) of the following steps of this handle.  No reference
- * counterpart: benchmark instrumentation. */
+ * q = A p; p.q) of the following steps of this handle: the binary64 CG matvec,
+ * or with precision 1 the binary32 PCG matvec of the inner solves.  Steps then
+ * run as individual launches (no graph).  No reference counterpart: benchmark
+ * instrumentation. */
 PFGB_API int pfgb_set_profiling(pfgb_handle* handle, int on);
 /* Total device time (ms) and number of the matvec launches of the last step. */
 PFGB_API int pfgb_profile_result(pfgb_handle* handle, double* ms, int* launches);

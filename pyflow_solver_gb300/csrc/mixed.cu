@@ -21,10 +21,12 @@
 // Both loops are WHILE conditional nodes of the step graph: the inner loop
 // stops at ||r_in|| <= tol_in ||r~|| or max_inner iterations, the outer loop
 // at ||b - A x|| <= tol_out ||b|| or max_outer passes.
+#include <cstddef>
 #include <cstdio>
 #include <string>
 #include <vector>
 
+#include "dred.cuh"
 #include "graph.cuh"
 #include "mixed.cuh"
 #include "pfgb_internal.h"
@@ -35,7 +37,15 @@ namespace pfgb {
 namespace mixed {
 
 constexpr int MT = 256;
-constexpr int BX = 32, BY = 8;
+constexpr int BX = 32, BY = 32;              // a tile: 32 x 32 cells, each thread a column of 4
+constexpr int RPT = BY / (MT / 32);
+
+// the rows ty of the tile that this thread owns (ty = warp, warp + 8, ...)
+#define MX_ROWS(...)                                        \
+  for (int r_ = 0; r_ < RPT; ++r_) {                        \
+    const int ty = (threadIdx.x >> 5) + r_ * (MT / 32);     \
+    __VA_ARGS__                                             \
+  }
 
 __device__ __forceinline__ float mg_diag(const Lvl& L, int j, int i) {
   float d = 0.f;
@@ -113,7 +123,8 @@ __global__ void __launch_bounds__(MT) k_mg_pre(const MixDesc* __restrict__ MD, c
     int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
     int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx) v = omega * L.f[(long)gj * L.ld + gi] / mg_diag(L, gj, gi);
+    if (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx)
+      v = __fdividef(omega * L.f[(long)gj * L.ld + gi], mg_diag(L, gj, gi));
     s1[jj + 2][ii + 2] = v;
   }
   __syncthreads();
@@ -124,20 +135,23 @@ __global__ void __launch_bounds__(MT) k_mg_pre(const MixDesc* __restrict__ MD, c
     if (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx) {
       auto at = [&](int j, int i) { return s1[j - j0 + 2][i - i0 + 2]; };
       const float d = mg_diag(L, gj, gi);
-      v = (1.f - omega) * s1[jj + 2][ii + 2] + omega * (L.f[(long)gj * L.ld + gi] + mg_nsum(L, gj, gi, at)) / d;
+      v = fmaf(1.f - omega, s1[jj + 2][ii + 2],
+               __fdividef(omega * (L.f[(long)gj * L.ld + gi] + mg_nsum(L, gj, gi, at)), d));
     }
     s2[jj + 1][ii + 1] = v;
   }
   __syncthreads();
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int gi = i0 + tx, gj = j0 + ty;
-  if (gi < L.nx && gj < L.ny) {
-    auto at = [&](int j, int i) { return s2[j - j0 + 1][i - i0 + 1]; };
-    const float t = s2[ty + 1][tx + 1];
-    const long o = (long)gj * L.ld + gi;
-    L.t[o] = t;
-    L.r[o] = L.f[o] - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
-  }
+  const int tx = threadIdx.x & 31;
+  MX_ROWS({
+    const int gi = i0 + tx, gj = j0 + ty;
+    if (gi < L.nx && gj < L.ny) {
+      auto at = [&](int j, int i) { return s2[j - j0 + 1][i - i0 + 1]; };
+      const float t = s2[ty + 1][tx + 1];
+      const long o = (long)gj * L.ld + gi;
+      L.t[o] = t;
+      L.r[o] = L.f[o] - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
+    }
+  })
 }
 
 // f_{l+1} = P^T r_l: each coarse cell gathers the residual of a 4 x 4 fine patch
@@ -145,24 +159,28 @@ __global__ void __launch_bounds__(MT) k_mg_restrict(const MixDesc* __restrict__ 
                                                      int l, int gate) {
   MX_TILE(gate)
   const Lvl F = M.lev[l], C = M.lev[l + 1];
-  const int I = tl.i0 + (threadIdx.x & 31), J = tl.j0 + (threadIdx.x >> 5);
-  if (I >= C.nx || J >= C.ny) return;
-  float s = 0.f;
+  const int I = tl.i0 + (threadIdx.x & 31);
+  MX_ROWS({
+    const int J = tl.j0 + ty;
+    if (I < C.nx && J < C.ny) {
+      float s = 0.f;
 #pragma unroll
-  for (int dj = -1; dj <= 2; ++dj) {
-    const float wy = rweight(dj, J, C.ny);
-    if (wy == 0.f) continue;
-    const int j = 2 * J + dj;
-    float row = 0.f;
+      for (int dj = -1; dj <= 2; ++dj) {
+        const float wy = rweight(dj, J, C.ny);
+        if (wy == 0.f) continue;
+        const int j = 2 * J + dj;
+        float row = 0.f;
 #pragma unroll
-    for (int di = -1; di <= 2; ++di) {
-      const float wx = rweight(di, I, C.nx);
-      if (wx == 0.f) continue;
-      row = fmaf(wx, F.r[(long)j * F.ld + (2 * I + di)], row);
+        for (int di = -1; di <= 2; ++di) {
+          const float wx = rweight(di, I, C.nx);
+          if (wx == 0.f) continue;
+          row = fmaf(wx, F.r[(long)j * F.ld + (2 * I + di)], row);
+        }
+        s = fmaf(wy, row, s);
+      }
+      C.f[(long)J * C.ld + I] = s;
     }
-    s = fmaf(wy, row, s);
-  }
-  C.f[(long)J * C.ld + I] = s;
+  })
 }
 
 // u_l = S(S(t_l + P u_{l+1})) with the bilinear P
@@ -188,19 +206,23 @@ __global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, 
     if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) {
       auto at = [&](int j, int i) { return w0[j - j0 + 2][i - i0 + 2]; };
       const float d = mg_diag(F, gj, gi);
-      v = (1.f - omega) * w0[jj + 2][ii + 2] + omega * (F.f[(long)gj * F.ld + gi] + mg_nsum(F, gj, gi, at)) / d;
+      v = fmaf(1.f - omega, w0[jj + 2][ii + 2],
+               __fdividef(omega * (F.f[(long)gj * F.ld + gi] + mg_nsum(F, gj, gi, at)), d));
     }
     w1[jj + 1][ii + 1] = v;
   }
   __syncthreads();
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int gi = i0 + tx, gj = j0 + ty;
-  if (gi < F.nx && gj < F.ny) {
-    auto at = [&](int j, int i) { return w1[j - j0 + 1][i - i0 + 1]; };
-    const float d = mg_diag(F, gj, gi);
-    const float v = (1.f - omega) * w1[ty + 1][tx + 1] + omega * (F.f[(long)gj * F.ld + gi] + mg_nsum(F, gj, gi, at)) / d;
-    F.u[(long)gj * F.ld + gi] = v;
-  }
+  const int tx = threadIdx.x & 31;
+  MX_ROWS({
+    const int gi = i0 + tx, gj = j0 + ty;
+    if (gi < F.nx && gj < F.ny) {
+      auto at = [&](int j, int i) { return w1[j - j0 + 1][i - i0 + 1]; };
+      const float d = mg_diag(F, gj, gi);
+      const float v = fmaf(1.f - omega, w1[ty + 1][tx + 1],
+                           __fdividef(omega * (F.f[(long)gj * F.ld + gi] + mg_nsum(F, gj, gi, at)), d));
+      F.u[(long)gj * F.ld + gi] = v;
+    }
+  })
 }
 
 // Levels of at most 64 x 64 cells run inside one CTA per instance: all of them
@@ -235,13 +257,21 @@ __device__ __forceinline__ float c_nsum(const CLvl& L, const float* a, int j, in
   return s;
 }
 
+// Cells of a shared-memory level, visited by the CTA as 32 rows of 32 threads
+// (no integer division on the index).
+#define C_FOR(Lv, ...)                                               \
+  for (int j = threadIdx.x >> 5; j < (Lv).ny; j += CT / 32)          \
+    for (int i = threadIdx.x & 31; i < (Lv).nx; i += 32) {           \
+      const int c = j * (Lv).nx + i;                                 \
+      __VA_ARGS__                                                    \
+    }
+
 // one damped-Jacobi sweep src -> dst on level L (all threads; ends with a barrier)
 __device__ __forceinline__ void c_sweep(const CLvl& L, const float* f, const float* src, float* dst, float omega) {
-  const int n = L.nx * L.ny;
-  for (int c = threadIdx.x; c < n; c += CT) {
-    const int j = c / L.nx, i = c - j * L.nx;
-    dst[L.off + c] = (1.f - omega) * src[L.off + c] + omega * (f[L.off + c] + c_nsum(L, src, j, i)) / c_diag(L, j, i);
-  }
+  C_FOR(L, {
+    dst[L.off + c] = fmaf(1.f - omega, src[L.off + c],
+                          __fdividef(omega * (f[L.off + c] + c_nsum(L, src, j, i)), c_diag(L, j, i)));
+  })
   __syncthreads();
 }
 
@@ -272,54 +302,38 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(const MixDesc* __restri
   float* t = sm + 2 * tot;
   float* e = sm + 3 * tot;
   float* w = sm + 4 * tot;
-  const int n0 = C.nx * C.ny;
-  for (int c = threadIdx.x; c < n0; c += CT) {
-    const int j = c / C.nx, i = c - j * C.nx;
+  C_FOR(L[0], {
     f[c] = C.f[(long)j * C.ld + i];
     u[c] = 0.f;
-  }
+  })
   __syncthreads();
   // x_{k+1} = x_k + V(f - A x_k): the first cycle starts from zero
   for (int cyc = 0; cyc < cycles; ++cyc) {
-    {
-      const CLvl& L0 = L[0];
-      for (int c = threadIdx.x; c < n0; c += CT) {
-        const int j = c / L0.nx, i = c - j * L0.nx;
-        t[c] = f[c] - (c_diag(L0, j, i) * u[c] - c_nsum(L0, u, j, i));
-      }
-      __syncthreads();
-    }
+    C_FOR(L[0], { t[c] = f[c] - (c_diag(L[0], j, i) * u[c] - c_nsum(L[0], u, j, i)); })
+    __syncthreads();
     float* rh = t;     // right-hand side of every level (level 0: the residual)
     for (int l = 0; l < nl; ++l) {
       const CLvl& Lv = L[l];
-      const int n = Lv.nx * Lv.ny;
       if (l == nl - 1) {
-        for (int c = threadIdx.x; c < n; c += CT) e[Lv.off + c] = 0.f;
+        C_FOR(Lv, { e[Lv.off + c] = 0.f; })
         __syncthreads();
         for (int s = 0; s < bottom_sweeps; ++s) c_sweep(Lv, rh, (s & 1) ? w : e, (s & 1) ? e : w, omega);
         if (bottom_sweeps & 1) {
-          for (int c = threadIdx.x; c < n; c += CT) e[Lv.off + c] = w[Lv.off + c];
+          C_FOR(Lv, { e[Lv.off + c] = w[Lv.off + c]; })
           __syncthreads();
         }
         break;
       }
       // two sweeps from zero: e = S(S(0))
-      for (int c = threadIdx.x; c < n; c += CT) {
-        const int j = c / Lv.nx, i = c - j * Lv.nx;
-        w[Lv.off + c] = omega * rh[Lv.off + c] / c_diag(Lv, j, i);
-      }
+      C_FOR(Lv, { w[Lv.off + c] = __fdividef(omega * rh[Lv.off + c], c_diag(Lv, j, i)); })
       __syncthreads();
       c_sweep(Lv, rh, w, e, omega);
       // residual rh - A e of this level into w, then rh_{l+1} = P^T w
-      for (int c = threadIdx.x; c < n; c += CT) {
-        const int j = c / Lv.nx, i = c - j * Lv.nx;
-        w[Lv.off + c] = rh[Lv.off + c] - (c_diag(Lv, j, i) * e[Lv.off + c] - c_nsum(Lv, e, j, i));
-      }
+      C_FOR(Lv, { w[Lv.off + c] = rh[Lv.off + c] - (c_diag(Lv, j, i) * e[Lv.off + c] - c_nsum(Lv, e, j, i)); })
       __syncthreads();
       const CLvl& Cv = L[l + 1];
-      const int nc = Cv.nx * Cv.ny;
-      for (int c = threadIdx.x; c < nc; c += CT) {
-        const int J = c / Cv.nx, I = c - J * Cv.nx;
+      C_FOR(Cv, {
+        const int J = j, I = i;
         float sres = 0.f;
         for (int dj = -1; dj <= 2; ++dj) {
           const float wy = rweight(dj, J, Cv.ny);
@@ -333,15 +347,13 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(const MixDesc* __restri
           sres = fmaf(wy, row, sres);
         }
         rh[Cv.off + c] = sres;
-      }
+      })
       __syncthreads();
     }
     for (int l = nl - 2; l >= 0; --l) {
       const CLvl& Lv = L[l];
       const CLvl& Cv = L[l + 1];
-      const int n = Lv.nx * Lv.ny;
-      for (int c = threadIdx.x; c < n; c += CT) {
-        const int j = c / Lv.nx, i = c - j * Lv.nx;
+      C_FOR(Lv, {
         const int I = i >> 1, J = j >> 1;
         const int I2 = (i & 1) ? I + 1 : I - 1, J2 = (j & 1) ? J + 1 : J - 1;
         const bool hx = I2 >= 0 && I2 < Cv.nx, hy = J2 >= 0 && J2 < Cv.ny;
@@ -352,41 +364,27 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(const MixDesc* __restri
         if (hy) pv = fmaf(wx * 0.25f, ec[J2 * Cv.nx + I], pv);
         if (hx && hy) pv = fmaf(0.0625f, ec[J2 * Cv.nx + I2], pv);
         w[Lv.off + c] = e[Lv.off + c] + pv;
-      }
+      })
       __syncthreads();
       c_sweep(Lv, rh, w, e, omega);
       c_sweep(Lv, rh, e, w, omega);
-      for (int c = threadIdx.x; c < n; c += CT) e[Lv.off + c] = w[Lv.off + c];
+      C_FOR(Lv, { e[Lv.off + c] = w[Lv.off + c]; })
       __syncthreads();
     }
-    for (int c = threadIdx.x; c < n0; c += CT) u[c] += e[c];
+    C_FOR(L[0], { u[c] += e[c]; })
     __syncthreads();
   }
-  for (int c = threadIdx.x; c < n0; c += CT) {
-    const int j = c / C.nx, i = c - j * C.nx;
-    C.u[(long)j * C.ld + i] = u[c];
-  }
+  C_FOR(L[0], { C.u[(long)j * C.ld + i] = u[c]; })
 }
 
 // ---- PCG and refinement kernels -------------------------------------------
+//
+// Reductions are deterministic binary64 sums over the instance's level-0 tiles
+// (tile-ordered partials; the last CTA of the instance completes them).
 
-__device__ __forceinline__ void mx_reduce(XASlot* slot, const XTerm* t, int nt, unsigned fl, long long* sacc,
-                                          long long* wred, int* ired) {
-  int top = INT_MIN;
-  for (int k = 0; k < nt; ++k) top = max(top, t[k].top);
-  top = xa_block_max(top, ired);
-  XCtx c;
-  c.clear();
-  c.flags = fl;
-  c.k0 = xa_window_digit(top);
-  for (int k = 0; k < nt; ++k) c.add(sacc, t[k]);
-  int anyslow = __syncthreads_or(c.slow);
-  xa_cta_commit(slot, c.pos, c.neg, c.k0, sacc, anyslow, c.flags, wred);
-}
+using RedSmem = DRedSmem<MT>;
 
-#define MX_SMEM_SLOT(name)                      \
-  __shared__ long long name[XA_DIGITS];         \
-  for (int k_ = threadIdx.x; k_ < XA_DIGITS; k_ += blockDim.x) name[k_] = 0;
+#define MX_RED(R, vals, outv) dred_sum<R, MT>(vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
 
 // x = 0, r64 = b; ||b||^2 and sum(b); counts the instances that refine
 __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
@@ -394,35 +392,28 @@ __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, 
   const MTile tl = TL[blockIdx.x];
   const MixDesc& M = MD[tl.inst];
   if (!*M.active) return;
-  MX_SMEM_SLOT(sa0);
-  MX_SMEM_SLOT(sa1);
-  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ RedSmem rsm;
   const Geo G = M.G;
-  XASlot* slots = M.slots;
   MixCtrl* ctrl = M.ctrl;
-  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
-  XTerm t0, t1;
-  xa_zero(t0);
-  xa_zero(t1);
-  unsigned f0 = 0u, f1 = 0u;
-  if (i < G.nx && j < G.ny) {
-    const long o = (long)j * G.ld + i;
-    const double bv = M.b[o];
-    M.x[o] = 0.0;
-    M.r64[o] = bv;
-    xa_term_prod(bv, bv, t0, f0);
-    xa_term_val(bv, t1, f1);
-  }
-  mx_reduce(&slots[M_RR64], &t0, 1, f0, sa0, wred, ired);
-  mx_reduce(&slots[M_SUM64], &t1, 1, f1, sa1, wred, ired);
-  XASlot* sl[2] = {&slots[M_RR64], &slots[M_SUM64]};
-  if (xa_finish(sl, 2, M.nt0) && threadIdx.x == 0) {
-    const double bb = slots[M_RR64].result;
-    ctrl->bnorm = __dsqrt_rn(bb);
-    ctrl->tol_abs_out = __dmul_rn(ctrl->tol_out, ctrl->bnorm);
+  const int i = tl.i0 + (threadIdx.x & 31);
+  double v[2] = {0.0, 0.0}, out[2];
+  MX_ROWS({
+    const int j = tl.j0 + ty;
+    if (i < G.nx && j < G.ny) {
+      const long o = (long)j * G.ld + i;
+      const double bv = M.b[o];
+      M.x[o] = 0.0;
+      M.r64[o] = bv;
+      v[0] += bv * bv;
+      v[1] += bv;
+    }
+  })
+  if (MX_RED(2, v, out) && threadIdx.x == 0) {
+    const double bb = out[0];
+    ctrl->bnorm = sqrt(bb);
+    ctrl->tol_abs_out = ctrl->tol_out * ctrl->bnorm;
     ctrl->rr64 = bb;
-    ctrl->sum64 = slots[M_SUM64].result;
+    ctrl->sum64 = out[1];
     ctrl->outer = 0;
     ctrl->inner = 0;
     ctrl->inner_total = 0;
@@ -468,58 +459,50 @@ __global__ void k_ml_guard(MixLoop* ml, int which, cudaGraphConditionalHandle co
 __global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                  MixLoop* ml) {
   MX_TILE(0)
-  MX_SMEM_SLOT(sa0);
-  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ RedSmem rsm;
   const Geo G = M.G;
   const Lvl L0 = M.lev[0];
-  XASlot* slots = M.slots;
   MixCtrl* ctrl = M.ctrl;
-  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
-  XTerm t0;
-  xa_zero(t0);
-  unsigned f0 = 0u;
-  if (i < G.nx && j < G.ny) {
-    const double rv = (i == 0 && j == 0) ? -__dsub_rn(ctrl->sum64, M.r64[0]) : M.r64[(long)j * G.ld + i];
-    const float rf = __double2float_rn(rv);
-    L0.f[(long)j * L0.ld + i] = rf;
-    M.e[(long)j * L0.ld + i] = 0.f;
-    xa_term_prod_f32(rf, rf, t0, f0);
-  }
-  mx_reduce(&slots[M_RT], &t0, 1, f0, sa0, wred, ired);
-  XASlot* sl[1] = {&slots[M_RT]};
-  if (xa_finish(sl, 1, M.nt0) && threadIdx.x == 0) {
-    const double rt = __dsqrt_rn(slots[M_RT].result);
+  const int i = tl.i0 + (threadIdx.x & 31);
+  double v[1] = {0.0}, out[1];
+  MX_ROWS({
+    const int j = tl.j0 + ty;
+    if (i < G.nx && j < G.ny) {
+      const double rv = (i == 0 && j == 0) ? -(ctrl->sum64 - M.r64[0]) : M.r64[(long)j * G.ld + i];
+      const float rf = __double2float_rn(rv);
+      L0.f[(long)j * L0.ld + i] = rf;
+      M.e[(long)j * L0.ld + i] = 0.f;
+      v[0] += (double)rf * (double)rf;
+    }
+  })
+  if (MX_RED(1, v, out) && threadIdx.x == 0) {
+    const double rt = sqrt(out[0]);
     ctrl->rt_norm = rt;
-    ctrl->tol_abs_in = __dmul_rn(ctrl->tol_in, rt);
+    ctrl->tol_abs_in = ctrl->tol_in * rt;
     ctrl->inner = 0;
     ctrl->inner_done = rt > 0.0 ? 0 : 1;
     if (rt > 0.0) atomicAdd(&ml->inner_active, 1);
   }
 }
 
-// rho = r.z (exact); beta = rho / rho_prev after the first inner iteration
+// rho = r.z; beta = rho / rho_prev after the first inner iteration
 __global__ void __launch_bounds__(MT) k_mx_rz(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
   MX_TILE(1)
-  MX_SMEM_SLOT(sa0);
-  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ RedSmem rsm;
   const Lvl L0 = M.lev[0];
-  XASlot* slots = M.slots;
   MixCtrl* ctrl = M.ctrl;
-  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
-  XTerm t0;
-  xa_zero(t0);
-  unsigned f0 = 0u;
-  if (i < L0.nx && j < L0.ny) {
-    const long o = (long)j * L0.ld + i;
-    xa_term_prod_f32(L0.f[o], L0.u[o], t0, f0);
-  }
-  mx_reduce(&slots[M_RZ], &t0, 1, f0, sa0, wred, ired);
-  XASlot* sl[1] = {&slots[M_RZ]};
-  if (xa_finish(sl, 1, M.nt0) && threadIdx.x == 0) {
-    const double rz = slots[M_RZ].result;
-    if (ctrl->inner > 0) ctrl->beta = __ddiv_rn(rz, ctrl->rho);
+  const int i = tl.i0 + (threadIdx.x & 31);
+  double v[1] = {0.0}, out[1];
+  MX_ROWS({
+    const int j = tl.j0 + ty;
+    if (i < L0.nx && j < L0.ny) {
+      const long o = (long)j * L0.ld + i;
+      v[0] += (double)L0.f[o] * (double)L0.u[o];
+    }
+  })
+  if (MX_RED(1, v, out) && threadIdx.x == 0) {
+    const double rz = out[0];
+    if (ctrl->inner > 0) ctrl->beta = rz / ctrl->rho;
     ctrl->rho = rz;
   }
 }
@@ -528,11 +511,8 @@ __global__ void __launch_bounds__(MT) k_mx_rz(const MixDesc* __restrict__ MD, co
 __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
   MX_TILE(1)
   __shared__ float pn[BY + 2][BX + 2];
-  MX_SMEM_SLOT(sa0);
-  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ RedSmem rsm;
   const Lvl L0 = M.lev[0];
-  XASlot* slots = M.slots;
   MixCtrl* ctrl = M.ctrl;
   const float* __restrict__ z = L0.u;
   const int k = *(volatile int*)&ctrl->inner;
@@ -551,26 +531,24 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD
     pn[jj + 1][ii + 1] = v;
   }
   __syncthreads();
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int gi = i0 + tx, gj = j0 + ty;
-  XTerm t0;
-  xa_zero(t0);
-  unsigned f0 = 0u;
-  if (gi < L0.nx && gj < L0.ny) {
-    auto at = [&](int j, int i) { return pn[j - j0 + 1][i - i0 + 1]; };
-    const float pv = pn[ty + 1][tx + 1];
-    const float qv = mg_diag(L0, gj, gi) * pv - mg_nsum(L0, gj, gi, at);
-    const long o = (long)gj * L0.ld + gi;
-    pnew[o] = pv;
-    M.q[o] = qv;
-    xa_term_prod_f32(pv, qv, t0, f0);
-  }
-  mx_reduce(&slots[M_PQ], &t0, 1, f0, sa0, wred, ired);
-  XASlot* sl[1] = {&slots[M_PQ]};
-  if (xa_finish(sl, 1, M.nt0) && threadIdx.x == 0) {
-    const double pq = slots[M_PQ].result;
-    ctrl->pq = pq;
-    ctrl->alpha = __ddiv_rn(ctrl->rho, pq);
+  const int tx = threadIdx.x & 31;
+  const int gi = i0 + tx;
+  double v[1] = {0.0}, out[1];
+  MX_ROWS({
+    const int gj = j0 + ty;
+    if (gi < L0.nx && gj < L0.ny) {
+      auto at = [&](int j, int i) { return pn[j - j0 + 1][i - i0 + 1]; };
+      const float pv = pn[ty + 1][tx + 1];
+      const float qv = mg_diag(L0, gj, gi) * pv - mg_nsum(L0, gj, gi, at);
+      const long o = (long)gj * L0.ld + gi;
+      pnew[o] = pv;
+      M.q[o] = qv;
+      v[0] += (double)pv * (double)qv;
+    }
+  })
+  if (MX_RED(1, v, out) && threadIdx.x == 0) {
+    ctrl->pq = out[0];
+    ctrl->alpha = ctrl->rho / out[0];
   }
 }
 
@@ -578,35 +556,31 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD
 __global__ void __launch_bounds__(MT) k_mx_update(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                    MixLoop* ml, cudaGraphConditionalHandle cond_inner, int use_cond) {
   MX_TILE(1)
-  MX_SMEM_SLOT(sa0);
-  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ RedSmem rsm;
   const Lvl L0 = M.lev[0];
-  XASlot* slots = M.slots;
   MixCtrl* ctrl = M.ctrl;
   const int k = *(volatile int*)&ctrl->inner;
   const float* __restrict__ p = (k & 1) ? M.p0 : M.p1;
   const float alpha = (float)ctrl->alpha;
-  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
-  XTerm t0;
-  xa_zero(t0);
-  unsigned f0 = 0u;
-  if (i < L0.nx && j < L0.ny) {
-    const long o = (long)j * L0.ld + i;
-    M.e[o] = fmaf(alpha, p[o], M.e[o]);
-    const float rv = fmaf(-alpha, M.q[o], L0.f[o]);
-    L0.f[o] = rv;
-    xa_term_prod_f32(rv, rv, t0, f0);
-  }
-  mx_reduce(&slots[M_RR], &t0, 1, f0, sa0, wred, ired);
-  XASlot* sl[1] = {&slots[M_RR]};
-  if (xa_finish(sl, 1, M.nt0) && threadIdx.x == 0) {
-    const double rr = slots[M_RR].result;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  double v[1] = {0.0}, out[1];
+  MX_ROWS({
+    const int j = tl.j0 + ty;
+    if (i < L0.nx && j < L0.ny) {
+      const long o = (long)j * L0.ld + i;
+      M.e[o] = fmaf(alpha, p[o], M.e[o]);
+      const float rv = fmaf(-alpha, M.q[o], L0.f[o]);
+      L0.f[o] = rv;
+      v[0] += (double)rv * (double)rv;
+    }
+  })
+  if (MX_RED(1, v, out) && threadIdx.x == 0) {
+    const double rr = out[0];
     const int it = k + 1;
     ctrl->inner = it;
     ctrl->inner_total += 1;
     ctrl->rr_in = rr;
-    if (!(__dsqrt_rn(rr) > ctrl->tol_abs_in) || it >= ctrl->max_inner) {
+    if (!(sqrt(rr) > ctrl->tol_abs_in) || it >= ctrl->max_inner) {
       ctrl->inner_done = 1;
       if (atomicSub(&ml->inner_active, 1) == 1 && use_cond) cudaGraphSetConditional(cond_inner, 0u);
     }
@@ -618,47 +592,45 @@ __global__ void __launch_bounds__(MT) k_mx_correct(const MixDesc* __restrict__ M
   MX_TILE(0)
   const Geo G = M.G;
   const long lde = M.lev[0].ld;
-  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
-  if (i >= G.nx || j >= G.ny) return;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  if (i >= G.nx) return;
   const double e0 = (double)M.e[0];
-  const long o = (long)j * G.ld + i;
-  M.x[o] = __dadd_rn(M.x[o], __dsub_rn((double)M.e[(long)j * lde + i], e0));
+  MX_ROWS({
+    const int j = tl.j0 + ty;
+    if (j < G.ny) {
+      const long o = (long)j * G.ld + i;
+      M.x[o] = __dadd_rn(M.x[o], __dsub_rn((double)M.e[(long)j * lde + i], e0));
+    }
+  })
 }
 
 // r64 = b - A x with the reference's pinned operator; ||r64||^2, sum(r64); outer test
 __global__ void __launch_bounds__(MT) k_mx_resid(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                   MixLoop* ml, cudaGraphConditionalHandle cond_outer, int use_cond) {
   MX_TILE(0)
-  MX_SMEM_SLOT(sa0);
-  MX_SMEM_SLOT(sa1);
-  __shared__ long long wred[(MT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ RedSmem rsm;
   const Geo G = M.G;
-  XASlot* slots = M.slots;
   MixCtrl* ctrl = M.ctrl;
-  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
-  XTerm t0, t1;
-  xa_zero(t0);
-  xa_zero(t1);
-  unsigned f0 = 0u, f1 = 0u;
-  if (i < G.nx && j < G.ny) {
-    View2<const double> X{M.x, G.ld};
-    const double ax = (i == 0 && j == 0) ? X(0, 0) : -lap_coherent_at(X, j, i, G.g);
-    const long o = (long)j * G.ld + i;
-    const double rv = __dsub_rn(M.b[o], ax);
-    M.r64[o] = rv;
-    xa_term_prod(rv, rv, t0, f0);
-    xa_term_val(rv, t1, f1);
-  }
-  mx_reduce(&slots[M_RR64], &t0, 1, f0, sa0, wred, ired);
-  mx_reduce(&slots[M_SUM64], &t1, 1, f1, sa1, wred, ired);
-  XASlot* sl[2] = {&slots[M_RR64], &slots[M_SUM64]};
-  if (xa_finish(sl, 2, M.nt0) && threadIdx.x == 0) {
-    const double rr = slots[M_RR64].result;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  double v[2] = {0.0, 0.0}, out[2];
+  View2<const double> X{M.x, G.ld};
+  MX_ROWS({
+    const int j = tl.j0 + ty;
+    if (i < G.nx && j < G.ny) {
+      const double ax = (i == 0 && j == 0) ? X(0, 0) : -lap_coherent_at(X, j, i, G.g);
+      const long o = (long)j * G.ld + i;
+      const double rv = __dsub_rn(M.b[o], ax);
+      M.r64[o] = rv;
+      v[0] += rv * rv;
+      v[1] += rv;
+    }
+  })
+  if (MX_RED(2, v, out) && threadIdx.x == 0) {
+    const double rr = out[0];
     ctrl->rr64 = rr;
-    ctrl->sum64 = slots[M_SUM64].result;
+    ctrl->sum64 = out[1];
     ctrl->outer += 1;
-    const bool conv = !(__dsqrt_rn(rr) > ctrl->tol_abs_out);
+    const bool conv = !(sqrt(rr) > ctrl->tol_abs_out);
     ctrl->converged = conv ? 1 : 0;
     if (conv || ctrl->outer >= ctrl->max_outer) {
       ctrl->outer_done = 1;
@@ -680,6 +652,14 @@ __global__ void k_mx_finish(const MixDesc* __restrict__ MD, int n) {
   c->info = m->converged ? 0 : M.maxiter_report;
   c->zero_rhs = (m->bnorm == 0.0) ? 1 : 0;
   c->bnrm2 = m->bnorm;
+}
+
+// Dependent binary32 FMAs for a few tens of microseconds (no memory waits):
+// keeps the stream busy while the host queues the launches behind it.
+__global__ void k_pad(float* sink, int n) {
+  float x = (float)threadIdx.x;
+  for (int i = 0; i < n; ++i) x = fmaf(x, 1.0000001f, 0.5f);
+  if (x == -1.f) *sink = x;
 }
 
 // ---- host side --------------------------------------------------------------
@@ -713,8 +693,9 @@ static void level_dims(int nx, int ny, std::vector<std::pair<int, int>>& dims, i
 }
 
 static void add_mtiles(std::vector<MTile>& v, int k, int nx, int ny) {
+  int loc = 0;
   for (int j0 = 0; j0 < ny; j0 += BY)
-    for (int i0 = 0; i0 < nx; i0 += BX) v.push_back(MTile{k, i0, j0, 0});
+    for (int i0 = 0; i0 < nx; i0 += BX) v.push_back(MTile{k, i0, j0, loc++});
 }
 
 int batch_create(const MixParams* prm, int n, Batch** out) {
@@ -738,8 +719,9 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     B->maxlev = std::max(B->maxlev, (int)dims[k].size());
     for (auto& d : dims[k]) bytes += 4 * up((size_t)round_up(d.first, 32) * d.second * sizeof(float));
     const size_t v0 = up((size_t)round_up(prm[k].nx, 32) * prm[k].ny * sizeof(float));
-    bytes += 4 * v0 + up((size_t)prm[k].ld64 * prm[k].ny * sizeof(double)) + up(M_COUNT * sizeof(XASlot)) +
-             up(sizeof(MixCtrl));
+    const size_t nt0 = (size_t)((prm[k].nx + BX - 1) / BX) * ((prm[k].ny + BY - 1) / BY);
+    bytes += 4 * v0 + up((size_t)prm[k].ld64 * prm[k].ny * sizeof(double)) + up(2 * nt0 * sizeof(double)) +
+             up(sizeof(unsigned)) + up(sizeof(MixCtrl));
   }
   // tile tables
   std::vector<MTile> tl[MAX_LEVELS], tlr[MAX_LEVELS], tpre[MAX_LEVELS];
@@ -755,7 +737,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   }
   for (int l = 0; l < B->maxlev; ++l)
     bytes += up(tl[l].size() * sizeof(MTile)) + up(tlr[l].size() * sizeof(MTile)) + up(tpre[l].size() * sizeof(MTile));
-  bytes += up(n * sizeof(MixDesc)) + up(sizeof(MixLoop));
+  bytes += up(n * sizeof(MixDesc)) + up(sizeof(MixLoop)) + up(sizeof(float));
   if (cudaMalloc(&B->ws, bytes) != cudaSuccess) {
     delete B;
     return set_error(PFGB_ENOMEM, "cudaMalloc of the mixed-solver workspace failed");
@@ -796,14 +778,15 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     M.p1 = (float*)take(v0);
     M.q = (float*)take(v0);
     M.r64 = (double*)take((size_t)prm[k].ld64 * prm[k].ny * sizeof(double));
-    M.slots = (XASlot*)take(M_COUNT * sizeof(XASlot));
+    M.nt0 = ((prm[k].nx + BX - 1) / BX) * ((prm[k].ny + BY - 1) / BY);
+    M.part = (double*)take(2 * (size_t)M.nt0 * sizeof(double));
+    M.ticket = (unsigned*)take(sizeof(unsigned));
     M.ctrl = (MixCtrl*)take(sizeof(MixCtrl));
     M.b = prm[k].b;
     M.x = prm[k].x;
     M.ctrl64 = prm[k].ctrl64;
     M.active = prm[k].active;
     M.maxiter_report = prm[k].maxiter_report;
-    M.nt0 = ((prm[k].nx + BX - 1) / BX) * ((prm[k].ny + BY - 1) / BY);
     MixCtrl hc = {};
     hc.tol_out = prm[k].tol_out;
     hc.tol_in = prm[k].tol_in;
@@ -827,6 +810,9 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   }
   B->dd = (MixDesc*)take(n * sizeof(MixDesc));
   B->loop = (MixLoop*)take(sizeof(MixLoop));
+  B->pad = (float*)take(sizeof(float));
+  B->gmax_o = gmax_o;
+  B->gmax_i = gmax_i;
   MixLoop ml0 = {0, 0, 0, 0, gmax_o, gmax_i, 0};
   cudaMemcpy(B->loop, &ml0, sizeof(MixLoop), cudaMemcpyHostToDevice);
   cudaError_t e = cudaMemcpy(B->dd, B->hd.data(), n * sizeof(MixDesc), cudaMemcpyHostToDevice);
@@ -838,6 +824,25 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     return set_error(PFGB_ECUDA, std::string("mixed batch set-up: ") + cudaGetErrorString(e));
   }
   *out = B;
+  return PFGB_OK;
+}
+
+int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer, int max_inner, int maxiter_report) {
+  if (k < 0 || k >= B->n) return set_error(PFGB_EINVAL, "instance index out of range");
+  if (max_outer < 1 || max_outer + 1 > B->gmax_o || max_inner < 1 || max_inner + 1 > B->gmax_i)
+    return set_error(PFGB_EINVAL, "mixed iteration limits above the batch's largest");
+  MixCtrl head = {};
+  head.tol_out = tol_out;
+  head.tol_in = tol_in;
+  head.max_outer = max_outer;
+  head.max_inner = max_inner;
+  // the four leading fields; the rest of the control block is rewritten by every solve
+  cudaError_t e = cudaMemcpy(B->hd[k].ctrl, &head, offsetof(MixCtrl, bnorm), cudaMemcpyHostToDevice);
+  B->hd[k].maxiter_report = maxiter_report;
+  if (e == cudaSuccess)
+    e = cudaMemcpy(reinterpret_cast<char*>(B->dd + k) + offsetof(MixDesc, maxiter_report), &maxiter_report,
+                   sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("mixed tolerances: ") + cudaGetErrorString(e));
   return PFGB_OK;
 }
 
@@ -909,6 +914,8 @@ int run_direct(Batch* B, cudaStream_t s) {
   const float omega = 0.8f;
   const int g0 = B->ntl[0];
   MixLoop h;
+  int timed_launches = 0;
+  if (B->ev_used) *B->ev_used = 0;
   auto read = [&]() -> bool {
     return cudaMemcpyAsync(&h, B->loop, sizeof(MixLoop), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
            cudaStreamSynchronize(s) == cudaSuccess;
@@ -923,7 +930,18 @@ int run_direct(Batch* B, cudaStream_t s) {
     k_mx_rz<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
     if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
     for (int pi = 0; h.inner_active > 0 && pi < h.gmax_i; ++pi) {
+      const bool timed = B->ev && 2 * timed_launches + 1 < B->nev;
+      if (timed) {
+        // the host has just waited for the stream: give it time to queue the event and the
+        // matvec behind a short arithmetic kernel, so that the interval holds the matvec alone
+        k_pad<<<1, 32, 0, s>>>(B->pad, 20000);
+        cudaEventRecord(B->ev[2 * timed_launches], s);
+      }
       k_mx_matvec<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
+      if (timed) {
+        cudaEventRecord(B->ev[2 * timed_launches + 1], s);
+        *B->ev_used = ++timed_launches;
+      }
       k_mx_update<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0);
       launch_vcycle(B, 1, omega, s);
       k_mx_rz<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);

@@ -8,7 +8,6 @@
 #include "graph.cuh"
 #include "stencil.cuh"
 #include "step64.cuh"
-#include "xacc.cuh"
 
 namespace pfgb {
 namespace mixed {
@@ -35,8 +34,6 @@ struct Geo {
   Grid2 g;
 };
 
-enum MixSlot { M_RR64 = 0, M_SUM64, M_RT, M_RZ, M_PQ, M_RR, M_COUNT };
-
 struct MixCtrl {
   double tol_out, tol_in;
   int max_outer, max_inner;
@@ -49,7 +46,7 @@ struct MixCtrl {
 
 // One tile of work of a mixed batch: instance and the tile's first cell.
 struct MTile {
-  int inst, i0, j0, pad;
+  int inst, i0, j0, loc;       // loc: index of the tile among its instance's tiles of the level
 };
 
 // Everything the mixed-precision kernels need about one instance.
@@ -62,7 +59,8 @@ struct MixDesc {
   double* r64;                 // binary64 refinement residual (pitch G.ld)
   const double* b;             // the step's right-hand side (binary64, pitch G.ld)
   double* x;                   // the step's pressure solution
-  XASlot* slots;
+  double* part;                // per-tile partial sums of the reductions (2 x nt0)
+  unsigned* ticket;            // arrival counter of the reductions
   MixCtrl* ctrl;
   Ctrl64* ctrl64;              // the step's control block (iteration summary)
   const int* active;           // the step's per-instance activity flag
@@ -91,6 +89,12 @@ struct Batch {
   int ntpre[MAX_LEVELS] = {};
   size_t coarse_smem = 0;                      // dynamic shared memory of the coarse CTA (largest instance)
   MixLoop* loop = nullptr;
+  int gmax_o = 1, gmax_i = 1;                  // trip bounds of the loop guards
+  // profiling (direct launches): events around each PCG matvec launch
+  cudaEvent_t* ev = nullptr;
+  int nev = 0;
+  int* ev_used = nullptr;
+  float* pad = nullptr;                        // sink of the profiling pad kernel
   char* ws = nullptr;
   size_t ws_bytes = 0;
 };
@@ -114,6 +118,8 @@ void batch_destroy(Batch* B);
 int append_solve(GraphChain& c, Batch* B);
 // The same with direct launches and host loop control (for profiling).
 int run_direct(Batch* B, cudaStream_t s);
+// New tolerances and iteration limits for instance k (limits within the loop guards).
+int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer, int max_inner, int maxiter_report);
 
 }  // namespace mixed
 }  // namespace pfgb

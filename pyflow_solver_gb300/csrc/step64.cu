@@ -1048,6 +1048,14 @@ int instance64_set_params(Instance64* I, int k, const pfgb_params* prm) {
   if (prm->lin_maxiter < 0 || prm->lin_maxiter > I->maxiter_max)
     return set_error(PFGB_EINVAL, "lin_maxiter above the batch's largest");
   if (prm->scheme < 0 || prm->scheme > 2) return set_error(PFGB_EINVAL, "unknown advection scheme");
+  if (I->mix) {
+    const double tol_out = prm->mixed_tol_outer > 0.0 ? prm->mixed_tol_outer : prm->lin_tol;
+    const double tol_in = prm->mixed_tol_inner > 0.0 ? prm->mixed_tol_inner : 1e-5;
+    const int max_outer = prm->mixed_max_outer > 0 ? prm->mixed_max_outer : 8;
+    const int max_inner = prm->mixed_max_inner > 0 ? prm->mixed_max_inner : 50;
+    if (int rc = mixed::set_tolerances(I->mix, k, tol_out, tol_in, max_outer, max_inner, prm->lin_maxiter))
+      return rc;
+  }
   InstDesc& D = I->hd[k];
   D.A.rtol = prm->lin_tol;
   D.A.maxiter = prm->lin_maxiter;
@@ -1067,16 +1075,22 @@ int instance64_set_graph(Instance64* I, int on) {
   return PFGB_OK;
 }
 
-// Per-launch timing of the matvec kernel in the following steps (single instance).
+// Per-launch timing of the (binary64 or binary32) matvec kernel in the following steps.
 int instance64_set_profiling(Instance64* I, int on) {
   if (on && I->ev.empty()) {
     int n = 2 * (I->maxiter_max > 0 ? I->maxiter_max : 1);
+    if (I->mix) n = std::max(n, 2 * I->mix->gmax_o * I->mix->gmax_i);
     I->ev.resize(n);
     for (int k = 0; k < n; ++k)
       if (cudaEventCreate(&I->ev[k]) != cudaSuccess) return set_error(PFGB_ECUDA, "cudaEventCreate failed");
   }
   I->profiling = on;
   I->ev_used = 0;
+  if (I->mix) {
+    I->mix->ev = on ? I->ev.data() : nullptr;
+    I->mix->nev = on ? (int)I->ev.size() : 0;
+    I->mix->ev_used = on ? &I->ev_used : nullptr;
+  }
   return PFGB_OK;
 }
 

@@ -105,3 +105,51 @@ def test_mixed_batch_equals_single_instances():
         for a, b in zip(fields(st), fields(states[k])):
             np.testing.assert_array_equal(a, b)
         assert all(d["Rp_converged"] for _, d in mine[1:])
+
+
+def test_step_arrays_and_slot_reuse():
+    """The array host path gives the same fields and records as step(); a slot
+    reused with new parameters equals a fresh run of the new request."""
+    from pyflow_solver_gb300 import ResidualManager, allocate_state, step
+    from pyflow_solver_gb300.batch import BatchedCavities
+    cases = [(64, 64, 100.0, 1.0, "quick"), (48, 32, 700.0, 1.4, "quick"), (32, 32, 250.0, 0.8, "upwind")]
+    for prec in ("fp64", "mixed"):
+        cfgs = []
+        for c in cases:
+            cfg = cfg_of(*c, maxiter=80)
+            cfg.precision = prec
+            cfgs.append(cfg)
+        sa = [allocate_state(c.nx, c.ny) for c in cfgs]
+        sb = [allocate_state(c.nx, c.ny) for c in cfgs]
+        A = BatchedCavities(cfgs, sa)
+        Bc = BatchedCavities(cfgs, sb)
+        for it in range(3):
+            ra = A.step()
+            ob = Bc.step_arrays()
+            cont = Bc.continuity(ob)
+            for k in range(len(cases)):
+                assert ra[k][0]["continuity"] == cont[k]
+                assert ra[k][1]["dt"] == ob["dt"][k]
+                assert ra[k][1]["cg_iterations"] == ob["cg_iterations"][k]
+        Bc.sync_meta()
+        for k in range(len(cases)):
+            for a, b in zip(fields(sa[k]), fields(sb[k])):
+                np.testing.assert_array_equal(a, b)
+            assert sa[k].meta["dt_prev"] == sb[k].meta["dt_prev"]
+            assert sa[k].meta["divergence_history"] == sb[k].meta["divergence_history"]
+        # slot 1 takes a new request (same grid, new Re and lid velocity)
+        new = cfg_of(48, 32, 2200.0, 0.6, "quick", maxiter=80)
+        new.precision = prec
+        Bc.set_params(1, new)
+        for _ in range(4):
+            Bc.step_arrays(active=[False, True, True])
+        Bc.sync_meta(1)
+        st = allocate_state(48, 32)
+        tr = ResidualManager()
+        for it in range(4):
+            step(new, st, tr, it)
+        for a, b in zip(fields(st), fields(sb[1])):
+            np.testing.assert_array_equal(a, b)
+        assert st.meta["dt_prev"] == sb[1].meta["dt_prev"]
+        A.close()
+        Bc.close()
