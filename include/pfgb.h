@@ -234,6 +234,21 @@ PFGB_API int pfgb_cg_solve_noalloc(int op, const double* b, double* x, int nx, i
                                    int precond, double jacobi_interior, double tol, int maxiter,
                                    void* stream, pfgb_solve_out* out);
 
+/* ---- tile autotuner ---------------------------------------------------------- */
+
+/* Time the three tile shapes of the binary64 CG kernel pair (32 x 8, 32 x 16,
+ * 32 x 32 cells per CTA) on this handle's own instances and keep the fastest
+ * for its following steps.  The exactly rounded reductions make every shape
+ * give identical results.  `variant` (may be NULL) receives the choice 0..2,
+ * `us_per_iteration` (may be NULL, else 3 doubles) the measured microseconds
+ * per CG iteration of each shape.  Synchronises `stream`; the handle's CG work
+ * vectors are overwritten (every step rewrites them).  A no-op with precision
+ * 1, whose pressure solve does not use these kernels.  No reference
+ * counterpart: the reference has no device kernels to tune. */
+PFGB_API int pfgb_autotune(pfgb_handle* handle, void* stream, int* variant, double* us_per_iteration);
+/* Select a CG tile shape directly (a choice cached from an earlier autotune). */
+PFGB_API int pfgb_set_cg_variant(pfgb_handle* handle, int variant);
+
 /* ---- measurement ----------------------------------------------------------- */
 
 /* Record CUDA events around every pressure-matvec launch (p = z + beta p;

@@ -79,6 +79,11 @@ class BatchedCavities:
             from .solvers import _handle
             graph = _handle.GRAPH_MODE
         _capi.check(_capi.load().pfgb_set_graph(h, 1 if graph else 0), "pfgb_set_graph")
+        from .solvers import _handle
+        self.cg_variant = None
+        if _handle.AUTOTUNE and params[0].precision == 0:
+            key = ("batch",) + tuple(sorted((int(s.nx), int(s.ny)) for s in self.states))
+            self.cg_variant = _handle.autotune(h, key)
 
     def __len__(self):
         return len(self.configs)

@@ -111,6 +111,16 @@ extern "C" int pfgb_cg_solve_noalloc(int op, const double* b, double* x, int nx,
                               out);
 }
 
+extern "C" int pfgb_autotune(pfgb_handle* handle, void* stream, int* variant, double* us_per_iteration) {
+  if (!handle) return set_error(PFGB_EINVAL, "null handle");
+  return instance64_autotune(handle->inst, (cudaStream_t)stream, variant, us_per_iteration);
+}
+
+extern "C" int pfgb_set_cg_variant(pfgb_handle* handle, int variant) {
+  if (!handle) return set_error(PFGB_EINVAL, "null handle");
+  return instance64_set_cg_variant(handle->inst, variant);
+}
+
 extern "C" int pfgb_set_graph(pfgb_handle* handle, int on) {
   if (!handle) return set_error(PFGB_EINVAL, "null handle");
   return instance64_set_graph(handle->inst, on);

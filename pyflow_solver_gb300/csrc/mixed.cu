@@ -21,6 +21,8 @@
 // Both loops are WHILE conditional nodes of the step graph: the inner loop
 // stops at ||r_in|| <= tol_in ||r~|| or max_inner iterations, the outer loop
 // at ||b - A x|| <= tol_out ||b|| or max_outer passes.
+#include <algorithm>
+#include <cmath>
 #include <cstddef>
 #include <cstdio>
 #include <string>
@@ -232,6 +234,7 @@ __global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, 
 // requires.  More cycles or sweeps do not lower the PCG iteration count.
 constexpr int CT = 1024;                     // threads of the coarse CTA
 constexpr int CMAX = 4096;                   // cells of its finest level
+constexpr int BMAX = 64;                     // bottom levels up to this size are solved exactly
 
 struct CLvl {                                // a shared-memory level
   int nx, ny, off;                           // off: offset into the level arrays
@@ -315,6 +318,18 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(const MixDesc* __restri
     for (int l = 0; l < nl; ++l) {
       const CLvl& Lv = L[l];
       if (l == nl - 1) {
+        const int nb = Lv.nx * Lv.ny;
+        if (M.binv) {
+          // exact bottom solve: e = A+ rh (at most BMAX cells)
+          for (int r = threadIdx.x; r < nb; r += CT) {
+            const float* row = M.binv + (long)r * nb;
+            float acc = 0.f;
+            for (int q = 0; q < nb; ++q) acc = fmaf(__ldg(row + q), rh[Lv.off + q], acc);
+            e[Lv.off + r] = acc;
+          }
+          __syncthreads();
+          break;
+        }
         C_FOR(Lv, { e[Lv.off + c] = 0.f; })
         __syncthreads();
         for (int s = 0; s < bottom_sweeps; ++s) c_sweep(Lv, rh, (s & 1) ? w : e, (s & 1) ? e : w, omega);
@@ -385,6 +400,7 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(const MixDesc* __restri
 using RedSmem = DRedSmem<MT>;
 
 #define MX_RED(R, vals, outv) dred_sum<R, MT>(vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
+#define MX_RED_FF(R, vals, outv) dred_sum_ff<R, MT>(vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
 
 // x = 0, r64 = b; ||b||^2 and sum(b); counts the instances that refine
 __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
@@ -464,7 +480,8 @@ __global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, 
   const Lvl L0 = M.lev[0];
   MixCtrl* ctrl = M.ctrl;
   const int i = tl.i0 + (threadIdx.x & 31);
-  double v[1] = {0.0}, out[1];
+  FF v[1] = {{0.f, 0.f}};
+  double out[1];
   MX_ROWS({
     const int j = tl.j0 + ty;
     if (i < G.nx && j < G.ny) {
@@ -472,10 +489,10 @@ __global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, 
       const float rf = __double2float_rn(rv);
       L0.f[(long)j * L0.ld + i] = rf;
       M.e[(long)j * L0.ld + i] = 0.f;
-      v[0] += (double)rf * (double)rf;
+      ff_add_prod(v[0], rf, rf);
     }
   })
-  if (MX_RED(1, v, out) && threadIdx.x == 0) {
+  if (MX_RED_FF(1, v, out) && threadIdx.x == 0) {
     const double rt = sqrt(out[0]);
     ctrl->rt_norm = rt;
     ctrl->tol_abs_in = ctrl->tol_in * rt;
@@ -492,15 +509,16 @@ __global__ void __launch_bounds__(MT) k_mx_rz(const MixDesc* __restrict__ MD, co
   const Lvl L0 = M.lev[0];
   MixCtrl* ctrl = M.ctrl;
   const int i = tl.i0 + (threadIdx.x & 31);
-  double v[1] = {0.0}, out[1];
+  FF v[1] = {{0.f, 0.f}};
+  double out[1];
   MX_ROWS({
     const int j = tl.j0 + ty;
     if (i < L0.nx && j < L0.ny) {
       const long o = (long)j * L0.ld + i;
-      v[0] += (double)L0.f[o] * (double)L0.u[o];
+      ff_add_prod(v[0], L0.f[o], L0.u[o]);
     }
   })
-  if (MX_RED(1, v, out) && threadIdx.x == 0) {
+  if (MX_RED_FF(1, v, out) && threadIdx.x == 0) {
     const double rz = out[0];
     if (ctrl->inner > 0) ctrl->beta = rz / ctrl->rho;
     ctrl->rho = rz;
@@ -533,7 +551,8 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD
   __syncthreads();
   const int tx = threadIdx.x & 31;
   const int gi = i0 + tx;
-  double v[1] = {0.0}, out[1];
+  FF v[1] = {{0.f, 0.f}};
+  double out[1];
   MX_ROWS({
     const int gj = j0 + ty;
     if (gi < L0.nx && gj < L0.ny) {
@@ -543,10 +562,10 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD
       const long o = (long)gj * L0.ld + gi;
       pnew[o] = pv;
       M.q[o] = qv;
-      v[0] += (double)pv * (double)qv;
+      ff_add_prod(v[0], pv, qv);
     }
   })
-  if (MX_RED(1, v, out) && threadIdx.x == 0) {
+  if (MX_RED_FF(1, v, out) && threadIdx.x == 0) {
     ctrl->pq = out[0];
     ctrl->alpha = ctrl->rho / out[0];
   }
@@ -563,7 +582,8 @@ __global__ void __launch_bounds__(MT) k_mx_update(const MixDesc* __restrict__ MD
   const float* __restrict__ p = (k & 1) ? M.p0 : M.p1;
   const float alpha = (float)ctrl->alpha;
   const int i = tl.i0 + (threadIdx.x & 31);
-  double v[1] = {0.0}, out[1];
+  FF v[1] = {{0.f, 0.f}};
+  double out[1];
   MX_ROWS({
     const int j = tl.j0 + ty;
     if (i < L0.nx && j < L0.ny) {
@@ -571,10 +591,10 @@ __global__ void __launch_bounds__(MT) k_mx_update(const MixDesc* __restrict__ MD
       M.e[o] = fmaf(alpha, p[o], M.e[o]);
       const float rv = fmaf(-alpha, M.q[o], L0.f[o]);
       L0.f[o] = rv;
-      v[0] += (double)rv * (double)rv;
+      ff_add_prod(v[0], rv, rv);
     }
   })
-  if (MX_RED(1, v, out) && threadIdx.x == 0) {
+  if (MX_RED_FF(1, v, out) && threadIdx.x == 0) {
     const double rr = out[0];
     const int it = k + 1;
     ctrl->inner = it;
@@ -676,8 +696,9 @@ static void level_dims(int nx, int ny, std::vector<std::pair<int, int>>& dims, i
     ly /= 2;
     dims.push_back({lx, ly});
   }
+  // levels of the coarse CTA: halve while possible until the level has at most BMAX cells
   int cn = 1, cx = lx, cy = ly;
-  while (cn < 8 && cx % 2 == 0 && cy % 2 == 0 && cx / 2 >= 2 && cy / 2 >= 2) {
+  while (cn < 8 && cx * cy > BMAX && cx % 2 == 0 && cy % 2 == 0 && cx / 2 >= 2 && cy / 2 >= 2) {
     cx /= 2;
     cy /= 2;
     ++cn;
@@ -690,6 +711,52 @@ static void level_dims(int nx, int ny, std::vector<std::pair<int, int>>& dims, i
     ax /= 2;
     ay /= 2;
   }
+}
+
+// Pseudo-inverse of the Neumann operator of an nx x ny level (face coefficients
+// cx, cy), as binary32 row-major n x n.  A is symmetric positive semidefinite
+// with the constants as its null space, so A+ = (A + J/n)^-1 - J/n with J the
+// all-ones matrix; the inverse is Gauss-Jordan elimination in binary64.
+static void neumann_pinv(int nx, int ny, double cx, double cy, std::vector<float>& out) {
+  const int n = nx * ny;
+  std::vector<double> a((size_t)n * 2 * n, 0.0);
+  auto A = [&](int r, int c) -> double& { return a[(size_t)r * 2 * n + c]; };
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      const int r = j * nx + i;
+      double d = 0.0;
+      if (i > 0) { d += cx; A(r, r - 1) -= cx; }
+      if (i < nx - 1) { d += cx; A(r, r + 1) -= cx; }
+      if (j > 0) { d += cy; A(r, r - nx) -= cy; }
+      if (j < ny - 1) { d += cy; A(r, r + nx) -= cy; }
+      A(r, r) += d;
+    }
+  for (int r = 0; r < n; ++r) {
+    for (int c = 0; c < n; ++c) A(r, c) += 1.0 / n;
+    A(r, n + r) = 1.0;
+  }
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(A(r, c)) > std::fabs(A(piv, c))) piv = r;
+    if (piv != c)
+      for (int k = 0; k < 2 * n; ++k) std::swap(A(c, k), A(piv, k));
+    const double inv = 1.0 / A(c, c);
+    for (int k = 0; k < 2 * n; ++k) A(c, k) *= inv;
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = A(r, c);
+      if (f != 0.0)
+        for (int k = 0; k < 2 * n; ++k) A(r, k) -= f * A(c, k);
+    }
+  }
+  out.assign((size_t)n * n, 0.f);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      // symmetrise the binary64 inverse before rounding, so the bottom operator is exactly symmetric
+      const double v = 0.5 * (A(r, n + c) + A(c, n + r)) - 1.0 / n;
+      out[(size_t)r * n + c] = (float)v;
+    }
 }
 
 static void add_mtiles(std::vector<MTile>& v, int k, int nx, int ny) {
@@ -706,6 +773,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   size_t bytes = 0;
   std::vector<std::vector<std::pair<int, int>>> dims(n);
   std::vector<int> cls(n), ctot(n);
+  std::vector<std::pair<int, int>> bdim(n);
   size_t smem = 0;
   for (int k = 0; k < n; ++k) {
     level_dims(prm[k].nx, prm[k].ny, dims[k], cls[k], ctot[k]);
@@ -716,6 +784,15 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
                                     "(nx and ny need enough factors of two)");
     }
     smem = std::max(smem, (size_t)5 * ctot[k] * sizeof(float));
+    {
+      int bx = last.first, by = last.second;
+      for (int l = 1; l < cls[k]; ++l) {
+        bx /= 2;
+        by /= 2;
+      }
+      bdim[k] = {bx, by};
+      if (bx * by <= BMAX) bytes += up((size_t)bx * by * bx * by * sizeof(float));
+    }
     B->maxlev = std::max(B->maxlev, (int)dims[k].size());
     for (auto& d : dims[k]) bytes += 4 * up((size_t)round_up(d.first, 32) * d.second * sizeof(float));
     const size_t v0 = up((size_t)round_up(prm[k].nx, 32) * prm[k].ny * sizeof(float));
@@ -782,6 +859,14 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     M.part = (double*)take(2 * (size_t)M.nt0 * sizeof(double));
     M.ticket = (unsigned*)take(sizeof(unsigned));
     M.ctrl = (MixCtrl*)take(sizeof(MixCtrl));
+    M.binv = nullptr;
+    if (bdim[k].first * bdim[k].second <= BMAX) {
+      std::vector<float> pinv;
+      neumann_pinv(bdim[k].first, bdim[k].second, (double)cx, (double)cy, pinv);
+      float* dst = (float*)take(pinv.size() * sizeof(float));
+      cudaMemcpy(dst, pinv.data(), pinv.size() * sizeof(float), cudaMemcpyHostToDevice);
+      M.binv = dst;
+    }
     M.b = prm[k].b;
     M.x = prm[k].x;
     M.ctrl64 = prm[k].ctrl64;

@@ -54,6 +54,7 @@ struct MixDesc {
   Geo G;                       // binary64 geometry of the refinement
   int nlev;                    // global levels; the last one is solved by the coarse CTA
   int coarse_levels;           // levels resolved inside the coarse CTA
+  const float* binv;           // pseudo-inverse of the bottom level (null: Jacobi sweeps instead)
   Lvl lev[MAX_LEVELS];
   float *e, *p0, *p1, *q;      // binary32 PCG vectors (pitch lev[0].ld)
   double* r64;                 // binary64 refinement residual (pitch G.ld)

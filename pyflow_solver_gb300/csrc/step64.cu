@@ -300,14 +300,16 @@ __global__ void k_loop_guard(LoopCtl* lc, cudaGraphConditionalHandle cond, int u
 // OP 1: A = lap_c with identity rows on the boundary ring (manufactured mode).
 // The iteration index k is read from the control block and selects the
 // ping-pong buffers: iteration k reads p[k & 1] and writes p[(k + 1) & 1].
-template <int OP>
+// R: rows per thread (the tile is 32 x 8R cells); the autotuner picks R per handle.
+template <int OP, int R = RPT>
 __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  constexpr int TYv = R * PB_Y;
   TILE_PROLOGUE
   Ctrl64* ctrl = D.ctrl;
   if (*(volatile int*)&ctrl->done) return;
-  __shared__ double pn[TY + 2][TX + 2];
-  __shared__ double gxs[TY][TX + 1];
-  __shared__ double gys[TY + 1][TX];
+  __shared__ double pn[TYv + 2][TX + 2];
+  __shared__ double gxs[TYv][TX + 1];
+  __shared__ double gys[TYv + 1][TX];
   __shared__ long long sacc[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
   __shared__ int ired[32];
@@ -319,10 +321,10 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
   const double* __restrict__ r = D.r;
   const int i0 = tl.i0, j0 = tl.j0;
   const double beta = (k > 0) ? ctrl->beta : 0.0;
-  for (int idx = threadIdx.x; idx < (TY + 2) * (TX + 2); idx += NT) {
+  for (int idx = threadIdx.x; idx < (TYv + 2) * (TX + 2); idx += NT) {
     int jj = idx / (TX + 2) - 1, ii = idx % (TX + 2) - 1;
     int gj = j0 + jj, gi = i0 + ii;
-    bool corner = (jj < 0 || jj >= TY) && (ii < 0 || ii >= TX);
+    bool corner = (jj < 0 || jj >= TYv) && (ii < 0 || ii >= TX);
     double val = 0.0;
     if (!corner && gj >= 0 && gj < G.ny && gi >= 0 && gi < G.nx) {
       long o = (long)gj * G.ld + gi;
@@ -332,14 +334,14 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
     pn[jj + 1][ii + 1] = val;
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < TY * (TX + 1); idx += NT) {
+  for (int idx = threadIdx.x; idx < TYv * (TX + 1); idx += NT) {
     int jj = idx / (TX + 1), ii = idx % (TX + 1) - 1;
     int gj = j0 + jj, gi = i0 + ii;
     double gv = 0.0;
     if (gj < G.ny && gi >= 0 && gi < G.nx - 1) gv = DIVH(SUB(pn[jj + 1][ii + 2], pn[jj + 1][ii + 1]), G.g.sx);
     gxs[jj][ii + 1] = gv;
   }
-  for (int idx = threadIdx.x; idx < (TY + 1) * TX; idx += NT) {
+  for (int idx = threadIdx.x; idx < (TYv + 1) * TX; idx += NT) {
     int jj = idx / TX - 1, ii = idx % TX;
     int gj = j0 + jj, gi = i0 + ii;
     double gv = 0.0;
@@ -348,10 +350,10 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
   }
   __syncthreads();
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  XTerm t[RPT];
+  XTerm t[R];
   unsigned fl = 0u;
 #pragma unroll
-  for (int rr = 0; rr < RPT; ++rr) {
+  for (int rr = 0; rr < R; ++rr) {
     xa_zero(t[rr]);
     int jj = ty + rr * PB_Y;
     int gj = j0 + jj, gi = i0 + tx;
@@ -370,7 +372,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
       xa_term_prod(pv, qv, t[rr], fl);
     }
   }
-  reduce_terms(&slots[S_PQ], t, RPT, fl, sacc, wred, ired);
+  reduce_terms(&slots[S_PQ], t, R, fl, sacc, wred, ired);
   XASlot* sl[1] = {&slots[S_PQ]};
   if (xa_finish(sl, 1, D.nt_cg) && threadIdx.x == 0) {
     const double pq = slots[S_PQ].result;
@@ -381,6 +383,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
 
 // x += alpha p; r -= alpha q; r.r; r.(M r).  An instance that finishes
 // leaves the loop control's active count; the last one stops the loop.
+template <int R = RPT>
 __global__ void __launch_bounds__(NT) k_cg_update(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
                                                    LoopCtl* lc, cudaGraphConditionalHandle cond, int use_cond) {
   TILE_PROLOGUE
@@ -398,10 +401,10 @@ __global__ void __launch_bounds__(NT) k_cg_update(const InstDesc* __restrict__ I
   const int i0 = tl.i0, j0 = tl.j0;
   const double alpha = ctrl->alpha;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  XTerm trr[RPT], trz[RPT];
+  XTerm trr[R], trz[R];
   unsigned f0 = 0u, f1 = 0u;
 #pragma unroll
-  for (int rr = 0; rr < RPT; ++rr) {
+  for (int rr = 0; rr < R; ++rr) {
     xa_zero(trr[rr]);
     xa_zero(trz[rr]);
     int gj = j0 + ty + rr * PB_Y, gi = i0 + tx;
@@ -415,8 +418,8 @@ __global__ void __launch_bounds__(NT) k_cg_update(const InstDesc* __restrict__ I
       xa_term_prod(rv, jacobi_apply(G, gj, gi, rv), trz[rr], f1);
     }
   }
-  reduce_terms(&slots[S_RR], trr, RPT, f0, sacc0, wred, ired);
-  reduce_terms(&slots[S_RZ], trz, RPT, f1, sacc1, wred, ired);
+  reduce_terms(&slots[S_RR], trr, R, f0, sacc0, wred, ired);
+  reduce_terms(&slots[S_RZ], trz, R, f1, sacc1, wred, ired);
   XASlot* sl[2] = {&slots[S_RR], &slots[S_RZ]};
   if (xa_finish(sl, 2, D.nt_cg) && threadIdx.x == 0) {
     double rr = slots[S_RR].result;
@@ -612,6 +615,9 @@ static void add_tiles(std::vector<Tile>& v, int k, int nx, int ny, int th) {
 
 static int count_tiles(int nx, int ny, int th) { return ((nx + TX - 1) / TX) * ((ny + th - 1) / th); }
 
+constexpr int NVAR = 3;                          // CG tile variants: rows per thread 1, 2, 4
+constexpr int VAR_R[NVAR] = {1, 2, 4};
+
 static Geo64 make_geo(int nx, int ny, long ld, double dx, double dy, double invd, int jacobi) {
   Geo64 G;
   G.nx = nx;
@@ -634,8 +640,13 @@ struct Instance64 {
   std::vector<InstDesc> hd;          // host copy of the descriptors
   InstDesc* dd = nullptr;            // device descriptors
   Tile* tpc = nullptr;               // per-cell tiles (32 x 8)
-  Tile* tcg = nullptr;               // CG tiles (32 x 16)
+  Tile* tcg = nullptr;               // CG tiles of the selected variant
   int ntpc = 0, ntcg = 0;
+  // CG tile variants 32 x 8R (R = 1, 2, 4 rows per thread); the autotuner selects one
+  Tile* tcgv[NVAR] = {};
+  int ntcgv[NVAR] = {};
+  std::vector<int> ntcg_inst[NVAR];  // per-instance CG tile counts of each variant
+  int cg_var = 1;
   LoopCtl* lc = nullptr;
   int maxiter_max = 0;
   char* ws = nullptr;
@@ -680,19 +691,25 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
   std::vector<size_t> vec(n);
   size_t bytes = 0;
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-  std::vector<Tile> tpc, tcg;
+  std::vector<Tile> tpc, tcgv[NVAR];
   for (int k = 0; k < n; ++k) {
     const long ld = round_up(prms[k].nx, 32);
     vec[k] = up((size_t)ld * prms[k].ny * sizeof(double));
     bytes += 8 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64));
     add_tiles(tpc, k, prms[k].nx, prms[k].ny, PB_Y);
-    add_tiles(tcg, k, prms[k].nx, prms[k].ny, TY);
+    for (int v = 0; v < NVAR; ++v) {
+      add_tiles(tcgv[v], k, prms[k].nx, prms[k].ny, VAR_R[v] * PB_Y);
+      I->ntcg_inst[v].push_back(count_tiles(prms[k].nx, prms[k].ny, VAR_R[v] * PB_Y));
+    }
     I->maxiter_max = std::max(I->maxiter_max, prms[k].lin_maxiter);
   }
   I->ntpc = (int)tpc.size();
-  I->ntcg = (int)tcg.size();
-  bytes += up(n * sizeof(InstDesc)) + up(tpc.size() * sizeof(Tile)) + up(tcg.size() * sizeof(Tile)) +
-           up(sizeof(LoopCtl)) + up(n * sizeof(StepIn)) + up(n * sizeof(StepOut64));
+  bytes += up(n * sizeof(InstDesc)) + up(tpc.size() * sizeof(Tile)) + up(sizeof(LoopCtl)) + up(n * sizeof(StepIn)) +
+           up(n * sizeof(StepOut64));
+  for (int v = 0; v < NVAR; ++v) {
+    I->ntcgv[v] = (int)tcgv[v].size();
+    bytes += up(tcgv[v].size() * sizeof(Tile));
+  }
   if (cudaMalloc(&I->ws, bytes) != cudaSuccess) {
     delete I;
     return set_error(PFGB_ENOMEM, "cudaMalloc of the workspace failed");
@@ -737,11 +754,13 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     D.slots = (XASlot*)take(S_COUNT * sizeof(XASlot));
     D.ctrl = (Ctrl64*)take(sizeof(Ctrl64));
     D.nt_pc = count_tiles(prm.nx, prm.ny, PB_Y);
-    D.nt_cg = count_tiles(prm.nx, prm.ny, TY);
+    D.nt_cg = I->ntcg_inst[I->cg_var][k];
   }
   I->dd = (InstDesc*)take(n * sizeof(InstDesc));
   I->tpc = (Tile*)take(tpc.size() * sizeof(Tile));
-  I->tcg = (Tile*)take(tcg.size() * sizeof(Tile));
+  for (int v = 0; v < NVAR; ++v) I->tcgv[v] = (Tile*)take(tcgv[v].size() * sizeof(Tile));
+  I->tcg = I->tcgv[I->cg_var];
+  I->ntcg = I->ntcgv[I->cg_var];
   I->lc = (LoopCtl*)take(sizeof(LoopCtl));
   I->in_d = (StepIn*)take(n * sizeof(StepIn));
   I->out_d = (StepOut64*)take(n * sizeof(StepOut64));
@@ -750,7 +769,8 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     I->hd[k].out = I->out_d + k;
   }
   cudaError_t e = cudaMemcpy(I->tpc, tpc.data(), tpc.size() * sizeof(Tile), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(I->tcg, tcg.data(), tcg.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+  for (int v = 0; v < NVAR; ++v)
+    if (e == cudaSuccess) e = cudaMemcpy(I->tcgv[v], tcgv[v].data(), tcgv[v].size() * sizeof(Tile), cudaMemcpyHostToDevice);
   LoopCtl lc0 = {0, 0, I->maxiter_max + 1, 0};
   if (e == cudaSuccess) e = cudaMemcpy(I->lc, &lc0, sizeof(LoopCtl), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMallocHost(&I->out_h, n * sizeof(StepOut64));
@@ -856,6 +876,19 @@ __global__ void k_loop_reset(LoopCtl* lc) {
   }
 }
 
+// The CG kernel pair of tile variant var.
+template <int OP>
+static void launch_matvec(int var, int grid, cudaStream_t s, const InstDesc* dd, const Tile* t) {
+  if (var == 0) k_cg_matvec<OP, 1><<<grid, NT, 0, s>>>(dd, t);
+  else if (var == 2) k_cg_matvec<OP, 4><<<grid, NT, 0, s>>>(dd, t);
+  else k_cg_matvec<OP, 2><<<grid, NT, 0, s>>>(dd, t);
+}
+static void launch_update(int var, int grid, cudaStream_t s, const InstDesc* dd, const Tile* t) {
+  if (var == 0) k_cg_update<1><<<grid, NT, 0, s>>>(dd, t, nullptr, 0ull, 0);
+  else if (var == 2) k_cg_update<4><<<grid, NT, 0, s>>>(dd, t, nullptr, 0ull, 0);
+  else k_cg_update<2><<<grid, NT, 0, s>>>(dd, t, nullptr, 0ull, 0);
+}
+
 // Direct launches of the projection stage (host loop bound = largest maxiter).
 static void enqueue_projection(Instance64* I, cudaStream_t s) {
   k_rhs<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
@@ -863,12 +896,12 @@ static void enqueue_projection(Instance64* I, cudaStream_t s) {
   for (int k = 0; k < I->maxiter_max; ++k) {
     const bool timed = I->profiling && (size_t)(2 * k + 1) < I->ev.size();
     if (timed) cudaEventRecord(I->ev[2 * k], s);
-    k_cg_matvec<0><<<I->ntcg, NT, 0, s>>>(I->dd, I->tcg);
+    launch_matvec<0>(I->cg_var, I->ntcg, s, I->dd, I->tcg);
     if (timed) {
       cudaEventRecord(I->ev[2 * k + 1], s);
       I->ev_used = k + 1;
     }
-    k_cg_update<<<I->ntcg, NT, 0, s>>>(I->dd, I->tcg, nullptr, 0ull, 0);
+    launch_update(I->cg_var, I->ntcg, s, I->dd, I->tcg);
   }
   k_post_resid<0><<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
   k_pin_correct<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
@@ -916,8 +949,10 @@ static int build_graph(Instance64* I, int mode) {
     c.kernel(k_cg_init, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc, I->lc);
     c.kernel(k_loop_arm, dim3(1), dim3(32), I->lc, cond, 1);
     body = c.while_loop_with(cond);
-    body.kernel(k_cg_matvec<0>, gc, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tcg);
-    body.kernel(k_cg_update, gc, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tcg, I->lc, cond, 1);
+    auto mv = I->cg_var == 0 ? k_cg_matvec<0, 1> : (I->cg_var == 2 ? k_cg_matvec<0, 4> : k_cg_matvec<0, 2>);
+    auto up = I->cg_var == 0 ? k_cg_update<1> : (I->cg_var == 2 ? k_cg_update<4> : k_cg_update<2>);
+    body.kernel(mv, gc, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tcg);
+    body.kernel(up, gc, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tcg, I->lc, cond, 1);
     body.kernel(k_loop_guard, dim3(1), dim3(32), I->lc, cond, 1);
   }
   c.kernel(k_post_resid<0>, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
@@ -1067,6 +1102,117 @@ int instance64_set_params(Instance64* I, int k, const pfgb_params* prm) {
   D.scheme = prm->scheme;
   I->P[k] = *prm;
   I->desc_dirty = true;
+  return PFGB_OK;
+}
+
+// ---- CG tile autotuner ----------------------------------------------------------
+//
+// The CG kernel pair (matvec + update) comes in three tile shapes, 32 x 8R cells
+// with R = 1, 2, 4 rows per thread.  The exact reductions make the result
+// independent of the shape, so the choice is free: the tuner times each
+// variant on this handle's own instances and keeps the fastest.
+
+__global__ void k_tune_fill(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
+  const int i = tl.i0 + (threadIdx.x & 31), j = tl.j0 + (threadIdx.x >> 5);
+  if (i >= G.nx || j >= G.ny) return;
+  const long o = (long)j * G.ld + i;
+  const double a = 0.5 + 1e-3 * (double)((i * 7919 + j * 104729) % 1000);
+  D.r[o] = a;
+  D.p0[o] = 1.0 - a;
+  D.p1[o] = a - 0.25;
+  D.x[o] = 0.0;
+}
+
+__global__ void k_tune_arm(const InstDesc* __restrict__ ID, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  Ctrl64* c = ID[k].ctrl;
+  c->done = 0;
+  c->iter = 0;
+  c->beta = 0.5;
+  c->alpha = 1e-3;
+  c->rho = 1.0;
+  c->atol = -1.0;
+}
+
+static void set_cg_variant(Instance64* I, int v) {
+  I->cg_var = v;
+  I->tcg = I->tcgv[v];
+  I->ntcg = I->ntcgv[v];
+  for (int k = 0; k < I->n; ++k) I->hd[k].nt_cg = I->ntcg_inst[v][k];
+  I->desc_dirty = true;
+  if (I->exec) {
+    cudaGraphExecDestroy(I->exec);
+    I->exec = nullptr;
+  }
+  if (I->graph) {
+    cudaGraphDestroy(I->graph);
+    I->graph = nullptr;
+  }
+  I->graph_mode = -1;
+}
+
+int instance64_set_cg_variant(Instance64* I, int v) {
+  if (v < 0 || v >= NVAR) return set_error(PFGB_EINVAL, "CG tile variant must be 0, 1 or 2");
+  set_cg_variant(I, v);
+  return PFGB_OK;
+}
+
+int instance64_autotune(Instance64* I, cudaStream_t s, int* chosen, double* us) {
+  if (I->mix) {  // the binary64 CG kernels do not run in the mixed form
+    if (chosen) *chosen = I->cg_var;
+    return PFGB_OK;
+  }
+  std::vector<InstDesc> saved = I->hd;
+  for (int k = 0; k < I->n; ++k) {
+    I->hd[k].active = 1;
+    I->hd[k].A.maxiter = 1 << 30;
+  }
+  float best = 1e30f;
+  int best_v = I->cg_var;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaError_t err = cudaSuccess;
+  for (int v = 0; v < NVAR && err == cudaSuccess; ++v) {
+    for (int k = 0; k < I->n; ++k) I->hd[k].nt_cg = I->ntcg_inst[v][k];
+    err = cudaMemcpyAsync(I->dd, I->hd.data(), I->n * sizeof(InstDesc), cudaMemcpyHostToDevice, s);
+    if (err != cudaSuccess) break;
+    k_tune_fill<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_tune_arm<<<(I->n + 127) / 128, 128, 0, s>>>(I->dd, I->n);
+    for (int w = 0; w < 2; ++w) {
+      launch_matvec<0>(v, I->ntcgv[v], s, I->dd, I->tcgv[v]);
+      launch_update(v, I->ntcgv[v], s, I->dd, I->tcgv[v]);
+    }
+    const int reps = 10;
+    cudaEventRecord(e0, s);
+    for (int w = 0; w < reps; ++w) {
+      launch_matvec<0>(v, I->ntcgv[v], s, I->dd, I->tcgv[v]);
+      launch_update(v, I->ntcgv[v], s, I->dd, I->tcgv[v]);
+    }
+    cudaEventRecord(e1, s);
+    err = cudaEventSynchronize(e1);
+    if (err != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const float per = 1e3f * ms / reps;
+    if (us) us[v] = per;
+    if (per < best) {
+      best = per;
+      best_v = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  I->hd = saved;
+  if (err == cudaSuccess) err = cudaGetLastError();
+  if (err != cudaSuccess) {
+    I->desc_dirty = true;
+    return set_error(PFGB_ECUDA, std::string("autotune: ") + cudaGetErrorString(err));
+  }
+  set_cg_variant(I, best_v);
+  if (chosen) *chosen = best_v;
   return PFGB_OK;
 }
 

@@ -8,6 +8,22 @@ from .. import _capi
 
 # Run each step as one CUDA graph (True) or as individual kernel launches.
 GRAPH_MODE = True
+# Pick the binary64 CG tile shape by timing (pfgb_autotune) once per grid size.
+AUTOTUNE = True
+_TUNED: dict = {}
+
+
+def autotune(handle, key) -> int:
+    """Tile variant of the binary64 CG kernels for this handle: timed once per key, then reused."""
+    lib = _capi.load()
+    if key in _TUNED:
+        _capi.check(lib.pfgb_set_cg_variant(handle, _TUNED[key]), "pfgb_set_cg_variant")
+        return _TUNED[key]
+    from .._device import stream_handle
+    v = ctypes.c_int()
+    _capi.check(lib.pfgb_autotune(handle, stream_handle(), ctypes.byref(v), None), "pfgb_autotune")
+    _TUNED[key] = v.value
+    return v.value
 
 
 class Instance:
@@ -20,6 +36,9 @@ class Instance:
         self._h = h
         self.params = params
         _capi.check(lib.pfgb_set_graph(h, 1 if GRAPH_MODE else 0), "pfgb_set_graph")
+        self.cg_variant = None
+        if AUTOTUNE and params.precision == 0:
+            self.cg_variant = autotune(h, ("single", params.nx, params.ny))
 
     @property
     def handle(self):
