@@ -148,12 +148,23 @@ class ClockSampler:
 
 # ---- kernel-launch accounting ------------------------------------------------
 
-def mg_levels(nx, ny):
-    """Global multigrid levels of the mixed solve (the last one is the coarse CTA's)."""
+def mg_levels(nx, ny, dx=None, dy=None):
+    """Global multigrid levels of the mixed solve (the last one is the coarse CTA's):
+    halve both axes, or only the strongly coupled one, while above 4096 cells."""
+    import numpy as np
+    dx = 1.0 / max(nx - 1, 1) if dx is None else dx
+    dy = 1.0 / max(ny - 1, 1) if dy is None else dy
+    cx, cy = float(np.float32(1.0 / (dx * dx))), float(np.float32(1.0 / (dy * dy)))
     n, lx, ly = 1, nx, ny
-    while n < 16 and lx % 2 == 0 and ly % 2 == 0 and lx // 2 >= 8 and ly // 2 >= 8 and lx * ly > 4096:
-        lx //= 2
-        ly //= 2
+    while n < 16 and lx * ly > 4096:
+        fx, fy = lx % 2 == 0 and lx // 2 >= 8, ly % 2 == 0 and ly // 2 >= 8
+        px, py = (2, 1) if cx > 2 * cy else ((1, 2) if cy > 2 * cx else (2, 2))
+        if not ((px == 1 or fx) and (py == 1 or fy)):
+            px, py = (2, 2) if (fx and fy) else ((2, 1) if fx else ((1, 2) if fy else (0, 0)))
+        if px == 0:
+            break
+        lx, ly = lx // px, ly // py
+        cx, cy = cx * py / px, cy * px / py
         n += 1
     return n
 
@@ -162,8 +173,8 @@ def launches_per_step(precision, cg_iters, passes, nlev):
     """Kernel launches of one step from its loop trip counts."""
     if precision == "fp64":
         return 11 + 3 * cg_iters
-    v = 3 * nlev - 2
-    return 13 + passes * (7 + v) + cg_iters * (4 + v)
+    v = 2 * nlev - 1                  # down-sweeps, the coarse CTA, up-sweeps
+    return 13 + passes * (6 + v) + cg_iters * (3 + v)
 
 
 # ---- CPU arm -----------------------------------------------------------------

@@ -59,6 +59,15 @@ struct View2 {
   __device__ __forceinline__ T& operator()(int j, int i) const { return p[(long)j * ld + i]; }
 };
 
+// The same view with loads through L2 (ld.global.cg): for arrays that other
+// SMs wrote earlier in the same launch.
+template <typename T>
+struct View2Cg {
+  const T* p;
+  long ld;
+  __device__ __forceinline__ T operator()(int j, int i) const { return __ldcg(p + (long)j * ld + i); }
+};
+
 // Ordered bit pattern of a non-negative double (NaN sorts above +inf), for
 // exact max reductions with 64-bit integer atomics.
 __device__ __forceinline__ unsigned long long abs_bits(double a) {

@@ -1,11 +1,21 @@
 // Deterministic binary64 sums over the tiles of one instance.
 //
-// Each CTA reduces its values with a fixed shuffle tree, writes the tile's
-// partial to part[r * nt + tile], and the last CTA of the instance to arrive
-// (an atomic ticket) adds the nt partials in tile order with a fixed tree as
-// well.  The result depends only on the instance's values and its tiling, not
-// on timing or on the other instances of a batch.  Binary32 products are exact
-// in binary64, so a dot of binary32 vectors is a sum of exact terms.
+// Each tile (a CTA, or a 256-thread group of a persistent CTA) reduces its
+// values with a fixed shuffle tree, writes the tile's partial to
+// part[r * nt + tile], and the last tile of the instance to arrive (an atomic
+// ticket) adds the nt partials in tile order with a fixed tree as well.  The
+// result depends only on the instance's values and its tiling, not on timing
+// or on the other instances of a batch.
+//
+// Sums of binary32 products use float-float accumulation: each product is
+// split exactly into p + e (e = fma(a, b, -p)) and added into an unevaluated
+// pair hi + lo with error-free transformations, about 44 significant bits --
+// the accuracy of a binary64 sum at a binary32 instruction cost (the binary64
+// pipe of this GPU issues at a small fraction of the binary32 rate).  The
+// pairs are combined by a fixed shuffle tree; each warp's pair is rounded to
+// binary64 and the tile's partial is the binary64 sum of its warps in order.
+//
+// X is the execution context (tid(), sync()) of persist.cuh; NT threads.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -16,73 +26,6 @@ struct DRedSmem {
   double w[4][NT / 32];
   int last;
 };
-
-// Sum of v over the CTA (fixed order); valid in thread 0.
-template <int R, int NT>
-__device__ __forceinline__ void dred_block(double (&v)[R], DRedSmem<NT>& sm) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    double x = v[r];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) sm.w[r][warp] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      double s = sm.w[r][0];
-      for (int k = 1; k < NT / 32; ++k) s += sm.w[r][k];
-      v[r] = s;
-    }
-  }
-  __syncthreads();
-}
-
-// All threads of the CTA call this.  Returns true in every thread of the CTA
-// that completes the instance's sums; out[] is then valid in thread 0.
-template <int R, int NT>
-__device__ __forceinline__ bool dred_sum(double (&v)[R], double* part, int nt, int tile, unsigned* ticket,
-                                         double (&out)[R], DRedSmem<NT>& sm) {
-  dred_block<R, NT>(v, sm);
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int r = 0; r < R; ++r) part[(long)r * nt + tile] = v[r];
-    __threadfence();
-    sm.last = (atomicAdd(ticket, 1u) == (unsigned)(nt - 1)) ? 1 : 0;
-  }
-  __syncthreads();
-  if (!sm.last) return false;
-  __threadfence();
-  double s[R];
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    s[r] = 0.0;
-    for (int k = threadIdx.x; k < nt; k += NT) s[r] += __ldcg(&part[(long)r * nt + k]);
-  }
-  dred_block<R, NT>(s, sm);
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int r = 0; r < R; ++r) out[r] = s[r];
-    *ticket = 0u;
-  }
-  return true;
-}
-
-}  // namespace pfgb
-
-namespace pfgb {
-
-// ---- float-float accumulation -------------------------------------------------
-//
-// Sums of binary32 products on the binary32 pipe: each product is split
-// exactly into p + e (e = fma(a, b, -p)) and added into an unevaluated pair
-// hi + lo with error-free transformations, about 44 significant bits -- the
-// accuracy of a binary64 sum at a binary32 instruction cost (the binary64 pipe
-// of this GPU issues at a small fraction of the binary32 rate).  The pairs are
-// combined by a fixed shuffle tree, then each warp's pair is rounded to
-// binary64 and the CTA partial is the binary64 sum of its warps in order.
 
 struct FF {
   float hi, lo;
@@ -112,59 +55,99 @@ __device__ __forceinline__ FF ff_merge(FF a, FF b) {
   return ff_renorm(t.hi, t.lo + (a.lo + b.lo));
 }
 
-// CTA sums of float-float values, then the instance's sum over tiles as dred_sum.
-template <int R, int NT>
-__device__ __forceinline__ bool dred_sum_ff(FF (&v)[R], double* part, int nt, int tile, unsigned* ticket,
-                                            double (&out)[R], DRedSmem<NT>& sm) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ __forceinline__ FF ff_warp_sum(FF x) {
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    FF x = v[r];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      FF y;
-      y.hi = __shfl_xor_sync(0xffffffffu, x.hi, o);
-      y.lo = __shfl_xor_sync(0xffffffffu, x.lo, o);
-      x = ff_merge(x, y);
-    }
-    if (lane == 0) sm.w[r][warp] = (double)x.hi + (double)x.lo;
+  for (int o = 16; o > 0; o >>= 1) {
+    FF y;
+    y.hi = __shfl_xor_sync(0xffffffffu, x.hi, o);
+    y.lo = __shfl_xor_sync(0xffffffffu, x.lo, o);
+    x = ff_merge(x, y);
   }
-  __syncthreads();
-  double d[R];
-#pragma unroll
-  for (int r = 0; r < R; ++r) d[r] = 0.0;
-  if (threadIdx.x == 0) {
+  return x;
+}
+
+// Sum over the tile of per-warp binary64 values already in sm.w[r][warp];
+// valid in tid 0.
+template <int R, int NT, class X>
+__device__ __forceinline__ void dred_warps(const X& x, double (&v)[R], DRedSmem<NT>& sm) {
+  x.sync();
+  if (x.tid() == 0) {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       double s = sm.w[r][0];
       for (int k = 1; k < NT / 32; ++k) s += sm.w[r][k];
-      d[r] = s;
+      v[r] = s;
     }
   }
-  __syncthreads();
-  // d[] holds the CTA sums in thread 0: the rest is dred_sum without its block step
-  if (threadIdx.x == 0) {
+  x.sync();
+}
+
+// Sum of v over the tile (fixed order); valid in tid 0.
+template <int R, int NT, class X>
+__device__ __forceinline__ void dred_block(const X& x, double (&v)[R], DRedSmem<NT>& sm) {
+  const int lane = x.tid() & 31, warp = x.tid() >> 5;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    double a = v[r];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) sm.w[r][warp] = a;
+  }
+  dred_warps<R, NT>(x, v, sm);
+}
+
+// The tile's partials (in tid 0) into the instance's sums: true in every
+// thread of the tile that completes them; out[] is then valid in tid 0.
+template <int R, int NT, class X>
+__device__ __forceinline__ bool dred_finish(const X& x, const double (&d)[R], double* part, int nt, int tile,
+                                            unsigned* ticket, double (&out)[R], DRedSmem<NT>& sm) {
+  if (x.tid() == 0) {
 #pragma unroll
     for (int r = 0; r < R; ++r) part[(long)r * nt + tile] = d[r];
     __threadfence();
     sm.last = (atomicAdd(ticket, 1u) == (unsigned)(nt - 1)) ? 1 : 0;
   }
-  __syncthreads();
+  x.sync();
   if (!sm.last) return false;
   __threadfence();
   double s[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     s[r] = 0.0;
-    for (int k = threadIdx.x; k < nt; k += NT) s[r] += __ldcg(&part[(long)r * nt + k]);
+    for (int k = x.tid(); k < nt; k += NT) s[r] += __ldcg(&part[(long)r * nt + k]);
   }
-  dred_block<R, NT>(s, sm);
-  if (threadIdx.x == 0) {
+  dred_block<R, NT>(x, s, sm);
+  if (x.tid() == 0) {
 #pragma unroll
     for (int r = 0; r < R; ++r) out[r] = s[r];
-    *ticket = 0u;
+    atomicExch(ticket, 0u);
   }
   return true;
+}
+
+// binary64 values
+template <int R, int NT, class X>
+__device__ __forceinline__ bool dred_sum(const X& x, double (&v)[R], double* part, int nt, int tile, unsigned* ticket,
+                                         double (&out)[R], DRedSmem<NT>& sm) {
+  dred_block<R, NT>(x, v, sm);
+  return dred_finish<R, NT>(x, v, part, nt, tile, ticket, out, sm);
+}
+
+// float-float values
+template <int R, int NT, class X>
+__device__ __forceinline__ bool dred_sum_ff(const X& x, FF (&v)[R], double* part, int nt, int tile, unsigned* ticket,
+                                            double (&out)[R], DRedSmem<NT>& sm) {
+  const int lane = x.tid() & 31, warp = x.tid() >> 5;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const FF a = ff_warp_sum(v[r]);
+    if (lane == 0) sm.w[r][warp] = (double)a.hi + (double)a.lo;
+  }
+  double d[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) d[r] = 0.0;
+  dred_warps<R, NT>(x, d, sm);
+  return dred_finish<R, NT>(x, d, part, nt, tile, ticket, out, sm);
 }
 
 }  // namespace pfgb

@@ -5,18 +5,22 @@
 // identity, b mean-free with b[0] = 0; src/pyflow/solvers/pressure_solver.py:97-128)
 // has x[0] = 0, and its rows k != 0 form the SPD matrix -lap_c without row and
 // column 0.  The refinement keeps x and the residual r = b - A x in binary64
-// (the reference stencil, exactly rounded norms); each correction e solves the
-// equivalent singular Neumann system -lap_c e = r~ in binary32, where r~ equals
-// r except r~_0 = -sum_{k != 0} r_k (which makes it consistent), and is shifted
-// by -e[0] so that x[0] stays 0.  The inner solve is CG preconditioned by a
+// (the reference stencil); each correction e solves the equivalent singular
+// Neumann system -lap_c e = r~ in binary32, where r~ equals r except
+// r~_0 = -sum_{k != 0} r_k (which makes it consistent), and is shifted by -e[0]
+// so that x[0] stays 0.  The inner solve is CG preconditioned by a
 // cell-centred geometric multigrid V-cycle: bilinear prolongation P (weights
-// 3/4, 1/4 per axis, reflected at the Neumann walls), restriction R = P^T,
-// coarse operators rediscretised with the same face coefficients (consistent
-// with R = P^T, which sums four children), two damped-Jacobi sweeps before and
-// after, and every level of at most 64 x 64 cells inside one CTA.  The cycle is
-// symmetric (R = P^T, adjoint smoothing), as PCG requires.
-// All dot products are exact (binary32 products are exact integers, summed in
-// the same superaccumulator as the binary64 path); alpha and beta are binary64.
+// 3/4, 1/4 per coarsened axis, reflected at the Neumann walls), restriction
+// R = P^T, coarse operators rediscretised consistently with R = P^T; both axes
+// are halved where the face coefficients are balanced, only the strongly
+// coupled one where they differ by more than 2x (semi-coarsening, for cells
+// longer in one direction); two damped-Jacobi sweeps before and after; every
+// level of at most 4096 cells inside one CTA, whose bottom level is solved by
+// its pseudo-inverse.  The cycle is symmetric (R = P^T, adjoint smoothing,
+// symmetric bottom solve), as PCG requires.
+// Dot products are float-float sums of exactly split binary32 products per
+// CTA and binary64 across CTAs in a fixed order (dred.cuh); alpha, beta and
+// every norm of the refinement are binary64.
 //
 // Both loops are WHILE conditional nodes of the step graph: the inner loop
 // stops at ||r_in|| <= tol_in ||r~|| or max_inner iterations, the outer loop
@@ -69,21 +73,42 @@ __device__ __forceinline__ float mg_nsum(const Lvl& L, int j, int i, F at) {
   return s;
 }
 
-// Bilinear prolongation (3/4 parent + 1/4 neighbour per axis, all of the
-// parent at a wall) and its transpose.
-// value of P e at fine cell (j, i), e the coarse correction
-__device__ __forceinline__ float prolong_at(const Lvl& C, int j, int i) {
-  const int I = i >> 1, J = j >> 1;
-  const int I2 = (i & 1) ? I + 1 : I - 1;
-  const int J2 = (j & 1) ? J + 1 : J - 1;
-  const bool hx = I2 >= 0 && I2 < C.nx, hy = J2 >= 0 && J2 < C.ny;
-  const float wx = hx ? 0.75f : 1.f, wy = hy ? 0.75f : 1.f;
-  const float* e = C.u;
-  float v = wx * wy * e[(long)J * C.ld + I];
-  if (hx) v = fmaf(0.25f * wy, e[(long)J * C.ld + I2], v);
-  if (hy) v = fmaf(wx * 0.25f, e[(long)J2 * C.ld + I], v);
-  if (hx && hy) v = fmaf(0.0625f, e[(long)J2 * C.ld + I2], v);
+// Bilinear prolongation along each coarsened axis (3/4 parent + 1/4 neighbour,
+// all of the parent at a wall; an axis that is not coarsened (factor 1) is
+// copied) and its transpose.  A level may halve both axes or, for cells much
+// longer in one direction, only the strongly coupled one (semi-coarsening).
+struct PAxis {
+  int p, p2;       // parent, second parent
+  float w, w2;     // their weights (w2 = 0: no second parent)
+};
+
+template <int K>
+__device__ __forceinline__ PAxis prolong_axis(int i, int nc) {
+  if (K == 1) return PAxis{i, i, 1.f, 0.f};
+  const int I = i >> 1, I2 = (i & 1) ? I + 1 : I - 1;
+  const bool h = I2 >= 0 && I2 < nc;
+  return PAxis{I, h ? I2 : I, h ? 0.75f : 1.f, h ? 0.25f : 0.f};
+}
+
+// value at fine cell (j, i) of P e, e of pitch ld on a coarse level of nx x ny cells
+template <int KX, int KY>
+__device__ __forceinline__ float prolong_k(const float* e, long ld, int nx, int ny, int j, int i) {
+  const PAxis ax = prolong_axis<KX>(i, nx), ay = prolong_axis<KY>(j, ny);
+  float v = ax.w * ay.w * e[(long)ay.p * ld + ax.p];
+  if (KX == 2 && ax.w2 != 0.f) v = fmaf(ax.w2 * ay.w, e[(long)ay.p * ld + ax.p2], v);
+  if (KY == 2 && ay.w2 != 0.f) v = fmaf(ax.w * ay.w2, e[(long)ay.p2 * ld + ax.p], v);
+  if (KX == 2 && KY == 2 && ax.w2 != 0.f && ay.w2 != 0.f) v = fmaf(ax.w2 * ay.w2, e[(long)ay.p2 * ld + ax.p2], v);
   return v;
+}
+
+__device__ __forceinline__ float prolong_val(const float* e, long ld, int nx, int ny, int kx, int ky, int j, int i) {
+  if (kx == 2 && ky == 2) return prolong_k<2, 2>(e, ld, nx, ny, j, i);
+  if (kx == 2) return prolong_k<2, 1>(e, ld, nx, ny, j, i);
+  return prolong_k<1, 2>(e, ld, nx, ny, j, i);
+}
+
+__device__ __forceinline__ float prolong_at(const Lvl& F, const Lvl& C, int j, int i) {
+  return prolong_val(C.u, C.ld, C.nx, C.ny, F.kx, F.ky, j, i);
 }
 
 // weight with which fine index i (offset d = i - 2I in {-1, 0, 1, 2}) enters coarse I (R = P^T)
@@ -92,6 +117,35 @@ __device__ __forceinline__ float rweight(int d, int I, int nc) {
   if (d == 2) return (I + 1 < nc) ? 0.25f : 0.f;
   if (d == 0) return (I == 0) ? 1.f : 0.75f;
   return (I == nc - 1) ? 1.f : 0.75f;          // d == 1
+}
+
+// (P^T w) at coarse cell (J, I): fine value (j, i) at w[(j - j0) * ld + (i - i0)], coarse
+// level nx x ny, factors KX, KY
+template <int KX, int KY>
+__device__ __forceinline__ float restrict_k(const float* w, long ld, int j0, int i0, int nx, int ny, int J, int I) {
+  float s = 0.f;
+#pragma unroll
+  for (int dj = (KY == 2 ? -1 : 0); dj <= (KY == 2 ? 2 : 0); ++dj) {
+    const float wy = KY == 2 ? rweight(dj, J, ny) : 1.f;
+    if (wy == 0.f) continue;
+    const int j = KY * J + dj;
+    float row = 0.f;
+#pragma unroll
+    for (int di = (KX == 2 ? -1 : 0); di <= (KX == 2 ? 2 : 0); ++di) {
+      const float wx = KX == 2 ? rweight(di, I, nx) : 1.f;
+      if (wx == 0.f) continue;
+      row = fmaf(wx, w[(long)(j - j0) * ld + (KX * I + di - i0)], row);
+    }
+    s = fmaf(wy, row, s);
+  }
+  return s;
+}
+
+__device__ __forceinline__ float restrict_val(const float* w, long ld, int j0, int i0, int nx, int ny, int kx, int ky,
+                                              int J, int I) {
+  if (kx == 2 && ky == 2) return restrict_k<2, 2>(w, ld, j0, i0, nx, ny, J, I);
+  if (kx == 2) return restrict_k<2, 1>(w, ld, j0, i0, nx, ny, J, I);
+  return restrict_k<1, 2>(w, ld, j0, i0, nx, ny, J, I);
 }
 
 // ---- V-cycle kernels -------------------------------------------------------
@@ -107,97 +161,98 @@ __device__ __forceinline__ bool mx_live(const MixDesc& M, int gate) {
   return gate == 0 || !*(volatile const int*)&c->inner_done;
 }
 
+using RedSmem = DRedSmem<MT>;
+
+#define MX_RED(R, vals, outv) dred_sum<R, MT>(vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
+#define MX_RED_FF(R, vals, outv) dred_sum_ff<R, MT>(vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
+
+// rho = r.z of a V-cycle's result; beta = rho / rho_prev after the first inner iteration
+__device__ __forceinline__ void set_rho(MixCtrl* ctrl, double rz) {
+  if (ctrl->inner > 0) ctrl->beta = rz / ctrl->rho;
+  ctrl->rho = rz;
+}
+
 #define MX_TILE(gate)                                      \
   const MTile tl = TL[blockIdx.x];                         \
   const MixDesc& M = MD[tl.inst];                          \
   if (!mx_live(M, gate)) return;
 
-// two damped-Jacobi sweeps from u = 0: t = S(S(0)) for A u = f, and the
-// residual r = f - A t of the tile
-__global__ void __launch_bounds__(MT) k_mg_pre(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
-                                                int gate, float omega) {
+// Down-sweep of level l, fused: two damped-Jacobi sweeps from u = 0 (t = S(S(0))
+// for A u = f), the residual r = f - A t, and its restriction f_{l+1} = P^T r.
+// The tile computes the first sweep on a 3-cell halo, t on 2 and r on 1, so
+// every coarse cell whose fine patch lies in the tile is complete; only t
+// goes back to memory (the up-sweep needs it).
+constexpr int H3 = 3;
+__global__ void __launch_bounds__(MT) k_mg_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
+                                                 int gate, float omega) {
   MX_TILE(gate)
-  const Lvl L = M.lev[l];
-  __shared__ float s1[BY + 4][BX + 4];
-  __shared__ float s2[BY + 2][BX + 2];
+  const Lvl L = M.lev[l], C = M.lev[l + 1];
+  __shared__ float s1[BY + 2 * H3][BX + 2 * H3];
+  __shared__ float s2[BY + 4][BX + 4];
+  __shared__ float rs[BY + 2][BX + 2];
   const int i0 = tl.i0, j0 = tl.j0;
-  for (int idx = threadIdx.x; idx < (BY + 4) * (BX + 4); idx += MT) {
-    int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
-    int gj = j0 + jj, gi = i0 + ii;
+  auto inside = [&](int gj, int gi) { return gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx; };
+  for (int idx = threadIdx.x; idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
+    const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
+    const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx)
-      v = __fdividef(omega * L.f[(long)gj * L.ld + gi], mg_diag(L, gj, gi));
-    s1[jj + 2][ii + 2] = v;
+    if (inside(gj, gi)) v = __fdividef(omega * L.f[(long)gj * L.ld + gi], mg_diag(L, gj, gi));
+    s1[jj + H3][ii + H3] = v;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < (BY + 4) * (BX + 4); idx += MT) {
+    const int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
+    const int gj = j0 + jj, gi = i0 + ii;
+    float v = 0.f;
+    if (inside(gj, gi)) {
+      auto at = [&](int j, int i) { return s1[j - j0 + H3][i - i0 + H3]; };
+      v = fmaf(1.f - omega, s1[jj + H3][ii + H3],
+               __fdividef(omega * (L.f[(long)gj * L.ld + gi] + mg_nsum(L, gj, gi, at)), mg_diag(L, gj, gi)));
+    }
+    s2[jj + 2][ii + 2] = v;
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < (BY + 2) * (BX + 2); idx += MT) {
-    int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
-    int gj = j0 + jj, gi = i0 + ii;
+    const int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
+    const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx) {
-      auto at = [&](int j, int i) { return s1[j - j0 + 2][i - i0 + 2]; };
-      const float d = mg_diag(L, gj, gi);
-      v = fmaf(1.f - omega, s1[jj + 2][ii + 2],
-               __fdividef(omega * (L.f[(long)gj * L.ld + gi] + mg_nsum(L, gj, gi, at)), d));
+    if (inside(gj, gi)) {
+      auto at = [&](int j, int i) { return s2[j - j0 + 2][i - i0 + 2]; };
+      const float t = s2[jj + 2][ii + 2];
+      const long o = (long)gj * L.ld + gi;
+      v = L.f[o] - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
+      if (jj >= 0 && jj < BY && ii >= 0 && ii < BX) L.t[o] = t;
     }
-    s2[jj + 1][ii + 1] = v;
+    rs[jj + 1][ii + 1] = v;
   }
   __syncthreads();
-  const int tx = threadIdx.x & 31;
-  MX_ROWS({
-    const int gi = i0 + tx, gj = j0 + ty;
-    if (gi < L.nx && gj < L.ny) {
-      auto at = [&](int j, int i) { return s2[j - j0 + 1][i - i0 + 1]; };
-      const float t = s2[ty + 1][tx + 1];
-      const long o = (long)gj * L.ld + gi;
-      L.t[o] = t;
-      L.r[o] = L.f[o] - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
-    }
-  })
-}
-
-// f_{l+1} = P^T r_l: each coarse cell gathers the residual of a 4 x 4 fine patch
-__global__ void __launch_bounds__(MT) k_mg_restrict(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
-                                                     int l, int gate) {
-  MX_TILE(gate)
-  const Lvl F = M.lev[l], C = M.lev[l + 1];
-  const int I = tl.i0 + (threadIdx.x & 31);
-  MX_ROWS({
-    const int J = tl.j0 + ty;
+  // coarse cells of this tile: (32 / kx) x (32 / ky)
+  const int cw = BX / L.kx, chh = BY / L.ky;
+  const int I0 = i0 / L.kx, J0 = j0 / L.ky;
+  for (int idx = threadIdx.x; idx < cw * chh; idx += MT) {
+    const int jj = idx / cw, ii = idx - jj * cw;
+    const int I = I0 + ii, J = J0 + jj;
     if (I < C.nx && J < C.ny) {
-      float s = 0.f;
-#pragma unroll
-      for (int dj = -1; dj <= 2; ++dj) {
-        const float wy = rweight(dj, J, C.ny);
-        if (wy == 0.f) continue;
-        const int j = 2 * J + dj;
-        float row = 0.f;
-#pragma unroll
-        for (int di = -1; di <= 2; ++di) {
-          const float wx = rweight(di, I, C.nx);
-          if (wx == 0.f) continue;
-          row = fmaf(wx, F.r[(long)j * F.ld + (2 * I + di)], row);
-        }
-        s = fmaf(wy, row, s);
-      }
-      C.f[(long)J * C.ld + I] = s;
+      // rs holds r at fine rows j0 - 1 .. j0 + BY and columns i0 - 1 .. i0 + BX
+      C.f[(long)J * C.ld + I] = restrict_val(&rs[0][0], BX + 2, j0 - 1, i0 - 1, C.nx, C.ny, L.kx, L.ky, J, I);
     }
-  })
+  }
 }
 
-// u_l = S(S(t_l + P u_{l+1})) with the bilinear P
+// u_l = S(S(t_l + P u_{l+1})) with the bilinear P; on level 0 also rho = r.z
 __global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
                                                  int gate, float omega) {
   MX_TILE(gate)
   const Lvl F = M.lev[l], C = M.lev[l + 1];
   __shared__ float w0[BY + 4][BX + 4];
   __shared__ float w1[BY + 2][BX + 2];
+  __shared__ RedSmem rsm;
   const int i0 = tl.i0, j0 = tl.j0;
   for (int idx = threadIdx.x; idx < (BY + 4) * (BX + 4); idx += MT) {
     int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
     int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) v = F.t[(long)gj * F.ld + gi] + prolong_at(C, gj, gi);
+    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) v = F.t[(long)gj * F.ld + gi] + prolong_at(F, C, gj, gi);
     w0[jj + 2][ii + 2] = v;
   }
   __syncthreads();
@@ -215,23 +270,30 @@ __global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, 
   }
   __syncthreads();
   const int tx = threadIdx.x & 31;
+  FF acc[1] = {{0.f, 0.f}};
   MX_ROWS({
     const int gi = i0 + tx, gj = j0 + ty;
     if (gi < F.nx && gj < F.ny) {
       auto at = [&](int j, int i) { return w1[j - j0 + 1][i - i0 + 1]; };
       const float d = mg_diag(F, gj, gi);
-      const float v = fmaf(1.f - omega, w1[ty + 1][tx + 1],
-                           __fdividef(omega * (F.f[(long)gj * F.ld + gi] + mg_nsum(F, gj, gi, at)), d));
+      const float fv = F.f[(long)gj * F.ld + gi];
+      const float v = fmaf(1.f - omega, w1[ty + 1][tx + 1], __fdividef(omega * (fv + mg_nsum(F, gj, gi, at)), d));
       F.u[(long)gj * F.ld + gi] = v;
+      if (l == 0) ff_add_prod(acc[0], fv, v);
     }
   })
+  // level 0: z = u is complete in this tile; rho = r.z of the PCG
+  if (l == 0) {
+    double out[1];
+    if (MX_RED_FF(1, acc, out) && threadIdx.x == 0) set_rho(M.ctrl, out[0]);
+  }
 }
 
-// Levels of at most 64 x 64 cells run inside one CTA per instance: all of them
+// Levels of at most 4096 cells run inside one CTA per instance: all of them
 // live in shared memory and one V-cycle (the same smoother, restriction and
-// prolongation as the global levels, eight Jacobi sweeps on the bottom level)
-// forms the coarse "solve" -- a fixed linear, symmetric operator, as PCG
-// requires.  More cycles or sweeps do not lower the PCG iteration count.
+// prolongation as the global levels; the bottom level, at most 64 cells, by its
+// pseudo-inverse, else eight Jacobi sweeps) forms the coarse "solve" -- a fixed
+// linear, symmetric operator, as PCG requires.
 constexpr int CT = 1024;                     // threads of the coarse CTA
 constexpr int CMAX = 4096;                   // cells of its finest level
 constexpr int BMAX = 64;                     // bottom levels up to this size are solved exactly
@@ -239,6 +301,7 @@ constexpr int BMAX = 64;                     // bottom levels up to this size ar
 struct CLvl {                                // a shared-memory level
   int nx, ny, off;                           // off: offset into the level arrays
   float cx, cy;
+  int kx, ky;                                // coarsening factors to the next level
 };
 
 __device__ __forceinline__ float c_diag(const CLvl& L, int j, int i) {
@@ -278,8 +341,8 @@ __device__ __forceinline__ void c_sweep(const CLvl& L, const float* f, const flo
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(CT) k_mg_coarse_cycles(const MixDesc* __restrict__ MD, int gate, int cycles,
-                                                          int bottom_sweeps, float omega) {
+__global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD, int gate, int bottom_sweeps,
+                                                   float omega) {
   const MixDesc& M = MD[blockIdx.x];
   if (!mx_live(M, gate)) return;
   const Lvl C = M.lev[M.nlev - 1];
@@ -293,103 +356,95 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(const MixDesc* __restri
       L[l].nx = nx;
       L[l].ny = ny;
       L[l].off = tot;
-      L[l].cx = C.cx;
-      L[l].cy = C.cy;
+      L[l].cx = M.ccx[l];
+      L[l].cy = M.ccy[l];
+      L[l].kx = M.ckx[l];
+      L[l].ky = M.cky[l];
       tot += nx * ny;
-      nx /= 2;
-      ny /= 2;
+      nx /= L[l].kx;
+      ny /= L[l].ky;
     }
   }
-  float* f = sm;
-  float* u = sm + tot;
-  float* t = sm + 2 * tot;
-  float* e = sm + 3 * tot;
-  float* w = sm + 4 * tot;
-  C_FOR(L[0], {
-    f[c] = C.f[(long)j * C.ld + i];
-    u[c] = 0.f;
-  })
+  float* rh = sm;            // right-hand side of every level (level 0: the entry level's f)
+  float* e = sm + tot;       // pre-smoothed iterate on the way down; the bottom solution
+  float* w = sm + 2 * tot;   // residual on the way down; each level's result on the way up
+  C_FOR(L[0], { rh[c] = C.f[(long)j * C.ld + i]; })
   __syncthreads();
-  // x_{k+1} = x_k + V(f - A x_k): the first cycle starts from zero
-  for (int cyc = 0; cyc < cycles; ++cyc) {
-    C_FOR(L[0], { t[c] = f[c] - (c_diag(L[0], j, i) * u[c] - c_nsum(L[0], u, j, i)); })
+  for (int l = 0; l + 1 < nl; ++l) {
+    const CLvl& Lv = L[l];
+    const float* r = rh + Lv.off;
+    // e = S(S(0)); the first sweep from zero is pointwise (omega rh / d) and is folded into the second
+    C_FOR(Lv, {
+      auto s1 = [&](int jj, int ii) { return __fdividef(omega * r[jj * Lv.nx + ii], c_diag(Lv, jj, ii)); };
+      float ns = 0.f;
+      if (i > 0) ns = fmaf(Lv.cx, s1(j, i - 1), ns);
+      if (i < Lv.nx - 1) ns = fmaf(Lv.cx, s1(j, i + 1), ns);
+      if (j > 0) ns = fmaf(Lv.cy, s1(j - 1, i), ns);
+      if (j < Lv.ny - 1) ns = fmaf(Lv.cy, s1(j + 1, i), ns);
+      e[Lv.off + c] = fmaf(1.f - omega, s1(j, i), __fdividef(omega * (r[c] + ns), c_diag(Lv, j, i)));
+    })
     __syncthreads();
-    float* rh = t;     // right-hand side of every level (level 0: the residual)
-    for (int l = 0; l < nl; ++l) {
-      const CLvl& Lv = L[l];
-      if (l == nl - 1) {
-        const int nb = Lv.nx * Lv.ny;
-        if (M.binv) {
-          // exact bottom solve: e = A+ rh (at most BMAX cells)
-          for (int r = threadIdx.x; r < nb; r += CT) {
-            const float* row = M.binv + (long)r * nb;
-            float acc = 0.f;
-            for (int q = 0; q < nb; ++q) acc = fmaf(__ldg(row + q), rh[Lv.off + q], acc);
-            e[Lv.off + r] = acc;
-          }
-          __syncthreads();
-          break;
-        }
-        C_FOR(Lv, { e[Lv.off + c] = 0.f; })
-        __syncthreads();
-        for (int s = 0; s < bottom_sweeps; ++s) c_sweep(Lv, rh, (s & 1) ? w : e, (s & 1) ? e : w, omega);
-        if (bottom_sweeps & 1) {
-          C_FOR(Lv, { e[Lv.off + c] = w[Lv.off + c]; })
-          __syncthreads();
-        }
-        break;
-      }
-      // two sweeps from zero: e = S(S(0))
-      C_FOR(Lv, { w[Lv.off + c] = __fdividef(omega * rh[Lv.off + c], c_diag(Lv, j, i)); })
-      __syncthreads();
-      c_sweep(Lv, rh, w, e, omega);
-      // residual rh - A e of this level into w, then rh_{l+1} = P^T w
-      C_FOR(Lv, { w[Lv.off + c] = rh[Lv.off + c] - (c_diag(Lv, j, i) * e[Lv.off + c] - c_nsum(Lv, e, j, i)); })
-      __syncthreads();
-      const CLvl& Cv = L[l + 1];
-      C_FOR(Cv, {
-        const int J = j, I = i;
-        float sres = 0.f;
-        for (int dj = -1; dj <= 2; ++dj) {
-          const float wy = rweight(dj, J, Cv.ny);
-          if (wy == 0.f) continue;
-          float row = 0.f;
-          for (int di = -1; di <= 2; ++di) {
-            const float wx = rweight(di, I, Cv.nx);
-            if (wx == 0.f) continue;
-            row = fmaf(wx, w[Lv.off + (2 * J + dj) * Lv.nx + (2 * I + di)], row);
-          }
-          sres = fmaf(wy, row, sres);
-        }
-        rh[Cv.off + c] = sres;
-      })
-      __syncthreads();
-    }
-    for (int l = nl - 2; l >= 0; --l) {
-      const CLvl& Lv = L[l];
-      const CLvl& Cv = L[l + 1];
-      C_FOR(Lv, {
-        const int I = i >> 1, J = j >> 1;
-        const int I2 = (i & 1) ? I + 1 : I - 1, J2 = (j & 1) ? J + 1 : J - 1;
-        const bool hx = I2 >= 0 && I2 < Cv.nx, hy = J2 >= 0 && J2 < Cv.ny;
-        const float wx = hx ? 0.75f : 1.f, wy = hy ? 0.75f : 1.f;
-        const float* ec = e + Cv.off;
-        float pv = wx * wy * ec[J * Cv.nx + I];
-        if (hx) pv = fmaf(0.25f * wy, ec[J * Cv.nx + I2], pv);
-        if (hy) pv = fmaf(wx * 0.25f, ec[J2 * Cv.nx + I], pv);
-        if (hx && hy) pv = fmaf(0.0625f, ec[J2 * Cv.nx + I2], pv);
-        w[Lv.off + c] = e[Lv.off + c] + pv;
-      })
-      __syncthreads();
-      c_sweep(Lv, rh, w, e, omega);
-      c_sweep(Lv, rh, e, w, omega);
-      C_FOR(Lv, { e[Lv.off + c] = w[Lv.off + c]; })
-      __syncthreads();
-    }
-    C_FOR(L[0], { u[c] += e[c]; })
+    // residual rh - A e of this level into w, then rh_{l+1} = P^T w
+    C_FOR(Lv, { w[Lv.off + c] = r[c] - (c_diag(Lv, j, i) * e[Lv.off + c] - c_nsum(Lv, e, j, i)); })
+    __syncthreads();
+    const CLvl& Cv = L[l + 1];
+    C_FOR(Cv, { rh[Cv.off + c] = restrict_val(w + Lv.off, Lv.nx, 0, 0, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i); })
     __syncthreads();
   }
-  C_FOR(L[0], { C.u[(long)j * C.ld + i] = u[c]; })
+  {
+    const CLvl& Lv = L[nl - 1];
+    const int nb = Lv.nx * Lv.ny;
+    if (M.binv) {
+      // exact bottom solve: e = A+ rh (at most BMAX cells)
+      for (int q0 = threadIdx.x; q0 < nb; q0 += CT) {
+        const float* row = M.binv + (long)q0 * nb;
+        float acc = 0.f;
+        for (int q = 0; q < nb; ++q) acc = fmaf(__ldg(row + q), rh[Lv.off + q], acc);
+        e[Lv.off + q0] = acc;
+      }
+      __syncthreads();
+    } else {
+      C_FOR(Lv, { e[Lv.off + c] = 0.f; })
+      __syncthreads();
+      for (int q = 0; q < bottom_sweeps; ++q) c_sweep(Lv, rh, (q & 1) ? w : e, (q & 1) ? e : w, omega);
+      if (bottom_sweeps & 1) {
+        C_FOR(Lv, { e[Lv.off + c] = w[Lv.off + c]; })
+        __syncthreads();
+      }
+    }
+  }
+  // up: w_l = S(S(e_l + P result_{l+1})); the bottom's result is in e, every other level's in w
+  for (int l = nl - 2; l >= 0; --l) {
+    const CLvl& Lv = L[l];
+    const CLvl& Cv = L[l + 1];
+    const float* ec = (l + 1 == nl - 1) ? e : w;
+    C_FOR(Lv, { w[Lv.off + c] = e[Lv.off + c] + prolong_val(ec + Cv.off, Cv.nx, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i); })
+    __syncthreads();
+    c_sweep(Lv, rh, w, e, omega);
+    c_sweep(Lv, rh, e, w, omega);
+  }
+  const float* z = (nl == 1) ? e : w;
+  C_FOR(L[0], { C.u[(long)j * C.ld + i] = z[c]; })
+  if (M.nlev == 1) {
+    // the V-cycle ran entirely here: rho = r.z over level 0, summed as the tile kernels do
+    __shared__ double wsum[CT / 32];
+    FF acc = {0.f, 0.f};
+    C_FOR(L[0], { ff_add_prod(acc, rh[c], z[c]); })
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      FF y;
+      y.hi = __shfl_xor_sync(0xffffffffu, acc.hi, o);
+      y.lo = __shfl_xor_sync(0xffffffffu, acc.lo, o);
+      acc = ff_merge(acc, y);
+    }
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)acc.hi + (double)acc.lo;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double rz = wsum[0];
+      for (int k = 1; k < CT / 32; ++k) rz += wsum[k];
+      set_rho(M.ctrl, rz);
+    }
+  }
 }
 
 // ---- PCG and refinement kernels -------------------------------------------
@@ -397,12 +452,10 @@ __global__ void __launch_bounds__(CT) k_mg_coarse_cycles(const MixDesc* __restri
 // Reductions are deterministic binary64 sums over the instance's level-0 tiles
 // (tile-ordered partials; the last CTA of the instance completes them).
 
-using RedSmem = DRedSmem<MT>;
 
-#define MX_RED(R, vals, outv) dred_sum<R, MT>(vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
-#define MX_RED_FF(R, vals, outv) dred_sum_ff<R, MT>(vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
-
-// x = 0, r64 = b; ||b||^2 and sum(b); counts the instances that refine
+// b -= mean(b), b[0] = 0 (pressure_solver.py:127-128, the mean from the exactly
+// rounded sum as in the binary64 path); x = 0, r64 = b; ||b||^2 and sum(b);
+// counts the instances that refine
 __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                  MixLoop* ml) {
   const MTile tl = TL[blockIdx.x];
@@ -411,13 +464,15 @@ __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, 
   __shared__ RedSmem rsm;
   const Geo G = M.G;
   MixCtrl* ctrl = M.ctrl;
+  const double mean = __ddiv_rn(*M.bsum, M.n_cells);
   const int i = tl.i0 + (threadIdx.x & 31);
   double v[2] = {0.0, 0.0}, out[2];
   MX_ROWS({
     const int j = tl.j0 + ty;
     if (i < G.nx && j < G.ny) {
       const long o = (long)j * G.ld + i;
-      const double bv = M.b[o];
+      const double bv = (i == 0 && j == 0) ? 0.0 : __dsub_rn(M.b[o], mean);
+      M.b[o] = bv;
       M.x[o] = 0.0;
       M.r64[o] = bv;
       v[0] += bv * bv;
@@ -425,6 +480,8 @@ __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, 
     }
   })
   if (MX_RED(2, v, out) && threadIdx.x == 0) {
+    M.ctrl64->mean = mean;
+    M.ctrl64->nan_flag = 0u;
     const double bb = out[0];
     ctrl->bnorm = sqrt(bb);
     ctrl->tol_abs_out = ctrl->tol_out * ctrl->bnorm;
@@ -499,29 +556,6 @@ __global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, 
     ctrl->inner = 0;
     ctrl->inner_done = rt > 0.0 ? 0 : 1;
     if (rt > 0.0) atomicAdd(&ml->inner_active, 1);
-  }
-}
-
-// rho = r.z; beta = rho / rho_prev after the first inner iteration
-__global__ void __launch_bounds__(MT) k_mx_rz(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
-  MX_TILE(1)
-  __shared__ RedSmem rsm;
-  const Lvl L0 = M.lev[0];
-  MixCtrl* ctrl = M.ctrl;
-  const int i = tl.i0 + (threadIdx.x & 31);
-  FF v[1] = {{0.f, 0.f}};
-  double out[1];
-  MX_ROWS({
-    const int j = tl.j0 + ty;
-    if (i < L0.nx && j < L0.ny) {
-      const long o = (long)j * L0.ld + i;
-      ff_add_prod(v[0], L0.f[o], L0.u[o]);
-    }
-  })
-  if (MX_RED_FF(1, v, out) && threadIdx.x == 0) {
-    const double rz = out[0];
-    if (ctrl->inner > 0) ctrl->beta = rz / ctrl->rho;
-    ctrl->rho = rz;
   }
 }
 
@@ -672,6 +706,7 @@ __global__ void k_mx_finish(const MixDesc* __restrict__ MD, int n) {
   c->info = m->converged ? 0 : M.maxiter_report;
   c->zero_rhs = (m->bnorm == 0.0) ? 1 : 0;
   c->bnrm2 = m->bnorm;
+  *M.res_out = m->rr64;      // ||b - A x||^2 of the final x (the refinement's own residual)
 }
 
 // Dependent binary32 FMAs for a few tens of microseconds (no memory waits):
@@ -686,31 +721,73 @@ __global__ void k_pad(float* sink, int n) {
 
 static long round_up(long a, long m) { return (a + m - 1) / m * m; }
 
-static void level_dims(int nx, int ny, std::vector<std::pair<int, int>>& dims, int& coarse_levels, int& coarse_tot) {
-  dims.clear();
-  int lx = nx, ly = ny;
-  dims.push_back({lx, ly});
-  while ((int)dims.size() < MAX_LEVELS && lx % 2 == 0 && ly % 2 == 0 && lx / 2 >= 8 && ly / 2 >= 8 &&
-         (long)lx * ly > CMAX) {
-    lx /= 2;
-    ly /= 2;
-    dims.push_back({lx, ly});
+// One level of a multigrid plan: size, face coefficients (binary64 before
+// rounding to the level's binary32) and the coarsening factors to the next level.
+struct PlanLvl {
+  int nx, ny;
+  double cx, cy;
+  int kx, ky;
+};
+
+struct Plan {
+  std::vector<PlanLvl> global;   // global levels (kernels over tiles); the last is the CTA's first
+  std::vector<PlanLvl> cta;      // levels of the coarse CTA (cta[0] == global.back())
+  int cta_tot = 0;               // cells of all CTA levels
+};
+
+// Coarsening from a level: halve both axes when the coupling is balanced, or only
+// the strongly coupled axis when one face coefficient exceeds twice the other
+// (point smoothers leave errors that are smooth along the strong axis only).
+static bool pick_coarsening(const PlanLvl& L, int minside, int& kx, int& ky) {
+  const bool fx = L.nx % 2 == 0 && L.nx / 2 >= minside, fy = L.ny % 2 == 0 && L.ny / 2 >= minside;
+  int px = 2, py = 2;
+  if (L.cx > 2.0 * L.cy) py = 1;
+  else if (L.cy > 2.0 * L.cx) px = 1;
+  auto ok = [&](int a, int b) { return (a == 1 || fx) && (b == 1 || fy); };
+  if (ok(px, py)) {
+    kx = px;
+    ky = py;
+    return true;
   }
-  // levels of the coarse CTA: halve while possible until the level has at most BMAX cells
-  int cn = 1, cx = lx, cy = ly;
-  while (cn < 8 && cx * cy > BMAX && cx % 2 == 0 && cy % 2 == 0 && cx / 2 >= 2 && cy / 2 >= 2) {
-    cx /= 2;
-    cy /= 2;
-    ++cn;
+  if (fx && fy) { kx = 2; ky = 2; return true; }
+  if (fx) { kx = 2; ky = 1; return true; }
+  if (fy) { kx = 1; ky = 2; return true; }
+  return false;
+}
+
+static PlanLvl coarsen(const PlanLvl& L, int kx, int ky) {
+  PlanLvl c;
+  c.nx = L.nx / kx;
+  c.ny = L.ny / ky;
+  c.cx = L.cx * ky / kx;
+  c.cy = L.cy * kx / ky;
+  c.kx = c.ky = 1;
+  return c;
+}
+
+static Plan make_plan(int nx, int ny, double dx, double dy) {
+  Plan P;
+  PlanLvl L{nx, ny, (double)(float)(1.0 / (dx * dx)), (double)(float)(1.0 / (dy * dy)), 1, 1};
+  P.global.push_back(L);
+  while ((int)P.global.size() < MAX_LEVELS && (long)L.nx * L.ny > CMAX) {
+    int kx, ky;
+    if (!pick_coarsening(L, 8, kx, ky)) break;
+    P.global.back().kx = kx;
+    P.global.back().ky = ky;
+    L = coarsen(L, kx, ky);
+    P.global.push_back(L);
   }
-  coarse_levels = cn;
-  coarse_tot = 0;
-  int ax = lx, ay = ly;
-  for (int l = 0; l < cn; ++l) {
-    coarse_tot += ax * ay;
-    ax /= 2;
-    ay /= 2;
+  P.cta.push_back(L);
+  while ((int)P.cta.size() < 8 && (long)L.nx * L.ny > BMAX) {
+    int kx, ky;
+    if (!pick_coarsening(L, 2, kx, ky)) break;
+    P.cta.back().kx = kx;
+    P.cta.back().ky = ky;
+    L = coarsen(L, kx, ky);
+    P.cta.push_back(L);
   }
+  for (const PlanLvl& c : P.cta) P.cta_tot += c.nx * c.ny;
+  return P;
 }
 
 // Pseudo-inverse of the Neumann operator of an nx x ny level (face coefficients
@@ -771,49 +848,38 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   B->hd.resize(n);
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   size_t bytes = 0;
-  std::vector<std::vector<std::pair<int, int>>> dims(n);
-  std::vector<int> cls(n), ctot(n);
-  std::vector<std::pair<int, int>> bdim(n);
+  std::vector<Plan> plan(n);
   size_t smem = 0;
   for (int k = 0; k < n; ++k) {
-    level_dims(prm[k].nx, prm[k].ny, dims[k], cls[k], ctot[k]);
-    const auto& last = dims[k].back();
-    if ((long)last.first * last.second > CMAX) {
+    plan[k] = make_plan(prm[k].nx, prm[k].ny, prm[k].dx, prm[k].dy);
+    const PlanLvl& last = plan[k].global.back();
+    if ((long)last.nx * last.ny > CMAX) {
       delete B;
       return set_error(PFGB_EINVAL, "mixed solver: the coarse multigrid level would exceed 4096 cells "
                                     "(nx and ny need enough factors of two)");
     }
-    smem = std::max(smem, (size_t)5 * ctot[k] * sizeof(float));
-    {
-      int bx = last.first, by = last.second;
-      for (int l = 1; l < cls[k]; ++l) {
-        bx /= 2;
-        by /= 2;
-      }
-      bdim[k] = {bx, by};
-      if (bx * by <= BMAX) bytes += up((size_t)bx * by * bx * by * sizeof(float));
-    }
-    B->maxlev = std::max(B->maxlev, (int)dims[k].size());
-    for (auto& d : dims[k]) bytes += 4 * up((size_t)round_up(d.first, 32) * d.second * sizeof(float));
+    smem = std::max(smem, (size_t)3 * plan[k].cta_tot * sizeof(float));
+    const PlanLvl& bot = plan[k].cta.back();
+    if (bot.nx * bot.ny <= BMAX) bytes += up((size_t)bot.nx * bot.ny * bot.nx * bot.ny * sizeof(float));
+    B->maxlev = std::max(B->maxlev, (int)plan[k].global.size());
+    for (auto& d : plan[k].global) bytes += 3 * up((size_t)round_up(d.nx, 32) * d.ny * sizeof(float));
     const size_t v0 = up((size_t)round_up(prm[k].nx, 32) * prm[k].ny * sizeof(float));
     const size_t nt0 = (size_t)((prm[k].nx + BX - 1) / BX) * ((prm[k].ny + BY - 1) / BY);
     bytes += 4 * v0 + up((size_t)prm[k].ld64 * prm[k].ny * sizeof(double)) + up(2 * nt0 * sizeof(double)) +
              up(sizeof(unsigned)) + up(sizeof(MixCtrl));
   }
   // tile tables
-  std::vector<MTile> tl[MAX_LEVELS], tlr[MAX_LEVELS], tpre[MAX_LEVELS];
+  std::vector<MTile> tl[MAX_LEVELS], tpre[MAX_LEVELS];
   for (int k = 0; k < n; ++k) {
-    const int nl = (int)dims[k].size();
+    const auto& gl = plan[k].global;
+    const int nl = (int)gl.size();
     for (int l = 0; l < nl; ++l) {
-      add_mtiles(tl[l], k, dims[k][l].first, dims[k][l].second);
-      if (l + 1 < nl) {
-        add_mtiles(tpre[l], k, dims[k][l].first, dims[k][l].second);
-        add_mtiles(tlr[l], k, dims[k][l + 1].first, dims[k][l + 1].second);
-      }
+      add_mtiles(tl[l], k, gl[l].nx, gl[l].ny);
+      if (l + 1 < nl) add_mtiles(tpre[l], k, gl[l].nx, gl[l].ny);
     }
   }
   for (int l = 0; l < B->maxlev; ++l)
-    bytes += up(tl[l].size() * sizeof(MTile)) + up(tlr[l].size() * sizeof(MTile)) + up(tpre[l].size() * sizeof(MTile));
+    bytes += up(tl[l].size() * sizeof(MTile)) + up(tpre[l].size() * sizeof(MTile));
   bytes += up(n * sizeof(MixDesc)) + up(sizeof(MixLoop)) + up(sizeof(float));
   if (cudaMalloc(&B->ws, bytes) != cudaSuccess) {
     delete B;
@@ -833,21 +899,28 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     M.G.g.ny = prm[k].ny;
     M.G.g.sx = spacing_for(prm[k].dx);
     M.G.g.sy = spacing_for(prm[k].dy);
-    M.nlev = (int)dims[k].size();
-    M.coarse_levels = cls[k];
-    const float cx = (float)(1.0 / (prm[k].dx * prm[k].dx)), cy = (float)(1.0 / (prm[k].dy * prm[k].dy));
+    const Plan& PL = plan[k];
+    M.nlev = (int)PL.global.size();
+    M.coarse_levels = (int)PL.cta.size();
+    for (int l = 0; l < M.coarse_levels; ++l) {
+      M.ccx[l] = (float)PL.cta[l].cx;
+      M.ccy[l] = (float)PL.cta[l].cy;
+      M.ckx[l] = PL.cta[l].kx;
+      M.cky[l] = PL.cta[l].ky;
+    }
     for (int l = 0; l < M.nlev; ++l) {
       Lvl& v = M.lev[l];
-      v.nx = dims[k][l].first;
-      v.ny = dims[k][l].second;
+      v.nx = PL.global[l].nx;
+      v.ny = PL.global[l].ny;
       v.ld = round_up(v.nx, 32);
-      v.cx = cx;
-      v.cy = cy;
+      v.cx = (float)PL.global[l].cx;
+      v.cy = (float)PL.global[l].cy;
+      v.kx = PL.global[l].kx;
+      v.ky = PL.global[l].ky;
       const size_t nb = (size_t)v.ld * v.ny * sizeof(float);
       v.u = (float*)take(nb);
       v.t = (float*)take(nb);
       v.f = (float*)take(nb);
-      v.r = (float*)take(nb);
     }
     const size_t v0 = (size_t)M.lev[0].ld * prm[k].ny * sizeof(float);
     M.e = (float*)take(v0);
@@ -860,14 +933,18 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     M.ticket = (unsigned*)take(sizeof(unsigned));
     M.ctrl = (MixCtrl*)take(sizeof(MixCtrl));
     M.binv = nullptr;
-    if (bdim[k].first * bdim[k].second <= BMAX) {
+    const PlanLvl& bot = PL.cta.back();
+    if (bot.nx * bot.ny <= BMAX) {
       std::vector<float> pinv;
-      neumann_pinv(bdim[k].first, bdim[k].second, (double)cx, (double)cy, pinv);
+      neumann_pinv(bot.nx, bot.ny, (double)(float)bot.cx, (double)(float)bot.cy, pinv);
       float* dst = (float*)take(pinv.size() * sizeof(float));
       cudaMemcpy(dst, pinv.data(), pinv.size() * sizeof(float), cudaMemcpyHostToDevice);
       M.binv = dst;
     }
     M.b = prm[k].b;
+    M.bsum = prm[k].bsum;
+    M.n_cells = (double)prm[k].nx * (double)prm[k].ny;
+    M.res_out = prm[k].res_out;
     M.x = prm[k].x;
     M.ctrl64 = prm[k].ctrl64;
     M.active = prm[k].active;
@@ -890,7 +967,6 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
       if (cnt) cudaMemcpy(dst, v.data(), v.size() * sizeof(MTile), cudaMemcpyHostToDevice);
     };
     put(tl[l], B->tl[l], B->ntl[l]);
-    put(tlr[l], B->tlr[l], B->ntlr[l]);
     put(tpre[l], B->tpre[l], B->ntpre[l]);
   }
   B->dd = (MixDesc*)take(n * sizeof(MixDesc));
@@ -903,7 +979,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   cudaError_t e = cudaMemcpy(B->dd, B->hd.data(), n * sizeof(MixDesc), cudaMemcpyHostToDevice);
   B->coarse_smem = smem;
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_mg_coarse_cycles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) {
     batch_destroy(B);
     return set_error(PFGB_ECUDA, std::string("mixed batch set-up: ") + cudaGetErrorString(e));
@@ -940,10 +1016,9 @@ void batch_destroy(Batch* B) {
 static void add_vcycle(GraphChain& c, Batch* B, int gate, float omega) {
   const MixDesc* dd = B->dd;
   for (int l = 0; l + 1 < B->maxlev; ++l) {
-    if (B->ntpre[l]) c.kernel(k_mg_pre, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, omega);
-    if (B->ntlr[l]) c.kernel(k_mg_restrict, dim3(B->ntlr[l]), dim3(MT), dd, (const MTile*)B->tlr[l], l, gate);
+    if (B->ntpre[l]) c.kernel(k_mg_down, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, omega);
   }
-  c.kernel_smem(k_mg_coarse_cycles, dim3(B->n), dim3(CT), B->coarse_smem, dd, gate, 1, 8, omega);
+  c.kernel_smem(k_mg_coarse, dim3(B->n), dim3(CT), B->coarse_smem, dd, gate, 8, omega);
   for (int l = B->maxlev - 2; l >= 0; --l)
     if (B->ntpre[l]) c.kernel(k_mg_post, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, omega);
 }
@@ -965,13 +1040,11 @@ int append_solve(GraphChain& c, Batch* B) {
   outer.kernel(k_ml_reset, dim3(1), dim3(32), B->loop, 1);
   outer.kernel(k_mx_prep, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop);
   add_vcycle(outer, B, 1, omega);
-  outer.kernel(k_mx_rz, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   outer.kernel(k_ml_arm, dim3(1), dim3(32), B->loop, 1, cond_inner, 1);
   GraphChain inner = outer.while_loop_with(cond_inner);
   inner.kernel(k_mx_matvec, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   inner.kernel(k_mx_update, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_inner, 1);
   add_vcycle(inner, B, 1, omega);
-  inner.kernel(k_mx_rz, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   inner.kernel(k_ml_guard, dim3(1), dim3(32), B->loop, 1, cond_inner, 1);
   outer.kernel(k_mx_correct, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   outer.kernel(k_mx_resid, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_outer, 1);
@@ -987,10 +1060,9 @@ int append_solve(GraphChain& c, Batch* B) {
 // profiling (ncu does not profile kernels of graphs with conditional nodes).
 static void launch_vcycle(Batch* B, int gate, float omega, cudaStream_t s) {
   for (int l = 0; l + 1 < B->maxlev; ++l) {
-    if (B->ntpre[l]) k_mg_pre<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, omega);
-    if (B->ntlr[l]) k_mg_restrict<<<B->ntlr[l], MT, 0, s>>>(B->dd, B->tlr[l], l, gate);
+    if (B->ntpre[l]) k_mg_down<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, omega);
   }
-  k_mg_coarse_cycles<<<B->n, CT, B->coarse_smem, s>>>(B->dd, gate, 1, 8, omega);
+  k_mg_coarse<<<B->n, CT, B->coarse_smem, s>>>(B->dd, gate, 8, omega);
   for (int l = B->maxlev - 2; l >= 0; --l)
     if (B->ntpre[l]) k_mg_post<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, omega);
 }
@@ -1012,7 +1084,6 @@ int run_direct(Batch* B, cudaStream_t s) {
     k_ml_reset<<<1, 32, 0, s>>>(B->loop, 1);
     k_mx_prep<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop);
     launch_vcycle(B, 1, omega, s);
-    k_mx_rz<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
     if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
     for (int pi = 0; h.inner_active > 0 && pi < h.gmax_i; ++pi) {
       const bool timed = B->ev && 2 * timed_launches + 1 < B->nev;
@@ -1029,8 +1100,7 @@ int run_direct(Batch* B, cudaStream_t s) {
       }
       k_mx_update<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0);
       launch_vcycle(B, 1, omega, s);
-      k_mx_rz<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
-      if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
+        if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
     }
     k_mx_correct<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
     k_mx_resid<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0);

@@ -15,16 +15,17 @@ namespace mixed {
 constexpr int MAX_LEVELS = 16;
 
 // One multigrid level: binary32 arrays of (ny, ld); cx, cy are the face
-// coefficients (1/dx^2, 1/dy^2 on every level: with R = P^T summing about four
-// children, the rediscretised coarse operator keeps the fine coefficients).
+// coefficients.  The coarse operators are rediscretised consistently with
+// R = P^T, which sums kx * ky children: cx' = cx ky / kx, cy' = cy kx / ky
+// (halving both axes keeps the coefficients).
 struct Lvl {
   int nx, ny;
   long ld;
   float cx, cy;
+  int kx, ky;   // coarsening factors (1 or 2) to the next level
   float* u;   // V-cycle result
   float* t;   // pre-smoothed iterate
   float* f;   // right-hand side (on level 0: the PCG residual)
-  float* r;   // residual f - A t after pre-smoothing
 };
 
 // binary64 geometry of the refinement
@@ -55,10 +56,15 @@ struct MixDesc {
   int nlev;                    // global levels; the last one is solved by the coarse CTA
   int coarse_levels;           // levels resolved inside the coarse CTA
   const float* binv;           // pseudo-inverse of the bottom level (null: Jacobi sweeps instead)
+  float ccx[8], ccy[8];        // face coefficients of the coarse CTA's levels
+  int ckx[8], cky[8];          // their coarsening factors to the next level
   Lvl lev[MAX_LEVELS];
   float *e, *p0, *p1, *q;      // binary32 PCG vectors (pitch lev[0].ld)
   double* r64;                 // binary64 refinement residual (pitch G.ld)
-  const double* b;             // the step's right-hand side (binary64, pitch G.ld)
+  double* b;                   // the step's right-hand side (binary64, pitch G.ld); mean removed here
+  const double* bsum;          // exactly rounded sum of the right-hand side (from the RHS kernel)
+  double n_cells;
+  double* res_out;             // where the final ||b - A x||^2 goes (the step's residual record)
   double* x;                   // the step's pressure solution
   double* part;                // per-tile partial sums of the reductions (2 x nt0)
   unsigned* ticket;            // arrival counter of the reductions
@@ -84,8 +90,6 @@ struct Batch {
   int maxlev = 0;                              // most global levels of any instance
   MTile* tl[MAX_LEVELS] = {};                  // tiles of level l of the instances that have it
   int ntl[MAX_LEVELS] = {};
-  MTile* tlr[MAX_LEVELS] = {};                 // tiles of level l+1 of the instances that restrict into it
-  int ntlr[MAX_LEVELS] = {};
   MTile* tpre[MAX_LEVELS] = {};                // tiles of level l of the instances that smooth on it (l < nlev-1)
   int ntpre[MAX_LEVELS] = {};
   size_t coarse_smem = 0;                      // dynamic shared memory of the coarse CTA (largest instance)
@@ -106,7 +110,9 @@ struct MixParams {
   long ld64;
   double tol_out, tol_in;
   int max_outer, max_inner;
-  const double* b;
+  double* b;
+  const double* bsum;
+  double* res_out;
   double* x;
   Ctrl64* ctrl64;
   const int* active;

@@ -22,11 +22,13 @@ struct Grid2 {
   Spacing sx, sy;
 };
 
-// forward difference gradient, zero on the high boundary
-__device__ __forceinline__ double grad_x(View2<const double> p, int j, int i, const Grid2& g) {
+// forward difference gradient, zero on the high boundary (V: any 2-D view)
+template <class V>
+__device__ __forceinline__ double grad_x(V p, int j, int i, const Grid2& g) {
   return (i < g.nx - 1) ? DIVH(SUB(p(j, i + 1), p(j, i)), g.sx) : 0.0;
 }
-__device__ __forceinline__ double grad_y(View2<const double> p, int j, int i, const Grid2& g) {
+template <class V>
+__device__ __forceinline__ double grad_y(V p, int j, int i, const Grid2& g) {
   return (j < g.ny - 1) ? DIVH(SUB(p(j + 1, i), p(j, i)), g.sy) : 0.0;
 }
 
@@ -39,7 +41,8 @@ __device__ __forceinline__ double div_coherent_at(View2<const double> u, View2<c
 }
 
 // laplacian_coherent = divergence_coherent(gradient_coherent(p))
-__device__ __forceinline__ double lap_coherent_at(View2<const double> p, int j, int i, const Grid2& g) {
+template <class V>
+__device__ __forceinline__ double lap_coherent_at(V p, int j, int i, const Grid2& g) {
   double gxi = grad_x(p, j, i, g);
   double xp = (i >= 1) ? DIVH(SUB(gxi, grad_x(p, j, i - 1, g)), g.sx) : DIVH(gxi, g.sx);
   double gyj = grad_y(p, j, i, g);

@@ -794,6 +794,8 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
       m.max_outer = prm.mixed_max_outer > 0 ? prm.mixed_max_outer : 8;
       m.max_inner = prm.mixed_max_inner > 0 ? prm.mixed_max_inner : 50;
       m.b = I->hd[k].b;
+      m.bsum = &I->hd[k].slots[S_BSUM].result;
+      m.res_out = &I->hd[k].slots[S_RES].result;
       m.x = I->hd[k].x;
       m.ctrl64 = I->hd[k].ctrl;
       // the instance's activity flag inside the device descriptor table
@@ -937,8 +939,7 @@ static int build_graph(Instance64* I, int mode) {
   c.kernel(k_rhs, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   GraphChain body(nullptr);
   if (I->mix) {
-    // b is finished (mean removed, b[0] = 0) by the CG init; the refinement solves A x = b
-    c.kernel(k_cg_init, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc, (LoopCtl*)nullptr);
+    // the refinement removes b's mean, pins b[0], solves A x = b and leaves ||b - A x||^2
     if (int rc = mixed::append_solve(c, I->mix)) return rc;
   } else {
     cudaGraphConditionalHandle cond = 0;
@@ -955,7 +956,7 @@ static int build_graph(Instance64* I, int mode) {
     body.kernel(up, gc, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tcg, I->lc, cond, 1);
     body.kernel(k_loop_guard, dim3(1), dim3(32), I->lc, cond, 1);
   }
-  c.kernel(k_post_resid<0>, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  if (!I->mix) c.kernel(k_post_resid<0>, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   c.kernel(k_pin_correct, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   c.kernel(k_post_diag, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   c.kernel(k_gather, g1, dim3(32), (const InstDesc*)I->dd, I->n);
@@ -1028,9 +1029,7 @@ static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
   if (mode == 0) enqueue_prologue(I, s);
   if (I->mix) {
     k_rhs<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-    k_cg_init<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc, nullptr);
     if (int rc = mixed::run_direct(I->mix, s)) return rc;
-    k_post_resid<0><<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
     k_pin_correct<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
     k_post_diag<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
     k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
