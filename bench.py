@@ -28,9 +28,10 @@ Line contents:
 * ``e2e``: the same metric through the public API with the fields in host
   memory: every step copies u, v, p host->device and back inside the timed
   (wall-clock) region.
-* ``roofline``: the pressure-matvec kernel (p = z + beta p; q = A p; p.q),
-  per-launch CUDA-event times during one more step; algorithmic bytes per
-  launch = 4 words per cell (read z, p_old; write p_new, q).
+* ``roofline``: the dominant kernel, timed with CUDA events during one more
+  step: in the mixed form the persistent pressure solve (one cooperative
+  launch; algorithmic bytes from ``mixed_solve_bytes``), in the binary64 form
+  the CG matvec (4 words per cell: read r, p_old; write p_new, q).
 * ``cpu_baseline``: the oracle port (NumPy restatement of the reference with
   its own reductions and CG sequence) on a bounded sample of the workload.
 * ``--impl reference``: that CPU port timed as the reference arm.
@@ -169,12 +170,14 @@ def mg_levels(nx, ny, dx=None, dy=None):
     return n
 
 
-def launches_per_step(precision, cg_iters, passes, nlev):
+def launches_per_step(precision, cg_iters, passes, nlev, persistent=True):
     """Kernel launches of one step from its loop trip counts."""
     if precision == "fp64":
         return 11 + 3 * cg_iters
+    if persistent:                    # prologue 3, RHS, loop reset, the solve, correction, diagnostics, gather
+        return 9
     v = 2 * nlev - 1                  # down-sweeps, the coarse CTA, up-sweeps
-    return 13 + passes * (6 + v) + cg_iters * (3 + v)
+    return 11 + passes * (6 + v) + cg_iters * (3 + v)
 
 
 # ---- CPU arm -----------------------------------------------------------------
@@ -286,8 +289,17 @@ def max_over_ranks(x, dist):
     return float(t.item())
 
 
-def matvec_roofline(lib, cfg, st, tr, it, cells, precision):
-    """Per-launch CUDA-event timing of the pressure matvec during one more step."""
+def mixed_solve_bytes(cells, inner, passes):
+    """Compulsory bytes of one persistent mixed solve (binary32 levels, binary64 refinement):
+    per inner iteration 16 (matvec) + 24 (update) + 22 (level-0 down- and up-sweep) + 7
+    (coarser levels) bytes per cell; per refinement pass 16 (prep) + 29 (its V-cycle) + 20
+    (correction) + 24 (binary64 residual); 32 for the start (mean removal, x = 0, r = b)."""
+    return cells * (32 + 89 * passes + 69 * inner)
+
+
+def kernel_roofline(lib, cfg, st, tr, it, cells, precision):
+    """Live CUDA-event timing of the dominant kernel during one more step: the
+    persistent solve (mixed) or the CG matvec (binary64)."""
     import ctypes
 
     import torch
@@ -299,20 +311,27 @@ def matvec_roofline(lib, cfg, st, tr, it, cells, precision):
     inst = instance_for(st, P)
     hbm, src = peaks()
     _capi.check(lib.pfgb_set_profiling(inst.handle, 1), "set_profiling")
-    step(cfg, st, tr, it)
+    _, _, diag = step(cfg, st, tr, it)
     ms, n = ctypes.c_double(), ctypes.c_int()
     _capi.check(lib.pfgb_profile_result(inst.handle, ctypes.byref(ms), ctypes.byref(n)), "profile_result")
     _capi.check(lib.pfgb_set_profiling(inst.handle, 0), "set_profiling")
     torch.cuda.synchronize()
-    word = 4 if precision == "mixed" else 8
     per_launch_s = ms.value / 1e3 / max(n.value, 1)
-    nbytes = 4 * word * cells
+    from pyflow_solver_gb300.solvers import _handle
+    if precision == "mixed" and _handle.PERSISTENT:
+        nbytes = mixed_solve_bytes(cells, diag["cg_iterations"], diag.get("refine_passes", 0))
+        kern, model = "mixed::k_mx_persist", "mixed_solve_bytes (bench.py)"
+    elif precision == "mixed":
+        nbytes = 4 * 4 * cells
+        kern, model = "mixed::k_mx_matvec", "4 binary32 words per cell"
+    else:
+        nbytes = 4 * 8 * cells
+        kern, model = "pfgb::k_cg_matvec", "4 binary64 words per cell"
     achieved = nbytes / per_launch_s / 1e9
-    kern = "mixed::k_mx_matvec" if precision == "mixed" else "pfgb::k_cg_matvec"
     return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": None, "kernel": kern, "peak_source": f"{src} (copy bandwidth)",
             "launches_timed": n.value, "per_launch_us": per_launch_s * 1e6,
-            "algorithmic_bytes_per_launch": nbytes}
+            "algorithmic_bytes_per_launch": nbytes, "bytes_model": model}
 
 
 def e2e_cavity(cfg, n, steps):
@@ -369,8 +388,8 @@ def bench_cavity(args, dist, world, rank, local):
     cg = [d["cg_iterations"] for d in diags]
     passes = [d.get("refine_passes", 0) for d in diags]
     nlev = mg_levels(n, n)
-    launches = sum(launches_per_step(args.precision, c, p, nlev) for c, p in zip(cg, passes))
-    roof = None if args.no_roofline else matvec_roofline(lib, cfg, st, tr, it, n * n, args.precision)
+    launches = sum(launches_per_step(args.precision, c, p, nlev, args.persistent) for c, p in zip(cg, passes))
+    roof = None if args.no_roofline else kernel_roofline(lib, cfg, st, tr, it, n * n, args.precision)
     extra = {}
     if args.precision == "mixed" and not args.no_plain:
         _, _, _, _, pms, pd = run("fp64", args.plain_steps, 1)
@@ -434,7 +453,7 @@ def bench_batched(args, dist, world, rank, local):
     maxit = [int(o["cg_iterations"].max()) for o in outs]
     maxpass = [int(o["refine_passes"].max()) for o in outs]
     nlev = max(mg_levels(nx, ny) for nx, ny, _, _ in inst)
-    launches = sum(launches_per_step(args.precision, c, p, nlev) for c, p in zip(maxit, maxpass))
+    launches = sum(launches_per_step(args.precision, c, p, nlev, args.persistent) for c, p in zip(maxit, maxpass))
     # end to end: the fields of all instances copied in (pinned host -> device) and out every step
     host = torch.empty(arena.numel(), dtype=torch.float64, pin_memory=True)
     host.copy_(arena)
@@ -517,6 +536,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--no-graph", action="store_true", help="individual launches instead of one graph per step")
+    ap.add_argument("--persistent", action="store_true",
+                    help="mixed form: the pressure solve as one persistent cooperative launch, not a kernel graph")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -532,6 +553,7 @@ def main():
         dist.init_process_group("nccl")
     from pyflow_solver_gb300.solvers import _handle
     _handle.GRAPH_MODE = not args.no_graph
+    _handle.PERSISTENT = args.persistent
     if args.workload in CAVITIES:
         line = bench_cavity(args, dist, world, rank, local)
     elif args.workload == "batched256":

@@ -234,6 +234,12 @@ PFGB_API int pfgb_cg_solve_noalloc(int op, const double* b, double* x, int nx, i
                                    int precond, double jacobi_interior, double tol, int maxiter,
                                    void* stream, pfgb_solve_out* out);
 
+/* With precision 1: run each step's pressure solve as one persistent cooperative
+ * launch (on; available where the device co-schedules one 1024-thread CTA per
+ * SM) or as a graph of per-phase kernels with WHILE loop nodes (off, the
+ * default).  Both give the same bits.  No reference counterpart. */
+PFGB_API int pfgb_set_persistent(pfgb_handle* handle, int on);
+
 /* ---- tile autotuner ---------------------------------------------------------- */
 
 /* Time the three tile shapes of the binary64 CG kernel pair (32 x 8, 32 x 16,
@@ -253,11 +259,12 @@ PFGB_API int pfgb_set_cg_variant(pfgb_handle* handle, int variant);
 
 /* Record CUDA events around every pressure-matvec launch (p = z + beta p;
  * q = A p; p.q) of the following steps of this handle: the binary64 CG matvec,
- * or with precision 1 the binary32 PCG matvec of the inner solves.  Steps then
- * run as individual launches (no graph).  No reference counterpart: benchmark
+ * or with precision 1 the binary32 PCG matvec of the inner solves -- or, when
+ * the persistent solve is on, around that one launch.  Steps then run as
+ * individual launches (no graph).  No reference counterpart: benchmark
  * instrumentation. */
 PFGB_API int pfgb_set_profiling(pfgb_handle* handle, int on);
-/* Total device time (ms) and number of the matvec launches of the last step. */
+/* Total device time (ms) and number of the timed launches of the last step. */
 PFGB_API int pfgb_profile_result(pfgb_handle* handle, double* ms, int* launches);
 /* Measured FP64 FMA issue rate of the current device, in 1e12 instructions/s.
  * No reference counterpart: the denominator of the FP64 roofline. */

@@ -89,6 +89,7 @@ SIGNATURES = {
     "pfgb_cg_solve": (_I, [_I, _P, _P, _I, _I, _D, _D, _I, _D, _D, _I, _P, ctypes.POINTER(SolveOut)]),
     "pfgb_cg_solve_noalloc": (_I, [_I, _P, _P, _I, _I, _D, _D, _I, _D, _D, _I, _P, ctypes.POINTER(SolveOut)]),
     "pfgb_set_graph": (_I, [_P, _I]),
+    "pfgb_set_persistent": (_I, [_P, _I]),
     "pfgb_autotune": (_I, [_P, _P, ctypes.POINTER(_I), c_double_p]),
     "pfgb_set_cg_variant": (_I, [_P, _I]),
     "pfgb_set_profiling": (_I, [_P, _I]),

@@ -80,6 +80,7 @@ class BatchedCavities:
             graph = _handle.GRAPH_MODE
         _capi.check(_capi.load().pfgb_set_graph(h, 1 if graph else 0), "pfgb_set_graph")
         from .solvers import _handle
+        _capi.check(_capi.load().pfgb_set_persistent(h, 1 if _handle.PERSISTENT else 0), "pfgb_set_persistent")
         self.cg_variant = None
         if _handle.AUTOTUNE and params[0].precision == 0:
             key = ("batch",) + tuple(sorted((int(s.nx), int(s.ny)) for s in self.states))

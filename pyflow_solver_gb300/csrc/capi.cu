@@ -121,6 +121,11 @@ extern "C" int pfgb_set_cg_variant(pfgb_handle* handle, int variant) {
   return instance64_set_cg_variant(handle->inst, variant);
 }
 
+extern "C" int pfgb_set_persistent(pfgb_handle* handle, int on) {
+  if (!handle) return set_error(PFGB_EINVAL, "null handle");
+  return instance64_set_persistent(handle->inst, on);
+}
+
 extern "C" int pfgb_set_graph(pfgb_handle* handle, int on) {
   if (!handle) return set_error(PFGB_EINVAL, "null handle");
   return instance64_set_graph(handle->inst, on);

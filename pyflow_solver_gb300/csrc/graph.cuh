@@ -37,6 +37,20 @@ class GraphChain {
     smem_ = 0;
   }
 
+  // Same, as a cooperative launch (all CTAs co-resident), with dynamic shared memory.
+  template <typename... P, typename... A>
+  void kernel_coop(void (*f)(P...), dim3 grid, dim3 block, size_t smem, A&&... args) {
+    if (err_ != cudaSuccess) return;
+    std::tuple<P...> vals(std::forward<A>(args)...);
+    smem_ = smem;
+    add_kernel(reinterpret_cast<void*>(f), grid, block, vals, std::index_sequence_for<P...>{});
+    smem_ = 0;
+    if (err_ != cudaSuccess) return;
+    cudaLaunchAttributeValue v = {};
+    v.cooperative = 1;
+    err_ = cudaGraphKernelNodeSetAttribute(last_, cudaLaunchAttributeCooperative, &v);
+  }
+
   // Append a WHILE node on an existing conditional handle (created on this
   // graph with cudaGraphConditionalHandleCreate; kernels upstream of the node
   // or in its body set it with cudaGraphSetConditional).  The body runs while

@@ -35,6 +35,7 @@
 #include "dred.cuh"
 #include "graph.cuh"
 #include "mixed.cuh"
+#include "persist.cuh"
 #include "pfgb_internal.h"
 #include "stencil.cuh"
 #include "step64.cuh"
@@ -45,13 +46,6 @@ namespace mixed {
 constexpr int MT = 256;
 constexpr int BX = 32, BY = 32;              // a tile: 32 x 32 cells, each thread a column of 4
 constexpr int RPT = BY / (MT / 32);
-
-// the rows ty of the tile that this thread owns (ty = warp, warp + 8, ...)
-#define MX_ROWS(...)                                        \
-  for (int r_ = 0; r_ < RPT; ++r_) {                        \
-    const int ty = (threadIdx.x >> 5) + r_ * (MT / 32);     \
-    __VA_ARGS__                                             \
-  }
 
 __device__ __forceinline__ float mg_diag(const Lvl& L, int j, int i) {
   float d = 0.f;
@@ -90,25 +84,25 @@ __device__ __forceinline__ PAxis prolong_axis(int i, int nc) {
   return PAxis{I, h ? I2 : I, h ? 0.75f : 1.f, h ? 0.25f : 0.f};
 }
 
-// value at fine cell (j, i) of P e, e of pitch ld on a coarse level of nx x ny cells
-template <int KX, int KY>
-__device__ __forceinline__ float prolong_k(const float* e, long ld, int nx, int ny, int j, int i) {
+// value at fine cell (j, i) of P e, e of pitch ld on a coarse level of nx x ny
+// cells, its values read through ld(pointer)
+template <int KX, int KY, class LD>
+__device__ __forceinline__ float prolong_k(LD ld, const float* e, long pitch, int nx, int ny, int j, int i) {
   const PAxis ax = prolong_axis<KX>(i, nx), ay = prolong_axis<KY>(j, ny);
-  float v = ax.w * ay.w * e[(long)ay.p * ld + ax.p];
-  if (KX == 2 && ax.w2 != 0.f) v = fmaf(ax.w2 * ay.w, e[(long)ay.p * ld + ax.p2], v);
-  if (KY == 2 && ay.w2 != 0.f) v = fmaf(ax.w * ay.w2, e[(long)ay.p2 * ld + ax.p], v);
-  if (KX == 2 && KY == 2 && ax.w2 != 0.f && ay.w2 != 0.f) v = fmaf(ax.w2 * ay.w2, e[(long)ay.p2 * ld + ax.p2], v);
+  float v = ax.w * ay.w * ld(e + (long)ay.p * pitch + ax.p);
+  if (KX == 2 && ax.w2 != 0.f) v = fmaf(ax.w2 * ay.w, ld(e + (long)ay.p * pitch + ax.p2), v);
+  if (KY == 2 && ay.w2 != 0.f) v = fmaf(ax.w * ay.w2, ld(e + (long)ay.p2 * pitch + ax.p), v);
+  if (KX == 2 && KY == 2 && ax.w2 != 0.f && ay.w2 != 0.f)
+    v = fmaf(ax.w2 * ay.w2, ld(e + (long)ay.p2 * pitch + ax.p2), v);
   return v;
 }
 
-__device__ __forceinline__ float prolong_val(const float* e, long ld, int nx, int ny, int kx, int ky, int j, int i) {
-  if (kx == 2 && ky == 2) return prolong_k<2, 2>(e, ld, nx, ny, j, i);
-  if (kx == 2) return prolong_k<2, 1>(e, ld, nx, ny, j, i);
-  return prolong_k<1, 2>(e, ld, nx, ny, j, i);
-}
-
-__device__ __forceinline__ float prolong_at(const Lvl& F, const Lvl& C, int j, int i) {
-  return prolong_val(C.u, C.ld, C.nx, C.ny, F.kx, F.ky, j, i);
+template <class LD>
+__device__ __forceinline__ float prolong_val(LD ld, const float* e, long pitch, int nx, int ny, int kx, int ky, int j,
+                                             int i) {
+  if (kx == 2 && ky == 2) return prolong_k<2, 2>(ld, e, pitch, nx, ny, j, i);
+  if (kx == 2) return prolong_k<2, 1>(ld, e, pitch, nx, ny, j, i);
+  return prolong_k<1, 2>(ld, e, pitch, nx, ny, j, i);
 }
 
 // weight with which fine index i (offset d = i - 2I in {-1, 0, 1, 2}) enters coarse I (R = P^T)
@@ -148,11 +142,13 @@ __device__ __forceinline__ float restrict_val(const float* w, long ld, int j0, i
   return restrict_k<1, 2>(w, ld, j0, i0, nx, ny, J, I);
 }
 
-// ---- V-cycle kernels -------------------------------------------------------
+// ---- phases ---------------------------------------------------------------
 //
-// Every kernel takes the instance table and a tile table; a CTA returns when
-// its instance sits the step out or has left the loop the kernel belongs to
-// (gate 0: the refinement loop, gate 1: the inner PCG loop).
+// Each phase function processes one 32 x 32 tile of one instance, written once
+// against an execution context (persist.cuh): the ordinary kernels below run it
+// as a 256-thread CTA, the persistent kernel as a 256-thread group.  The caller
+// has checked that the instance is live: it has not sat the step out or left
+// the loop the phase belongs to (gate 0: the refinement loop, 1: the inner PCG).
 
 __device__ __forceinline__ bool mx_live(const MixDesc& M, int gate) {
   if (!*M.active) return false;
@@ -163,121 +159,146 @@ __device__ __forceinline__ bool mx_live(const MixDesc& M, int gate) {
 
 using RedSmem = DRedSmem<MT>;
 
-#define MX_RED(R, vals, outv) dred_sum<R, MT>(vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
-#define MX_RED_FF(R, vals, outv) dred_sum_ff<R, MT>(vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
+// control-block fields written by the finalising tile of an earlier phase
+template <typename T>
+__device__ __forceinline__ T cget(const T* p) {
+  return __ldcg(p);
+}
 
 // rho = r.z of a V-cycle's result; beta = rho / rho_prev after the first inner iteration
 __device__ __forceinline__ void set_rho(MixCtrl* ctrl, double rz) {
-  if (ctrl->inner > 0) ctrl->beta = rz / ctrl->rho;
+  if (cget(&ctrl->inner) > 0) ctrl->beta = rz / cget(&ctrl->rho);
   ctrl->rho = rz;
 }
 
-#define MX_TILE(gate)                                      \
-  const MTile tl = TL[blockIdx.x];                         \
-  const MixDesc& M = MD[tl.inst];                          \
-  if (!mx_live(M, gate)) return;
+// the rows ty of the tile that this thread owns (ty = warp, warp + 8, ...)
+#define MX_ROWS_X(...)                                      \
+  for (int r_ = 0; r_ < RPT; ++r_) {                        \
+    const int ty = (x.tid() >> 5) + r_ * (MT / 32);         \
+    __VA_ARGS__                                             \
+  }
+
+#define X_RED(R, vals, outv) dred_sum<R, MT>(x, vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
+#define X_RED_FF(R, vals, outv) dred_sum_ff<R, MT>(x, vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
+
+constexpr int H3 = 3;
+struct DownSmem {
+  float s1[BY + 2 * H3][BX + 2 * H3];
+  float s2[BY + 4][BX + 4];
+  float rs[BY + 2][BX + 2];
+};
+struct PostSmem {
+  float w0[BY + 4][BX + 4];
+  float w1[BY + 2][BX + 2];
+  RedSmem rsm;
+};
+struct MatvecSmem {
+  float pn[BY + 2][BX + 2];
+  RedSmem rsm;
+};
+union TileSmem {
+  DownSmem d;
+  PostSmem p;
+  MatvecSmem m;
+  RedSmem r;
+};
 
 // Down-sweep of level l, fused: two damped-Jacobi sweeps from u = 0 (t = S(S(0))
 // for A u = f), the residual r = f - A t, and its restriction f_{l+1} = P^T r.
 // The tile computes the first sweep on a 3-cell halo, t on 2 and r on 1, so
 // every coarse cell whose fine patch lies in the tile is complete; only t
 // goes back to memory (the up-sweep needs it).
-constexpr int H3 = 3;
-__global__ void __launch_bounds__(MT) k_mg_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
-                                                 int gate, float omega) {
-  MX_TILE(gate)
+template <class X>
+__device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTile& tl, int l, float omega,
+                                        DownSmem& sm) {
   const Lvl L = M.lev[l], C = M.lev[l + 1];
-  __shared__ float s1[BY + 2 * H3][BX + 2 * H3];
-  __shared__ float s2[BY + 4][BX + 4];
-  __shared__ float rs[BY + 2][BX + 2];
   const int i0 = tl.i0, j0 = tl.j0;
   auto inside = [&](int gj, int gi) { return gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx; };
-  for (int idx = threadIdx.x; idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
+  for (int idx = x.tid(); idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
     const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
     const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (inside(gj, gi)) v = __fdividef(omega * L.f[(long)gj * L.ld + gi], mg_diag(L, gj, gi));
-    s1[jj + H3][ii + H3] = v;
+    if (inside(gj, gi)) v = __fdividef(omega * x.ld(L.f + (long)gj * L.ld + gi), mg_diag(L, gj, gi));
+    sm.s1[jj + H3][ii + H3] = v;
   }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < (BY + 4) * (BX + 4); idx += MT) {
+  x.sync();
+  for (int idx = x.tid(); idx < (BY + 4) * (BX + 4); idx += MT) {
     const int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
     const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
     if (inside(gj, gi)) {
-      auto at = [&](int j, int i) { return s1[j - j0 + H3][i - i0 + H3]; };
-      v = fmaf(1.f - omega, s1[jj + H3][ii + H3],
-               __fdividef(omega * (L.f[(long)gj * L.ld + gi] + mg_nsum(L, gj, gi, at)), mg_diag(L, gj, gi)));
+      auto at = [&](int j, int i) { return sm.s1[j - j0 + H3][i - i0 + H3]; };
+      v = fmaf(1.f - omega, sm.s1[jj + H3][ii + H3],
+               __fdividef(omega * (x.ld(L.f + (long)gj * L.ld + gi) + mg_nsum(L, gj, gi, at)), mg_diag(L, gj, gi)));
     }
-    s2[jj + 2][ii + 2] = v;
+    sm.s2[jj + 2][ii + 2] = v;
   }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < (BY + 2) * (BX + 2); idx += MT) {
+  x.sync();
+  for (int idx = x.tid(); idx < (BY + 2) * (BX + 2); idx += MT) {
     const int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
     const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
     if (inside(gj, gi)) {
-      auto at = [&](int j, int i) { return s2[j - j0 + 2][i - i0 + 2]; };
-      const float t = s2[jj + 2][ii + 2];
+      auto at = [&](int j, int i) { return sm.s2[j - j0 + 2][i - i0 + 2]; };
+      const float t = sm.s2[jj + 2][ii + 2];
       const long o = (long)gj * L.ld + gi;
-      v = L.f[o] - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
+      v = x.ld(L.f + o) - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
       if (jj >= 0 && jj < BY && ii >= 0 && ii < BX) L.t[o] = t;
     }
-    rs[jj + 1][ii + 1] = v;
+    sm.rs[jj + 1][ii + 1] = v;
   }
-  __syncthreads();
+  x.sync();
   // coarse cells of this tile: (32 / kx) x (32 / ky)
   const int cw = BX / L.kx, chh = BY / L.ky;
   const int I0 = i0 / L.kx, J0 = j0 / L.ky;
-  for (int idx = threadIdx.x; idx < cw * chh; idx += MT) {
+  for (int idx = x.tid(); idx < cw * chh; idx += MT) {
     const int jj = idx / cw, ii = idx - jj * cw;
     const int I = I0 + ii, J = J0 + jj;
-    if (I < C.nx && J < C.ny) {
-      // rs holds r at fine rows j0 - 1 .. j0 + BY and columns i0 - 1 .. i0 + BX
-      C.f[(long)J * C.ld + I] = restrict_val(&rs[0][0], BX + 2, j0 - 1, i0 - 1, C.nx, C.ny, L.kx, L.ky, J, I);
-    }
+    // sm.rs holds r at fine rows j0 - 1 .. j0 + BY and columns i0 - 1 .. i0 + BX
+    if (I < C.nx && J < C.ny)
+      C.f[(long)J * C.ld + I] = restrict_val(&sm.rs[0][0], BX + 2, j0 - 1, i0 - 1, C.nx, C.ny, L.kx, L.ky, J, I);
   }
 }
 
 // u_l = S(S(t_l + P u_{l+1})) with the bilinear P; on level 0 also rho = r.z
-__global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
-                                                 int gate, float omega) {
-  MX_TILE(gate)
+template <class X>
+__device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTile& tl, int l, float omega,
+                                        PostSmem& sm) {
   const Lvl F = M.lev[l], C = M.lev[l + 1];
-  __shared__ float w0[BY + 4][BX + 4];
-  __shared__ float w1[BY + 2][BX + 2];
-  __shared__ RedSmem rsm;
+  RedSmem& rsm = sm.rsm;
   const int i0 = tl.i0, j0 = tl.j0;
-  for (int idx = threadIdx.x; idx < (BY + 4) * (BX + 4); idx += MT) {
-    int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
-    int gj = j0 + jj, gi = i0 + ii;
+  auto ldx = [&](const float* p) { return x.ld(p); };
+  for (int idx = x.tid(); idx < (BY + 4) * (BX + 4); idx += MT) {
+    const int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
+    const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) v = F.t[(long)gj * F.ld + gi] + prolong_at(F, C, gj, gi);
-    w0[jj + 2][ii + 2] = v;
+    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx)
+      v = x.ld(F.t + (long)gj * F.ld + gi) + prolong_val(ldx, C.u, C.ld, C.nx, C.ny, F.kx, F.ky, gj, gi);
+    sm.w0[jj + 2][ii + 2] = v;
   }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < (BY + 2) * (BX + 2); idx += MT) {
-    int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
-    int gj = j0 + jj, gi = i0 + ii;
+  x.sync();
+  for (int idx = x.tid(); idx < (BY + 2) * (BX + 2); idx += MT) {
+    const int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
+    const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
     if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) {
-      auto at = [&](int j, int i) { return w0[j - j0 + 2][i - i0 + 2]; };
+      auto at = [&](int j, int i) { return sm.w0[j - j0 + 2][i - i0 + 2]; };
       const float d = mg_diag(F, gj, gi);
-      v = fmaf(1.f - omega, w0[jj + 2][ii + 2],
-               __fdividef(omega * (F.f[(long)gj * F.ld + gi] + mg_nsum(F, gj, gi, at)), d));
+      v = fmaf(1.f - omega, sm.w0[jj + 2][ii + 2],
+               __fdividef(omega * (x.ld(F.f + (long)gj * F.ld + gi) + mg_nsum(F, gj, gi, at)), d));
     }
-    w1[jj + 1][ii + 1] = v;
+    sm.w1[jj + 1][ii + 1] = v;
   }
-  __syncthreads();
-  const int tx = threadIdx.x & 31;
+  x.sync();
+  const int tx = x.tid() & 31;
   FF acc[1] = {{0.f, 0.f}};
-  MX_ROWS({
+  MX_ROWS_X({
     const int gi = i0 + tx, gj = j0 + ty;
     if (gi < F.nx && gj < F.ny) {
-      auto at = [&](int j, int i) { return w1[j - j0 + 1][i - i0 + 1]; };
+      auto at = [&](int j, int i) { return sm.w1[j - j0 + 1][i - i0 + 1]; };
       const float d = mg_diag(F, gj, gi);
-      const float fv = F.f[(long)gj * F.ld + gi];
-      const float v = fmaf(1.f - omega, w1[ty + 1][tx + 1], __fdividef(omega * (fv + mg_nsum(F, gj, gi, at)), d));
+      const float fv = x.ld(F.f + (long)gj * F.ld + gi);
+      const float v = fmaf(1.f - omega, sm.w1[ty + 1][tx + 1], __fdividef(omega * (fv + mg_nsum(F, gj, gi, at)), d));
       F.u[(long)gj * F.ld + gi] = v;
       if (l == 0) ff_add_prod(acc[0], fv, v);
     }
@@ -285,7 +306,207 @@ __global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, 
   // level 0: z = u is complete in this tile; rho = r.z of the PCG
   if (l == 0) {
     double out[1];
-    if (MX_RED_FF(1, acc, out) && threadIdx.x == 0) set_rho(M.ctrl, out[0]);
+    if (X_RED_FF(1, acc, out) && x.tid() == 0) set_rho(M.ctrl, out[0]);
+  }
+}
+
+// b -= mean(b), b[0] = 0 (pressure_solver.py:127-128, the mean from the exactly
+// rounded sum as in the binary64 path); x = 0, r64 = b; ||b||^2 and sum(b);
+// counts the instances that refine
+template <class X>
+__device__ __forceinline__ void ph_init(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml, RedSmem& rsm) {
+  const Geo G = M.G;
+  MixCtrl* ctrl = M.ctrl;
+  const double mean = __ddiv_rn(cget(M.bsum), M.n_cells);
+  const int i = tl.i0 + (x.tid() & 31);
+  double v[2] = {0.0, 0.0}, out[2];
+  MX_ROWS_X({
+    const int j = tl.j0 + ty;
+    if (i < G.nx && j < G.ny) {
+      const long o = (long)j * G.ld + i;
+      const double bv = (i == 0 && j == 0) ? 0.0 : __dsub_rn(x.ld(M.b + o), mean);
+      M.b[o] = bv;
+      M.x[o] = 0.0;
+      M.r64[o] = bv;
+      v[0] += bv * bv;
+      v[1] += bv;
+    }
+  })
+  if (X_RED(2, v, out) && x.tid() == 0) {
+    M.ctrl64->mean = mean;
+    M.ctrl64->nan_flag = 0u;
+    const double bb = out[0];
+    ctrl->bnorm = sqrt(bb);
+    ctrl->tol_abs_out = cget(&ctrl->tol_out) * ctrl->bnorm;
+    ctrl->rr64 = bb;
+    ctrl->sum64 = out[1];
+    ctrl->outer = 0;
+    ctrl->inner = 0;
+    ctrl->inner_total = 0;
+    ctrl->inner_done = 1;
+    ctrl->converged = (bb == 0.0) ? 1 : 0;
+    ctrl->outer_done = (bb == 0.0) ? 1 : 0;
+    if (bb != 0.0) atomicAdd(&ml->outer_active, 1);
+  }
+}
+
+// r~ = float(r64) with r~_0 = -sum_{k != 0} r64_k; e = 0; ||r~||^2; starts an inner solve
+template <class X>
+__device__ __forceinline__ void ph_prep(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml, RedSmem& rsm) {
+  const Geo G = M.G;
+  const Lvl L0 = M.lev[0];
+  MixCtrl* ctrl = M.ctrl;
+  const int i = tl.i0 + (x.tid() & 31);
+  FF v[1] = {{0.f, 0.f}};
+  double out[1];
+  MX_ROWS_X({
+    const int j = tl.j0 + ty;
+    if (i < G.nx && j < G.ny) {
+      const double rv = (i == 0 && j == 0) ? -(cget(&ctrl->sum64) - x.ld(M.r64)) : x.ld(M.r64 + (long)j * G.ld + i);
+      const float rf = __double2float_rn(rv);
+      L0.f[(long)j * L0.ld + i] = rf;
+      M.e[(long)j * L0.ld + i] = 0.f;
+      ff_add_prod(v[0], rf, rf);
+    }
+  })
+  if (X_RED_FF(1, v, out) && x.tid() == 0) {
+    const double rt = sqrt(out[0]);
+    ctrl->rt_norm = rt;
+    ctrl->tol_abs_in = cget(&ctrl->tol_in) * rt;
+    ctrl->inner = 0;
+    ctrl->inner_done = rt > 0.0 ? 0 : 1;
+    if (rt > 0.0) atomicAdd(&ml->inner_active, 1);
+  }
+}
+
+// p_new = z (first) or z + beta p_old; q = A p_new (binary32 Neumann operator); p.q
+template <class X>
+__device__ __forceinline__ void ph_matvec(const X& x, const MixDesc& M, const MTile& tl, MatvecSmem& sm) {
+  RedSmem& rsm = sm.rsm;
+  const Lvl L0 = M.lev[0];
+  MixCtrl* ctrl = M.ctrl;
+  const float* z = L0.u;
+  const int k = cget(&ctrl->inner);
+  const float* pold = (k & 1) ? M.p1 : M.p0;
+  float* pnew = (k & 1) ? M.p0 : M.p1;
+  const float beta = (float)cget(&ctrl->beta);
+  const int i0 = tl.i0, j0 = tl.j0;
+  for (int idx = x.tid(); idx < (BY + 2) * (BX + 2); idx += MT) {
+    const int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
+    const int gj = j0 + jj, gi = i0 + ii;
+    float v = 0.f;
+    if (gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx) {
+      const long o = (long)gj * L0.ld + gi;
+      v = (k == 0) ? x.ld(z + o) : fmaf(beta, x.ld(pold + o), x.ld(z + o));
+    }
+    sm.pn[jj + 1][ii + 1] = v;
+  }
+  x.sync();
+  const int tx = x.tid() & 31;
+  const int gi = i0 + tx;
+  FF v[1] = {{0.f, 0.f}};
+  double out[1];
+  MX_ROWS_X({
+    const int gj = j0 + ty;
+    if (gi < L0.nx && gj < L0.ny) {
+      auto at = [&](int j, int i) { return sm.pn[j - j0 + 1][i - i0 + 1]; };
+      const float pv = sm.pn[ty + 1][tx + 1];
+      const float qv = mg_diag(L0, gj, gi) * pv - mg_nsum(L0, gj, gi, at);
+      const long o = (long)gj * L0.ld + gi;
+      pnew[o] = pv;
+      M.q[o] = qv;
+      ff_add_prod(v[0], pv, qv);
+    }
+  })
+  if (X_RED_FF(1, v, out) && x.tid() == 0) {
+    ctrl->pq = out[0];
+    ctrl->alpha = cget(&ctrl->rho) / out[0];
+  }
+}
+
+// e += alpha p; r -= alpha q; ||r||^2 and the inner stopping test
+template <class X>
+__device__ __forceinline__ void ph_update(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml,
+                                          cudaGraphConditionalHandle cond_inner, int use_cond, RedSmem& rsm) {
+  const Lvl L0 = M.lev[0];
+  MixCtrl* ctrl = M.ctrl;
+  const int k = cget(&ctrl->inner);
+  const float* p = (k & 1) ? M.p0 : M.p1;
+  const float alpha = (float)cget(&ctrl->alpha);
+  const int i = tl.i0 + (x.tid() & 31);
+  FF v[1] = {{0.f, 0.f}};
+  double out[1];
+  MX_ROWS_X({
+    const int j = tl.j0 + ty;
+    if (i < L0.nx && j < L0.ny) {
+      const long o = (long)j * L0.ld + i;
+      M.e[o] = fmaf(alpha, x.ld(p + o), x.ld(M.e + o));
+      const float rv = fmaf(-alpha, x.ld(M.q + o), x.ld(L0.f + o));
+      L0.f[o] = rv;
+      ff_add_prod(v[0], rv, rv);
+    }
+  })
+  if (X_RED_FF(1, v, out) && x.tid() == 0) {
+    const double rr = out[0];
+    const int it = k + 1;
+    ctrl->inner = it;
+    ctrl->inner_total = cget(&ctrl->inner_total) + 1;
+    ctrl->rr_in = rr;
+    if (!(sqrt(rr) > cget(&ctrl->tol_abs_in)) || it >= cget(&ctrl->max_inner)) {
+      ctrl->inner_done = 1;
+      if (atomicSub(&ml->inner_active, 1) == 1 && use_cond) cudaGraphSetConditional(cond_inner, 0u);
+    }
+  }
+}
+
+// x += e - e[0] (binary64)
+template <class X>
+__device__ __forceinline__ void ph_correct(const X& x, const MixDesc& M, const MTile& tl) {
+  const Geo G = M.G;
+  const long lde = M.lev[0].ld;
+  const int i = tl.i0 + (x.tid() & 31);
+  const double e0 = (double)x.ld(M.e);
+  MX_ROWS_X({
+    const int j = tl.j0 + ty;
+    if (i < G.nx && j < G.ny) {
+      const long o = (long)j * G.ld + i;
+      M.x[o] = __dadd_rn(x.ld(M.x + o), __dsub_rn((double)x.ld(M.e + (long)j * lde + i), e0));
+    }
+  })
+}
+
+// r64 = b - A x with the reference's pinned operator; ||r64||^2, sum(r64); outer test
+template <class X>
+__device__ __forceinline__ void ph_resid(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml,
+                                         cudaGraphConditionalHandle cond_outer, int use_cond, RedSmem& rsm) {
+  const Geo G = M.G;
+  MixCtrl* ctrl = M.ctrl;
+  const int i = tl.i0 + (x.tid() & 31);
+  double v[2] = {0.0, 0.0}, out[2];
+  const auto Xv = x.view(M.x, G.ld);
+  MX_ROWS_X({
+    const int j = tl.j0 + ty;
+    if (i < G.nx && j < G.ny) {
+      const double ax = (i == 0 && j == 0) ? Xv(0, 0) : -lap_coherent_at(Xv, j, i, G.g);
+      const long o = (long)j * G.ld + i;
+      const double rv = __dsub_rn(x.ld(M.b + o), ax);
+      M.r64[o] = rv;
+      v[0] += rv * rv;
+      v[1] += rv;
+    }
+  })
+  if (X_RED(2, v, out) && x.tid() == 0) {
+    const double rr = out[0];
+    ctrl->rr64 = rr;
+    ctrl->sum64 = out[1];
+    const int outer = cget(&ctrl->outer) + 1;
+    ctrl->outer = outer;
+    const bool conv = !(sqrt(rr) > cget(&ctrl->tol_abs_out));
+    ctrl->converged = conv ? 1 : 0;
+    if (conv || outer >= cget(&ctrl->max_outer)) {
+      ctrl->outer_done = 1;
+      if (atomicSub(&ml->outer_active, 1) == 1 && use_cond) cudaGraphSetConditional(cond_outer, 0u);
+    }
   }
 }
 
@@ -341,13 +562,11 @@ __device__ __forceinline__ void c_sweep(const CLvl& L, const float* f, const flo
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD, int gate, int bottom_sweeps,
-                                                   float omega) {
-  const MixDesc& M = MD[blockIdx.x];
-  if (!mx_live(M, gate)) return;
+// The coarse V-cycle of instance M by the whole 1024-thread CTA; sm: 3 x (its
+// levels' cells) floats of shared memory.
+__device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, float omega, float* sm) {
   const Lvl C = M.lev[M.nlev - 1];
   const int nl = M.coarse_levels;
-  extern __shared__ float sm[];
   CLvl L[8];
   int tot = 0;
   {
@@ -368,7 +587,7 @@ __global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD
   float* rh = sm;            // right-hand side of every level (level 0: the entry level's f)
   float* e = sm + tot;       // pre-smoothed iterate on the way down; the bottom solution
   float* w = sm + 2 * tot;   // residual on the way down; each level's result on the way up
-  C_FOR(L[0], { rh[c] = C.f[(long)j * C.ld + i]; })
+  C_FOR(L[0], { rh[c] = __ldcg(C.f + (long)j * C.ld + i); })
   __syncthreads();
   for (int l = 0; l + 1 < nl; ++l) {
     const CLvl& Lv = L[l];
@@ -414,11 +633,14 @@ __global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD
     }
   }
   // up: w_l = S(S(e_l + P result_{l+1})); the bottom's result is in e, every other level's in w
+  auto lds = [](const float* p) { return *p; };
   for (int l = nl - 2; l >= 0; --l) {
     const CLvl& Lv = L[l];
     const CLvl& Cv = L[l + 1];
     const float* ec = (l + 1 == nl - 1) ? e : w;
-    C_FOR(Lv, { w[Lv.off + c] = e[Lv.off + c] + prolong_val(ec + Cv.off, Cv.nx, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i); })
+    C_FOR(Lv, {
+      w[Lv.off + c] = e[Lv.off + c] + prolong_val(lds, ec + Cv.off, Cv.nx, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i);
+    })
     __syncthreads();
     c_sweep(Lv, rh, w, e, omega);
     c_sweep(Lv, rh, e, w, omega);
@@ -426,17 +648,11 @@ __global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD
   const float* z = (nl == 1) ? e : w;
   C_FOR(L[0], { C.u[(long)j * C.ld + i] = z[c]; })
   if (M.nlev == 1) {
-    // the V-cycle ran entirely here: rho = r.z over level 0, summed as the tile kernels do
+    // the V-cycle ran entirely here: rho = r.z over level 0, summed as the tile phases do
     __shared__ double wsum[CT / 32];
     FF acc = {0.f, 0.f};
     C_FOR(L[0], { ff_add_prod(acc, rh[c], z[c]); })
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      FF y;
-      y.hi = __shfl_xor_sync(0xffffffffu, acc.hi, o);
-      y.lo = __shfl_xor_sync(0xffffffffu, acc.lo, o);
-      acc = ff_merge(acc, y);
-    }
+    acc = ff_warp_sum(acc);
     if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)acc.hi + (double)acc.lo;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -445,56 +661,46 @@ __global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD
       set_rho(M.ctrl, rz);
     }
   }
+  __syncthreads();
 }
 
-// ---- PCG and refinement kernels -------------------------------------------
-//
-// Reductions are deterministic binary64 sums over the instance's level-0 tiles
-// (tile-ordered partials; the last CTA of the instance completes them).
+// ---- kernels: one tile per 256-thread CTA -----------------------------------
 
+#define CTA_TILE(gate)                          \
+  const MTile tl = TL[blockIdx.x];              \
+  const MixDesc& M = MD[tl.inst];               \
+  if (!mx_live(M, gate)) return;                \
+  const CtaCtx x{};
 
-// b -= mean(b), b[0] = 0 (pressure_solver.py:127-128, the mean from the exactly
-// rounded sum as in the binary64 path); x = 0, r64 = b; ||b||^2 and sum(b);
-// counts the instances that refine
+__global__ void __launch_bounds__(MT) k_mg_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
+                                                 int gate, float omega) {
+  CTA_TILE(gate)
+  __shared__ DownSmem sm;
+  ph_down(x, M, tl, l, omega, sm);
+}
+
+__global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
+                                                 int gate, float omega) {
+  CTA_TILE(gate)
+  __shared__ PostSmem sm;
+  ph_post(x, M, tl, l, omega, sm);
+}
+
+__global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD, int gate, int bottom_sweeps,
+                                                   float omega) {
+  const MixDesc& M = MD[blockIdx.x];
+  if (!mx_live(M, gate)) return;
+  extern __shared__ float csm[];
+  coarse_cycle(M, bottom_sweeps, omega, csm);
+}
+
 __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                  MixLoop* ml) {
   const MTile tl = TL[blockIdx.x];
   const MixDesc& M = MD[tl.inst];
   if (!*M.active) return;
   __shared__ RedSmem rsm;
-  const Geo G = M.G;
-  MixCtrl* ctrl = M.ctrl;
-  const double mean = __ddiv_rn(*M.bsum, M.n_cells);
-  const int i = tl.i0 + (threadIdx.x & 31);
-  double v[2] = {0.0, 0.0}, out[2];
-  MX_ROWS({
-    const int j = tl.j0 + ty;
-    if (i < G.nx && j < G.ny) {
-      const long o = (long)j * G.ld + i;
-      const double bv = (i == 0 && j == 0) ? 0.0 : __dsub_rn(M.b[o], mean);
-      M.b[o] = bv;
-      M.x[o] = 0.0;
-      M.r64[o] = bv;
-      v[0] += bv * bv;
-      v[1] += bv;
-    }
-  })
-  if (MX_RED(2, v, out) && threadIdx.x == 0) {
-    M.ctrl64->mean = mean;
-    M.ctrl64->nan_flag = 0u;
-    const double bb = out[0];
-    ctrl->bnorm = sqrt(bb);
-    ctrl->tol_abs_out = ctrl->tol_out * ctrl->bnorm;
-    ctrl->rr64 = bb;
-    ctrl->sum64 = out[1];
-    ctrl->outer = 0;
-    ctrl->inner = 0;
-    ctrl->inner_total = 0;
-    ctrl->inner_done = 1;
-    ctrl->converged = (bb == 0.0) ? 1 : 0;
-    ctrl->outer_done = (bb == 0.0) ? 1 : 0;
-    if (bb != 0.0) atomicAdd(&ml->outer_active, 1);
-  }
+  ph_init(CtaCtx{}, M, tl, ml, rsm);
 }
 
 __global__ void k_ml_reset(MixLoop* ml, int which) {
@@ -503,6 +709,9 @@ __global__ void k_ml_reset(MixLoop* ml, int which) {
     ml->outer_active = 0;
     ml->guard_o = 0;
     ml->tripped = 0;
+    ml->gb.count = 0u;
+    ml->gb.err = 0;
+    __threadfence();
   } else {
     ml->inner_active = 0;
     ml->guard_i = 0;
@@ -528,185 +737,151 @@ __global__ void k_ml_guard(MixLoop* ml, int which, cudaGraphConditionalHandle co
   }
 }
 
-// r~ = float(r64) with r~_0 = -sum_{k != 0} r64_k; e = 0; ||r~||^2; starts an inner solve
 __global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                  MixLoop* ml) {
-  MX_TILE(0)
+  CTA_TILE(0)
   __shared__ RedSmem rsm;
-  const Geo G = M.G;
-  const Lvl L0 = M.lev[0];
-  MixCtrl* ctrl = M.ctrl;
-  const int i = tl.i0 + (threadIdx.x & 31);
-  FF v[1] = {{0.f, 0.f}};
-  double out[1];
-  MX_ROWS({
-    const int j = tl.j0 + ty;
-    if (i < G.nx && j < G.ny) {
-      const double rv = (i == 0 && j == 0) ? -(ctrl->sum64 - M.r64[0]) : M.r64[(long)j * G.ld + i];
-      const float rf = __double2float_rn(rv);
-      L0.f[(long)j * L0.ld + i] = rf;
-      M.e[(long)j * L0.ld + i] = 0.f;
-      ff_add_prod(v[0], rf, rf);
-    }
-  })
-  if (MX_RED_FF(1, v, out) && threadIdx.x == 0) {
-    const double rt = sqrt(out[0]);
-    ctrl->rt_norm = rt;
-    ctrl->tol_abs_in = ctrl->tol_in * rt;
-    ctrl->inner = 0;
-    ctrl->inner_done = rt > 0.0 ? 0 : 1;
-    if (rt > 0.0) atomicAdd(&ml->inner_active, 1);
-  }
+  ph_prep(x, M, tl, ml, rsm);
 }
 
-// p_new = z (first) or z + beta p_old; q = A p_new (binary32 Neumann operator); p.q
 __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
-  MX_TILE(1)
-  __shared__ float pn[BY + 2][BX + 2];
-  __shared__ RedSmem rsm;
-  const Lvl L0 = M.lev[0];
-  MixCtrl* ctrl = M.ctrl;
-  const float* __restrict__ z = L0.u;
-  const int k = *(volatile int*)&ctrl->inner;
-  const float* __restrict__ pold = (k & 1) ? M.p1 : M.p0;
-  float* __restrict__ pnew = (k & 1) ? M.p0 : M.p1;
-  const float beta = (float)ctrl->beta;
-  const int i0 = tl.i0, j0 = tl.j0;
-  for (int idx = threadIdx.x; idx < (BY + 2) * (BX + 2); idx += MT) {
-    int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
-    int gj = j0 + jj, gi = i0 + ii;
-    float v = 0.f;
-    if (gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx) {
-      const long o = (long)gj * L0.ld + gi;
-      v = (k == 0) ? z[o] : fmaf(beta, pold[o], z[o]);
-    }
-    pn[jj + 1][ii + 1] = v;
-  }
-  __syncthreads();
-  const int tx = threadIdx.x & 31;
-  const int gi = i0 + tx;
-  FF v[1] = {{0.f, 0.f}};
-  double out[1];
-  MX_ROWS({
-    const int gj = j0 + ty;
-    if (gi < L0.nx && gj < L0.ny) {
-      auto at = [&](int j, int i) { return pn[j - j0 + 1][i - i0 + 1]; };
-      const float pv = pn[ty + 1][tx + 1];
-      const float qv = mg_diag(L0, gj, gi) * pv - mg_nsum(L0, gj, gi, at);
-      const long o = (long)gj * L0.ld + gi;
-      pnew[o] = pv;
-      M.q[o] = qv;
-      ff_add_prod(v[0], pv, qv);
-    }
-  })
-  if (MX_RED_FF(1, v, out) && threadIdx.x == 0) {
-    ctrl->pq = out[0];
-    ctrl->alpha = ctrl->rho / out[0];
-  }
+  CTA_TILE(1)
+  __shared__ MatvecSmem sm;
+  ph_matvec(x, M, tl, sm);
 }
 
-// e += alpha p; r -= alpha q; ||r||^2 and the inner stopping test
 __global__ void __launch_bounds__(MT) k_mx_update(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                    MixLoop* ml, cudaGraphConditionalHandle cond_inner, int use_cond) {
-  MX_TILE(1)
+  CTA_TILE(1)
   __shared__ RedSmem rsm;
-  const Lvl L0 = M.lev[0];
-  MixCtrl* ctrl = M.ctrl;
-  const int k = *(volatile int*)&ctrl->inner;
-  const float* __restrict__ p = (k & 1) ? M.p0 : M.p1;
-  const float alpha = (float)ctrl->alpha;
-  const int i = tl.i0 + (threadIdx.x & 31);
-  FF v[1] = {{0.f, 0.f}};
-  double out[1];
-  MX_ROWS({
-    const int j = tl.j0 + ty;
-    if (i < L0.nx && j < L0.ny) {
-      const long o = (long)j * L0.ld + i;
-      M.e[o] = fmaf(alpha, p[o], M.e[o]);
-      const float rv = fmaf(-alpha, M.q[o], L0.f[o]);
-      L0.f[o] = rv;
-      ff_add_prod(v[0], rv, rv);
-    }
-  })
-  if (MX_RED_FF(1, v, out) && threadIdx.x == 0) {
-    const double rr = out[0];
-    const int it = k + 1;
-    ctrl->inner = it;
-    ctrl->inner_total += 1;
-    ctrl->rr_in = rr;
-    if (!(sqrt(rr) > ctrl->tol_abs_in) || it >= ctrl->max_inner) {
-      ctrl->inner_done = 1;
-      if (atomicSub(&ml->inner_active, 1) == 1 && use_cond) cudaGraphSetConditional(cond_inner, 0u);
-    }
-  }
+  ph_update(x, M, tl, ml, cond_inner, use_cond, rsm);
 }
 
-// x += e - e[0] (binary64)
 __global__ void __launch_bounds__(MT) k_mx_correct(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
-  MX_TILE(0)
-  const Geo G = M.G;
-  const long lde = M.lev[0].ld;
-  const int i = tl.i0 + (threadIdx.x & 31);
-  if (i >= G.nx) return;
-  const double e0 = (double)M.e[0];
-  MX_ROWS({
-    const int j = tl.j0 + ty;
-    if (j < G.ny) {
-      const long o = (long)j * G.ld + i;
-      M.x[o] = __dadd_rn(M.x[o], __dsub_rn((double)M.e[(long)j * lde + i], e0));
-    }
-  })
+  CTA_TILE(0)
+  ph_correct(x, M, tl);
 }
 
-// r64 = b - A x with the reference's pinned operator; ||r64||^2, sum(r64); outer test
 __global__ void __launch_bounds__(MT) k_mx_resid(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                   MixLoop* ml, cudaGraphConditionalHandle cond_outer, int use_cond) {
-  MX_TILE(0)
+  CTA_TILE(0)
   __shared__ RedSmem rsm;
-  const Geo G = M.G;
-  MixCtrl* ctrl = M.ctrl;
-  const int i = tl.i0 + (threadIdx.x & 31);
-  double v[2] = {0.0, 0.0}, out[2];
-  View2<const double> X{M.x, G.ld};
-  MX_ROWS({
-    const int j = tl.j0 + ty;
-    if (i < G.nx && j < G.ny) {
-      const double ax = (i == 0 && j == 0) ? X(0, 0) : -lap_coherent_at(X, j, i, G.g);
-      const long o = (long)j * G.ld + i;
-      const double rv = __dsub_rn(M.b[o], ax);
-      M.r64[o] = rv;
-      v[0] += rv * rv;
-      v[1] += rv;
-    }
-  })
-  if (MX_RED(2, v, out) && threadIdx.x == 0) {
-    const double rr = out[0];
-    ctrl->rr64 = rr;
-    ctrl->sum64 = out[1];
-    ctrl->outer += 1;
-    const bool conv = !(sqrt(rr) > ctrl->tol_abs_out);
-    ctrl->converged = conv ? 1 : 0;
-    if (conv || ctrl->outer >= ctrl->max_outer) {
-      ctrl->outer_done = 1;
-      if (atomicSub(&ml->outer_active, 1) == 1 && use_cond) cudaGraphSetConditional(cond_outer, 0u);
-    }
-  }
+  ph_resid(x, M, tl, ml, cond_outer, use_cond, rsm);
 }
 
 // summary of the mixed solve for the step record
-__global__ void k_mx_finish(const MixDesc* __restrict__ MD, int n) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const MixDesc& M = MD[k];
+__device__ __forceinline__ void mx_finish_one(const MixDesc& M) {
   if (!*M.active) return;
   const MixCtrl* m = M.ctrl;
   Ctrl64* c = M.ctrl64;
-  c->iter = m->inner_total;
-  c->refine_passes = m->outer;
-  c->info = m->converged ? 0 : M.maxiter_report;
-  c->zero_rhs = (m->bnorm == 0.0) ? 1 : 0;
-  c->bnrm2 = m->bnorm;
-  *M.res_out = m->rr64;      // ||b - A x||^2 of the final x (the refinement's own residual)
+  c->iter = cget(&m->inner_total);
+  c->refine_passes = cget(&m->outer);
+  c->info = cget(&m->converged) ? 0 : M.maxiter_report;
+  const double bn = cget(&m->bnorm);
+  c->zero_rhs = (bn == 0.0) ? 1 : 0;
+  c->bnrm2 = bn;
+  *M.res_out = cget(&m->rr64);      // ||b - A x||^2 of the final x (the refinement's own residual)
+}
+
+__global__ void k_mx_finish(const MixDesc* __restrict__ MD, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) mx_finish_one(MD[k]);
+}
+
+// ---- the persistent solve ------------------------------------------------------
+//
+// The whole refinement of every instance in one cooperative launch: one
+// 1024-thread CTA per SM, each CTA four 256-thread groups that take the tiles of
+// a phase in turn, and a grid barrier between phases.  The loop decisions
+// (instances still refining, still in the inner solve) are read after a
+// barrier, so every CTA takes the same branch.  The phases are the functions
+// the ordinary kernels run, on the same tiles in the same order, so the
+// results are the same bits.  Loop trip bounds stop a solve whose instances do
+// not report; a barrier that waits too long sets the error flag, and every CTA
+// returns at its next barrier.
+
+struct PersistArgs {
+  const MixDesc* dd;
+  int n, maxlev;
+  const MTile* tl0;
+  int nt0;
+  const MTile* tpre[MAX_LEVELS];
+  int ntpre[MAX_LEVELS];
+  MixLoop* ml;
+  float omega;
+  int bottom_sweeps;
+};
+
+__global__ void __launch_bounds__(CT, 1) k_mx_persist(PersistArgs A) {
+  extern __shared__ __align__(16) unsigned char psm[];
+  const GroupCtx x{(int)(threadIdx.x >> 8)};
+  TileSmem& ts = reinterpret_cast<TileSmem*>(psm)[x.g];
+  const int ngroups = gridDim.x * 4;
+  const int gid = blockIdx.x * 4 + x.g;
+  MixLoop* ml = A.ml;
+  GridBar* gb = &ml->gb;
+  auto vcycle = [&]() -> bool {
+    for (int l = 0; l + 1 < A.maxlev; ++l) {
+      for (int t = gid; t < A.ntpre[l]; t += ngroups) {
+        const MTile tl = A.tpre[l][t];
+        const MixDesc& M = A.dd[tl.inst];
+        if (mx_live(M, 1)) ph_down(x, M, tl, l, A.omega, ts.d);
+      }
+      if (!grid_sync(gb)) return false;
+    }
+    for (int k = blockIdx.x; k < A.n; k += gridDim.x) {
+      const MixDesc& M = A.dd[k];
+      if (mx_live(M, 1)) coarse_cycle(M, A.bottom_sweeps, A.omega, reinterpret_cast<float*>(psm));
+    }
+    if (!grid_sync(gb)) return false;
+    for (int l = A.maxlev - 2; l >= 0; --l) {
+      for (int t = gid; t < A.ntpre[l]; t += ngroups) {
+        const MTile tl = A.tpre[l][t];
+        const MixDesc& M = A.dd[tl.inst];
+        if (mx_live(M, 1)) ph_post(x, M, tl, l, A.omega, ts.p);
+      }
+      if (!grid_sync(gb)) return false;
+    }
+    return true;
+  };
+#define PERSIST_TILES(gate, body)                                  \
+  for (int t = gid; t < A.nt0; t += ngroups) {                     \
+    const MTile tl = A.tl0[t];                                     \
+    const MixDesc& M = A.dd[tl.inst];                              \
+    if (mx_live(M, gate)) { body; }                                \
+  }
+  for (int t = gid; t < A.nt0; t += ngroups) {
+    const MTile tl = A.tl0[t];
+    const MixDesc& M = A.dd[tl.inst];
+    if (*M.active) ph_init(x, M, tl, ml, ts.r);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) ml->inner_active = 0;
+  if (!grid_sync(gb)) return;
+  int pass = 0;
+  for (; pass < ml->gmax_o; ++pass) {
+    if (cget(&ml->outer_active) == 0) break;
+    PERSIST_TILES(0, ph_prep(x, M, tl, ml, ts.r))
+    if (!grid_sync(gb)) return;
+    if (!vcycle()) return;
+    int it = 0;
+    for (; it < ml->gmax_i; ++it) {
+      if (cget(&ml->inner_active) == 0) break;
+      PERSIST_TILES(1, ph_matvec(x, M, tl, ts.m))
+      if (!grid_sync(gb)) return;
+      PERSIST_TILES(1, ph_update(x, M, tl, ml, 0ull, 0, ts.r))
+      if (!grid_sync(gb)) return;
+      if (!vcycle()) return;
+    }
+    if (it == ml->gmax_i && cget(&ml->inner_active) > 0 && blockIdx.x == 0 && threadIdx.x == 0) ml->tripped = 1;
+    PERSIST_TILES(0, ph_correct(x, M, tl))
+    if (!grid_sync(gb)) return;
+    PERSIST_TILES(0, ph_resid(x, M, tl, ml, 0ull, 0, ts.r))
+    if (blockIdx.x == 0 && threadIdx.x == 0) ml->inner_active = 0;
+    if (!grid_sync(gb)) return;
+  }
+  if (pass == ml->gmax_o && cget(&ml->outer_active) > 0 && blockIdx.x == 0 && threadIdx.x == 0) ml->tripped = 1;
+#undef PERSIST_TILES
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < A.n; k += gridDim.x * blockDim.x) mx_finish_one(A.dd[k]);
 }
 
 // Dependent binary32 FMAs for a few tens of microseconds (no memory waits):
@@ -974,12 +1149,28 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   B->pad = (float*)take(sizeof(float));
   B->gmax_o = gmax_o;
   B->gmax_i = gmax_i;
-  MixLoop ml0 = {0, 0, 0, 0, gmax_o, gmax_i, 0};
+  MixLoop ml0 = {0, 0, 0, 0, gmax_o, gmax_i, 0, {0u, 0u, 0, 0}};
   cudaMemcpy(B->loop, &ml0, sizeof(MixLoop), cudaMemcpyHostToDevice);
   cudaError_t e = cudaMemcpy(B->dd, B->hd.data(), n * sizeof(MixDesc), cudaMemcpyHostToDevice);
   B->coarse_smem = smem;
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) {
+    // the persistent solve: one 1024-thread CTA per SM, if the device co-schedules them
+    const size_t psmem = std::max(4 * sizeof(TileSmem), smem);
+    int dev = 0, sms = 0, coop = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (coop && cudaFuncSetAttribute(k_mx_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mx_persist, CT, psmem) == cudaSuccess && occ >= 1) {
+      B->persist_ok = 1;
+      B->persist = 0;      // opt-in (pfgb_set_persistent): the kernel graph is faster on GB300
+      B->pgrid = sms;
+      B->psmem = psmem;
+    }
+    cudaGetLastError();   // a refused attribute or query only disables the persistent form
+  }
   if (e != cudaSuccess) {
     batch_destroy(B);
     return set_error(PFGB_ECUDA, std::string("mixed batch set-up: ") + cudaGetErrorString(e));
@@ -1023,8 +1214,37 @@ static void add_vcycle(GraphChain& c, Batch* B, int gate, float omega) {
     if (B->ntpre[l]) c.kernel(k_mg_post, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, omega);
 }
 
+static PersistArgs persist_args(const Batch* B, float omega) {
+  PersistArgs a = {};
+  a.dd = B->dd;
+  a.n = B->n;
+  a.maxlev = B->maxlev;
+  a.tl0 = B->tl[0];
+  a.nt0 = B->ntl[0];
+  for (int l = 0; l < MAX_LEVELS; ++l) {
+    a.tpre[l] = B->tpre[l];
+    a.ntpre[l] = B->ntpre[l];
+  }
+  a.ml = B->loop;
+  a.omega = omega;
+  a.bottom_sweeps = 8;
+  return a;
+}
+
+int set_persistent(Batch* B, int on) {
+  B->persist = (on && B->persist_ok) ? 1 : 0;
+  return PFGB_OK;
+}
+
 int append_solve(GraphChain& c, Batch* B) {
   const float omega = 0.8f;
+  if (B->persist) {
+    c.kernel(k_ml_reset, dim3(1), dim3(32), B->loop, 0);
+    c.kernel_coop(k_mx_persist, dim3(B->pgrid), dim3(CT), B->psmem, persist_args(B, omega));
+    if (c.status() != cudaSuccess)
+      return set_error(PFGB_ECUDA, std::string("building the persistent solve: ") + cudaGetErrorString(c.status()));
+    return PFGB_OK;
+  }
   const MixDesc* dd = B->dd;
   const dim3 g0(B->ntl[0]);
   cudaGraphConditionalHandle cond_outer = 0, cond_inner = 0;
@@ -1069,6 +1289,23 @@ static void launch_vcycle(Batch* B, int gate, float omega, cudaStream_t s) {
 
 int run_direct(Batch* B, cudaStream_t s) {
   const float omega = 0.8f;
+  if (B->persist) {
+    k_ml_reset<<<1, 32, 0, s>>>(B->loop, 0);
+    PersistArgs a = persist_args(B, omega);
+    void* args[] = {&a};
+    const bool timed = B->ev && B->nev >= 2;
+    if (timed) {
+      k_pad<<<1, 32, 0, s>>>(B->pad, 20000);
+      cudaEventRecord(B->ev[0], s);
+    }
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_mx_persist, dim3(B->pgrid), dim3(CT), args, B->psmem, s);
+    if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("persistent solve launch: ") + cudaGetErrorString(e));
+    if (timed) {
+      cudaEventRecord(B->ev[1], s);
+      *B->ev_used = 1;
+    }
+    return PFGB_OK;
+  }
   const int g0 = B->ntl[0];
   MixLoop h;
   int timed_launches = 0;

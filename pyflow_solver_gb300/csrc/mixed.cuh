@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "graph.cuh"
+#include "persist.cuh"
 #include "stencil.cuh"
 #include "step64.cuh"
 
@@ -81,6 +82,7 @@ struct MixLoop {
   int guard_o, guard_i;
   int gmax_o, gmax_i;
   int tripped;
+  GridBar gb;     // barrier of the persistent solve
 };
 
 struct Batch {
@@ -100,6 +102,11 @@ struct Batch {
   int nev = 0;
   int* ev_used = nullptr;
   float* pad = nullptr;                        // sink of the profiling pad kernel
+  // the persistent form of the solve (one cooperative launch)
+  int persist_ok = 0;                          // the device co-schedules its CTAs
+  int persist = 0;                             // in use
+  int pgrid = 0;
+  size_t psmem = 0;
   char* ws = nullptr;
   size_t ws_bytes = 0;
 };
@@ -125,6 +132,8 @@ void batch_destroy(Batch* B);
 int append_solve(GraphChain& c, Batch* B);
 // The same with direct launches and host loop control (for profiling).
 int run_direct(Batch* B, cudaStream_t s);
+// Use the persistent cooperative solve (on, where the device allows it) or the kernel graph.
+int set_persistent(Batch* B, int on);
 // New tolerances and iteration limits for instance k (limits within the loop guards).
 int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer, int max_inner, int maxiter_report);
 

@@ -12,6 +12,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "common.cuh"
+
 namespace pfgb {
 namespace mixed {
 
@@ -20,6 +22,9 @@ struct CtaCtx {
   __device__ __forceinline__ void sync() const { __syncthreads(); }
   template <typename T>
   __device__ __forceinline__ T ld(const T* p) const { return *p; }
+  __device__ __forceinline__ View2<const double> view(const double* p, long ld) const {
+    return View2<const double>{p, ld};
+  }
 };
 
 struct GroupCtx {
@@ -30,17 +35,22 @@ struct GroupCtx {
   }
   template <typename T>
   __device__ __forceinline__ T ld(const T* p) const { return __ldcg(p); }
+  __device__ __forceinline__ View2Cg<double> view(const double* p, long ld) const { return View2Cg<double>{p, ld}; }
 };
 
 // Grid-wide barrier of a cooperative launch with a bounded wait.  Every CTA
-// calls it the same number of times.  A CTA that waits longer than the limit
-// (or finds the error flag set) marks the error and returns false; its caller
-// then leaves the kernel, and every other CTA fails its next barrier at once.
+// calls it the same number of times.  The arrival counter only grows: a CTA
+// arriving as number a waits until the counter reaches the next multiple of
+// the grid size (release on arrival, acquire on the polls, so the writes of
+// every CTA before the barrier are visible to every CTA after it).  A CTA that
+// waits longer than the limit (or finds the error flag set) marks the error
+// and returns false; its caller leaves the kernel, and every other CTA fails
+// its next barrier at once.  The counter is zeroed before each launch.
 struct GridBar {
   unsigned count;
-  unsigned gen;
+  unsigned pad0;
   int err;
-  int pad;
+  int pad1;
 };
 
 constexpr unsigned long long GRID_SPIN_LIMIT = 1ull << 22;
@@ -50,28 +60,25 @@ __device__ __forceinline__ bool grid_sync(GridBar* gb) {
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned* genp = &gb->gen;
     if (*(volatile int*)&gb->err) {
       ok = 0;
     } else {
-      const unsigned g = *genp;
-      __threadfence();
-      if (atomicAdd(&gb->count, 1u) == gridDim.x - 1) {
-        atomicExch(&gb->count, 0u);
-        __threadfence();
-        atomicAdd(&gb->gen, 1u);
-      } else {
-        unsigned long long spins = 0;
-        while (*genp == g) {
-          if (++spins > GRID_SPIN_LIMIT || *(volatile int*)&gb->err) {
-            atomicExch(&gb->err, 1);
-            ok = 0;
-            break;
-          }
-          __nanosleep(64);
+      const unsigned n = gridDim.x;
+      unsigned arrived;
+      asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(arrived) : "l"(&gb->count) : "memory");
+      const unsigned target = (arrived / n + 1) * n;
+      unsigned long long spins = 0;
+      while (true) {
+        unsigned cur;
+        asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->count) : "memory");
+        if ((int)(cur - target) >= 0) break;
+        if (++spins > GRID_SPIN_LIMIT || *(volatile int*)&gb->err) {
+          atomicExch(&gb->err, 1);
+          ok = 0;
+          break;
         }
+        __nanosleep(20);
       }
-      __threadfence();
     }
     s_ok = ok;
   }

@@ -25,8 +25,10 @@
 #include <algorithm>
 #include <vector>
 
+#include "dred.cuh"
 #include "graph.cuh"
 #include "mixed.cuh"
+#include "persist.cuh"
 #include "pfgb_internal.h"
 #include "stencil.cuh"
 #include "step64.cuh"
@@ -149,6 +151,7 @@ __global__ void k_dt(const InstDesc* __restrict__ ID, int n) {
   ctrl->safeguard = safeguard;
   ctrl->cfl = py_max(DIV(MUL(umax, dt), a.dx), DIV(MUL(vmax, dt), a.dy));
   ctrl->dtm = py_max(dt, 1e-14);
+  ctrl->rdtm = 1.0 / ctrl->dtm;
 }
 
 // dt given by the caller of a stand-alone projection (instance 0)
@@ -157,6 +160,7 @@ __global__ void k_set_dt(const InstDesc* __restrict__ ID, double dt) {
   Ctrl64* ctrl = ID[0].ctrl;
   ctrl->dt = dt;
   ctrl->dtm = py_max(dt, 1e-14);
+  ctrl->rdtm = 1.0 / ctrl->dtm;
   ctrl->safeguard = 0;
 }
 
@@ -568,6 +572,168 @@ __global__ void __launch_bounds__(NT) k_post_diag(const InstDesc* __restrict__ I
   xa_finish(sl, 3, D.nt_pc);
 }
 
+// ---------------------------------------------------------------------------
+// The same kernels for the mixed-precision form.  The arithmetic of every cell
+// is the binary64 code above, except that divisions by the spacing and by dt
+// are products with the reciprocal; the sums are deterministic binary64 sums
+// over the instance's tiles (dred.cuh) instead of exactly rounded ones.  Both
+// differences are at the level of one rounding, far inside the 1e-6 the mixed
+// form is held to, and keep a result identical alone and in any batch.
+
+using StepRed = DRedSmem<NT>;
+#define STEP_RED(R, vals, outv) dred_sum<R, NT>(mixed::CtaCtx{}, vals, D.part, D.nt_pc, tl.loc, D.ticket, outv, rsm)
+
+struct RecipGrid {
+  double rx, ry;
+};
+__device__ __forceinline__ RecipGrid recips(const Geo64& G) { return RecipGrid{G.rdx, G.rdy}; }
+
+__device__ __forceinline__ double gx_r(View2<const double> p, int j, int i, int nx, double rx) {
+  return (i < nx - 1) ? MUL(SUB(p(j, i + 1), p(j, i)), rx) : 0.0;
+}
+__device__ __forceinline__ double gy_r(View2<const double> p, int j, int i, int ny, double ry) {
+  return (j < ny - 1) ? MUL(SUB(p(j + 1, i), p(j, i)), ry) : 0.0;
+}
+__device__ __forceinline__ double div_c_r(View2<const double> u, View2<const double> v, int j, int i,
+                                          const RecipGrid& r) {
+  const double xp = (i >= 1) ? MUL(SUB(u(j, i), u(j, i - 1)), r.rx) : MUL(u(j, 0), r.rx);
+  const double yp = (j >= 1) ? MUL(SUB(v(j, i), v(j - 1, i)), r.ry) : MUL(v(0, i), r.ry);
+  return ADD(xp, yp);
+}
+__device__ __forceinline__ double neg_lap_pinned_r(View2<const double> p, int j, int i, int nx, int ny,
+                                                   const RecipGrid& r) {
+  if (i == 0 && j == 0) return p(0, 0);
+  const double gxi = gx_r(p, j, i, nx, r.rx);
+  const double xp = (i >= 1) ? MUL(SUB(gxi, gx_r(p, j, i - 1, nx, r.rx)), r.rx) : MUL(gxi, r.rx);
+  const double gyj = gy_r(p, j, i, ny, r.ry);
+  const double yp = (j >= 1) ? MUL(SUB(gyj, gy_r(p, j - 1, i, ny, r.ry)), r.ry) : MUL(gyj, r.ry);
+  return -ADD(xp, yp);
+}
+
+// max|u|, max|v| and ||div_central(u, v; 1, 1)||^2 (the safeguard's baseline)
+__global__ void __launch_bounds__(NT) k_prestep_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
+  __shared__ StepRed rsm;
+  Ctrl64* ctrl = D.ctrl;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
+  View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds};
+  double v[1] = {0.0}, out[1];
+  unsigned long long ub = 0ull, vb = 0ull;
+  if (i < G.nx && j < G.ny) {
+    ub = abs_bits(U(j, i));
+    vb = abs_bits(V(j, i));
+    const double d = div_central_at(U, V, j, i, G.nx, G.ny, 1.0, 1.0);
+    v[0] = d * d;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ub = max(ub, __shfl_xor_sync(0xffffffffu, ub, o));
+    vb = max(vb, __shfl_xor_sync(0xffffffffu, vb, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (ub) atomicMax(&ctrl->umax_bits, ub);
+    if (vb) atomicMax(&ctrl->vmax_bits, vb);
+  }
+  if (STEP_RED(1, v, out) && threadIdx.x == 0) {
+    const double um = __longlong_as_double((long long)*(volatile unsigned long long*)&ctrl->umax_bits);
+    const double vm = __longlong_as_double((long long)*(volatile unsigned long long*)&ctrl->vmax_bits);
+    ctrl->umax = ADD(um, 1e-12);
+    ctrl->vmax = ADD(vm, 1e-12);
+    ctrl->umax_bits = 0ull;
+    ctrl->vmax_bits = 0ull;
+    D.slots[S_DIVC_BEFORE].result = out[0];
+    ctrl->div_before = sqrt(out[0]);
+  }
+}
+
+// b = -div_c(u*, v*) / max(dt, 1e-14); sum(b) (for the mean) and ||div_c||^2
+__global__ void __launch_bounds__(NT) k_rhs_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
+  __shared__ StepRed rsm;
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
+  const RecipGrid rg = recips(G);
+  double v[2] = {0.0, 0.0}, out[2];
+  if (i < G.nx && j < G.ny) {
+    View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
+    const double d = div_c_r(US, VS, j, i, rg);
+    const double bv = MUL(-d, D.ctrl->rdtm);
+    D.b[(long)j * G.ld + i] = bv;
+    v[0] = bv;
+    v[1] = d * d;
+  }
+  if (STEP_RED(2, v, out) && threadIdx.x == 0) {
+    D.slots[S_BSUM].result = out[0];
+    D.slots[S_DIVSTAR].result = out[1];
+  }
+}
+
+// p = x - x[0]; u = u* - dt gx(p), v likewise; lid; sums of (u - u_old)^2, (v - v_old)^2
+__global__ void __launch_bounds__(NT) k_pin_correct_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
+  __shared__ StepRed rsm;
+  Ctrl64* ctrl = D.ctrl;
+  const LidArgs L = D.L;
+  const RecipGrid rg = recips(G);
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
+  double v[2] = {0.0, 0.0}, out[2];
+  int bad = 0;
+  if (i < G.nx && j < G.ny) {
+    const double dt = ctrl->dt;
+    View2<const double> X{D.x, G.ld};
+    const double x0 = X(0, 0);
+    const double pv = SUB(X(j, i), x0);
+    const double gx = (i < G.nx - 1) ? MUL(SUB(SUB(X(j, i + 1), x0), pv), rg.rx) : 0.0;
+    const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(X(j + 1, i), x0), pv), rg.ry) : 0.0;
+    const long o = (long)j * D.usld + i;
+    const long os = (long)j * G.lds + i;
+    const double uc = SUB(D.us[o], MUL(dt, gx));
+    const double vc = SUB(D.vs[o], MUL(dt, gy));
+    D.us[o] = uc;
+    D.vs[o] = vc;
+    D.pi[os] = pv;
+    const double uf = (L.has_lid && j == G.ny - 1) ? L.lid : uc;
+    const double du = SUB(uf, D.ui[os]);
+    const double dv = SUB(vc, D.vi[os]);
+    D.ui[os] = uf;
+    D.vi[os] = vc;
+    v[0] = du * du;
+    v[1] = dv * dv;
+    bad = !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->nan_flag, 1u);
+  if (STEP_RED(2, v, out) && threadIdx.x == 0) {
+    D.slots[S_RU].result = out[0];
+    D.slots[S_RV].result = out[1];
+  }
+}
+
+// ||div_c(u*, v*)||^2 after the correction, ||A p - b||^2, ||div_central(u, v; 1, 1)||^2
+__global__ void __launch_bounds__(NT) k_post_diag_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  TILE_PROLOGUE
+  __shared__ StepRed rsm;
+  const RecipGrid rg = recips(G);
+  const int i = tl.i0 + (threadIdx.x & 31);
+  const int j = tl.j0 + (threadIdx.x >> 5);
+  double v[3] = {0.0, 0.0, 0.0}, out[3];
+  if (i < G.nx && j < G.ny) {
+    View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
+    View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds}, P{D.pi, G.lds};
+    const double d = div_c_r(US, VS, j, i, rg);
+    const double lr = SUB(neg_lap_pinned_r(P, j, i, G.nx, G.ny, rg), D.b[(long)j * G.ld + i]);
+    const double c = div_central_at(U, V, j, i, G.nx, G.ny, 1.0, 1.0);
+    v[0] = d * d;
+    v[1] = lr * lr;
+    v[2] = c * c;
+  }
+  if (STEP_RED(3, v, out) && threadIdx.x == 0) {
+    D.slots[S_DIVAFTER].result = out[0];
+    D.slots[S_LINRES].result = out[1];
+    D.slots[S_CONT].result = out[2];
+  }
+}
+
 // one StepOut64 record per instance
 __global__ void k_gather(const InstDesc* __restrict__ ID, int n) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -609,8 +775,9 @@ static Spacing make_spacing(double h) { return spacing_for(h); }
 
 // tiles of height th covering an nx x ny grid of instance k
 static void add_tiles(std::vector<Tile>& v, int k, int nx, int ny, int th) {
+  int loc = 0;
   for (int j0 = 0; j0 < ny; j0 += th)
-    for (int i0 = 0; i0 < nx; i0 += TX) v.push_back(Tile{k, i0, j0, 0});
+    for (int i0 = 0; i0 < nx; i0 += TX) v.push_back(Tile{k, i0, j0, loc++});
 }
 
 static int count_tiles(int nx, int ny, int th) { return ((nx + TX - 1) / TX) * ((ny + th - 1) / th); }
@@ -630,6 +797,8 @@ static Geo64 make_geo(int nx, int ny, long ld, double dx, double dy, double invd
   G.g.sy = make_spacing(dy);
   G.invd = invd;
   G.jacobi = jacobi;
+  G.rdx = 1.0 / dx;
+  G.rdy = 1.0 / dy;
   return G;
 }
 
@@ -695,7 +864,8 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
   for (int k = 0; k < n; ++k) {
     const long ld = round_up(prms[k].nx, 32);
     vec[k] = up((size_t)ld * prms[k].ny * sizeof(double));
-    bytes += 8 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64));
+    bytes += 8 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64)) +
+             up(3 * (size_t)count_tiles(prms[k].nx, prms[k].ny, PB_Y) * sizeof(double)) + up(sizeof(unsigned));
     add_tiles(tpc, k, prms[k].nx, prms[k].ny, PB_Y);
     for (int v = 0; v < NVAR; ++v) {
       add_tiles(tcgv[v], k, prms[k].nx, prms[k].ny, VAR_R[v] * PB_Y);
@@ -755,6 +925,8 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     D.ctrl = (Ctrl64*)take(sizeof(Ctrl64));
     D.nt_pc = count_tiles(prm.nx, prm.ny, PB_Y);
     D.nt_cg = I->ntcg_inst[I->cg_var][k];
+    D.part = (double*)take(3 * (size_t)D.nt_pc * sizeof(double));
+    D.ticket = (unsigned*)take(sizeof(unsigned));
   }
   I->dd = (InstDesc*)take(n * sizeof(InstDesc));
   I->tpc = (Tile*)take(tpc.size() * sizeof(Tile));
@@ -912,7 +1084,8 @@ static void enqueue_projection(Instance64* I, cudaStream_t s) {
 }
 
 static void enqueue_prologue(Instance64* I, cudaStream_t s) {
-  k_prestep<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  if (I->mix) k_prestep_m<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  else k_prestep<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
   k_dt<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
   k_predict<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
 }
@@ -932,11 +1105,11 @@ static int build_graph(Instance64* I, int mode) {
   const dim3 gp(I->ntpc), gc(I->ntcg), g1((I->n + 31) / 32);
   GraphChain c(I->graph);
   if (mode == 0) {
-    c.kernel(k_prestep, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+    c.kernel(I->mix ? k_prestep_m : k_prestep, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
     c.kernel(k_dt, g1, dim3(32), (const InstDesc*)I->dd, I->n);
     c.kernel(k_predict, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   }
-  c.kernel(k_rhs, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  c.kernel(I->mix ? k_rhs_m : k_rhs, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   GraphChain body(nullptr);
   if (I->mix) {
     // the refinement removes b's mean, pins b[0], solves A x = b and leaves ||b - A x||^2
@@ -957,8 +1130,8 @@ static int build_graph(Instance64* I, int mode) {
     body.kernel(k_loop_guard, dim3(1), dim3(32), I->lc, cond, 1);
   }
   if (!I->mix) c.kernel(k_post_resid<0>, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
-  c.kernel(k_pin_correct, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
-  c.kernel(k_post_diag, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  c.kernel(I->mix ? k_pin_correct_m : k_pin_correct, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  c.kernel(I->mix ? k_post_diag_m : k_post_diag, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   c.kernel(k_gather, g1, dim3(32), (const InstDesc*)I->dd, I->n);
   if (c.status() != cudaSuccess || (!I->mix && body.status() != cudaSuccess)) {
     cudaError_t be = c.status() != cudaSuccess ? c.status() : body.status();
@@ -1001,6 +1174,8 @@ static int read_out(Instance64* I, cudaStream_t s, pfgb_step_out* out) {
     if (I->mix) {
       mixed::MixLoop ml;
       e = cudaMemcpy(&ml, I->mix->loop, sizeof(ml), cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess && ml.gb.err)
+        return set_error(PFGB_ESTATE, "the persistent solve's grid barrier timed out (its CTAs were not co-resident)");
       tripped = (e == cudaSuccess) ? ml.tripped : 0;
     } else {
       LoopCtl lc;
@@ -1028,10 +1203,10 @@ static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
   }
   if (mode == 0) enqueue_prologue(I, s);
   if (I->mix) {
-    k_rhs<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_rhs_m<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
     if (int rc = mixed::run_direct(I->mix, s)) return rc;
-    k_pin_correct<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-    k_post_diag<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_pin_correct_m<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_post_diag_m<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
     k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
   } else {
     enqueue_projection(I, s);
@@ -1212,6 +1387,21 @@ int instance64_autotune(Instance64* I, cudaStream_t s, int* chosen, double* us) 
   }
   set_cg_variant(I, best_v);
   if (chosen) *chosen = best_v;
+  return PFGB_OK;
+}
+
+int instance64_set_persistent(Instance64* I, int on) {
+  if (!I->mix) return PFGB_OK;
+  mixed::set_persistent(I->mix, on);
+  if (I->exec) {
+    cudaGraphExecDestroy(I->exec);
+    I->exec = nullptr;
+  }
+  if (I->graph) {
+    cudaGraphDestroy(I->graph);
+    I->graph = nullptr;
+  }
+  I->graph_mode = -1;
   return PFGB_OK;
 }
 

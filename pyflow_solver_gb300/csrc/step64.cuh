@@ -43,6 +43,7 @@ struct Ctrl64 {
   double umax, vmax;                         // + 1e-12 applied
   double div_before;
   double dt, dtm, cfl;
+  double rdtm;          // 1 / dtm (the mixed form multiplies by it)
   int safeguard;
   // CG
   int iter, done, info, zero_rhs;
@@ -68,6 +69,7 @@ struct Geo64 {
   Grid2 g;
   double invd;        // interior Jacobi entry 1/(2/dx^2 + 2/dy^2)
   int jacobi;
+  double rdx, rdy;    // 1/dx, 1/dy (the mixed form multiplies by them)
 };
 
 struct CGArgs {
@@ -87,7 +89,7 @@ struct LidArgs {
 
 // One tile of work: instance index and the tile's first cell.
 struct Tile {
-  int inst, i0, j0, pad;
+  int inst, i0, j0, loc;       // loc: index of the tile among its instance's tiles of the table
 };
 
 // Everything the kernels need about one instance.
@@ -109,6 +111,8 @@ struct InstDesc {
   const StepIn* in;
   StepOut64* out;
   int nt_pc, nt_cg;            // this instance's tiles in the per-cell / CG tile tables
+  double* part;                // per-tile partial sums of the deterministic reductions (3 x nt_pc)
+  unsigned* ticket;            // their arrival counter
 };
 
 // Batch-wide loop control of a WHILE node: the number of instances still

@@ -8,6 +8,9 @@ from .. import _capi
 
 # Run each step as one CUDA graph (True) or as individual kernel launches.
 GRAPH_MODE = True
+# Mixed form: the pressure solve as one persistent cooperative launch (True) or
+# as a graph of per-phase kernels (False, the faster on GB300); both give the same bits.
+PERSISTENT = False
 # Pick the binary64 CG tile shape by timing (pfgb_autotune) once per grid size.
 AUTOTUNE = True
 _TUNED: dict = {}
@@ -36,6 +39,7 @@ class Instance:
         self._h = h
         self.params = params
         _capi.check(lib.pfgb_set_graph(h, 1 if GRAPH_MODE else 0), "pfgb_set_graph")
+        _capi.check(lib.pfgb_set_persistent(h, 1 if PERSISTENT else 0), "pfgb_set_persistent")
         self.cg_variant = None
         if AUTOTUNE and params.precision == 0:
             self.cg_variant = autotune(h, ("single", params.nx, params.ny))

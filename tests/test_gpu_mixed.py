@@ -109,3 +109,24 @@ def test_mixed_graph_and_direct_launches_agree():
     for a, b in zip(out[0][0], out[1][0]):
         np.testing.assert_array_equal(a, b)
     assert out[0][1] == out[1][1]
+
+
+def test_persistent_solve_equals_kernel_graph():
+    """The persistent cooperative solve and the graph of per-phase kernels give the same bits."""
+    from pyflow_solver_gb300 import ResidualManager, _capi, allocate_state, interior_view, step
+    from pyflow_solver_gb300.solvers._handle import instance_for
+    from pyflow_solver_gb300.solvers.solver import step_params
+    lib = _capi.load()
+    for nx, ny in ((96, 64), (128, 128), (48, 40)):
+        cfg = cavity(nx, ny, 700.0, 1.3, precision="mixed")
+        runs = []
+        for persistent in (1, 0):
+            st = allocate_state(nx, ny)
+            P, *_ = step_params(cfg, nx, ny)
+            _capi.check(lib.pfgb_set_persistent(instance_for(st, P).handle, persistent), "set_persistent")
+            tr = ResidualManager()
+            diags = [step(cfg, st, tr, it)[2] for it in range(4)]
+            runs.append(([interior_view(st.fields[k]).cpu().numpy() for k in "uvp"], diags))
+        for a, b in zip(runs[0][0], runs[1][0]):
+            np.testing.assert_array_equal(a, b)
+        assert runs[0][1] == runs[1][1]
