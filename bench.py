@@ -289,6 +289,16 @@ def max_over_ranks(x, dist):
     return float(t.item())
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the roofline
+# kernel, from the ncu captures summarised in profiles/ (two launches each, averaged).
+TRAFFIC = {
+    ("cavity512", "mixed::k_mx_matvec"): 1.60e6,      # profiles/roofline_traffic.md
+    ("cavity2048", "mixed::k_mx_matvec"): 34.11e6,
+    ("cavity2048", "pfgb::k_cg_matvec"): 94.64e6,
+    ("cavity512", "pfgb::k_cg_matvec"): 4.27e6,       # profiles/k_cg_matvec_fp64_512.md
+}
+
+
 def mixed_solve_bytes(cells, inner, passes):
     """Compulsory bytes of one persistent mixed solve (binary32 levels, binary64 refinement):
     per inner iteration 16 (matvec) + 24 (update) + 22 (level-0 down- and up-sweep) + 7
@@ -297,7 +307,7 @@ def mixed_solve_bytes(cells, inner, passes):
     return cells * (32 + 89 * passes + 69 * inner)
 
 
-def kernel_roofline(lib, cfg, st, tr, it, cells, precision):
+def kernel_roofline(lib, cfg, st, tr, it, cells, precision, workload=None):
     """Live CUDA-event timing of the dominant kernel during one more step: the
     persistent solve (mixed) or the CG matvec (binary64)."""
     import ctypes
@@ -329,7 +339,7 @@ def kernel_roofline(lib, cfg, st, tr, it, cells, precision):
         kern, model = "pfgb::k_cg_matvec", "4 binary64 words per cell"
     achieved = nbytes / per_launch_s / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": None, "kernel": kern, "peak_source": f"{src} (copy bandwidth)",
+            "traffic": TRAFFIC.get((workload, kern)), "kernel": kern, "peak_source": f"{src} (copy bandwidth)",
             "launches_timed": n.value, "per_launch_us": per_launch_s * 1e6,
             "algorithmic_bytes_per_launch": nbytes, "bytes_model": model}
 
@@ -389,7 +399,7 @@ def bench_cavity(args, dist, world, rank, local):
     passes = [d.get("refine_passes", 0) for d in diags]
     nlev = mg_levels(n, n)
     launches = sum(launches_per_step(args.precision, c, p, nlev, args.persistent) for c, p in zip(cg, passes))
-    roof = None if args.no_roofline else kernel_roofline(lib, cfg, st, tr, it, n * n, args.precision)
+    roof = None if args.no_roofline else kernel_roofline(lib, cfg, st, tr, it, n * n, args.precision, wl)
     extra = {}
     if args.precision == "mixed" and not args.no_plain:
         _, _, _, _, pms, pd = run("fp64", args.plain_steps, 1)

@@ -162,10 +162,14 @@ PFGB_API int pfgb_batch_set_params(pfgb_handle* handle, int k, const pfgb_params
 PFGB_API int pfgb_project(pfgb_handle* handle, double* u, double* v, double* p, long ld, double dt,
                           void* stream, pfgb_step_out* out);
 
-/* Run pfgb_step as one CUDA graph (default on) or as individual launches.
- * The graph is built on the first step and rebuilt when the state arrays
- * move; the CG loop is a WHILE conditional node, so the device decides when
- * it stops.  Both modes give identical results.  No reference counterpart. */
+/* Run pfgb_step as one CUDA graph (on = 1, the default) or as individual
+ * launches (0).  The graph is built on the first step and rebuilt when the
+ * state arrays move; the CG loop is a WHILE conditional node, so the device
+ * decides when it stops.  With on = 1 consecutive kernels are joined by
+ * programmatic dependent-launch edges (the next kernel is launched while the
+ * previous one runs and waits for it on the device); on = 2 builds the graph
+ * with ordinary edges.  All modes give identical results.  No reference
+ * counterpart. */
 PFGB_API int pfgb_set_graph(pfgb_handle* handle, int on);
 
 /* ---- array operators (device arrays, no synchronisation) --------------- */

@@ -78,7 +78,7 @@ class BatchedCavities:
         if graph is None:
             from .solvers import _handle
             graph = _handle.GRAPH_MODE
-        _capi.check(_capi.load().pfgb_set_graph(h, 1 if graph else 0), "pfgb_set_graph")
+        _capi.check(_capi.load().pfgb_set_graph(h, int(graph)), "pfgb_set_graph")
         from .solvers import _handle
         _capi.check(_capi.load().pfgb_set_persistent(h, 1 if _handle.PERSISTENT else 0), "pfgb_set_persistent")
         self.cg_variant = None

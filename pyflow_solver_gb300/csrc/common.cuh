@@ -68,6 +68,15 @@ struct View2Cg {
   __device__ __forceinline__ T operator()(int j, int i) const { return __ldcg(p + (long)j * ld + i); }
 };
 
+// Programmatic dependent launch: let the graph's next kernel start launching
+// now, then wait until this kernel's predecessor has completed and its writes
+// are visible.  Every kernel of a step graph begins with it (a no-op for a
+// kernel that was not launched as a programmatic dependent).
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Ordered bit pattern of a non-negative double (NaN sorts above +inf), for
 // exact max reductions with 64-bit integer atomics.
 __device__ __forceinline__ unsigned long long abs_bits(double a) {

@@ -14,7 +14,9 @@ namespace pfgb {
 
 class GraphChain {
  public:
-  explicit GraphChain(cudaGraph_t g) : g_(g) {}
+  // pdl: join consecutive kernel nodes by programmatic edges (the next kernel
+  // is launched while the previous one runs and waits in pdl_enter)
+  explicit GraphChain(cudaGraph_t g, bool pdl = false) : g_(g), pdl_(pdl) {}
 
   cudaGraph_t graph() const { return g_; }
   cudaError_t status() const { return err_; }
@@ -43,8 +45,11 @@ class GraphChain {
     if (err_ != cudaSuccess) return;
     std::tuple<P...> vals(std::forward<A>(args)...);
     smem_ = smem;
+    no_pdl_ = true;
     add_kernel(reinterpret_cast<void*>(f), grid, block, vals, std::index_sequence_for<P...>{});
+    no_pdl_ = false;
     smem_ = 0;
+    last_is_kernel_ = false;   // the node after a cooperative launch waits for it in the ordinary way
     if (err_ != cudaSuccess) return;
     cudaLaunchAttributeValue v = {};
     v.cooperative = 1;
@@ -67,7 +72,8 @@ class GraphChain {
     if (err_ != cudaSuccess) return GraphChain(nullptr, err_);
     last_ = node;
     has_last_ = true;
-    return GraphChain(p.conditional.phGraph_out[0]);
+    last_is_kernel_ = false;
+    return GraphChain(p.conditional.phGraph_out[0], pdl_);
   }
 
  private:
@@ -84,10 +90,32 @@ class GraphChain {
     kp.kernelParams = argp;
     kp.extra = nullptr;
     cudaGraphNode_t node;
+    if (pdl_ && !no_pdl_ && has_last_ && last_is_kernel_) {
+      cudaGraphNodeParams np = {};
+      np.type = cudaGraphNodeTypeKernel;
+      np.kernel.func = kp.func;
+      np.kernel.gridDim = kp.gridDim;
+      np.kernel.blockDim = kp.blockDim;
+      np.kernel.sharedMemBytes = kp.sharedMemBytes;
+      np.kernel.kernelParams = kp.kernelParams;
+      np.kernel.extra = kp.extra;
+      cudaGraphEdgeData ed = {};
+      ed.from_port = cudaGraphKernelNodePortProgrammatic;
+      ed.type = cudaGraphDependencyTypeProgrammatic;
+      const cudaError_t pe = cudaGraphAddNode(&node, g_, &last_, &ed, 1, &np);
+      if (pe == cudaSuccess) {
+        last_ = node;
+        ++n_prog_;
+        return;
+      }
+      cudaGetLastError();   // not supported here: an ordinary edge
+      last_prog_err_ = pe;
+    }
     err_ = cudaGraphAddKernelNode(&node, g_, has_last_ ? &last_ : nullptr, has_last_ ? 1 : 0, &kp);
     if (err_ == cudaSuccess) {
       last_ = node;
       has_last_ = true;
+      last_is_kernel_ = true;
     }
   }
 
@@ -96,6 +124,13 @@ class GraphChain {
   bool has_last_ = false;
   cudaError_t err_ = cudaSuccess;
   size_t smem_ = 0;
+  bool pdl_ = false;
+  bool no_pdl_ = false;
+  bool last_is_kernel_ = false;
+
+ public:
+  int n_prog_ = 0;                              // kernel nodes joined by a programmatic edge
+  cudaError_t last_prog_err_ = cudaSuccess;     // why the last programmatic edge was refused
 };
 
 }  // namespace pfgb

@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -674,6 +675,7 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, float omega, f
 
 __global__ void __launch_bounds__(MT) k_mg_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
                                                  int gate, float omega) {
+  pdl_enter();
   CTA_TILE(gate)
   __shared__ DownSmem sm;
   ph_down(x, M, tl, l, omega, sm);
@@ -681,6 +683,7 @@ __global__ void __launch_bounds__(MT) k_mg_down(const MixDesc* __restrict__ MD, 
 
 __global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
                                                  int gate, float omega) {
+  pdl_enter();
   CTA_TILE(gate)
   __shared__ PostSmem sm;
   ph_post(x, M, tl, l, omega, sm);
@@ -688,6 +691,7 @@ __global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, 
 
 __global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD, int gate, int bottom_sweeps,
                                                    float omega) {
+  pdl_enter();
   const MixDesc& M = MD[blockIdx.x];
   if (!mx_live(M, gate)) return;
   extern __shared__ float csm[];
@@ -696,6 +700,7 @@ __global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD
 
 __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                  MixLoop* ml) {
+  pdl_enter();
   const MTile tl = TL[blockIdx.x];
   const MixDesc& M = MD[tl.inst];
   if (!*M.active) return;
@@ -704,6 +709,7 @@ __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, 
 }
 
 __global__ void k_ml_reset(MixLoop* ml, int which) {
+  pdl_enter();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (which == 0) {
     ml->outer_active = 0;
@@ -720,6 +726,7 @@ __global__ void k_ml_reset(MixLoop* ml, int which) {
 
 // condition of a loop = some instance still in it
 __global__ void k_ml_arm(MixLoop* ml, int which, cudaGraphConditionalHandle cond, int use_cond) {
+  pdl_enter();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int a = which == 0 ? ml->outer_active : ml->inner_active;
   if (use_cond) cudaGraphSetConditional(cond, a > 0 ? 1u : 0u);
@@ -727,6 +734,7 @@ __global__ void k_ml_arm(MixLoop* ml, int which, cudaGraphConditionalHandle cond
 
 // last node of a loop body: stops the loop after its trip bound whatever the instances report
 __global__ void k_ml_guard(MixLoop* ml, int which, cudaGraphConditionalHandle cond, int use_cond) {
+  pdl_enter();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int g = which == 0 ? ++ml->guard_o : ++ml->guard_i;
   const int gmax = which == 0 ? ml->gmax_o : ml->gmax_i;
@@ -739,12 +747,14 @@ __global__ void k_ml_guard(MixLoop* ml, int which, cudaGraphConditionalHandle co
 
 __global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                  MixLoop* ml) {
+  pdl_enter();
   CTA_TILE(0)
   __shared__ RedSmem rsm;
   ph_prep(x, M, tl, ml, rsm);
 }
 
 __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
+  pdl_enter();
   CTA_TILE(1)
   __shared__ MatvecSmem sm;
   ph_matvec(x, M, tl, sm);
@@ -752,18 +762,21 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD
 
 __global__ void __launch_bounds__(MT) k_mx_update(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                    MixLoop* ml, cudaGraphConditionalHandle cond_inner, int use_cond) {
+  pdl_enter();
   CTA_TILE(1)
   __shared__ RedSmem rsm;
   ph_update(x, M, tl, ml, cond_inner, use_cond, rsm);
 }
 
 __global__ void __launch_bounds__(MT) k_mx_correct(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
+  pdl_enter();
   CTA_TILE(0)
   ph_correct(x, M, tl);
 }
 
 __global__ void __launch_bounds__(MT) k_mx_resid(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                   MixLoop* ml, cudaGraphConditionalHandle cond_outer, int use_cond) {
+  pdl_enter();
   CTA_TILE(0)
   __shared__ RedSmem rsm;
   ph_resid(x, M, tl, ml, cond_outer, use_cond, rsm);
@@ -784,6 +797,7 @@ __device__ __forceinline__ void mx_finish_one(const MixDesc& M) {
 }
 
 __global__ void k_mx_finish(const MixDesc* __restrict__ MD, int n) {
+  pdl_enter();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) mx_finish_one(MD[k]);
 }
@@ -1270,6 +1284,9 @@ int append_solve(GraphChain& c, Batch* B) {
   outer.kernel(k_mx_resid, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_outer, 1);
   outer.kernel(k_ml_guard, dim3(1), dim3(32), B->loop, 0, cond_outer, 1);
   c.kernel(k_mx_finish, dim3((B->n + 31) / 32), dim3(32), dd, B->n);
+  if (std::getenv("PFGB_GRAPH_DEBUG"))
+    std::fprintf(stderr, "pfgb mixed graph: programmatic edges outer %d inner %d; last refusal: %s\n", outer.n_prog_,
+                 inner.n_prog_, cudaGetErrorString(inner.last_prog_err_));
   cudaError_t st = c.status() != cudaSuccess ? c.status() : (outer.status() != cudaSuccess ? outer.status() : inner.status());
   if (st != cudaSuccess) return set_error(PFGB_ECUDA, std::string("building the mixed solve: ") + cudaGetErrorString(st));
   return PFGB_OK;

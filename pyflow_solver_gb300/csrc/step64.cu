@@ -18,6 +18,7 @@
 // Every CG kernel returns at once when the device control block says the
 // solve is done, so a fixed launch sequence reproduces scipy's early exit.
 #include <cstddef>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -40,6 +41,8 @@ constexpr int TX = 32;        // tile width (one warp per tile row)
 constexpr int TY = 16;        // tile height of the CG kernels (2 rows per thread)
 constexpr int RPT = TY / (NT / TX);   // rows per thread in the CG kernels (2)
 constexpr int PB_Y = NT / TX;         // tile height of the per-cell kernels (8)
+constexpr int PB_R = 4;               // the mixed-form per-cell kernels: 32 x 32 tiles, 4 rows per thread
+constexpr int TY_M = PB_R * PB_Y;
 
 __device__ __forceinline__ double jacobi_apply(const Geo64& G, int j, int i, double r) {
   if (!G.jacobi) return r;
@@ -76,6 +79,7 @@ __device__ __forceinline__ void zero_sacc(long long* sacc) {
 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NT) k_prestep(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
@@ -93,7 +97,7 @@ __global__ void __launch_bounds__(NT) k_prestep(const InstDesc* __restrict__ ID,
   if (i < G.nx && j < G.ny) {
     ub = abs_bits(U(j, i));
     vb = abs_bits(V(j, i));
-    double d = div_central_at(U, V, j, i, G.nx, G.ny, 1.0, 1.0);
+    double d = div_central_unit(U, V, j, i, G.nx, G.ny);
     xa_term_prod(d, d, t, fl);
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -119,6 +123,7 @@ __global__ void __launch_bounds__(NT) k_prestep(const InstDesc* __restrict__ ID,
 
 // dt selection, exactly the Python float sequence of solver.py:25-62 (one thread per instance)
 __global__ void k_dt(const InstDesc* __restrict__ ID, int n) {
+  pdl_enter();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const InstDesc& Dd = ID[k];
@@ -166,6 +171,7 @@ __global__ void k_set_dt(const InstDesc* __restrict__ ID, double dt) {
 
 // predictor: u* = u - dt*conv_u(u,v), v* likewise (solver.py:73-95)
 __global__ void __launch_bounds__(NT) k_predict(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   const int i = tl.i0 + (threadIdx.x & 31);
   const int j = tl.j0 + (threadIdx.x >> 5);
@@ -188,6 +194,7 @@ __global__ void __launch_bounds__(NT) k_predict(const InstDesc* __restrict__ ID,
 
 // RHS: b = -div_c(u*,v*)/max(dt,1e-14); sum(b); ||div_c(u*,v*)||^2
 __global__ void __launch_bounds__(NT) k_rhs(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
@@ -220,6 +227,7 @@ __global__ void __launch_bounds__(NT) k_rhs(const InstDesc* __restrict__ ID, con
 // Instances that start iterating are counted in the loop control.
 __global__ void __launch_bounds__(NT) k_cg_init(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
                                                  LoopCtl* lc) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
@@ -283,6 +291,7 @@ __global__ void __launch_bounds__(NT) k_cg_init(const InstDesc* __restrict__ ID,
 
 // Arms a WHILE loop: its condition is "some instance still iterates".
 __global__ void k_loop_arm(LoopCtl* lc, cudaGraphConditionalHandle cond, int use_cond) {
+  pdl_enter();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   lc->guard = 0;
   lc->tripped = 0;
@@ -291,6 +300,7 @@ __global__ void k_loop_arm(LoopCtl* lc, cudaGraphConditionalHandle cond, int use
 
 // Last node of a WHILE body: stops the loop after guard_max trips in any case.
 __global__ void k_loop_guard(LoopCtl* lc, cudaGraphConditionalHandle cond, int use_cond) {
+  pdl_enter();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int g = ++lc->guard;
   if (g >= lc->guard_max && lc->active > 0) {
@@ -307,6 +317,7 @@ __global__ void k_loop_guard(LoopCtl* lc, cudaGraphConditionalHandle cond, int u
 // R: rows per thread (the tile is 32 x 8R cells); the autotuner picks R per handle.
 template <int OP, int R = RPT>
 __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   constexpr int TYv = R * PB_Y;
   TILE_PROLOGUE
   Ctrl64* ctrl = D.ctrl;
@@ -390,6 +401,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
 template <int R = RPT>
 __global__ void __launch_bounds__(NT) k_cg_update(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
                                                    LoopCtl* lc, cudaGraphConditionalHandle cond, int use_cond) {
+  pdl_enter();
   TILE_PROLOGUE
   Ctrl64* ctrl = D.ctrl;
   if (*(volatile int*)&ctrl->done) return;
@@ -460,6 +472,7 @@ __device__ __forceinline__ double apply_A(View2<const double> X, int j, int i, c
 // ||b - A x||^2 (the true residual of interface.solve)
 template <int OP>
 __global__ void __launch_bounds__(NT) k_post_resid(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
@@ -487,6 +500,7 @@ __global__ void __launch_bounds__(NT) k_post_resid(const InstDesc* __restrict__ 
 //   interior row and the sums of (u-u_old)^2 are formed.
 // mode 1 (projection only): us/vs are the state's own u/v, corrected in place.
 __global__ void __launch_bounds__(NT) k_pin_correct(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
@@ -540,6 +554,7 @@ __global__ void __launch_bounds__(NT) k_pin_correct(const InstDesc* __restrict__
 
 // ||div_c(u_corr)||^2, ||A p - b||^2, ||div_central(u,v;1,1)||^2
 __global__ void __launch_bounds__(NT) k_post_diag(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS], sacc2[XA_DIGITS];
   __shared__ long long wred[(NT / 32) * XA_WLIMBS];
@@ -562,7 +577,7 @@ __global__ void __launch_bounds__(NT) k_post_diag(const InstDesc* __restrict__ I
     xa_term_prod(d, d, t0, f0);
     double lr = SUB(apply_A<0>(P, j, i, G.g), D.b[(long)j * G.ld + i]);
     xa_term_prod(lr, lr, t1, f1);
-    double c = div_central_at(U, V, j, i, G.nx, G.ny, 1.0, 1.0);
+    double c = div_central_unit(U, V, j, i, G.nx, G.ny);
     xa_term_prod(c, c, t2, f2);
   }
   reduce_terms(&slots[S_DIVAFTER], &t0, 1, f0, sacc0, wred, ired);
@@ -581,7 +596,12 @@ __global__ void __launch_bounds__(NT) k_post_diag(const InstDesc* __restrict__ I
 // form is held to, and keep a result identical alone and in any batch.
 
 using StepRed = DRedSmem<NT>;
-#define STEP_RED(R, vals, outv) dred_sum<R, NT>(mixed::CtaCtx{}, vals, D.part, D.nt_pc, tl.loc, D.ticket, outv, rsm)
+#define STEP_RED(R, vals, outv) dred_sum<R, NT>(mixed::CtaCtx{}, vals, D.part, D.nt_m, tl.loc, D.ticket, outv, rsm)
+#define M_ROWS(...)                                         \
+  for (int r_ = 0; r_ < PB_R; ++r_) {                       \
+    const int j = tl.j0 + (threadIdx.x >> 5) + r_ * PB_Y;   \
+    __VA_ARGS__                                             \
+  }
 
 struct RecipGrid {
   double rx, ry;
@@ -612,20 +632,22 @@ __device__ __forceinline__ double neg_lap_pinned_r(View2<const double> p, int j,
 
 // max|u|, max|v| and ||div_central(u, v; 1, 1)||^2 (the safeguard's baseline)
 __global__ void __launch_bounds__(NT) k_prestep_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ StepRed rsm;
   Ctrl64* ctrl = D.ctrl;
   const int i = tl.i0 + (threadIdx.x & 31);
-  const int j = tl.j0 + (threadIdx.x >> 5);
   View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds};
   double v[1] = {0.0}, out[1];
   unsigned long long ub = 0ull, vb = 0ull;
-  if (i < G.nx && j < G.ny) {
-    ub = abs_bits(U(j, i));
-    vb = abs_bits(V(j, i));
-    const double d = div_central_at(U, V, j, i, G.nx, G.ny, 1.0, 1.0);
-    v[0] = d * d;
-  }
+  M_ROWS({
+    if (i < G.nx && j < G.ny) {
+      ub = max(ub, abs_bits(U(j, i)));
+      vb = max(vb, abs_bits(V(j, i)));
+      const double d = div_central_unit(U, V, j, i, G.nx, G.ny);
+      v[0] += d * d;
+    }
+  })
   for (int o = 16; o > 0; o >>= 1) {
     ub = max(ub, __shfl_xor_sync(0xffffffffu, ub, o));
     vb = max(vb, __shfl_xor_sync(0xffffffffu, vb, o));
@@ -646,22 +668,92 @@ __global__ void __launch_bounds__(NT) k_prestep_m(const InstDesc* __restrict__ I
   }
 }
 
+// Predictor of the mixed form: the convective derivative in binary32 on
+// binary32 copies of u and v, the update u* = u - dt conv in binary64.  The
+// rounding of the inputs perturbs conv by about eps32 |f| / dx, so dt conv by
+// about CFL eps32 |f| (CFL <= 0.5): a few 1e-8 of the field, inside the 1e-6 the
+// mixed form is held to.  Same stencils, clamping and sign tests as advection.py.
+__device__ __forceinline__ float q_comb(float dp, float d0, float dm, bool pos) {
+  // phi_e - phi_w of the QUICK interpolants from the three face differences
+  return pos ? (0.375f * dp + 0.75f * d0) - 0.125f * dm : (0.375f * dm + 0.75f * d0) - 0.125f * dp;
+}
+
+__global__ void __launch_bounds__(NT) k_predict_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
+  TILE_PROLOGUE
+  __shared__ float su[TY_M + 4][TX + 4], sv[TY_M + 4][TX + 4];
+  const int i0 = tl.i0, j0 = tl.j0;
+  View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds};
+  const int L = G.nx - 1, T = G.ny - 1;
+  // u and v as binary32 on a 2-cell halo; outside the grid the clamped (edge-padded) values
+  for (int idx = threadIdx.x; idx < (TY_M + 4) * (TX + 4); idx += NT) {
+    const int jj = idx / (TX + 4) - 2, ii = idx % (TX + 4) - 2;
+    const int gj = clampi(j0 + jj, 0, T), gi = clampi(i0 + ii, 0, L);
+    su[jj + 2][ii + 2] = __double2float_rn(U(gj, gi));
+    sv[jj + 2][ii + 2] = __double2float_rn(V(gj, gi));
+  }
+  __syncthreads();
+  const double dt = D.ctrl->dt;
+  const float rdx = (float)G.rdx, rdy = (float)G.rdy;
+  const int i = i0 + (threadIdx.x & 31);
+  const int tx = threadIdx.x & 31;
+  M_ROWS({
+    if (i < G.nx && j < G.ny) {
+      const int lj = j - j0 + 2, li = tx + 2;
+      const double u0 = U(j, i), v0 = V(j, i);
+      double un = u0, vn = v0;
+      if (D.scheme != 2) {
+        const float uc = su[lj][li], vc = sv[lj][li];
+        float cu, cv;
+        if (D.scheme == 1) {
+          auto conv = [&](float (*f)[TX + 4]) {
+            // clamped neighbours: the staged halo already holds the edge values
+            const float fx_p = f[lj][li + 1] - f[lj][li], fx_0 = f[lj][li] - f[lj][li - 1],
+                        fx_m = f[lj][li - 1] - f[lj][li - 2];
+            const float fy_p = f[lj + 1][li] - f[lj][li], fy_0 = f[lj][li] - f[lj - 1][li],
+                        fy_m = f[lj - 1][li] - f[lj - 2][li];
+            return uc * q_comb(fx_p, fx_0, fx_m, uc >= 0.f) * rdx + vc * q_comb(fy_p, fy_0, fy_m, vc >= 0.f) * rdy;
+          };
+          cu = conv(su);
+          cv = conv(sv);
+        } else {
+          auto conv = [&](float (*f)[TX + 4]) {
+            const float f0 = f[lj][li];
+            const float fx = (uc > 0.f) ? ((i > 0) ? f0 - f[lj][li - 1] : 0.f) : f[lj][li + 1] - f0;
+            const float fy = (vc > 0.f) ? ((j > 0) ? f0 - f[lj - 1][li] : 0.f) : f[lj + 1][li] - f0;
+            return uc * (fx * rdx) + vc * (fy * rdy);
+          };
+          cu = conv(su);
+          cv = conv(sv);
+        }
+        un = SUB(u0, MUL(dt, (double)cu));
+        vn = SUB(v0, MUL(dt, (double)cv));
+      }
+      D.us[(long)j * D.usld + i] = un;
+      D.vs[(long)j * D.usld + i] = vn;
+    }
+  })
+}
+
 // b = -div_c(u*, v*) / max(dt, 1e-14); sum(b) (for the mean) and ||div_c||^2
 __global__ void __launch_bounds__(NT) k_rhs_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ StepRed rsm;
   const int i = tl.i0 + (threadIdx.x & 31);
-  const int j = tl.j0 + (threadIdx.x >> 5);
   const RecipGrid rg = recips(G);
+  const double rdt = D.ctrl->rdtm;
+  View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
   double v[2] = {0.0, 0.0}, out[2];
-  if (i < G.nx && j < G.ny) {
-    View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
-    const double d = div_c_r(US, VS, j, i, rg);
-    const double bv = MUL(-d, D.ctrl->rdtm);
-    D.b[(long)j * G.ld + i] = bv;
-    v[0] = bv;
-    v[1] = d * d;
-  }
+  M_ROWS({
+    if (i < G.nx && j < G.ny) {
+      const double d = div_c_r(US, VS, j, i, rg);
+      const double bv = MUL(-d, rdt);
+      D.b[(long)j * G.ld + i] = bv;
+      v[0] += bv;
+      v[1] += d * d;
+    }
+  })
   if (STEP_RED(2, v, out) && threadIdx.x == 0) {
     D.slots[S_BSUM].result = out[0];
     D.slots[S_DIVSTAR].result = out[1];
@@ -670,38 +762,40 @@ __global__ void __launch_bounds__(NT) k_rhs_m(const InstDesc* __restrict__ ID, c
 
 // p = x - x[0]; u = u* - dt gx(p), v likewise; lid; sums of (u - u_old)^2, (v - v_old)^2
 __global__ void __launch_bounds__(NT) k_pin_correct_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ StepRed rsm;
   Ctrl64* ctrl = D.ctrl;
   const LidArgs L = D.L;
   const RecipGrid rg = recips(G);
   const int i = tl.i0 + (threadIdx.x & 31);
-  const int j = tl.j0 + (threadIdx.x >> 5);
+  const double dt = ctrl->dt;
+  View2<const double> X{D.x, G.ld};
+  const double x0 = X(0, 0);
   double v[2] = {0.0, 0.0}, out[2];
   int bad = 0;
-  if (i < G.nx && j < G.ny) {
-    const double dt = ctrl->dt;
-    View2<const double> X{D.x, G.ld};
-    const double x0 = X(0, 0);
-    const double pv = SUB(X(j, i), x0);
-    const double gx = (i < G.nx - 1) ? MUL(SUB(SUB(X(j, i + 1), x0), pv), rg.rx) : 0.0;
-    const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(X(j + 1, i), x0), pv), rg.ry) : 0.0;
-    const long o = (long)j * D.usld + i;
-    const long os = (long)j * G.lds + i;
-    const double uc = SUB(D.us[o], MUL(dt, gx));
-    const double vc = SUB(D.vs[o], MUL(dt, gy));
-    D.us[o] = uc;
-    D.vs[o] = vc;
-    D.pi[os] = pv;
-    const double uf = (L.has_lid && j == G.ny - 1) ? L.lid : uc;
-    const double du = SUB(uf, D.ui[os]);
-    const double dv = SUB(vc, D.vi[os]);
-    D.ui[os] = uf;
-    D.vi[os] = vc;
-    v[0] = du * du;
-    v[1] = dv * dv;
-    bad = !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
-  }
+  M_ROWS({
+    if (i < G.nx && j < G.ny) {
+      const double pv = SUB(X(j, i), x0);
+      const double gx = (i < G.nx - 1) ? MUL(SUB(SUB(X(j, i + 1), x0), pv), rg.rx) : 0.0;
+      const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(X(j + 1, i), x0), pv), rg.ry) : 0.0;
+      const long o = (long)j * D.usld + i;
+      const long os = (long)j * G.lds + i;
+      const double uc = SUB(D.us[o], MUL(dt, gx));
+      const double vc = SUB(D.vs[o], MUL(dt, gy));
+      D.us[o] = uc;
+      D.vs[o] = vc;
+      D.pi[os] = pv;
+      const double uf = (L.has_lid && j == G.ny - 1) ? L.lid : uc;
+      const double du = SUB(uf, D.ui[os]);
+      const double dv = SUB(vc, D.vi[os]);
+      D.ui[os] = uf;
+      D.vi[os] = vc;
+      v[0] += du * du;
+      v[1] += dv * dv;
+      bad |= !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
+    }
+  })
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->nan_flag, 1u);
   if (STEP_RED(2, v, out) && threadIdx.x == 0) {
     D.slots[S_RU].result = out[0];
@@ -711,22 +805,24 @@ __global__ void __launch_bounds__(NT) k_pin_correct_m(const InstDesc* __restrict
 
 // ||div_c(u*, v*)||^2 after the correction, ||A p - b||^2, ||div_central(u, v; 1, 1)||^2
 __global__ void __launch_bounds__(NT) k_post_diag_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+  pdl_enter();
   TILE_PROLOGUE
   __shared__ StepRed rsm;
   const RecipGrid rg = recips(G);
   const int i = tl.i0 + (threadIdx.x & 31);
-  const int j = tl.j0 + (threadIdx.x >> 5);
+  View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
+  View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds}, P{D.pi, G.lds};
   double v[3] = {0.0, 0.0, 0.0}, out[3];
-  if (i < G.nx && j < G.ny) {
-    View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
-    View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds}, P{D.pi, G.lds};
-    const double d = div_c_r(US, VS, j, i, rg);
-    const double lr = SUB(neg_lap_pinned_r(P, j, i, G.nx, G.ny, rg), D.b[(long)j * G.ld + i]);
-    const double c = div_central_at(U, V, j, i, G.nx, G.ny, 1.0, 1.0);
-    v[0] = d * d;
-    v[1] = lr * lr;
-    v[2] = c * c;
-  }
+  M_ROWS({
+    if (i < G.nx && j < G.ny) {
+      const double d = div_c_r(US, VS, j, i, rg);
+      const double lr = SUB(neg_lap_pinned_r(P, j, i, G.nx, G.ny, rg), D.b[(long)j * G.ld + i]);
+      const double c = div_central_unit(U, V, j, i, G.nx, G.ny);
+      v[0] += d * d;
+      v[1] += lr * lr;
+      v[2] += c * c;
+    }
+  })
   if (STEP_RED(3, v, out) && threadIdx.x == 0) {
     D.slots[S_DIVAFTER].result = out[0];
     D.slots[S_LINRES].result = out[1];
@@ -736,6 +832,7 @@ __global__ void __launch_bounds__(NT) k_post_diag_m(const InstDesc* __restrict__
 
 // one StepOut64 record per instance
 __global__ void k_gather(const InstDesc* __restrict__ ID, int n) {
+  pdl_enter();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const InstDesc& Dd = ID[k];
@@ -809,6 +906,8 @@ struct Instance64 {
   std::vector<InstDesc> hd;          // host copy of the descriptors
   InstDesc* dd = nullptr;            // device descriptors
   Tile* tpc = nullptr;               // per-cell tiles (32 x 8)
+  Tile* tpcm = nullptr;              // per-cell tiles of the mixed form (32 x 32)
+  int ntpcm = 0;
   Tile* tcg = nullptr;               // CG tiles of the selected variant
   int ntpc = 0, ntcg = 0;
   // CG tile variants 32 x 8R (R = 1, 2, 4 rows per thread); the autotuner selects one
@@ -860,13 +959,14 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
   std::vector<size_t> vec(n);
   size_t bytes = 0;
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-  std::vector<Tile> tpc, tcgv[NVAR];
+  std::vector<Tile> tpc, tpcm, tcgv[NVAR];
   for (int k = 0; k < n; ++k) {
     const long ld = round_up(prms[k].nx, 32);
     vec[k] = up((size_t)ld * prms[k].ny * sizeof(double));
     bytes += 8 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64)) +
              up(3 * (size_t)count_tiles(prms[k].nx, prms[k].ny, PB_Y) * sizeof(double)) + up(sizeof(unsigned));
     add_tiles(tpc, k, prms[k].nx, prms[k].ny, PB_Y);
+    add_tiles(tpcm, k, prms[k].nx, prms[k].ny, TY_M);
     for (int v = 0; v < NVAR; ++v) {
       add_tiles(tcgv[v], k, prms[k].nx, prms[k].ny, VAR_R[v] * PB_Y);
       I->ntcg_inst[v].push_back(count_tiles(prms[k].nx, prms[k].ny, VAR_R[v] * PB_Y));
@@ -874,8 +974,9 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     I->maxiter_max = std::max(I->maxiter_max, prms[k].lin_maxiter);
   }
   I->ntpc = (int)tpc.size();
-  bytes += up(n * sizeof(InstDesc)) + up(tpc.size() * sizeof(Tile)) + up(sizeof(LoopCtl)) + up(n * sizeof(StepIn)) +
-           up(n * sizeof(StepOut64));
+  I->ntpcm = (int)tpcm.size();
+  bytes += up(n * sizeof(InstDesc)) + up(tpc.size() * sizeof(Tile)) + up(tpcm.size() * sizeof(Tile)) +
+           up(sizeof(LoopCtl)) + up(n * sizeof(StepIn)) + up(n * sizeof(StepOut64));
   for (int v = 0; v < NVAR; ++v) {
     I->ntcgv[v] = (int)tcgv[v].size();
     bytes += up(tcgv[v].size() * sizeof(Tile));
@@ -924,12 +1025,14 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     D.slots = (XASlot*)take(S_COUNT * sizeof(XASlot));
     D.ctrl = (Ctrl64*)take(sizeof(Ctrl64));
     D.nt_pc = count_tiles(prm.nx, prm.ny, PB_Y);
+    D.nt_m = count_tiles(prm.nx, prm.ny, TY_M);
     D.nt_cg = I->ntcg_inst[I->cg_var][k];
     D.part = (double*)take(3 * (size_t)D.nt_pc * sizeof(double));
     D.ticket = (unsigned*)take(sizeof(unsigned));
   }
   I->dd = (InstDesc*)take(n * sizeof(InstDesc));
   I->tpc = (Tile*)take(tpc.size() * sizeof(Tile));
+  I->tpcm = (Tile*)take(tpcm.size() * sizeof(Tile));
   for (int v = 0; v < NVAR; ++v) I->tcgv[v] = (Tile*)take(tcgv[v].size() * sizeof(Tile));
   I->tcg = I->tcgv[I->cg_var];
   I->ntcg = I->ntcgv[I->cg_var];
@@ -941,6 +1044,7 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     I->hd[k].out = I->out_d + k;
   }
   cudaError_t e = cudaMemcpy(I->tpc, tpc.data(), tpc.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(I->tpcm, tpcm.data(), tpcm.size() * sizeof(Tile), cudaMemcpyHostToDevice);
   for (int v = 0; v < NVAR; ++v)
     if (e == cudaSuccess) e = cudaMemcpy(I->tcgv[v], tcgv[v].data(), tcgv[v].size() * sizeof(Tile), cudaMemcpyHostToDevice);
   LoopCtl lc0 = {0, 0, I->maxiter_max + 1, 0};
@@ -1043,6 +1147,7 @@ static int upload_desc(Instance64* I, cudaStream_t s) {
 }
 
 __global__ void k_loop_reset(LoopCtl* lc) {
+  pdl_enter();
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     lc->active = 0;
     lc->guard = 0;
@@ -1084,10 +1189,11 @@ static void enqueue_projection(Instance64* I, cudaStream_t s) {
 }
 
 static void enqueue_prologue(Instance64* I, cudaStream_t s) {
-  if (I->mix) k_prestep_m<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  if (I->mix) k_prestep_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
   else k_prestep<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
   k_dt<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
-  k_predict<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  if (I->mix) k_predict_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
+  else k_predict<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
 }
 
 // Build the step graph (mode 0: full step; mode 1: stand-alone projection).
@@ -1102,14 +1208,17 @@ static int build_graph(Instance64* I, int mode) {
   }
   cudaError_t e = cudaGraphCreate(&I->graph, 0);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("cudaGraphCreate: ") + cudaGetErrorString(e));
-  const dim3 gp(I->ntpc), gc(I->ntcg), g1((I->n + 31) / 32);
-  GraphChain c(I->graph);
+  const dim3 gp(I->ntpc), gc(I->ntcg), g1((I->n + 31) / 32), gm(I->ntpcm);
+  GraphChain c(I->graph, I->use_graph == 1);
   if (mode == 0) {
-    c.kernel(I->mix ? k_prestep_m : k_prestep, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+    if (I->mix) c.kernel(k_prestep_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
+    else c.kernel(k_prestep, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
     c.kernel(k_dt, g1, dim3(32), (const InstDesc*)I->dd, I->n);
-    c.kernel(k_predict, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+    if (I->mix) c.kernel(k_predict_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
+    else c.kernel(k_predict, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   }
-  c.kernel(I->mix ? k_rhs_m : k_rhs, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  if (I->mix) c.kernel(k_rhs_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
+  else c.kernel(k_rhs, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   GraphChain body(nullptr);
   if (I->mix) {
     // the refinement removes b's mean, pins b[0], solves A x = b and leaves ||b - A x||^2
@@ -1130,13 +1239,21 @@ static int build_graph(Instance64* I, int mode) {
     body.kernel(k_loop_guard, dim3(1), dim3(32), I->lc, cond, 1);
   }
   if (!I->mix) c.kernel(k_post_resid<0>, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
-  c.kernel(I->mix ? k_pin_correct_m : k_pin_correct, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
-  c.kernel(I->mix ? k_post_diag_m : k_post_diag, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  if (I->mix) {
+    c.kernel(k_pin_correct_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
+    c.kernel(k_post_diag_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
+  } else {
+    c.kernel(k_pin_correct, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+    c.kernel(k_post_diag, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
+  }
   c.kernel(k_gather, g1, dim3(32), (const InstDesc*)I->dd, I->n);
   if (c.status() != cudaSuccess || (!I->mix && body.status() != cudaSuccess)) {
     cudaError_t be = c.status() != cudaSuccess ? c.status() : body.status();
     return set_error(PFGB_ECUDA, std::string("building the step graph: ") + cudaGetErrorString(be));
   }
+  if (std::getenv("PFGB_GRAPH_DEBUG"))
+    std::fprintf(stderr, "pfgb graph: %d programmatic edges in the top chain; last refusal: %s\n", c.n_prog_,
+                 cudaGetErrorString(c.last_prog_err_));
   e = cudaGraphInstantiate(&I->exec, I->graph, 0);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
   I->graph_mode = mode;
@@ -1203,10 +1320,10 @@ static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
   }
   if (mode == 0) enqueue_prologue(I, s);
   if (I->mix) {
-    k_rhs_m<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_rhs_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
     if (int rc = mixed::run_direct(I->mix, s)) return rc;
-    k_pin_correct_m<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-    k_post_diag_m<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+    k_pin_correct_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
+    k_post_diag_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
     k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
   } else {
     enqueue_projection(I, s);
@@ -1406,7 +1523,19 @@ int instance64_set_persistent(Instance64* I, int on) {
 }
 
 int instance64_set_graph(Instance64* I, int on) {
-  I->use_graph = on ? 1 : 0;
+  const int m = (on == 2) ? 2 : (on ? 1 : 0);
+  if (m != I->use_graph) {
+    if (I->exec) {
+      cudaGraphExecDestroy(I->exec);
+      I->exec = nullptr;
+    }
+    if (I->graph) {
+      cudaGraphDestroy(I->graph);
+      I->graph = nullptr;
+    }
+    I->graph_mode = -1;
+  }
+  I->use_graph = m;
   return PFGB_OK;
 }
 

@@ -6,7 +6,8 @@ import ctypes
 from .. import _capi
 
 
-# Run each step as one CUDA graph (True) or as individual kernel launches.
+# Run each step as one CUDA graph (True; 2: without programmatic dependent-launch
+# edges) or as individual kernel launches (False).
 GRAPH_MODE = True
 # Mixed form: the pressure solve as one persistent cooperative launch (True) or
 # as a graph of per-phase kernels (False, the faster on GB300); both give the same bits.
@@ -38,7 +39,7 @@ class Instance:
         _capi.check(lib.pfgb_create(ctypes.byref(params), ctypes.byref(h)), "pfgb_create")
         self._h = h
         self.params = params
-        _capi.check(lib.pfgb_set_graph(h, 1 if GRAPH_MODE else 0), "pfgb_set_graph")
+        _capi.check(lib.pfgb_set_graph(h, int(GRAPH_MODE)), "pfgb_set_graph")
         _capi.check(lib.pfgb_set_persistent(h, 1 if PERSISTENT else 0), "pfgb_set_persistent")
         self.cg_variant = None
         if AUTOTUNE and params.precision == 0:

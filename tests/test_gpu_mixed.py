@@ -59,10 +59,11 @@ def run_pair(cfg, steps):
     return worst, diags
 
 
-@pytest.mark.parametrize("nx,ny,Re,lid,steps", [(64, 64, 100.0, 1.0, 12), (96, 48, 800.0, 1.5, 6),
-                                               (128, 128, 1000.0, 1.0, 4)])
-def test_mixed_step_matches_converged_fp64(nx, ny, Re, lid, steps):
-    worst, diags = run_pair(cavity(nx, ny, Re, lid), steps)
+@pytest.mark.parametrize("nx,ny,Re,lid,steps,scheme", [(64, 64, 100.0, 1.0, 12, "quick"), (96, 48, 800.0, 1.5, 6, "quick"),
+                                                      (128, 128, 1000.0, 1.0, 4, "quick"),
+                                                      (80, 64, 300.0, 1.2, 6, "upwind")])
+def test_mixed_step_matches_converged_fp64(nx, ny, Re, lid, steps, scheme):
+    worst, diags = run_pair(cavity(nx, ny, Re, lid, advection_scheme=scheme), steps)
     assert max(worst.values()) <= TOL, worst
     for d in diags[1:]:
         assert d["Rp_converged"], d
@@ -97,7 +98,7 @@ def test_mixed_graph_and_direct_launches_agree():
     from pyflow_solver_gb300.solvers import _handle
     cfg = SimpleNamespace(**vars(cavity(64, 48, 400.0, 1.0)), precision="mixed")
     out = []
-    for mode in (True, False):
+    for mode in (True, False, 2):          # graph with programmatic edges, direct, plain graph
         _handle.GRAPH_MODE = mode
         try:
             st = allocate_state(64, 48)
@@ -106,8 +107,9 @@ def test_mixed_graph_and_direct_launches_agree():
             _handle.GRAPH_MODE = True
         out.append(([interior_view(st.fields[k]).cpu().numpy() for k in "uvp"],
                     [(d["cg_iterations"], d["refine_passes"], d["dt"]) for d in diags]))
-    for a, b in zip(out[0][0], out[1][0]):
-        np.testing.assert_array_equal(a, b)
+    for o in out[1:]:
+        for a, b in zip(out[0][0], o[0]):
+            np.testing.assert_array_equal(a, b)
     assert out[0][1] == out[1][1]
 
 

@@ -62,9 +62,12 @@ def test_direct_launches_equal_graph_replay():
     _handle.GRAPH_MODE = False
     try:
         direct = gpu_trajectory(cfg, cfg.nx, cfg.ny, 12)
+        _handle.GRAPH_MODE = 2
+        plain_graph = gpu_trajectory(cfg, cfg.nx, cfg.ny, 12)
     finally:
         _handle.GRAPH_MODE = True
     check_bitwise(direct, graph, "graph vs direct")
+    check_bitwise(plain_graph, graph, "graph with and without programmatic edges")
 
 
 def test_p1_cavity64_cli_spacing_bitwise():
