@@ -172,6 +172,11 @@ __device__ __forceinline__ void set_rho(MixCtrl* ctrl, double rz) {
   ctrl->rho = rz;
 }
 
+// level-0 right-hand side (the PCG residual) of the current inner iteration
+__device__ __forceinline__ float* f_cur(const MixDesc& M) {
+  return (cget(&M.ctrl->inner) & 1) ? M.f0b : M.lev[0].f;
+}
+
 // the rows ty of the tile that this thread owns (ty = warp, warp + 8, ...)
 #define MX_ROWS_X(...)                                      \
   for (int r_ = 0; r_ < RPT; ++r_) {                        \
@@ -184,6 +189,7 @@ __device__ __forceinline__ void set_rho(MixCtrl* ctrl, double rz) {
 
 constexpr int H3 = 3;
 struct DownSmem {
+  float sf[BY + 2 * H3][BX + 2 * H3];   // f on the 3-cell halo
   float s1[BY + 2 * H3][BX + 2 * H3];
   float s2[BY + 4][BX + 4];
   float rs[BY + 2][BX + 2];
@@ -191,18 +197,15 @@ struct DownSmem {
 struct PostSmem {
   float w0[BY + 4][BX + 4];
   float w1[BY + 2][BX + 2];
+  float sf[BY + 2][BX + 2];             // f on the 1-cell halo
   RedSmem rsm;
 };
 struct MatvecSmem {
   float pn[BY + 2][BX + 2];
   RedSmem rsm;
 };
-union TileSmem {
-  DownSmem d;
-  PostSmem p;
-  MatvecSmem m;
-  RedSmem r;
-};
+struct UpdDownSmem;
+union TileSmem;
 
 // Down-sweep of level l, fused: two damped-Jacobi sweeps from u = 0 (t = S(S(0))
 // for A u = f), the residual r = f - A t, and its restriction f_{l+1} = P^T r.
@@ -212,14 +215,20 @@ union TileSmem {
 template <class X>
 __device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTile& tl, int l, float omega,
                                         DownSmem& sm) {
-  const Lvl L = M.lev[l], C = M.lev[l + 1];
+  Lvl L = M.lev[l];
+  const Lvl C = M.lev[l + 1];
+  if (l == 0) L.f = f_cur(M);
   const int i0 = tl.i0, j0 = tl.j0;
   auto inside = [&](int gj, int gi) { return gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx; };
   for (int idx = x.tid(); idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
     const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
     const int gj = j0 + jj, gi = i0 + ii;
-    float v = 0.f;
-    if (inside(gj, gi)) v = __fdividef(omega * x.ld(L.f + (long)gj * L.ld + gi), mg_diag(L, gj, gi));
+    float f = 0.f, v = 0.f;
+    if (inside(gj, gi)) {
+      f = x.ld(L.f + (long)gj * L.ld + gi);
+      v = __fdividef(omega * f, mg_diag(L, gj, gi));
+    }
+    sm.sf[jj + H3][ii + H3] = f;
     sm.s1[jj + H3][ii + H3] = v;
   }
   x.sync();
@@ -230,7 +239,7 @@ __device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTil
     if (inside(gj, gi)) {
       auto at = [&](int j, int i) { return sm.s1[j - j0 + H3][i - i0 + H3]; };
       v = fmaf(1.f - omega, sm.s1[jj + H3][ii + H3],
-               __fdividef(omega * (x.ld(L.f + (long)gj * L.ld + gi) + mg_nsum(L, gj, gi, at)), mg_diag(L, gj, gi)));
+               __fdividef(omega * (sm.sf[jj + H3][ii + H3] + mg_nsum(L, gj, gi, at)), mg_diag(L, gj, gi)));
     }
     sm.s2[jj + 2][ii + 2] = v;
   }
@@ -242,9 +251,8 @@ __device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTil
     if (inside(gj, gi)) {
       auto at = [&](int j, int i) { return sm.s2[j - j0 + 2][i - i0 + 2]; };
       const float t = sm.s2[jj + 2][ii + 2];
-      const long o = (long)gj * L.ld + gi;
-      v = x.ld(L.f + o) - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
-      if (jj >= 0 && jj < BY && ii >= 0 && ii < BX) L.t[o] = t;
+      v = sm.sf[jj + H3][ii + H3] - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
+      if (jj >= 0 && jj < BY && ii >= 0 && ii < BX) L.t[(long)gj * L.ld + gi] = t;
     }
     sm.rs[jj + 1][ii + 1] = v;
   }
@@ -265,17 +273,23 @@ __device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTil
 template <class X>
 __device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTile& tl, int l, float omega,
                                         PostSmem& sm) {
-  const Lvl F = M.lev[l], C = M.lev[l + 1];
+  Lvl F = M.lev[l];
+  const Lvl C = M.lev[l + 1];
+  if (l == 0) F.f = f_cur(M);
   RedSmem& rsm = sm.rsm;
   const int i0 = tl.i0, j0 = tl.j0;
   auto ldx = [&](const float* p) { return x.ld(p); };
   for (int idx = x.tid(); idx < (BY + 4) * (BX + 4); idx += MT) {
     const int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
     const int gj = j0 + jj, gi = i0 + ii;
-    float v = 0.f;
-    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx)
-      v = x.ld(F.t + (long)gj * F.ld + gi) + prolong_val(ldx, C.u, C.ld, C.nx, C.ny, F.kx, F.ky, gj, gi);
+    float v = 0.f, f = 0.f;
+    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) {
+      const long o = (long)gj * F.ld + gi;
+      v = x.ld(F.t + o) + prolong_val(ldx, C.u, C.ld, C.nx, C.ny, F.kx, F.ky, gj, gi);
+      if (jj >= -1 && jj <= BY && ii >= -1 && ii <= BX) f = x.ld(F.f + o);
+    }
     sm.w0[jj + 2][ii + 2] = v;
+    if (jj >= -1 && jj <= BY && ii >= -1 && ii <= BX) sm.sf[jj + 1][ii + 1] = f;
   }
   x.sync();
   for (int idx = x.tid(); idx < (BY + 2) * (BX + 2); idx += MT) {
@@ -285,8 +299,7 @@ __device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTil
     if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) {
       auto at = [&](int j, int i) { return sm.w0[j - j0 + 2][i - i0 + 2]; };
       const float d = mg_diag(F, gj, gi);
-      v = fmaf(1.f - omega, sm.w0[jj + 2][ii + 2],
-               __fdividef(omega * (x.ld(F.f + (long)gj * F.ld + gi) + mg_nsum(F, gj, gi, at)), d));
+      v = fmaf(1.f - omega, sm.w0[jj + 2][ii + 2], __fdividef(omega * (sm.sf[jj + 1][ii + 1] + mg_nsum(F, gj, gi, at)), d));
     }
     sm.w1[jj + 1][ii + 1] = v;
   }
@@ -298,7 +311,7 @@ __device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTil
     if (gi < F.nx && gj < F.ny) {
       auto at = [&](int j, int i) { return sm.w1[j - j0 + 1][i - i0 + 1]; };
       const float d = mg_diag(F, gj, gi);
-      const float fv = x.ld(F.f + (long)gj * F.ld + gi);
+      const float fv = sm.sf[ty + 1][tx + 1];
       const float v = fmaf(1.f - omega, sm.w1[ty + 1][tx + 1], __fdividef(omega * (fv + mg_nsum(F, gj, gi, at)), d));
       F.u[(long)gj * F.ld + gi] = v;
       if (l == 0) ff_add_prod(acc[0], fv, v);
@@ -425,28 +438,54 @@ __device__ __forceinline__ void ph_matvec(const X& x, const MixDesc& M, const MT
   }
 }
 
-// e += alpha p; r -= alpha q; ||r||^2 and the inner stopping test
+// e += alpha p; r -= alpha q (from residual buffer k & 1 into buffer (k + 1) & 1);
+// ||r||^2 and the inner stopping test; then, for an instance with a level below,
+// the fused down-sweep of level 0 on the new residual (its 3-cell halo formed
+// from the old residual and q, which no tile of this phase writes).
+struct UpdDownSmem {
+  float sf[BY + 2 * H3][BX + 2 * H3];
+  DownSmem d;
+  RedSmem rsm;
+};
+
 template <class X>
-__device__ __forceinline__ void ph_update(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml,
-                                          cudaGraphConditionalHandle cond_inner, int use_cond, RedSmem& rsm) {
-  const Lvl L0 = M.lev[0];
+__device__ __forceinline__ void ph_update_down(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml,
+                                               cudaGraphConditionalHandle cond_inner, int use_cond, float omega,
+                                               UpdDownSmem& sm) {
+  RedSmem& rsm = sm.rsm;
+  Lvl L0 = M.lev[0];
   MixCtrl* ctrl = M.ctrl;
   const int k = cget(&ctrl->inner);
+  const float* fo = (k & 1) ? M.f0b : L0.f;
+  float* fn = (k & 1) ? L0.f : M.f0b;
   const float* p = (k & 1) ? M.p0 : M.p1;
   const float alpha = (float)cget(&ctrl->alpha);
   const int i = tl.i0 + (x.tid() & 31);
   FF v[1] = {{0.f, 0.f}};
   double out[1];
-  MX_ROWS_X({
-    const int j = tl.j0 + ty;
+  float pv[RPT], ev[RPT], qv[RPT], rv0[RPT];
+#pragma unroll
+  for (int r_ = 0; r_ < RPT; ++r_) {
+    const int j = tl.j0 + (x.tid() >> 5) + r_ * (MT / 32);
     if (i < L0.nx && j < L0.ny) {
       const long o = (long)j * L0.ld + i;
-      M.e[o] = fmaf(alpha, x.ld(p + o), x.ld(M.e + o));
-      const float rv = fmaf(-alpha, x.ld(M.q + o), x.ld(L0.f + o));
-      L0.f[o] = rv;
+      pv[r_] = x.ld(p + o);
+      ev[r_] = x.ld(M.e + o);
+      qv[r_] = x.ld(M.q + o);
+      rv0[r_] = x.ld(fo + o);
+    }
+  }
+#pragma unroll
+  for (int r_ = 0; r_ < RPT; ++r_) {
+    const int j = tl.j0 + (x.tid() >> 5) + r_ * (MT / 32);
+    if (i < L0.nx && j < L0.ny) {
+      const long o = (long)j * L0.ld + i;
+      M.e[o] = fmaf(alpha, pv[r_], ev[r_]);
+      const float rv = fmaf(-alpha, qv[r_], rv0[r_]);
+      fn[o] = rv;
       ff_add_prod(v[0], rv, rv);
     }
-  })
+  }
   if (X_RED_FF(1, v, out) && x.tid() == 0) {
     const double rr = out[0];
     const int it = k + 1;
@@ -458,7 +497,74 @@ __device__ __forceinline__ void ph_update(const X& x, const MixDesc& M, const MT
       if (atomicSub(&ml->inner_active, 1) == 1 && use_cond) cudaGraphSetConditional(cond_inner, 0u);
     }
   }
+  if (M.nlev < 2) return;
+  // the new residual on the tile and a 3-cell halo, then the down-sweep as ph_down
+  const int i0 = tl.i0, j0 = tl.j0;
+  auto inside = [&](int gj, int gi) { return gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx; };
+  for (int idx = x.tid(); idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
+    const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
+    const int gj = j0 + jj, gi = i0 + ii;
+    float r = 0.f;
+    if (inside(gj, gi)) {
+      const long o = (long)gj * L0.ld + gi;
+      r = fmaf(-alpha, x.ld(M.q + o), x.ld(fo + o));
+    }
+    sm.sf[jj + H3][ii + H3] = r;
+  }
+  x.sync();
+  const Lvl C = M.lev[1];
+  DownSmem& d = sm.d;
+  auto fval = [&](int gj, int gi) { return sm.sf[gj - j0 + H3][gi - i0 + H3]; };
+  for (int idx = x.tid(); idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
+    const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
+    const int gj = j0 + jj, gi = i0 + ii;
+    float s1 = 0.f;
+    if (inside(gj, gi)) s1 = __fdividef(omega * fval(gj, gi), mg_diag(L0, gj, gi));
+    d.s1[jj + H3][ii + H3] = s1;
+  }
+  x.sync();
+  for (int idx = x.tid(); idx < (BY + 4) * (BX + 4); idx += MT) {
+    const int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
+    const int gj = j0 + jj, gi = i0 + ii;
+    float s2 = 0.f;
+    if (inside(gj, gi)) {
+      auto at = [&](int j, int i) { return d.s1[j - j0 + H3][i - i0 + H3]; };
+      s2 = fmaf(1.f - omega, d.s1[jj + H3][ii + H3],
+                __fdividef(omega * (fval(gj, gi) + mg_nsum(L0, gj, gi, at)), mg_diag(L0, gj, gi)));
+    }
+    d.s2[jj + 2][ii + 2] = s2;
+  }
+  x.sync();
+  for (int idx = x.tid(); idx < (BY + 2) * (BX + 2); idx += MT) {
+    const int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
+    const int gj = j0 + jj, gi = i0 + ii;
+    float rr = 0.f;
+    if (inside(gj, gi)) {
+      auto at = [&](int j, int i) { return d.s2[j - j0 + 2][i - i0 + 2]; };
+      const float t = d.s2[jj + 2][ii + 2];
+      rr = fval(gj, gi) - (mg_diag(L0, gj, gi) * t - mg_nsum(L0, gj, gi, at));
+      if (jj >= 0 && jj < BY && ii >= 0 && ii < BX) L0.t[(long)gj * L0.ld + gi] = t;
+    }
+    d.rs[jj + 1][ii + 1] = rr;
+  }
+  x.sync();
+  const int cw = BX / L0.kx, chh = BY / L0.ky;
+  const int I0 = i0 / L0.kx, J0 = j0 / L0.ky;
+  for (int idx = x.tid(); idx < cw * chh; idx += MT) {
+    const int jj = idx / cw, ii = idx - jj * cw;
+    const int I = I0 + ii, J = J0 + jj;
+    if (I < C.nx && J < C.ny)
+      C.f[(long)J * C.ld + I] = restrict_val(&d.rs[0][0], BX + 2, j0 - 1, i0 - 1, C.nx, C.ny, L0.kx, L0.ky, J, I);
+  }
 }
+
+union TileSmem {
+  DownSmem d;
+  PostSmem p;
+  MatvecSmem m;
+  UpdDownSmem u;
+  RedSmem r;
+};
 
 // x += e - e[0] (binary64)
 template <class X>
@@ -467,13 +573,21 @@ __device__ __forceinline__ void ph_correct(const X& x, const MixDesc& M, const M
   const long lde = M.lev[0].ld;
   const int i = tl.i0 + (x.tid() & 31);
   const double e0 = (double)x.ld(M.e);
-  MX_ROWS_X({
-    const int j = tl.j0 + ty;
+  double xv[RPT];
+  float ev[RPT];
+#pragma unroll
+  for (int r_ = 0; r_ < RPT; ++r_) {
+    const int j = tl.j0 + (x.tid() >> 5) + r_ * (MT / 32);
     if (i < G.nx && j < G.ny) {
-      const long o = (long)j * G.ld + i;
-      M.x[o] = __dadd_rn(x.ld(M.x + o), __dsub_rn((double)x.ld(M.e + (long)j * lde + i), e0));
+      xv[r_] = x.ld(M.x + (long)j * G.ld + i);
+      ev[r_] = x.ld(M.e + (long)j * lde + i);
     }
-  })
+  }
+#pragma unroll
+  for (int r_ = 0; r_ < RPT; ++r_) {
+    const int j = tl.j0 + (x.tid() >> 5) + r_ * (MT / 32);
+    if (i < G.nx && j < G.ny) M.x[(long)j * G.ld + i] = __dadd_rn(xv[r_], __dsub_rn((double)ev[r_], e0));
+  }
 }
 
 // r64 = b - A x with the reference's pinned operator; ||r64||^2, sum(r64); outer test
@@ -566,7 +680,8 @@ __device__ __forceinline__ void c_sweep(const CLvl& L, const float* f, const flo
 // The coarse V-cycle of instance M by the whole 1024-thread CTA; sm: 3 x (its
 // levels' cells) floats of shared memory.
 __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, float omega, float* sm) {
-  const Lvl C = M.lev[M.nlev - 1];
+  Lvl C = M.lev[M.nlev - 1];
+  if (M.nlev == 1) C.f = f_cur(M);
   const int nl = M.coarse_levels;
   CLvl L[8];
   int tot = 0;
@@ -760,12 +875,13 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD
   ph_matvec(x, M, tl, sm);
 }
 
-__global__ void __launch_bounds__(MT) k_mx_update(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
-                                                   MixLoop* ml, cudaGraphConditionalHandle cond_inner, int use_cond) {
+__global__ void __launch_bounds__(MT) k_mx_update_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
+                                                        MixLoop* ml, cudaGraphConditionalHandle cond_inner, int use_cond,
+                                                        float omega) {
   pdl_enter();
   CTA_TILE(1)
-  __shared__ RedSmem rsm;
-  ph_update(x, M, tl, ml, cond_inner, use_cond, rsm);
+  __shared__ UpdDownSmem sm;
+  ph_update_down(x, M, tl, ml, cond_inner, use_cond, omega, sm);
 }
 
 __global__ void __launch_bounds__(MT) k_mx_correct(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
@@ -834,8 +950,8 @@ __global__ void __launch_bounds__(CT, 1) k_mx_persist(PersistArgs A) {
   const int gid = blockIdx.x * 4 + x.g;
   MixLoop* ml = A.ml;
   GridBar* gb = &ml->gb;
-  auto vcycle = [&]() -> bool {
-    for (int l = 0; l + 1 < A.maxlev; ++l) {
+  auto vcycle = [&](int l0) -> bool {
+    for (int l = l0; l + 1 < A.maxlev; ++l) {
       for (int t = gid; t < A.ntpre[l]; t += ngroups) {
         const MTile tl = A.tpre[l][t];
         const MixDesc& M = A.dd[tl.inst];
@@ -876,15 +992,15 @@ __global__ void __launch_bounds__(CT, 1) k_mx_persist(PersistArgs A) {
     if (cget(&ml->outer_active) == 0) break;
     PERSIST_TILES(0, ph_prep(x, M, tl, ml, ts.r))
     if (!grid_sync(gb)) return;
-    if (!vcycle()) return;
+    if (!vcycle(0)) return;
     int it = 0;
     for (; it < ml->gmax_i; ++it) {
       if (cget(&ml->inner_active) == 0) break;
       PERSIST_TILES(1, ph_matvec(x, M, tl, ts.m))
       if (!grid_sync(gb)) return;
-      PERSIST_TILES(1, ph_update(x, M, tl, ml, 0ull, 0, ts.r))
+      PERSIST_TILES(1, ph_update_down(x, M, tl, ml, 0ull, 0, A.omega, ts.u))
       if (!grid_sync(gb)) return;
-      if (!vcycle()) return;
+      if (!vcycle(1)) return;
     }
     if (it == ml->gmax_i && cget(&ml->inner_active) > 0 && blockIdx.x == 0 && threadIdx.x == 0) ml->tripped = 1;
     PERSIST_TILES(0, ph_correct(x, M, tl))
@@ -1054,7 +1170,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     for (auto& d : plan[k].global) bytes += 3 * up((size_t)round_up(d.nx, 32) * d.ny * sizeof(float));
     const size_t v0 = up((size_t)round_up(prm[k].nx, 32) * prm[k].ny * sizeof(float));
     const size_t nt0 = (size_t)((prm[k].nx + BX - 1) / BX) * ((prm[k].ny + BY - 1) / BY);
-    bytes += 4 * v0 + up((size_t)prm[k].ld64 * prm[k].ny * sizeof(double)) + up(2 * nt0 * sizeof(double)) +
+    bytes += 5 * v0 + up((size_t)prm[k].ld64 * prm[k].ny * sizeof(double)) + up(2 * nt0 * sizeof(double)) +
              up(sizeof(unsigned)) + up(sizeof(MixCtrl));
   }
   // tile tables
@@ -1113,6 +1229,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     }
     const size_t v0 = (size_t)M.lev[0].ld * prm[k].ny * sizeof(float);
     M.e = (float*)take(v0);
+    M.f0b = (float*)take(v0);
     M.p0 = (float*)take(v0);
     M.p1 = (float*)take(v0);
     M.q = (float*)take(v0);
@@ -1218,9 +1335,10 @@ void batch_destroy(Batch* B) {
   delete B;
 }
 
-static void add_vcycle(GraphChain& c, Batch* B, int gate, float omega) {
+// the V-cycle from down-sweep level l0 on (l0 = 1: level 0's down-sweep is fused into the update)
+static void add_vcycle(GraphChain& c, Batch* B, int gate, float omega, int l0 = 0) {
   const MixDesc* dd = B->dd;
-  for (int l = 0; l + 1 < B->maxlev; ++l) {
+  for (int l = l0; l + 1 < B->maxlev; ++l) {
     if (B->ntpre[l]) c.kernel(k_mg_down, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, omega);
   }
   c.kernel_smem(k_mg_coarse, dim3(B->n), dim3(CT), B->coarse_smem, dd, gate, 8, omega);
@@ -1277,8 +1395,8 @@ int append_solve(GraphChain& c, Batch* B) {
   outer.kernel(k_ml_arm, dim3(1), dim3(32), B->loop, 1, cond_inner, 1);
   GraphChain inner = outer.while_loop_with(cond_inner);
   inner.kernel(k_mx_matvec, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
-  inner.kernel(k_mx_update, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_inner, 1);
-  add_vcycle(inner, B, 1, omega);
+  inner.kernel(k_mx_update_down, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_inner, 1, omega);
+  add_vcycle(inner, B, 1, omega, 1);
   inner.kernel(k_ml_guard, dim3(1), dim3(32), B->loop, 1, cond_inner, 1);
   outer.kernel(k_mx_correct, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   outer.kernel(k_mx_resid, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_outer, 1);
@@ -1295,8 +1413,8 @@ int append_solve(GraphChain& c, Batch* B) {
 // Host-driven form of append_solve with direct launches: the loop decisions
 // are read back from the loop control after each stopping test.  Used for
 // profiling (ncu does not profile kernels of graphs with conditional nodes).
-static void launch_vcycle(Batch* B, int gate, float omega, cudaStream_t s) {
-  for (int l = 0; l + 1 < B->maxlev; ++l) {
+static void launch_vcycle(Batch* B, int gate, float omega, cudaStream_t s, int l0 = 0) {
+  for (int l = l0; l + 1 < B->maxlev; ++l) {
     if (B->ntpre[l]) k_mg_down<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, omega);
   }
   k_mg_coarse<<<B->n, CT, B->coarse_smem, s>>>(B->dd, gate, 8, omega);
@@ -1352,8 +1470,8 @@ int run_direct(Batch* B, cudaStream_t s) {
         cudaEventRecord(B->ev[2 * timed_launches + 1], s);
         *B->ev_used = ++timed_launches;
       }
-      k_mx_update<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0);
-      launch_vcycle(B, 1, omega, s);
+      k_mx_update_down<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0, omega);
+      launch_vcycle(B, 1, omega, s, 1);
         if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
     }
     k_mx_correct<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);

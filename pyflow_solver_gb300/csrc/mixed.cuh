@@ -61,6 +61,8 @@ struct MixDesc {
   int ckx[8], cky[8];          // their coarsening factors to the next level
   Lvl lev[MAX_LEVELS];
   float *e, *p0, *p1, *q;      // binary32 PCG vectors (pitch lev[0].ld)
+  float* f0b;                  // the second level-0 residual buffer: iteration k reads r from
+                               // buffer k & 1 (lev[0].f is buffer 0) and writes buffer (k + 1) & 1
   double* r64;                 // binary64 refinement residual (pitch G.ld)
   double* b;                   // the step's right-hand side (binary64, pitch G.ld); mean removed here
   const double* bsum;          // exactly rounded sum of the right-hand side (from the RHS kernel)

@@ -697,10 +697,22 @@ __global__ void __launch_bounds__(NT) k_predict_m(const InstDesc* __restrict__ I
   const float rdx = (float)G.rdx, rdy = (float)G.rdy;
   const int i = i0 + (threadIdx.x & 31);
   const int tx = threadIdx.x & 31;
-  M_ROWS({
+  double ub[PB_R], vb[PB_R];
+#pragma unroll
+  for (int r = 0; r < PB_R; ++r) {
+    const int j = j0 + (threadIdx.x >> 5) + r * PB_Y;
+    const bool in = i < G.nx && j < G.ny;
+    ub[r] = in ? U(j, i) : 0.0;
+    vb[r] = in ? V(j, i) : 0.0;
+  }
+  double* __restrict__ us = D.us;
+  double* __restrict__ vs = D.vs;
+#pragma unroll
+  for (int r_ = 0; r_ < PB_R; ++r_) {
+    const int j = j0 + (threadIdx.x >> 5) + r_ * PB_Y;
     if (i < G.nx && j < G.ny) {
       const int lj = j - j0 + 2, li = tx + 2;
-      const double u0 = U(j, i), v0 = V(j, i);
+      const double u0 = ub[r_], v0 = vb[r_];
       double un = u0, vn = v0;
       if (D.scheme != 2) {
         const float uc = su[lj][li], vc = sv[lj][li];
@@ -729,10 +741,10 @@ __global__ void __launch_bounds__(NT) k_predict_m(const InstDesc* __restrict__ I
         un = SUB(u0, MUL(dt, (double)cu));
         vn = SUB(v0, MUL(dt, (double)cv));
       }
-      D.us[(long)j * D.usld + i] = un;
-      D.vs[(long)j * D.usld + i] = vn;
+      us[(long)j * D.usld + i] = un;
+      vs[(long)j * D.usld + i] = vn;
     }
-  })
+  }
 }
 
 // b = -div_c(u*, v*) / max(dt, 1e-14); sum(b) (for the mean) and ||div_c||^2
@@ -745,22 +757,32 @@ __global__ void __launch_bounds__(NT) k_rhs_m(const InstDesc* __restrict__ ID, c
   const double rdt = D.ctrl->rdtm;
   View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
   double v[2] = {0.0, 0.0}, out[2];
-  M_ROWS({
+  double dv[PB_R];
+#pragma unroll
+  for (int r = 0; r < PB_R; ++r) {
+    const int j = tl.j0 + (threadIdx.x >> 5) + r * PB_Y;
+    dv[r] = (i < G.nx && j < G.ny) ? div_c_r(US, VS, j, i, rg) : 0.0;
+  }
+  double* __restrict__ b = D.b;
+#pragma unroll
+  for (int r = 0; r < PB_R; ++r) {
+    const int j = tl.j0 + (threadIdx.x >> 5) + r * PB_Y;
     if (i < G.nx && j < G.ny) {
-      const double d = div_c_r(US, VS, j, i, rg);
-      const double bv = MUL(-d, rdt);
-      D.b[(long)j * G.ld + i] = bv;
+      const double bv = MUL(-dv[r], rdt);
+      b[(long)j * G.ld + i] = bv;
       v[0] += bv;
-      v[1] += d * d;
+      v[1] += dv[r] * dv[r];
     }
-  })
+  }
   if (STEP_RED(2, v, out) && threadIdx.x == 0) {
     D.slots[S_BSUM].result = out[0];
     D.slots[S_DIVSTAR].result = out[1];
   }
 }
 
-// p = x - x[0]; u = u* - dt gx(p), v likewise; lid; sums of (u - u_old)^2, (v - v_old)^2
+// p = x - x[0]; u = u* - dt gx(p), v likewise; lid; sums of (u - u_old)^2, (v - v_old)^2.
+// All loads of the thread's four rows are issued before any store (the arrays
+// are distinct, so the stores cannot feed the loads).
 __global__ void __launch_bounds__(NT) k_pin_correct_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
   pdl_enter();
   TILE_PROLOGUE
@@ -770,32 +792,56 @@ __global__ void __launch_bounds__(NT) k_pin_correct_m(const InstDesc* __restrict
   const RecipGrid rg = recips(G);
   const int i = tl.i0 + (threadIdx.x & 31);
   const double dt = ctrl->dt;
-  View2<const double> X{D.x, G.ld};
-  const double x0 = X(0, 0);
+  const double* __restrict__ xs = D.x;
+  double* __restrict__ us = D.us;
+  double* __restrict__ vs = D.vs;
+  double* __restrict__ ui = D.ui;
+  double* __restrict__ vi = D.vi;
+  double* __restrict__ pi = D.pi;
+  const double x0 = xs[0];
+  double xc[PB_R], xe[PB_R], xn[PB_R], u1[PB_R], v1[PB_R], u0[PB_R], v0[PB_R];
+  bool in[PB_R];
+#pragma unroll
+  for (int r = 0; r < PB_R; ++r) {
+    const int j = tl.j0 + (threadIdx.x >> 5) + r * PB_Y;
+    in[r] = i < G.nx && j < G.ny;
+    if (in[r]) {
+      const long ox = (long)j * G.ld + i, o = (long)j * D.usld + i, os = (long)j * G.lds + i;
+      xc[r] = xs[ox];
+      xe[r] = (i < G.nx - 1) ? xs[ox + 1] : 0.0;
+      xn[r] = (j < G.ny - 1) ? xs[ox + G.ld] : 0.0;
+      u1[r] = us[o];
+      v1[r] = vs[o];
+      u0[r] = ui[os];
+      v0[r] = vi[os];
+    }
+  }
   double v[2] = {0.0, 0.0}, out[2];
   int bad = 0;
-  M_ROWS({
-    if (i < G.nx && j < G.ny) {
-      const double pv = SUB(X(j, i), x0);
-      const double gx = (i < G.nx - 1) ? MUL(SUB(SUB(X(j, i + 1), x0), pv), rg.rx) : 0.0;
-      const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(X(j + 1, i), x0), pv), rg.ry) : 0.0;
+#pragma unroll
+  for (int r = 0; r < PB_R; ++r) {
+    const int j = tl.j0 + (threadIdx.x >> 5) + r * PB_Y;
+    if (in[r]) {
+      const double pv = SUB(xc[r], x0);
+      const double gx = (i < G.nx - 1) ? MUL(SUB(SUB(xe[r], x0), pv), rg.rx) : 0.0;
+      const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(xn[r], x0), pv), rg.ry) : 0.0;
       const long o = (long)j * D.usld + i;
       const long os = (long)j * G.lds + i;
-      const double uc = SUB(D.us[o], MUL(dt, gx));
-      const double vc = SUB(D.vs[o], MUL(dt, gy));
-      D.us[o] = uc;
-      D.vs[o] = vc;
-      D.pi[os] = pv;
+      const double uc = SUB(u1[r], MUL(dt, gx));
+      const double vc = SUB(v1[r], MUL(dt, gy));
+      us[o] = uc;
+      vs[o] = vc;
+      pi[os] = pv;
       const double uf = (L.has_lid && j == G.ny - 1) ? L.lid : uc;
-      const double du = SUB(uf, D.ui[os]);
-      const double dv = SUB(vc, D.vi[os]);
-      D.ui[os] = uf;
-      D.vi[os] = vc;
+      const double du = SUB(uf, u0[r]);
+      const double dv = SUB(vc, v0[r]);
+      ui[os] = uf;
+      vi[os] = vc;
       v[0] += du * du;
       v[1] += dv * dv;
       bad |= !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
     }
-  })
+  }
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->nan_flag, 1u);
   if (STEP_RED(2, v, out) && threadIdx.x == 0) {
     D.slots[S_RU].result = out[0];
