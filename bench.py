@@ -42,7 +42,6 @@ from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -280,6 +279,13 @@ def timed_steps(fn, steps, stream, flush, dist):
     return ms, outs
 
 
+def pct(ms):
+    """p50/p95/p99 of per-step times (ms)."""
+    v = sorted(ms)
+    pick = lambda q: v[min(len(v) - 1, int(q * (len(v) - 1) + 0.5))]  # noqa: E731
+    return {"p50": pick(0.50), "p95": pick(0.95), "p99": pick(0.99)} if v else None
+
+
 def max_over_ranks(x, dist):
     if dist is None:
         return x
@@ -427,6 +433,7 @@ def bench_cavity(args, dist, world, rank, local):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "cg_iterations_per_step": cg, "refine_passes_per_step": passes},
         **extra,
+        "step_latency_ms": pct(ms),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clocks.summary(),
     }
@@ -490,6 +497,7 @@ def bench_batched(args, dist, world, rank, local):
                    "l2": "flushed between timed steps (256 MiB write)",
                    "max_cg_iterations_per_step": maxit, "max_refine_passes_per_step": maxpass,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
+        "step_latency_ms": pct(ms),
         "roofline": None, "cpu_baseline": None, "e2e": e2e, "gpu_launches": launches,
         "gpu_launches_note": "from the largest loop trip counts of each step", "clocks": clocks.summary(),
     }

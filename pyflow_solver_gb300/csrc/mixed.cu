@@ -85,25 +85,23 @@ __device__ __forceinline__ PAxis prolong_axis(int i, int nc) {
   return PAxis{I, h ? I2 : I, h ? 0.75f : 1.f, h ? 0.25f : 0.f};
 }
 
-// value at fine cell (j, i) of P e, e of pitch ld on a coarse level of nx x ny
-// cells, its values read through ld(pointer)
-template <int KX, int KY, class LD>
-__device__ __forceinline__ float prolong_k(LD ld, const float* e, long pitch, int nx, int ny, int j, int i) {
+// value at fine cell (j, i) of P e on a coarse level of nx x ny cells, the
+// coarse values read through at(J, I)
+template <int KX, int KY, class AT>
+__device__ __forceinline__ float prolong_k(AT at, int nx, int ny, int j, int i) {
   const PAxis ax = prolong_axis<KX>(i, nx), ay = prolong_axis<KY>(j, ny);
-  float v = ax.w * ay.w * ld(e + (long)ay.p * pitch + ax.p);
-  if (KX == 2 && ax.w2 != 0.f) v = fmaf(ax.w2 * ay.w, ld(e + (long)ay.p * pitch + ax.p2), v);
-  if (KY == 2 && ay.w2 != 0.f) v = fmaf(ax.w * ay.w2, ld(e + (long)ay.p2 * pitch + ax.p), v);
-  if (KX == 2 && KY == 2 && ax.w2 != 0.f && ay.w2 != 0.f)
-    v = fmaf(ax.w2 * ay.w2, ld(e + (long)ay.p2 * pitch + ax.p2), v);
+  float v = ax.w * ay.w * at(ay.p, ax.p);
+  if (KX == 2 && ax.w2 != 0.f) v = fmaf(ax.w2 * ay.w, at(ay.p, ax.p2), v);
+  if (KY == 2 && ay.w2 != 0.f) v = fmaf(ax.w * ay.w2, at(ay.p2, ax.p), v);
+  if (KX == 2 && KY == 2 && ax.w2 != 0.f && ay.w2 != 0.f) v = fmaf(ax.w2 * ay.w2, at(ay.p2, ax.p2), v);
   return v;
 }
 
-template <class LD>
-__device__ __forceinline__ float prolong_val(LD ld, const float* e, long pitch, int nx, int ny, int kx, int ky, int j,
-                                             int i) {
-  if (kx == 2 && ky == 2) return prolong_k<2, 2>(ld, e, pitch, nx, ny, j, i);
-  if (kx == 2) return prolong_k<2, 1>(ld, e, pitch, nx, ny, j, i);
-  return prolong_k<1, 2>(ld, e, pitch, nx, ny, j, i);
+template <class AT>
+__device__ __forceinline__ float prolong_val(AT at, int nx, int ny, int kx, int ky, int j, int i) {
+  if (kx == 2 && ky == 2) return prolong_k<2, 2>(at, nx, ny, j, i);
+  if (kx == 2) return prolong_k<2, 1>(at, nx, ny, j, i);
+  return prolong_k<1, 2>(at, nx, ny, j, i);
 }
 
 // weight with which fine index i (offset d = i - 2I in {-1, 0, 1, 2}) enters coarse I (R = P^T)
@@ -278,14 +276,16 @@ __device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTil
   if (l == 0) F.f = f_cur(M);
   RedSmem& rsm = sm.rsm;
   const int i0 = tl.i0, j0 = tl.j0;
-  auto ldx = [&](const float* p) { return x.ld(p); };
+  const float* cu = C.u;
+  const long cld = C.ld;
+  auto cat = [&x, cu, cld](int J, int I) { return x.ld(cu + (long)J * cld + I); };
   for (int idx = x.tid(); idx < (BY + 4) * (BX + 4); idx += MT) {
     const int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
     const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f, f = 0.f;
     if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) {
       const long o = (long)gj * F.ld + gi;
-      v = x.ld(F.t + o) + prolong_val(ldx, C.u, C.ld, C.nx, C.ny, F.kx, F.ky, gj, gi);
+      v = x.ld(F.t + o) + prolong_val(cat, C.nx, C.ny, F.kx, F.ky, gj, gi);
       if (jj >= -1 && jj <= BY && ii >= -1 && ii <= BX) f = x.ld(F.f + o);
     }
     sm.w0[jj + 2][ii + 2] = v;
@@ -749,13 +749,15 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, float omega, f
     }
   }
   // up: w_l = S(S(e_l + P result_{l+1})); the bottom's result is in e, every other level's in w
-  auto lds = [](const float* p) { return *p; };
   for (int l = nl - 2; l >= 0; --l) {
     const CLvl& Lv = L[l];
     const CLvl& Cv = L[l + 1];
     const float* ec = (l + 1 == nl - 1) ? e : w;
+    const float* ecl = ec + Cv.off;
+    const int cnx = Cv.nx;
+    auto catc = [ecl, cnx](int J, int I) { return ecl[J * cnx + I]; };
     C_FOR(Lv, {
-      w[Lv.off + c] = e[Lv.off + c] + prolong_val(lds, ec + Cv.off, Cv.nx, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i);
+      w[Lv.off + c] = e[Lv.off + c] + prolong_val(catc, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i);
     })
     __syncthreads();
     c_sweep(Lv, rh, w, e, omega);

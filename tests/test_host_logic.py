@@ -72,3 +72,25 @@ def test_batched_workload_matches_fixture_draws():
     tr = serving_trace(duration=2.0)
     assert 300 < len(tr) < 500 and all(a.arrival < b.arrival for a, b in zip(tr, tr[1:]))
     assert {r.side for r in tr} <= {32, 64, 128, 256, 512, 1024}
+
+
+def test_serving_slot_plan_and_latency_percentiles():
+    from pyflow_solver_gb300.serving import Served, ServeReport, slot_plan
+    plan = slot_plan([32, 64, 128], 1e9, lambda s: s * s * 100, weights=[1, 1, 2])
+    assert plan == {32: int(0.25e9 // (32 * 32 * 100)), 64: int(0.25e9 // (64 * 64 * 100)),
+                    128: int(0.5e9 // (128 * 128 * 100))}
+    rep = ServeReport(completed=[Served(k, 32, 0.0, 10, finish=float(k + 1)) for k in range(100)])
+    pct = rep.latency_percentiles()
+    assert pct["p50"] == 51.0 and pct["p95"] == 95.0 and pct["p99"] == 99.0
+
+
+def test_bench_accounting_helpers():
+    import bench
+    assert bench.mg_levels(512, 512) == 4 and bench.mg_levels(2048, 2048) == 6 and bench.mg_levels(64, 64) == 1
+    # elongated cells coarsen the strongly coupled axis only: 256 x 64 -> 128 x 64 -> 64 x 64
+    assert bench.mg_levels(128, 32) == 1 and bench.mg_levels(256, 64) == 3
+    assert bench.launches_per_step("fp64", 300, 0, 1) == 11 + 900
+    assert bench.launches_per_step("mixed", 10, 2, 4, persistent=True) == 9
+    assert bench.launches_per_step("mixed", 10, 2, 4, persistent=False) == 11 + 2 * (6 + 7) + 10 * (3 + 7)
+    assert bench.mixed_solve_bytes(100, 10, 2) == 100 * (32 + 178 + 690)
+    assert bench.pct([3.0, 1.0, 2.0]) == {"p50": 2.0, "p95": 3.0, "p99": 3.0}
