@@ -132,3 +132,40 @@ def test_persistent_solve_equals_kernel_graph():
         for a, b in zip(runs[0][0], runs[1][0]):
             np.testing.assert_array_equal(a, b)
         assert runs[0][1] == runs[1][1]
+
+
+def test_mixed_error_report_fields_and_centerline(capsys):
+    """Worst relative error of the mixed step against the converged binary64 oracle, per
+    field and for the u centerline (u[:, nx // 2], the driver's u_centerline), step by step
+    from the same state."""
+    import torch
+
+    from pyflow_solver_gb300 import ResidualManager, allocate_state, interior_view, step
+    report = {}
+    for nx, ny, Re in ((64, 64, 100.0), (128, 128, 1000.0)):
+        cfg = cavity(nx, ny, Re, 1.0)
+        gcfg = SimpleNamespace(**vars(cfg), precision="mixed")
+        ocfg = SimpleNamespace(**vars(cfg), oracle_pressure="converged")
+        st = allocate_state(nx, ny)
+        tw = ost.allocate_state(nx, ny)
+        tr, otr = ResidualManager(), ost.ResidualManager()
+        worst = {"u": 0.0, "v": 0.0, "p": 0.0, "u_centerline": 0.0}
+        for it in range(6):
+            for k in "uvp":
+                interior_view(st.fields[k]).copy_(torch.from_numpy(ost.interior(tw.fields[k])))
+            st.meta = {"dt_prev": tw.meta.get("dt_prev", 1e-2),
+                       "divergence_history": list(tw.meta.get("divergence_history", []))}
+            step(gcfg, st, tr, it)
+            ost.step(ocfg, tw, otr, it, red="exact")
+            for k in "uvp":
+                got, ref = interior_view(st.fields[k]).cpu().numpy(), ost.interior(tw.fields[k])
+                if np.max(np.abs(ref)) > 0:
+                    worst[k] = max(worst[k], rel(got, ref))
+            gu, ou = interior_view(st.fields["u"]).cpu().numpy()[:, nx // 2], ost.interior(tw.fields["u"])[:, nx // 2]
+            if np.max(np.abs(ou)) > 0:
+                worst["u_centerline"] = max(worst["u_centerline"], rel(gu, ou))
+        report[f"{nx}x{ny} Re {Re:g}"] = worst
+    with capsys.disabled():
+        for k, w in report.items():
+            print(f"\nmixed vs converged binary64, {k}: " + ", ".join(f"{f} {e:.2e}" for f, e in w.items()))
+    assert all(e <= TOL for w in report.values() for e in w.values()), report
