@@ -629,8 +629,11 @@ __device__ __forceinline__ void ph_resid(const X& x, const MixDesc& M, const MTi
 // live in shared memory and one V-cycle (the same smoother, restriction and
 // prolongation as the global levels; the bottom level, at most 64 cells, by its
 // pseudo-inverse, else eight Jacobi sweeps) forms the coarse "solve" -- a fixed
-// linear, symmetric operator, as PCG requires.
-constexpr int CT = 1024;                     // threads of the coarse CTA
+// linear, symmetric operator, as PCG requires.  The CTA has NT threads (1024, or
+// 512 for batches of more instances than SMs, two CTAs to an SM); every sum is
+// taken in an order that does not depend on NT, so both give the same bits.
+constexpr int CT = 1024;                     // threads of the coarse CTA (and of the persistent CTAs)
+constexpr int CT2 = 512;                     // the batch form
 constexpr int CMAX = 4096;                   // cells of its finest level
 constexpr int BMAX = 64;                     // bottom levels up to this size are solved exactly
 
@@ -659,16 +662,17 @@ __device__ __forceinline__ float c_nsum(const CLvl& L, const float* a, int j, in
   return s;
 }
 
-// Cells of a shared-memory level, visited by the CTA as 32 rows of 32 threads
-// (no integer division on the index).
+// Cells of a shared-memory level, visited by the CTA's NT / 32 warps, a row of 32
+// cells to a warp (no integer division on the index).
 #define C_FOR(Lv, ...)                                               \
-  for (int j = threadIdx.x >> 5; j < (Lv).ny; j += CT / 32)          \
+  for (int j = threadIdx.x >> 5; j < (Lv).ny; j += NT / 32)          \
     for (int i = threadIdx.x & 31; i < (Lv).nx; i += 32) {           \
       const int c = j * (Lv).nx + i;                                 \
       __VA_ARGS__                                                    \
     }
 
 // one damped-Jacobi sweep src -> dst on level L (all threads; ends with a barrier)
+template <int NT>
 __device__ __forceinline__ void c_sweep(const CLvl& L, const float* f, const float* src, float* dst, float omega) {
   C_FOR(L, {
     dst[L.off + c] = fmaf(1.f - omega, src[L.off + c],
@@ -677,29 +681,34 @@ __device__ __forceinline__ void c_sweep(const CLvl& L, const float* f, const flo
   __syncthreads();
 }
 
-// The coarse V-cycle of instance M by the whole 1024-thread CTA; sm: 3 x (its
+// The coarse V-cycle of instance M by the whole NT-thread CTA; sm: 3 x (its
 // levels' cells) floats of shared memory.
+template <int NT>
 __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, float omega, float* sm) {
   Lvl C = M.lev[M.nlev - 1];
   if (M.nlev == 1) C.f = f_cur(M);
   const int nl = M.coarse_levels;
-  CLvl L[8];
-  int tot = 0;
-  {
-    int nx = C.nx, ny = C.ny;
+  // the level table in shared memory (a local array indexed by the level would live in local memory)
+  __shared__ CLvl L[8];
+  __shared__ int s_tot;
+  if (threadIdx.x == 0) {
+    int nx = C.nx, ny = C.ny, t = 0;
     for (int l = 0; l < nl; ++l) {
       L[l].nx = nx;
       L[l].ny = ny;
-      L[l].off = tot;
+      L[l].off = t;
       L[l].cx = M.ccx[l];
       L[l].cy = M.ccy[l];
       L[l].kx = M.ckx[l];
       L[l].ky = M.cky[l];
-      tot += nx * ny;
+      t += nx * ny;
       nx /= L[l].kx;
       ny /= L[l].ky;
     }
+    s_tot = t;
   }
+  __syncthreads();
+  const int tot = s_tot;
   float* rh = sm;            // right-hand side of every level (level 0: the entry level's f)
   float* e = sm + tot;       // pre-smoothed iterate on the way down; the bottom solution
   float* w = sm + 2 * tot;   // residual on the way down; each level's result on the way up
@@ -730,18 +739,40 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, float omega, f
     const CLvl& Lv = L[nl - 1];
     const int nb = Lv.nx * Lv.ny;
     if (M.binv) {
-      // exact bottom solve: e = A+ rh (at most BMAX cells)
-      for (int q0 = threadIdx.x; q0 < nb; q0 += CT) {
-        const float* row = M.binv + (long)q0 * nb;
-        float acc = 0.f;
-        for (int q = 0; q < nb; ++q) acc = fmaf(__ldg(row + q), rh[Lv.off + q], acc);
-        e[Lv.off + q0] = acc;
+      // exact bottom solve: e = A+ rh (at most BMAX cells).  A+ is exactly symmetric, so
+      // column q0 is read for row q0 (consecutive threads, consecutive addresses); the
+      // sum over q is split into NS slices of QS terms, added in slice order through w
+      // (dead on the way down past the restrictions).
+      constexpr int NS = 16, QS = BMAX / NS;
+      if (nb == BMAX && tot >= NS * BMAX) {
+        for (int v = threadIdx.x; v < NS * BMAX; v += NT) {
+          const int q0 = v % BMAX, h = v / BMAX;
+          float acc = 0.f;
+#pragma unroll
+          for (int k = 0; k < QS; ++k) {
+            const int q = h * QS + k;
+            acc = fmaf(__ldg(M.binv + (long)q * nb + q0), rh[Lv.off + q], acc);
+          }
+          w[v] = acc;
+        }
+        __syncthreads();
+        if (threadIdx.x < BMAX) {
+          float sacc = w[threadIdx.x];
+          for (int k = 1; k < NS; ++k) sacc += w[k * BMAX + threadIdx.x];
+          e[Lv.off + threadIdx.x] = sacc;
+        }
+      } else {
+        for (int q0 = threadIdx.x; q0 < nb; q0 += NT) {
+          float acc = 0.f;
+          for (int q = 0; q < nb; ++q) acc = fmaf(__ldg(M.binv + (long)q * nb + q0), rh[Lv.off + q], acc);
+          e[Lv.off + q0] = acc;
+        }
       }
       __syncthreads();
     } else {
       C_FOR(Lv, { e[Lv.off + c] = 0.f; })
       __syncthreads();
-      for (int q = 0; q < bottom_sweeps; ++q) c_sweep(Lv, rh, (q & 1) ? w : e, (q & 1) ? e : w, omega);
+      for (int q = 0; q < bottom_sweeps; ++q) c_sweep<NT>(Lv, rh, (q & 1) ? w : e, (q & 1) ? e : w, omega);
       if (bottom_sweeps & 1) {
         C_FOR(Lv, { e[Lv.off + c] = w[Lv.off + c]; })
         __syncthreads();
@@ -760,18 +791,25 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, float omega, f
       w[Lv.off + c] = e[Lv.off + c] + prolong_val(catc, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i);
     })
     __syncthreads();
-    c_sweep(Lv, rh, w, e, omega);
-    c_sweep(Lv, rh, e, w, omega);
+    c_sweep<NT>(Lv, rh, w, e, omega);
+    c_sweep<NT>(Lv, rh, e, w, omega);
   }
   const float* z = (nl == 1) ? e : w;
   C_FOR(L[0], { C.u[(long)j * C.ld + i] = z[c]; })
   if (M.nlev == 1) {
-    // the V-cycle ran entirely here: rho = r.z over level 0, summed as the tile phases do
+    // the V-cycle ran entirely here: rho = r.z over level 0, summed as the tile phases do,
+    // as 1024 lanes (row j to lane-row j mod 32) whatever NT is
     __shared__ double wsum[CT / 32];
-    FF acc = {0.f, 0.f};
-    C_FOR(L[0], { ff_add_prod(acc, rh[c], z[c]); })
-    acc = ff_warp_sum(acc);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)acc.hi + (double)acc.lo;
+    const CLvl& L0 = L[0];
+#pragma unroll
+    for (int m = 0; m < CT / NT; ++m) {
+      const int vw = (threadIdx.x >> 5) + m * (NT / 32);
+      FF acc = {0.f, 0.f};
+      for (int j = vw; j < L0.ny; j += CT / 32)
+        for (int i = threadIdx.x & 31; i < L0.nx; i += 32) ff_add_prod(acc, rh[j * L0.nx + i], z[j * L0.nx + i]);
+      acc = ff_warp_sum(acc);
+      if ((threadIdx.x & 31) == 0) wsum[vw] = (double)acc.hi + (double)acc.lo;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       double rz = wsum[0];
@@ -806,13 +844,15 @@ __global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, 
   ph_post(x, M, tl, l, omega, sm);
 }
 
-__global__ void __launch_bounds__(CT) k_mg_coarse(const MixDesc* __restrict__ MD, int gate, int bottom_sweeps,
-                                                   float omega) {
+// one CTA per instance
+template <int NT>
+__global__ void __launch_bounds__(NT, CT / NT) k_mg_coarse(const MixDesc* __restrict__ MD, int gate, int bottom_sweeps,
+                                                            float omega) {
   pdl_enter();
   const MixDesc& M = MD[blockIdx.x];
   if (!mx_live(M, gate)) return;
   extern __shared__ float csm[];
-  coarse_cycle(M, bottom_sweeps, omega, csm);
+  coarse_cycle<NT>(M, bottom_sweeps, omega, csm);
 }
 
 __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
@@ -926,7 +966,9 @@ __global__ void k_mx_finish(const MixDesc* __restrict__ MD, int n) {
 // 1024-thread CTA per SM, each CTA four 256-thread groups that take the tiles of
 // a phase in turn, and a grid barrier between phases.  The loop decisions
 // (instances still refining, still in the inner solve) are read after a
-// barrier, so every CTA takes the same branch.  The phases are the functions
+// barrier, so every CTA takes the same branch.  A group that takes several
+// tiles of a phase passes its barrier between them (a phase's first loop may
+// write shared arrays its last loop still reads).  The phases are the functions
 // the ordinary kernels run, on the same tiles in the same order, so the
 // results are the same bits.  Loop trip bounds stop a solve whose instances do
 // not report; a barrier that waits too long sets the error flag, and every CTA
@@ -958,12 +1000,13 @@ __global__ void __launch_bounds__(CT, 1) k_mx_persist(PersistArgs A) {
         const MTile tl = A.tpre[l][t];
         const MixDesc& M = A.dd[tl.inst];
         if (mx_live(M, 1)) ph_down(x, M, tl, l, A.omega, ts.d);
+        x.sync();
       }
       if (!grid_sync(gb)) return false;
     }
     for (int k = blockIdx.x; k < A.n; k += gridDim.x) {
       const MixDesc& M = A.dd[k];
-      if (mx_live(M, 1)) coarse_cycle(M, A.bottom_sweeps, A.omega, reinterpret_cast<float*>(psm));
+      if (mx_live(M, 1)) coarse_cycle<CT>(M, A.bottom_sweeps, A.omega, reinterpret_cast<float*>(psm));
     }
     if (!grid_sync(gb)) return false;
     for (int l = A.maxlev - 2; l >= 0; --l) {
@@ -971,6 +1014,7 @@ __global__ void __launch_bounds__(CT, 1) k_mx_persist(PersistArgs A) {
         const MTile tl = A.tpre[l][t];
         const MixDesc& M = A.dd[tl.inst];
         if (mx_live(M, 1)) ph_post(x, M, tl, l, A.omega, ts.p);
+        x.sync();
       }
       if (!grid_sync(gb)) return false;
     }
@@ -981,11 +1025,13 @@ __global__ void __launch_bounds__(CT, 1) k_mx_persist(PersistArgs A) {
     const MTile tl = A.tl0[t];                                     \
     const MixDesc& M = A.dd[tl.inst];                              \
     if (mx_live(M, gate)) { body; }                                \
+    x.sync();                                                      \
   }
   for (int t = gid; t < A.nt0; t += ngroups) {
     const MTile tl = A.tl0[t];
     const MixDesc& M = A.dd[tl.inst];
     if (*M.active) ph_init(x, M, tl, ml, ts.r);
+    x.sync();
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) ml->inner_active = 0;
   if (!grid_sync(gb)) return;
@@ -1287,7 +1333,19 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   cudaError_t e = cudaMemcpy(B->dd, B->hd.data(), n * sizeof(MixDesc), cudaMemcpyHostToDevice);
   B->coarse_smem = smem;
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k_mg_coarse<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mg_coarse<CT2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) {
+    // more coarse CTAs than one wave of 1024-thread CTAs holds: 512-thread CTAs, two to an SM
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (n > sms && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mg_coarse<CT2>, CT2, smem) == cudaSuccess &&
+        occ >= 2)
+      B->coarse_nt = CT2;
+    cudaGetLastError();
+  }
   if (e == cudaSuccess) {
     // the persistent solve: one 1024-thread CTA per SM, if the device co-schedules them
     const size_t psmem = std::max(4 * sizeof(TileSmem), smem);
@@ -1343,7 +1401,10 @@ static void add_vcycle(GraphChain& c, Batch* B, int gate, float omega, int l0 = 
   for (int l = l0; l + 1 < B->maxlev; ++l) {
     if (B->ntpre[l]) c.kernel(k_mg_down, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, omega);
   }
-  c.kernel_smem(k_mg_coarse, dim3(B->n), dim3(CT), B->coarse_smem, dd, gate, 8, omega);
+  if (B->coarse_nt == CT2)
+    c.kernel_smem(k_mg_coarse<CT2>, dim3(B->n), dim3(CT2), B->coarse_smem, dd, gate, 8, omega);
+  else
+    c.kernel_smem(k_mg_coarse<CT>, dim3(B->n), dim3(CT), B->coarse_smem, dd, gate, 8, omega);
   for (int l = B->maxlev - 2; l >= 0; --l)
     if (B->ntpre[l]) c.kernel(k_mg_post, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, omega);
 }
@@ -1419,7 +1480,10 @@ static void launch_vcycle(Batch* B, int gate, float omega, cudaStream_t s, int l
   for (int l = l0; l + 1 < B->maxlev; ++l) {
     if (B->ntpre[l]) k_mg_down<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, omega);
   }
-  k_mg_coarse<<<B->n, CT, B->coarse_smem, s>>>(B->dd, gate, 8, omega);
+  if (B->coarse_nt == CT2)
+    k_mg_coarse<CT2><<<B->n, CT2, B->coarse_smem, s>>>(B->dd, gate, 8, omega);
+  else
+    k_mg_coarse<CT><<<B->n, CT, B->coarse_smem, s>>>(B->dd, gate, 8, omega);
   for (int l = B->maxlev - 2; l >= 0; --l)
     if (B->ntpre[l]) k_mg_post<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, omega);
 }

@@ -97,6 +97,7 @@ struct Batch {
   MTile* tpre[MAX_LEVELS] = {};                // tiles of level l of the instances that smooth on it (l < nlev-1)
   int ntpre[MAX_LEVELS] = {};
   size_t coarse_smem = 0;                      // dynamic shared memory of the coarse CTA (largest instance)
+  int coarse_nt = 1024;                        // threads of the coarse CTA (512: two to an SM)
   MixLoop* loop = nullptr;
   int gmax_o = 1, gmax_i = 1;                  // trip bounds of the loop guards
   // profiling (direct launches): events around each PCG matvec launch

@@ -107,6 +107,36 @@ def test_mixed_batch_equals_single_instances():
         assert all(d["Rp_converged"] for _, d in mine[1:])
 
 
+def test_wide_mixed_batch_equals_single_instances():
+    """A mixed batch with more instances than the GPU has SMs runs its coarse cycles as
+    512-thread CTAs, two to an SM; every sum there is taken in the 1024-thread order, so
+    instances still get the bits of their single-instance runs (1024-thread CTAs)."""
+    import torch
+
+    from pyflow_solver_gb300 import ResidualManager, allocate_state, step
+    from pyflow_solver_gb300.batch import BatchedCavities
+    n = torch.cuda.get_device_properties(0).multi_processor_count + 8
+    rng = np.random.default_rng(5)
+    sizes = [(16, 16), (32, 32), (64, 32), (48, 64), (64, 64), (8, 8), (24, 40)]
+    cfgs = []
+    for k in range(n):
+        nx, ny = sizes[k % len(sizes)]
+        cfg = cfg_of(nx, ny, float(rng.uniform(100, 3000)), float(rng.uniform(0.5, 2.0)), "quick")
+        cfg.precision = "mixed"
+        cfgs.append(cfg)
+    states = [allocate_state(c.nx, c.ny) for c in cfgs]
+    B = BatchedCavities(cfgs, states)
+    outs = [B.step() for _ in range(3)]
+    for k in list(range(len(sizes))) + [n - 1]:
+        cfg = cfgs[k]
+        st = allocate_state(cfg.nx, cfg.ny)
+        tr = ResidualManager()
+        for it in range(3):
+            assert step(cfg, st, tr, it)[1:] == outs[it][k], (k, it)
+        for a, b in zip(fields(st), fields(states[k])):
+            np.testing.assert_array_equal(a, b)
+
+
 def test_step_arrays_and_slot_reuse():
     """The array host path gives the same fields and records as step(); a slot
     reused with new parameters equals a fresh run of the new request."""

@@ -134,6 +134,27 @@ def test_persistent_solve_equals_kernel_graph():
         assert runs[0][1] == runs[1][1]
 
 
+def test_persistent_groups_taking_several_tiles():
+    """At 2048 x 2048 the persistent solve's four groups per CTA take several tiles of level 0
+    and of level 1 in turn (more tiles than groups); the bits equal the kernel graph's."""
+    from pyflow_solver_gb300 import ResidualManager, _capi, allocate_state, interior_view, step
+    from pyflow_solver_gb300.solvers._handle import instance_for
+    from pyflow_solver_gb300.solvers.solver import step_params
+    lib = _capi.load()
+    cfg = cavity(2048, 2048, 1000.0, 1.0, precision="mixed")
+    runs = []
+    for persistent in (1, 0):
+        st = allocate_state(2048, 2048)
+        P, *_ = step_params(cfg, 2048, 2048)
+        _capi.check(lib.pfgb_set_persistent(instance_for(st, P).handle, persistent), "set_persistent")
+        tr = ResidualManager()
+        diags = [step(cfg, st, tr, it)[2] for it in range(3)]
+        runs.append(([interior_view(st.fields[k]).cpu().numpy() for k in "uvp"], diags))
+    for a, b in zip(runs[0][0], runs[1][0]):
+        np.testing.assert_array_equal(a, b)
+    assert runs[0][1] == runs[1][1]
+
+
 def test_mixed_error_report_fields_and_centerline(capsys):
     """Worst relative error of the mixed step against the converged binary64 oracle, per
     field and for the u centerline (u[:, nx // 2], the driver's u_centerline), step by step
