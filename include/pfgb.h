@@ -65,10 +65,15 @@ typedef struct pfgb_params {
    * multigrid-preconditioned CG with relative tolerance mixed_tol_inner (1e-5
    * when 0); at most mixed_max_outer passes (8 when 0) of mixed_max_inner
    * inner iterations (50 when 0).  nx and ny must halve down to at most 1024
-   * cells on the coarsest multigrid level. */
+   * cells on the coarsest multigrid level.  The refinement starts from the
+   * pressure the state holds (shifted so that its cell 0 is 0) when that leaves a
+   * residual no larger than ||b||, else from zero; mixed_cold_start = 1 starts
+   * every solve from zero, as the reference's CG does.  Each inner solve also
+   * stops once its residual is below a quarter of the outer target. */
   double mixed_tol_outer, mixed_tol_inner;
   int mixed_max_outer, mixed_max_inner;
-  int reserved[4];
+  int mixed_cold_start;
+  int reserved[3];
 } pfgb_params;
 
 /* Host-side state.meta carried into a step (solver.py:32,46-50). */

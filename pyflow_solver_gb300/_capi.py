@@ -27,7 +27,8 @@ class Params(ctypes.Structure):
         ("precision", ctypes.c_int),
         ("mixed_tol_outer", ctypes.c_double), ("mixed_tol_inner", ctypes.c_double),
         ("mixed_max_outer", ctypes.c_int), ("mixed_max_inner", ctypes.c_int),
-        ("reserved", ctypes.c_int * 4),
+        ("mixed_cold_start", ctypes.c_int),
+        ("reserved", ctypes.c_int * 3),
     ]
 
 

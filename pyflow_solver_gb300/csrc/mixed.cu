@@ -182,8 +182,21 @@ __device__ __forceinline__ float* f_cur(const MixDesc& M) {
     __VA_ARGS__                                             \
   }
 
-#define X_RED(R, vals, outv) dred_sum<R, MT>(x, vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
-#define X_RED_FF(R, vals, outv) dred_sum_ff<R, MT>(x, vals, M.part, M.nt0, tl.loc, M.ticket, outv, rsm)
+// an instance-wide sum of R values per tile (M.part holds MAX_RED per tile)
+template <int R, class X>
+__device__ __forceinline__ bool x_red(const X& x, const MixDesc& M, const MTile& tl, double (&v)[R], double (&out)[R],
+                                      RedSmem& rsm) {
+  static_assert(R <= MAX_RED, "reduction wider than the partial-sum array");
+  return dred_sum<R, MT>(x, v, M.part, M.nt0, tl.loc, M.ticket, out, rsm);
+}
+template <int R, class X>
+__device__ __forceinline__ bool x_red(const X& x, const MixDesc& M, const MTile& tl, FF (&v)[R], double (&out)[R],
+                                      RedSmem& rsm) {
+  static_assert(R <= MAX_RED, "reduction wider than the partial-sum array");
+  return dred_sum_ff<R, MT>(x, v, M.part, M.nt0, tl.loc, M.ticket, out, rsm);
+}
+#define X_RED(R, vals, outv) x_red<R>(x, M, tl, vals, outv, rsm)
+#define X_RED_FF(R, vals, outv) x_red<R>(x, M, tl, vals, outv, rsm)
 
 constexpr int H3 = 3;
 struct DownSmem {
@@ -324,59 +337,100 @@ __device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTil
   }
 }
 
+// the previous pressure shifted to x[0] = 0 (the pinned cell), as a 2-D view
+struct ShiftView {
+  const double* p;
+  long ld;
+  double s;
+  __device__ __forceinline__ double operator()(int j, int i) const { return __dsub_rn(__ldcg(p + (long)j * ld + i), s); }
+};
+
 // b -= mean(b), b[0] = 0 (pressure_solver.py:127-128, the mean from the exactly
-// rounded sum as in the binary64 path); x = 0, r64 = b; ||b||^2 and sum(b);
-// counts the instances that refine
+// rounded sum as in the binary64 path); ||b||^2 and sum(b).  Cold start: x = 0,
+// r64 = b.  Warm start: x = p_prev - p_prev[0] (the state's pressure, which the
+// step has not yet replaced) and r64 = b - A x with the reference's pinned
+// operator, plus ||r64||^2 and sum(r64); the finalising tile keeps it when
+// ||r64|| <= ||b|| and otherwise marks the solve cold (the first pass then
+// restarts from x = 0, r = b).  Counts the instances that refine.
 template <class X>
 __device__ __forceinline__ void ph_init(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml, RedSmem& rsm) {
   const Geo G = M.G;
   MixCtrl* ctrl = M.ctrl;
   const double mean = __ddiv_rn(cget(M.bsum), M.n_cells);
+  const bool warm = cget(&ctrl->warm) != 0;
+  const double* P = warm ? *M.pprev : nullptr;
+  const ShiftView Xv{P, M.ldp, P ? __ldcg(P) : 0.0};
   const int i = tl.i0 + (x.tid() & 31);
-  double v[2] = {0.0, 0.0}, out[2];
+  double v[4] = {0.0, 0.0, 0.0, 0.0}, out[4];
   MX_ROWS_X({
     const int j = tl.j0 + ty;
     if (i < G.nx && j < G.ny) {
       const long o = (long)j * G.ld + i;
       const double bv = (i == 0 && j == 0) ? 0.0 : __dsub_rn(x.ld(M.b + o), mean);
       M.b[o] = bv;
-      M.x[o] = 0.0;
-      M.r64[o] = bv;
       v[0] += bv * bv;
       v[1] += bv;
+      if (P) {
+        const double xv = Xv(j, i);
+        const double ax = (i == 0 && j == 0) ? xv : -lap_coherent_at(Xv, j, i, G.g);
+        const double rv = __dsub_rn(bv, ax);
+        M.x[o] = xv;
+        M.r64[o] = rv;
+        v[2] += rv * rv;
+        v[3] += rv;
+      } else {
+        M.x[o] = 0.0;
+        M.r64[o] = bv;
+      }
     }
   })
-  if (X_RED(2, v, out) && x.tid() == 0) {
+  if (X_RED(4, v, out) && x.tid() == 0) {
     M.ctrl64->mean = mean;
     M.ctrl64->nan_flag = 0u;
     const double bb = out[0];
     ctrl->bnorm = sqrt(bb);
     ctrl->tol_abs_out = cget(&ctrl->tol_out) * ctrl->bnorm;
-    ctrl->rr64 = bb;
-    ctrl->sum64 = out[1];
     ctrl->outer = 0;
     ctrl->inner = 0;
     ctrl->inner_total = 0;
     ctrl->inner_done = 1;
-    ctrl->converged = (bb == 0.0) ? 1 : 0;
-    ctrl->outer_done = (bb == 0.0) ? 1 : 0;
-    if (bb != 0.0) atomicAdd(&ml->outer_active, 1);
+    bool done;
+    if (P && out[2] <= bb) {            // the warm guess is no worse than zero (false for a NaN)
+      ctrl->cold = 0;
+      ctrl->rr64 = out[2];
+      ctrl->sum64 = out[3];
+      done = !(sqrt(out[2]) > ctrl->tol_abs_out);
+    } else {                            // from zero; a rejected warm guess still takes one pass to reset x
+      ctrl->cold = P ? 1 : 0;
+      ctrl->rr64 = bb;
+      ctrl->sum64 = out[1];
+      done = !P && bb == 0.0;
+    }
+    ctrl->converged = done ? 1 : 0;
+    ctrl->outer_done = done ? 1 : 0;
+    if (!done) atomicAdd(&ml->outer_active, 1);
   }
 }
 
-// r~ = float(r64) with r~_0 = -sum_{k != 0} r64_k; e = 0; ||r~||^2; starts an inner solve
+// r~ = float(r64) with r~_0 = -sum_{k != 0} r64_k; e = 0; ||r~||^2; starts an inner solve.
+// The first pass of a cold-marked solve takes r64 = b and resets x = 0 instead.
+// The inner solve stops at ||r_in|| <= max(tol_in ||r~||, tol_abs_out / 4): a
+// quarter of the outer target is as far as this pass needs to go.
 template <class X>
 __device__ __forceinline__ void ph_prep(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml, RedSmem& rsm) {
   const Geo G = M.G;
   const Lvl L0 = M.lev[0];
   MixCtrl* ctrl = M.ctrl;
+  const bool restart = cget(&ctrl->cold) != 0 && cget(&ctrl->outer) == 0;
+  const double* rsrc = restart ? M.b : M.r64;
   const int i = tl.i0 + (x.tid() & 31);
   FF v[1] = {{0.f, 0.f}};
   double out[1];
   MX_ROWS_X({
     const int j = tl.j0 + ty;
     if (i < G.nx && j < G.ny) {
-      const double rv = (i == 0 && j == 0) ? -(cget(&ctrl->sum64) - x.ld(M.r64)) : x.ld(M.r64 + (long)j * G.ld + i);
+      if (restart) M.x[(long)j * G.ld + i] = 0.0;
+      const double rv = (i == 0 && j == 0) ? -(cget(&ctrl->sum64) - x.ld(rsrc)) : x.ld(rsrc + (long)j * G.ld + i);
       const float rf = __double2float_rn(rv);
       L0.f[(long)j * L0.ld + i] = rf;
       M.e[(long)j * L0.ld + i] = 0.f;
@@ -386,7 +440,7 @@ __device__ __forceinline__ void ph_prep(const X& x, const MixDesc& M, const MTil
   if (X_RED_FF(1, v, out) && x.tid() == 0) {
     const double rt = sqrt(out[0]);
     ctrl->rt_norm = rt;
-    ctrl->tol_abs_in = cget(&ctrl->tol_in) * rt;
+    ctrl->tol_abs_in = fmax(cget(&ctrl->tol_in) * rt, 0.25 * cget(&ctrl->tol_abs_out));
     ctrl->inner = 0;
     ctrl->inner_done = rt > 0.0 ? 0 : 1;
     if (rt > 0.0) atomicAdd(&ml->inner_active, 1);
@@ -1218,7 +1272,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     for (auto& d : plan[k].global) bytes += 3 * up((size_t)round_up(d.nx, 32) * d.ny * sizeof(float));
     const size_t v0 = up((size_t)round_up(prm[k].nx, 32) * prm[k].ny * sizeof(float));
     const size_t nt0 = (size_t)((prm[k].nx + BX - 1) / BX) * ((prm[k].ny + BY - 1) / BY);
-    bytes += 5 * v0 + up((size_t)prm[k].ld64 * prm[k].ny * sizeof(double)) + up(2 * nt0 * sizeof(double)) +
+    bytes += 5 * v0 + up((size_t)prm[k].ld64 * prm[k].ny * sizeof(double)) + up(MAX_RED * nt0 * sizeof(double)) +
              up(sizeof(unsigned)) + up(sizeof(MixCtrl));
   }
   // tile tables
@@ -1283,7 +1337,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     M.q = (float*)take(v0);
     M.r64 = (double*)take((size_t)prm[k].ld64 * prm[k].ny * sizeof(double));
     M.nt0 = ((prm[k].nx + BX - 1) / BX) * ((prm[k].ny + BY - 1) / BY);
-    M.part = (double*)take(2 * (size_t)M.nt0 * sizeof(double));
+    M.part = (double*)take(MAX_RED * (size_t)M.nt0 * sizeof(double));
     M.ticket = (unsigned*)take(sizeof(unsigned));
     M.ctrl = (MixCtrl*)take(sizeof(MixCtrl));
     M.binv = nullptr;
@@ -1300,6 +1354,8 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     M.n_cells = (double)prm[k].nx * (double)prm[k].ny;
     M.res_out = prm[k].res_out;
     M.x = prm[k].x;
+    M.pprev = prm[k].pprev;
+    M.ldp = prm[k].ldp;
     M.ctrl64 = prm[k].ctrl64;
     M.active = prm[k].active;
     M.maxiter_report = prm[k].maxiter_report;
@@ -1308,6 +1364,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     hc.tol_in = prm[k].tol_in;
     hc.max_outer = prm[k].max_outer;
     hc.max_inner = prm[k].max_inner;
+    hc.warm = prm[k].warm ? 1 : 0;
     hc.inner_done = 1;
     hc.outer_done = 1;
     cudaMemcpy(M.ctrl, &hc, sizeof(MixCtrl), cudaMemcpyHostToDevice);
@@ -1370,7 +1427,8 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   return PFGB_OK;
 }
 
-int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer, int max_inner, int maxiter_report) {
+int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer, int max_inner, int warm,
+                   int maxiter_report) {
   if (k < 0 || k >= B->n) return set_error(PFGB_EINVAL, "instance index out of range");
   if (max_outer < 1 || max_outer + 1 > B->gmax_o || max_inner < 1 || max_inner + 1 > B->gmax_i)
     return set_error(PFGB_EINVAL, "mixed iteration limits above the batch's largest");
@@ -1379,7 +1437,8 @@ int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer
   head.tol_in = tol_in;
   head.max_outer = max_outer;
   head.max_inner = max_inner;
-  // the four leading fields; the rest of the control block is rewritten by every solve
+  head.warm = warm ? 1 : 0;
+  // the leading fields up to bnorm; the rest of the control block is rewritten by every solve
   cudaError_t e = cudaMemcpy(B->hd[k].ctrl, &head, offsetof(MixCtrl, bnorm), cudaMemcpyHostToDevice);
   B->hd[k].maxiter_report = maxiter_report;
   if (e == cudaSuccess)

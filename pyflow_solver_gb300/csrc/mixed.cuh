@@ -14,6 +14,7 @@ namespace pfgb {
 namespace mixed {
 
 constexpr int MAX_LEVELS = 16;
+constexpr int MAX_RED = 4;     // most sums one tile reduction carries
 
 // One multigrid level: binary32 arrays of (ny, ld); cx, cy are the face
 // coefficients.  The coarse operators are rediscretised consistently with
@@ -39,11 +40,13 @@ struct Geo {
 struct MixCtrl {
   double tol_out, tol_in;
   int max_outer, max_inner;
+  int warm;                    // start from the previous pressure (else from zero)
   double bnorm, tol_abs_out, rr64, sum64;
   double rt_norm, tol_abs_in;
   double rho, beta, pq, alpha, rr_in;
   int outer, inner, inner_total, converged;
   int inner_done, outer_done;
+  int cold;                    // this solve's first pass starts from zero (the warm guess was worse)
 };
 
 // One tile of work of a mixed batch: instance and the tile's first cell.
@@ -69,7 +72,9 @@ struct MixDesc {
   double n_cells;
   double* res_out;             // where the final ||b - A x||^2 goes (the step's residual record)
   double* x;                   // the step's pressure solution
-  double* part;                // per-tile partial sums of the reductions (2 x nt0)
+  const double* const* pprev;  // where the step's pressure field pointer lives (interior, pitch ldp)
+  long ldp;
+  double* part;                // per-tile partial sums of the reductions (MAX_RED x nt0)
   unsigned* ticket;            // arrival counter of the reductions
   MixCtrl* ctrl;
   Ctrl64* ctrl64;              // the step's control block (iteration summary)
@@ -124,6 +129,9 @@ struct MixParams {
   const double* bsum;
   double* res_out;
   double* x;
+  const double* const* pprev;
+  long ldp;
+  int warm;
   Ctrl64* ctrl64;
   const int* active;
   int maxiter_report;
@@ -138,7 +146,8 @@ int run_direct(Batch* B, cudaStream_t s);
 // Use the persistent cooperative solve (on, where the device allows it) or the kernel graph.
 int set_persistent(Batch* B, int on);
 // New tolerances and iteration limits for instance k (limits within the loop guards).
-int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer, int max_inner, int maxiter_report);
+int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer, int max_inner, int warm,
+                   int maxiter_report);
 
 }  // namespace mixed
 }  // namespace pfgb

@@ -1119,6 +1119,10 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
       m.bsum = &I->hd[k].slots[S_BSUM].result;
       m.res_out = &I->hd[k].slots[S_RES].result;
       m.x = I->hd[k].x;
+      // the pressure field of the bound state, read through the descriptor (rebound every step)
+      m.pprev = reinterpret_cast<const double* const*>(reinterpret_cast<const char*>(I->dd + k) + offsetof(InstDesc, pi));
+      m.ldp = I->hd[k].G.lds;
+      m.warm = prm.mixed_cold_start ? 0 : 1;
       m.ctrl64 = I->hd[k].ctrl;
       // the instance's activity flag inside the device descriptor table
       m.active = reinterpret_cast<const int*>(reinterpret_cast<const char*>(I->dd + k) + offsetof(InstDesc, active));
@@ -1425,7 +1429,8 @@ int instance64_set_params(Instance64* I, int k, const pfgb_params* prm) {
     const double tol_in = prm->mixed_tol_inner > 0.0 ? prm->mixed_tol_inner : 1e-5;
     const int max_outer = prm->mixed_max_outer > 0 ? prm->mixed_max_outer : 8;
     const int max_inner = prm->mixed_max_inner > 0 ? prm->mixed_max_inner : 50;
-    if (int rc = mixed::set_tolerances(I->mix, k, tol_out, tol_in, max_outer, max_inner, prm->lin_maxiter))
+    if (int rc = mixed::set_tolerances(I->mix, k, tol_out, tol_in, max_outer, max_inner, prm->mixed_cold_start ? 0 : 1,
+                                       prm->lin_maxiter))
       return rc;
   }
   InstDesc& D = I->hd[k];

@@ -67,7 +67,7 @@ class Instance:
 def params_key(p: _capi.Params):
     return (p.nx, p.ny, p.dx, p.dy, p.nu, p.cfl_target, p.cfl_growth, p.lin_tol, p.lin_maxiter, p.scheme,
             p.enable_jacobi, p.jacobi_interior, p.has_lid, p.lid_velocity, p.precision, p.mixed_tol_outer,
-            p.mixed_tol_inner, p.mixed_max_outer, p.mixed_max_inner)
+            p.mixed_tol_inner, p.mixed_max_outer, p.mixed_max_inner, p.mixed_cold_start)
 
 
 def instance_for(state, params: _capi.Params, slot: str = "_pfgb_step") -> Instance:

@@ -13,7 +13,10 @@ receives one record of scalars and forms the dicts exactly as the reference.
 ``config.precision = "mixed"`` selects the mixed-precision form: the pressure
 system is solved to ``||b - A x|| <= lin_tol ||b||`` by binary64 iterative
 refinement around a binary32 multigrid-preconditioned CG (``mixed_tol_inner``,
-``mixed_max_outer``, ``mixed_max_inner``); everything else stays binary64.
+``mixed_max_outer``, ``mixed_max_inner``); everything else stays binary64.  The
+refinement starts from the state's previous pressure (``mixed_warm_start``,
+default True; it falls back to zero when that guess is worse than zero), so the
+same stopping test is met with fewer multigrid cycles on a slowly changing flow.
 
 Not restated (host side effects outside the array path): the ``print`` output
 of the diagnostic mode is limited to its scalar lines, and JSONL logging /
@@ -62,6 +65,7 @@ def step_params(config, nx: int, ny: int):
         P.mixed_tol_inner = float(getattr(config, "mixed_tol_inner", 1e-5))
         P.mixed_max_outer = int(getattr(config, "mixed_max_outer", 8))
         P.mixed_max_inner = int(getattr(config, "mixed_max_inner", 50))
+        P.mixed_cold_start = 0 if getattr(config, "mixed_warm_start", True) else 1
     return P, dx, dy, nu
 
 
