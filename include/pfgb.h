@@ -243,6 +243,17 @@ PFGB_API int pfgb_cg_solve_noalloc(int op, const double* b, double* x, int nx, i
                                    int precond, double jacobi_interior, double tol, int maxiter,
                                    void* stream, pfgb_solve_out* out);
 
+/* Page-lock the host range [ptr, ptr + bytes) (cudaHostRegister, portable) so
+ * that copies between it and device memory are direct DMA transfers, without a
+ * staging copy through a driver buffer.  For callers that keep their fields in
+ * host arrays and step them in place: the arrays are registered once and every
+ * step's transfers go straight into and out of them.  Fails (PFGB_ECUDA, nothing
+ * registered) when the range overlaps a registered one.  pfgb_host_unregister
+ * releases a range by its start address; an array must be unregistered before
+ * its memory is freed.  No reference counterpart. */
+PFGB_API int pfgb_host_register(void* ptr, size_t bytes);
+PFGB_API int pfgb_host_unregister(void* ptr);
+
 /* With precision 1: run each step's pressure solve as one persistent cooperative
  * launch (on; available where the device co-schedules one 1024-thread CTA per
  * SM) or as a graph of per-phase kernels with WHILE loop nodes (off, the

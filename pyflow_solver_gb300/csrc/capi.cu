@@ -121,6 +121,26 @@ extern "C" int pfgb_set_cg_variant(pfgb_handle* handle, int variant) {
   return instance64_set_cg_variant(handle->inst, variant);
 }
 
+extern "C" int pfgb_host_register(void* ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return set_error(PFGB_EINVAL, "empty host range");
+  const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterPortable);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(PFGB_ECUDA, std::string("cudaHostRegister: ") + cudaGetErrorString(e));
+  }
+  return PFGB_OK;
+}
+
+extern "C" int pfgb_host_unregister(void* ptr) {
+  if (!ptr) return set_error(PFGB_EINVAL, "null host pointer");
+  const cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(PFGB_ECUDA, std::string("cudaHostUnregister: ") + cudaGetErrorString(e));
+  }
+  return PFGB_OK;
+}
+
 extern "C" int pfgb_set_persistent(pfgb_handle* handle, int on) {
   if (!handle) return set_error(PFGB_EINVAL, "null handle");
   return instance64_set_persistent(handle->inst, on);

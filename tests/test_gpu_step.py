@@ -138,6 +138,38 @@ def test_host_numpy_fields_are_updated_in_place():
         np.testing.assert_array_equal(host.fields[k], twin.fields[k])
 
 
+def test_host_fields_page_locked_in_place():
+    """Host NumPy fields of at least 1 MiB are page-locked in place and stepped through the
+    state's persistent device copies: same bits as a device-resident state, the same arrays
+    updated in place, and the registration released when the arrays are freed."""
+    import gc
+    from types import SimpleNamespace
+
+    from pyflow_solver_gb300 import ResidualManager, allocate_state
+    from pyflow_solver_gb300.core.ghost_fields import State
+    from pyflow_solver_gb300.solvers import fields as F
+    from pyflow_solver_gb300.solvers.solver import step
+    n = 384
+    cfg = SimpleNamespace(nx=n, ny=n, lx=1.0, ly=1.0, Re=400.0, lid_velocity=1.0, advection_scheme="quick",
+                          lin_tol=1e-8, lin_maxiter=300, diagnostics=False, precision="mixed")
+    host = State(n, n, {k: np.zeros((n + 2, n + 2)) for k in "uvp"})
+    arrs = dict(host.fields)
+    dev = allocate_state(n, n)
+    tr_h, tr_d = ResidualManager(), ResidualManager()
+    for it in range(3):
+        _, rh, dh = step(cfg, host, tr_h, it)
+        _, rd, dd = step(cfg, dev, tr_d, it)
+        assert rh == rd and dh == dd
+    ptrs = [a.__array_interface__["data"][0] for a in arrs.values()]
+    assert all(p in F._registered for p in ptrs)
+    for k in "uvp":
+        assert host.fields[k] is arrs[k]
+        np.testing.assert_array_equal(host.fields[k], dev.fields[k].cpu().numpy())
+    del host, arrs
+    gc.collect()
+    assert not any(p in F._registered for p in ptrs)
+
+
 def test_pressure_solver_standalone_matches_twin():
     from types import SimpleNamespace
 
