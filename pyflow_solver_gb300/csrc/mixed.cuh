@@ -30,11 +30,21 @@ struct Lvl {
   float* f;   // right-hand side (on level 0: the PCG residual)
 };
 
+// Relaxation weights of the multigrid smoother: the two sweeps before and after
+// each coarse correction are x += w D^-1 (f - A x) with w1 and w2 (the two roots of
+// the degree-2 Chebyshev polynomial on the upper part of the spectrum of D^-1 A);
+// wb is the weight of the damped-Jacobi sweeps of a bottom level without a
+// pseudo-inverse.
+struct Smooth {
+  float w1, w2, wb;
+};
+
 // binary64 geometry of the refinement
 struct Geo {
   int nx, ny;
   long ld;
   Grid2 g;
+  double rdx, rdy;             // 1/dx, 1/dy
 };
 
 struct MixCtrl {
@@ -105,6 +115,7 @@ struct Batch {
   int coarse_nt = 1024;                        // threads of the coarse CTA (512: two to an SM)
   MixLoop* loop = nullptr;
   int gmax_o = 1, gmax_i = 1;                  // trip bounds of the loop guards
+  Smooth sw = {0.8f, 0.8f, 0.8f};              // smoother weights
   // profiling (direct launches): events around each PCG matvec launch
   cudaEvent_t* ev = nullptr;
   int nev = 0;

@@ -92,6 +92,52 @@ def test_mixed_trajectory_stays_close():
         assert rel(interior_view(st.fields[k]).cpu().numpy(), ost.interior(tw.fields[k])) <= 1e-5, k
 
 
+def test_mixed_warm_start_and_fallback():
+    """The refinement starts from the state's pressure.  A guess worse than zero (noise, or a
+    NaN) falls back to the cold start and gives its bits exactly; a good guess (the pressure
+    of the previous step) gives the cold start's fields within the mixed tolerance."""
+    import torch
+
+    from pyflow_solver_gb300 import ResidualManager, SimulationDriver, allocate_state, interior_view, step
+    nx, ny = 96, 64
+    base = cavity(nx, ny, 600.0, 1.0, precision="mixed")
+    st0 = allocate_state(nx, ny)
+    for _ in SimulationDriver(base, st0, ResidualManager()).run(max_steps=6):
+        pass
+
+    def run(p_fill, warm):
+        st = allocate_state(nx, ny)
+        for k in "uvp":
+            st.fields[k].copy_(st0.fields[k])
+        if p_fill is not None:
+            p_fill(interior_view(st.fields["p"]))
+        st.meta = {"dt_prev": st0.meta["dt_prev"], "divergence_history": list(st0.meta["divergence_history"])}
+        cfg = SimpleNamespace(**vars(base), mixed_warm_start=warm)
+        _, res, diag = step(cfg, st, ResidualManager(), 6)
+        return [interior_view(st.fields[k]).cpu().numpy() for k in "uvp"], res, diag
+
+    g = torch.Generator(device="cpu").manual_seed(3)
+    noise = (1e3 * torch.randn(ny, nx, generator=g, dtype=torch.float64))
+
+    def fill_noise(pi):
+        pi.copy_(noise.to(pi.device))
+
+    def fill_nan(pi):
+        pi[ny // 2, nx // 3] = float("nan")
+
+    cold = run(None, False)
+    for fill in (fill_noise, fill_nan):
+        fb = run(fill, True)
+        for a, b in zip(cold[0], fb[0]):
+            np.testing.assert_array_equal(a, b)
+        assert fb[1] == cold[1] and fb[2] == cold[2]
+    warm = run(None, True)
+    assert warm[2]["Rp_converged"]
+    assert warm[2]["cg_iterations"] <= cold[2]["cg_iterations"]
+    for a, b in zip(warm[0], cold[0]):
+        assert rel(a, b) <= TOL
+
+
 def test_mixed_graph_and_direct_launches_agree():
     """The graph (device-side loop control) and the host-driven direct form give the same bits."""
     from pyflow_solver_gb300 import ResidualManager, SimulationDriver, allocate_state, interior_view
