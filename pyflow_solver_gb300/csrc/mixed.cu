@@ -1273,15 +1273,17 @@ static void neumann_pinv(int nx, int ny, double cx, double cy, std::vector<float
 // The smoother: the error of a sweep x += w D^-1 (f - A x) is multiplied by
 // (1 - w lambda) on each eigenvalue lambda of D^-1 A, which lies in [0, 2] for these
 // operators.  Two sweeps with w = 1 / the roots of the degree-2 Chebyshev polynomial
-// of [0.5, 2] -- the modes a coarse level cannot represent -- multiply them by at
-// most 1 / T2(5/3) = 0.22, against 0.36 for two damped-Jacobi sweeps with w = 0.8.
-// The factors commute, so the sweeps after the coarse correction (in reverse
-// order) are the adjoint of those before and the V-cycle stays symmetric.
-// PFGB_MG_SMOOTHER=jacobi selects the damped-Jacobi pair, cheb:<a> the Chebyshev
-// pair of [a, 2].
+// of [a, 2] bound that product by 1 / T2((2 + a) / (2 - a)) on [a, 2]: 0.22 on
+// [0.5, 2], where the modes that full coarsening cannot represent lie, against 0.36
+// for two damped-Jacobi sweeps with w = 0.8.  a = 0.4 (0.29 on [0.4, 2], more damping
+// of the modes just below) took the fewest iterations over the 512^2, 2048^2 and
+// batched cavities (a from 0.3 to 0.75 measured).  The factors commute, so the sweeps
+// after the coarse correction (in reverse order) are the adjoint of those before and
+// the V-cycle stays symmetric.  PFGB_MG_SMOOTHER=jacobi selects the damped-Jacobi
+// pair, cheb:<a> the Chebyshev pair of [a, 2].
 static Smooth make_smoother() {
   Smooth s = {0.8f, 0.8f, 0.8f};
-  double a = 0.5;
+  double a = 0.4;
   if (const char* ev = std::getenv("PFGB_MG_SMOOTHER")) {
     const std::string v(ev);
     if (v == "jacobi") return s;
