@@ -68,6 +68,42 @@ __device__ __forceinline__ float mg_nsum(const Lvl& L, int j, int i, F at) {
   return s;
 }
 
+// The interior forms of the tile phases.  A tile whose region with a halo of h
+// cells keeps at least one cell away from every wall has no wall cell in it:
+// every cell has four neighbours, the full diagonal and, on a coarsened axis,
+// both parents.  Those forms run the per-cell arithmetic of the general form
+// operation for operation (the diagonal summed in the same order, the same fma
+// chains), so both give the same bits; what goes is the per-cell wall logic.
+__device__ __forceinline__ bool tile_interior(const MTile& tl, int nx, int ny, int h) {
+  return tl.i0 - h >= 1 && tl.j0 - h >= 1 && tl.i0 + BX + h <= nx - 1 && tl.j0 + BY + h <= ny - 1;
+}
+
+// the diagonal of a cell with four neighbours, summed as mg_diag sums it
+__device__ __forceinline__ float mg_diag_in(const Lvl& L) {
+  float d = 0.f;
+  d += L.cx;
+  d += L.cx;
+  d += L.cy;
+  d += L.cy;
+  return d;
+}
+
+template <bool IN>
+__device__ __forceinline__ float lv_diag(const Lvl& L, float din, int j, int i) {
+  return IN ? din : mg_diag(L, j, i);
+}
+
+template <bool IN, typename F>
+__device__ __forceinline__ float lv_nsum(const Lvl& L, int j, int i, F at) {
+  if (!IN) return mg_nsum(L, j, i, at);
+  float s = 0.f;
+  s = fmaf(L.cx, at(j, i - 1), s);
+  s = fmaf(L.cx, at(j, i + 1), s);
+  s = fmaf(L.cy, at(j - 1, i), s);
+  s = fmaf(L.cy, at(j + 1, i), s);
+  return s;
+}
+
 // Bilinear prolongation along each coarsened axis (3/4 parent + 1/4 neighbour,
 // all of the parent at a wall; an axis that is not coarsened (factor 1) is
 // copied) and its transpose.  A level may halve both axes or, for cells much
@@ -141,6 +177,55 @@ __device__ __forceinline__ float restrict_val(const float* w, long ld, int j0, i
   return restrict_k<1, 2>(w, ld, j0, i0, nx, ny, J, I);
 }
 
+// prolong_k and restrict_k for cells away from the walls (both parents, weights
+// 3/4 and 1/4 on a coarsened axis), in the same operation order
+template <int KX, int KY, class AT>
+__device__ __forceinline__ float prolong_k_in(AT at, int j, int i) {
+  const int I = KX == 2 ? (i >> 1) : i, I2 = KX == 2 ? ((i & 1) ? I + 1 : I - 1) : i;
+  const int J = KY == 2 ? (j >> 1) : j, J2 = KY == 2 ? ((j & 1) ? J + 1 : J - 1) : j;
+  const float wx = KX == 2 ? 0.75f : 1.f, wy = KY == 2 ? 0.75f : 1.f;
+  float v = wx * wy * at(J, I);
+  if (KX == 2) v = fmaf(0.25f * wy, at(J, I2), v);
+  if (KY == 2) v = fmaf(wx * 0.25f, at(J2, I), v);
+  if (KX == 2 && KY == 2) v = fmaf(0.25f * 0.25f, at(J2, I2), v);
+  return v;
+}
+
+template <bool IN, class AT>
+__device__ __forceinline__ float prolong_lv(AT at, int nx, int ny, int kx, int ky, int j, int i) {
+  if (!IN) return prolong_val(at, nx, ny, kx, ky, j, i);
+  if (kx == 2 && ky == 2) return prolong_k_in<2, 2>(at, j, i);
+  if (kx == 2) return prolong_k_in<2, 1>(at, j, i);
+  return prolong_k_in<1, 2>(at, j, i);
+}
+
+template <int KX, int KY>
+__device__ __forceinline__ float restrict_k_in(const float* w, long ld, int j0, int i0, int J, int I) {
+  float s = 0.f;
+#pragma unroll
+  for (int dj = (KY == 2 ? -1 : 0); dj <= (KY == 2 ? 2 : 0); ++dj) {
+    const float wy = KY == 2 ? ((dj == -1 || dj == 2) ? 0.25f : 0.75f) : 1.f;
+    const int j = KY * J + dj;
+    float row = 0.f;
+#pragma unroll
+    for (int di = (KX == 2 ? -1 : 0); di <= (KX == 2 ? 2 : 0); ++di) {
+      const float wx = KX == 2 ? ((di == -1 || di == 2) ? 0.25f : 0.75f) : 1.f;
+      row = fmaf(wx, w[(long)(j - j0) * ld + (KX * I + di - i0)], row);
+    }
+    s = fmaf(wy, row, s);
+  }
+  return s;
+}
+
+template <bool IN>
+__device__ __forceinline__ float restrict_lv(const float* w, long ld, int j0, int i0, int nx, int ny, int kx, int ky,
+                                             int J, int I) {
+  if (!IN) return restrict_val(w, ld, j0, i0, nx, ny, kx, ky, J, I);
+  if (kx == 2 && ky == 2) return restrict_k_in<2, 2>(w, ld, j0, i0, J, I);
+  if (kx == 2) return restrict_k_in<2, 1>(w, ld, j0, i0, J, I);
+  return restrict_k_in<1, 2>(w, ld, j0, i0, J, I);
+}
+
 // ---- phases ---------------------------------------------------------------
 //
 // Each phase function processes one 32 x 32 tile of one instance, written once
@@ -209,6 +294,7 @@ struct PostSmem {
   float w0[BY + 4][BX + 4];
   float w1[BY + 2][BX + 2];
   float sf[BY + 2][BX + 2];             // f on the 1-cell halo
+  float cs[BY + 6][BX + 6];             // the coarse values the tile's prolongation reads
   RedSmem rsm;
 };
 struct MatvecSmem {
@@ -223,21 +309,22 @@ union TileSmem;
 // The tile computes the first sweep on a 3-cell halo, t on 2 and r on 1, so
 // every coarse cell whose fine patch lies in the tile is complete; only t
 // goes back to memory (the up-sweep needs it).
-template <class X>
-__device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTile& tl, int l, Smooth sw,
+template <bool IN, class X>
+__device__ __forceinline__ void ph_down_t(const X& x, const MixDesc& M, const MTile& tl, int l, Smooth sw,
                                         DownSmem& sm) {
   Lvl L = M.lev[l];
   const Lvl C = M.lev[l + 1];
   if (l == 0) L.f = f_cur(M);
   const int i0 = tl.i0, j0 = tl.j0;
-  auto inside = [&](int gj, int gi) { return gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx; };
+  const float din = mg_diag_in(L);
+  auto inside = [&](int gj, int gi) { return IN || (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx); };
   for (int idx = x.tid(); idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
     const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
     const int gj = j0 + jj, gi = i0 + ii;
     float f = 0.f, v = 0.f;
     if (inside(gj, gi)) {
       f = x.ld(L.f + (long)gj * L.ld + gi);
-      v = __fdividef(sw.w1 * f, mg_diag(L, gj, gi));
+      v = __fdividef(sw.w1 * f, lv_diag<IN>(L, din, gj, gi));
     }
     sm.sf[jj + H3][ii + H3] = f;
     sm.s1[jj + H3][ii + H3] = v;
@@ -250,7 +337,7 @@ __device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTil
     if (inside(gj, gi)) {
       auto at = [&](int j, int i) { return sm.s1[j - j0 + H3][i - i0 + H3]; };
       v = fmaf(1.f - sw.w2, sm.s1[jj + H3][ii + H3],
-               __fdividef(sw.w2 * (sm.sf[jj + H3][ii + H3] + mg_nsum(L, gj, gi, at)), mg_diag(L, gj, gi)));
+               __fdividef(sw.w2 * (sm.sf[jj + H3][ii + H3] + lv_nsum<IN>(L, gj, gi, at)), lv_diag<IN>(L, din, gj, gi)));
     }
     sm.s2[jj + 2][ii + 2] = v;
   }
@@ -262,7 +349,7 @@ __device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTil
     if (inside(gj, gi)) {
       auto at = [&](int j, int i) { return sm.s2[j - j0 + 2][i - i0 + 2]; };
       const float t = sm.s2[jj + 2][ii + 2];
-      v = sm.sf[jj + H3][ii + H3] - (mg_diag(L, gj, gi) * t - mg_nsum(L, gj, gi, at));
+      v = sm.sf[jj + H3][ii + H3] - (lv_diag<IN>(L, din, gj, gi) * t - lv_nsum<IN>(L, gj, gi, at));
       if (jj >= 0 && jj < BY && ii >= 0 && ii < BX) L.t[(long)gj * L.ld + gi] = t;
     }
     sm.rs[jj + 1][ii + 1] = v;
@@ -275,44 +362,67 @@ __device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTil
     const int jj = idx / cw, ii = idx - jj * cw;
     const int I = I0 + ii, J = J0 + jj;
     // sm.rs holds r at fine rows j0 - 1 .. j0 + BY and columns i0 - 1 .. i0 + BX
-    if (I < C.nx && J < C.ny)
-      C.f[(long)J * C.ld + I] = restrict_val(&sm.rs[0][0], BX + 2, j0 - 1, i0 - 1, C.nx, C.ny, L.kx, L.ky, J, I);
+    if (IN || (I < C.nx && J < C.ny))
+      C.f[(long)J * C.ld + I] = restrict_lv<IN>(&sm.rs[0][0], BX + 2, j0 - 1, i0 - 1, C.nx, C.ny, L.kx, L.ky, J, I);
   }
 }
 
-// u_l = S(S(t_l + P u_{l+1})) with the bilinear P; on level 0 also rho = r.z
 template <class X>
-__device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTile& tl, int l, Smooth sw,
+__device__ __forceinline__ void ph_down(const X& x, const MixDesc& M, const MTile& tl, int l, Smooth sw,
+                                        DownSmem& sm) {
+  if (M.interior && tile_interior(tl, M.lev[l].nx, M.lev[l].ny, H3)) ph_down_t<true>(x, M, tl, l, sw, sm);
+  else ph_down_t<false>(x, M, tl, l, sw, sm);
+}
+
+// u_l = S(S(t_l + P u_{l+1})) with the bilinear P; on level 0 also rho = r.z
+template <bool IN, class X>
+__device__ __forceinline__ void ph_post_t(const X& x, const MixDesc& M, const MTile& tl, int l, Smooth sw,
                                         PostSmem& sm) {
   Lvl F = M.lev[l];
   const Lvl C = M.lev[l + 1];
   if (l == 0) F.f = f_cur(M);
   RedSmem& rsm = sm.rsm;
   const int i0 = tl.i0, j0 = tl.j0;
-  const float* cu = C.u;
-  const long cld = C.ld;
-  auto cat = [&x, cu, cld](int J, int I) { return x.ld(cu + (long)J * cld + I); };
+  const float din = mg_diag_in(F);
+  // every global load first (t on the 2-cell halo, f on 1, the coarse patch the
+  // prolongation reads: its parents of fine cells i0-2 .. i0+BX+1, at most 38 x 38),
+  // then the prolongation from shared memory
+  const int Ilo = max(0, max(0, i0 - 2) / F.kx - 1), Ihi = min(C.nx - 1, (i0 + BX + 1) / F.kx + 1);
+  const int Jlo = max(0, max(0, j0 - 2) / F.ky - 1), Jhi = min(C.ny - 1, (j0 + BY + 1) / F.ky + 1);
+  const int cw = Ihi - Ilo + 1, ch = Jhi - Jlo + 1;
   for (int idx = x.tid(); idx < (BY + 4) * (BX + 4); idx += MT) {
     const int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
     const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f, f = 0.f;
-    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) {
+    if (IN || (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx)) {
       const long o = (long)gj * F.ld + gi;
-      v = x.ld(F.t + o) + prolong_val(cat, C.nx, C.ny, F.kx, F.ky, gj, gi);
+      v = x.ld(F.t + o);
       if (jj >= -1 && jj <= BY && ii >= -1 && ii <= BX) f = x.ld(F.f + o);
     }
     sm.w0[jj + 2][ii + 2] = v;
     if (jj >= -1 && jj <= BY && ii >= -1 && ii <= BX) sm.sf[jj + 1][ii + 1] = f;
+  }
+  for (int idx = x.tid(); idx < cw * ch; idx += MT) {
+    const int r = idx / cw, c = idx - r * cw;
+    sm.cs[r][c] = x.ld(C.u + (long)(Jlo + r) * C.ld + Ilo + c);
+  }
+  x.sync();
+  auto cat = [&sm, Ilo, Jlo](int J, int I) { return sm.cs[J - Jlo][I - Ilo]; };
+  for (int idx = x.tid(); idx < (BY + 4) * (BX + 4); idx += MT) {
+    const int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
+    const int gj = j0 + jj, gi = i0 + ii;
+    if (IN || (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx))
+      sm.w0[jj + 2][ii + 2] = sm.w0[jj + 2][ii + 2] + prolong_lv<IN>(cat, C.nx, C.ny, F.kx, F.ky, gj, gi);
   }
   x.sync();
   for (int idx = x.tid(); idx < (BY + 2) * (BX + 2); idx += MT) {
     const int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
     const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx) {
+    if (IN || (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx)) {
       auto at = [&](int j, int i) { return sm.w0[j - j0 + 2][i - i0 + 2]; };
-      const float d = mg_diag(F, gj, gi);
-      v = fmaf(1.f - sw.w2, sm.w0[jj + 2][ii + 2], __fdividef(sw.w2 * (sm.sf[jj + 1][ii + 1] + mg_nsum(F, gj, gi, at)), d));
+      const float d = lv_diag<IN>(F, din, gj, gi);
+      v = fmaf(1.f - sw.w2, sm.w0[jj + 2][ii + 2], __fdividef(sw.w2 * (sm.sf[jj + 1][ii + 1] + lv_nsum<IN>(F, gj, gi, at)), d));
     }
     sm.w1[jj + 1][ii + 1] = v;
   }
@@ -321,11 +431,11 @@ __device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTil
   FF acc[1] = {{0.f, 0.f}};
   MX_ROWS_X({
     const int gi = i0 + tx, gj = j0 + ty;
-    if (gi < F.nx && gj < F.ny) {
+    if (IN || (gi < F.nx && gj < F.ny)) {
       auto at = [&](int j, int i) { return sm.w1[j - j0 + 1][i - i0 + 1]; };
-      const float d = mg_diag(F, gj, gi);
+      const float d = lv_diag<IN>(F, din, gj, gi);
       const float fv = sm.sf[ty + 1][tx + 1];
-      const float v = fmaf(1.f - sw.w1, sm.w1[ty + 1][tx + 1], __fdividef(sw.w1 * (fv + mg_nsum(F, gj, gi, at)), d));
+      const float v = fmaf(1.f - sw.w1, sm.w1[ty + 1][tx + 1], __fdividef(sw.w1 * (fv + lv_nsum<IN>(F, gj, gi, at)), d));
       F.u[(long)gj * F.ld + gi] = v;
       if (l == 0) ff_add_prod(acc[0], fv, v);
     }
@@ -335,6 +445,13 @@ __device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTil
     double out[1];
     if (X_RED_FF(1, acc, out) && x.tid() == 0) set_rho(M.ctrl, out[0]);
   }
+}
+
+template <class X>
+__device__ __forceinline__ void ph_post(const X& x, const MixDesc& M, const MTile& tl, int l, Smooth sw,
+                                        PostSmem& sm) {
+  if (M.interior && tile_interior(tl, M.lev[l].nx, M.lev[l].ny, 2)) ph_post_t<true>(x, M, tl, l, sw, sm);
+  else ph_post_t<false>(x, M, tl, l, sw, sm);
 }
 
 // -A x at a cell k != 0 of the refinement's operator: the reference's coherent
@@ -468,8 +585,8 @@ __device__ __forceinline__ void ph_prep(const X& x, const MixDesc& M, const MTil
 }
 
 // p_new = z (first) or z + beta p_old; q = A p_new (binary32 Neumann operator); p.q
-template <class X>
-__device__ __forceinline__ void ph_matvec(const X& x, const MixDesc& M, const MTile& tl, MatvecSmem& sm) {
+template <bool IN, class X>
+__device__ __forceinline__ void ph_matvec_t(const X& x, const MixDesc& M, const MTile& tl, MatvecSmem& sm) {
   RedSmem& rsm = sm.rsm;
   const Lvl L0 = M.lev[0];
   MixCtrl* ctrl = M.ctrl;
@@ -479,11 +596,12 @@ __device__ __forceinline__ void ph_matvec(const X& x, const MixDesc& M, const MT
   float* pnew = (k & 1) ? M.p0 : M.p1;
   const float beta = (float)cget(&ctrl->beta);
   const int i0 = tl.i0, j0 = tl.j0;
+  const float din = mg_diag_in(L0);
   for (int idx = x.tid(); idx < (BY + 2) * (BX + 2); idx += MT) {
     const int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
     const int gj = j0 + jj, gi = i0 + ii;
     float v = 0.f;
-    if (gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx) {
+    if (IN || (gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx)) {
       const long o = (long)gj * L0.ld + gi;
       v = (k == 0) ? x.ld(z + o) : fmaf(beta, x.ld(pold + o), x.ld(z + o));
     }
@@ -496,10 +614,10 @@ __device__ __forceinline__ void ph_matvec(const X& x, const MixDesc& M, const MT
   double out[1];
   MX_ROWS_X({
     const int gj = j0 + ty;
-    if (gi < L0.nx && gj < L0.ny) {
+    if (IN || (gi < L0.nx && gj < L0.ny)) {
       auto at = [&](int j, int i) { return sm.pn[j - j0 + 1][i - i0 + 1]; };
       const float pv = sm.pn[ty + 1][tx + 1];
-      const float qv = mg_diag(L0, gj, gi) * pv - mg_nsum(L0, gj, gi, at);
+      const float qv = lv_diag<IN>(L0, din, gj, gi) * pv - lv_nsum<IN>(L0, gj, gi, at);
       const long o = (long)gj * L0.ld + gi;
       pnew[o] = pv;
       M.q[o] = qv;
@@ -512,6 +630,12 @@ __device__ __forceinline__ void ph_matvec(const X& x, const MixDesc& M, const MT
   }
 }
 
+template <class X>
+__device__ __forceinline__ void ph_matvec(const X& x, const MixDesc& M, const MTile& tl, MatvecSmem& sm) {
+  if (M.interior && tile_interior(tl, M.lev[0].nx, M.lev[0].ny, 1)) ph_matvec_t<true>(x, M, tl, sm);
+  else ph_matvec_t<false>(x, M, tl, sm);
+}
+
 // e += alpha p; r -= alpha q (from residual buffer k & 1 into buffer (k + 1) & 1);
 // ||r||^2 and the inner stopping test; then, for an instance with a level below,
 // the fused down-sweep of level 0 on the new residual (its 3-cell halo formed
@@ -522,8 +646,8 @@ struct UpdDownSmem {
   RedSmem rsm;
 };
 
-template <class X>
-__device__ __forceinline__ void ph_update_down(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml,
+template <bool IN, class X>
+__device__ __forceinline__ void ph_update_down_t(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml,
                                                cudaGraphConditionalHandle cond_inner, int use_cond, Smooth sw,
                                                UpdDownSmem& sm) {
   RedSmem& rsm = sm.rsm;
@@ -574,7 +698,8 @@ __device__ __forceinline__ void ph_update_down(const X& x, const MixDesc& M, con
   if (M.nlev < 2) return;
   // the new residual on the tile and a 3-cell halo, then the down-sweep as ph_down
   const int i0 = tl.i0, j0 = tl.j0;
-  auto inside = [&](int gj, int gi) { return gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx; };
+  const float din = mg_diag_in(L0);
+  auto inside = [&](int gj, int gi) { return IN || (gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx); };
   for (int idx = x.tid(); idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
     const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
     const int gj = j0 + jj, gi = i0 + ii;
@@ -593,7 +718,7 @@ __device__ __forceinline__ void ph_update_down(const X& x, const MixDesc& M, con
     const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
     const int gj = j0 + jj, gi = i0 + ii;
     float s1 = 0.f;
-    if (inside(gj, gi)) s1 = __fdividef(sw.w1 * fval(gj, gi), mg_diag(L0, gj, gi));
+    if (inside(gj, gi)) s1 = __fdividef(sw.w1 * fval(gj, gi), lv_diag<IN>(L0, din, gj, gi));
     d.s1[jj + H3][ii + H3] = s1;
   }
   x.sync();
@@ -604,7 +729,7 @@ __device__ __forceinline__ void ph_update_down(const X& x, const MixDesc& M, con
     if (inside(gj, gi)) {
       auto at = [&](int j, int i) { return d.s1[j - j0 + H3][i - i0 + H3]; };
       s2 = fmaf(1.f - sw.w2, d.s1[jj + H3][ii + H3],
-                __fdividef(sw.w2 * (fval(gj, gi) + mg_nsum(L0, gj, gi, at)), mg_diag(L0, gj, gi)));
+                __fdividef(sw.w2 * (fval(gj, gi) + lv_nsum<IN>(L0, gj, gi, at)), lv_diag<IN>(L0, din, gj, gi)));
     }
     d.s2[jj + 2][ii + 2] = s2;
   }
@@ -616,7 +741,7 @@ __device__ __forceinline__ void ph_update_down(const X& x, const MixDesc& M, con
     if (inside(gj, gi)) {
       auto at = [&](int j, int i) { return d.s2[j - j0 + 2][i - i0 + 2]; };
       const float t = d.s2[jj + 2][ii + 2];
-      rr = fval(gj, gi) - (mg_diag(L0, gj, gi) * t - mg_nsum(L0, gj, gi, at));
+      rr = fval(gj, gi) - (lv_diag<IN>(L0, din, gj, gi) * t - lv_nsum<IN>(L0, gj, gi, at));
       if (jj >= 0 && jj < BY && ii >= 0 && ii < BX) L0.t[(long)gj * L0.ld + gi] = t;
     }
     d.rs[jj + 1][ii + 1] = rr;
@@ -627,9 +752,17 @@ __device__ __forceinline__ void ph_update_down(const X& x, const MixDesc& M, con
   for (int idx = x.tid(); idx < cw * chh; idx += MT) {
     const int jj = idx / cw, ii = idx - jj * cw;
     const int I = I0 + ii, J = J0 + jj;
-    if (I < C.nx && J < C.ny)
-      C.f[(long)J * C.ld + I] = restrict_val(&d.rs[0][0], BX + 2, j0 - 1, i0 - 1, C.nx, C.ny, L0.kx, L0.ky, J, I);
+    if (IN || (I < C.nx && J < C.ny))
+      C.f[(long)J * C.ld + I] = restrict_lv<IN>(&d.rs[0][0], BX + 2, j0 - 1, i0 - 1, C.nx, C.ny, L0.kx, L0.ky, J, I);
   }
+}
+
+template <class X>
+__device__ __forceinline__ void ph_update_down(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml,
+                                               cudaGraphConditionalHandle cond_inner, int use_cond, Smooth sw,
+                                               UpdDownSmem& sm) {
+  if (M.interior && tile_interior(tl, M.lev[0].nx, M.lev[0].ny, H3)) ph_update_down_t<true>(x, M, tl, ml, cond_inner, use_cond, sw, sm);
+  else ph_update_down_t<false>(x, M, tl, ml, cond_inner, use_cond, sw, sm);
 }
 
 union TileSmem {
@@ -992,7 +1125,7 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD
   ph_matvec(x, M, tl, sm);
 }
 
-__global__ void __launch_bounds__(MT) k_mx_update_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
+__global__ void __launch_bounds__(MT, 5) k_mx_update_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                         MixLoop* ml, cudaGraphConditionalHandle cond_inner, int use_cond,
                                                         Smooth sw) {
   pdl_enter();
@@ -1354,6 +1487,10 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   char* c = B->ws;
   auto take = [&](size_t b) { char* r = c; c += up(b); return r; };
   int gmax_i = 1, gmax_o = 1;
+  // PFGB_TILE_INTERIOR=0 sends every tile through the general phase forms (the
+  // interior forms give the same bits; the switch lets that be checked)
+  const char* tiv = std::getenv("PFGB_TILE_INTERIOR");
+  const int interior = (tiv && std::string(tiv) == "0") ? 0 : 1;
   for (int k = 0; k < n; ++k) {
     MixDesc& M = B->hd[k];
     M.G.nx = prm[k].nx;
@@ -1396,6 +1533,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     M.q = (float*)take(v0);
     M.r64 = (double*)take((size_t)prm[k].ld64 * prm[k].ny * sizeof(double));
     M.nt0 = ((prm[k].nx + BX - 1) / BX) * ((prm[k].ny + BY - 1) / BY);
+    M.interior = interior;
     M.part = (double*)take(MAX_RED * (size_t)M.nt0 * sizeof(double));
     M.ticket = (unsigned*)take(sizeof(unsigned));
     M.ctrl = (MixCtrl*)take(sizeof(MixCtrl));

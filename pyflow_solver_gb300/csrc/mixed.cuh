@@ -91,6 +91,7 @@ struct MixDesc {
   const int* active;           // the step's per-instance activity flag
   int maxiter_report;
   int nt0;                     // tiles of level 0 (= tiles of the binary64 grid)
+  int interior;                // tiles away from the walls take the interior forms of the phases
 };
 
 // Batch-wide control of the two WHILE loops.
