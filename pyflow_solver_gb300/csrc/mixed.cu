@@ -474,12 +474,11 @@ __device__ __forceinline__ double lap_recip_at(V p, int j, int i, const Geo& G) 
   return __dadd_rn(xp, yp);
 }
 
-// the previous pressure shifted to x[0] = 0 (the pinned cell), as a 2-D view
-struct ShiftView {
+// the previous pressure as a 2-D view (loads through L2)
+struct PrevView {
   const double* p;
   long ld;
-  double s;
-  __device__ __forceinline__ double operator()(int j, int i) const { return __dsub_rn(__ldcg(p + (long)j * ld + i), s); }
+  __device__ __forceinline__ double operator()(int j, int i) const { return __ldcg(p + (long)j * ld + i); }
 };
 
 // b -= mean(b), b[0] = 0 (pressure_solver.py:127-128, the mean from the exactly
@@ -496,7 +495,8 @@ __device__ __forceinline__ void ph_init(const X& x, const MixDesc& M, const MTil
   const double mean = __ddiv_rn(cget(M.bsum), M.n_cells);
   const bool warm = cget(&ctrl->warm) != 0;
   const double* P = warm ? *M.pprev : nullptr;
-  const ShiftView Xv{P, M.ldp, P ? __ldcg(P) : 0.0};
+  const PrevView Pv{P, M.ldp};
+  const double p0 = P ? __ldcg(P) : 0.0;
   const int i = tl.i0 + (x.tid() & 31);
   double v[4] = {0.0, 0.0, 0.0, 0.0}, out[4];
   MX_ROWS_X({
@@ -508,8 +508,10 @@ __device__ __forceinline__ void ph_init(const X& x, const MixDesc& M, const MTil
       v[0] += bv * bv;
       v[1] += bv;
       if (P) {
-        const double xv = Xv(j, i);
-        const double ax = (i == 0 && j == 0) ? xv : -lap_recip_at(Xv, j, i, G);
+        // x0 = p - p[0]; A x0 = -lap(p) away from the pinned cell (differences do not see the
+        // shift, up to a rounding the refinement's own residual corrects)
+        const double xv = __dsub_rn(Pv(j, i), p0);
+        const double ax = (i == 0 && j == 0) ? xv : -lap_recip_at(Pv, j, i, G);
         const double rv = __dsub_rn(bv, ax);
         M.x[o] = xv;
         M.r64[o] = rv;
@@ -879,17 +881,19 @@ __device__ __forceinline__ float c_nsum(const CLvl& L, const float* a, int j, in
       __VA_ARGS__                                                    \
     }
 
-// one damped-Jacobi sweep src -> dst on level L (all threads; ends with a barrier)
+// one weighted-Jacobi sweep src -> dst on level L (all threads; ends with a barrier);
+// dg holds every cell's diagonal
 template <int NT>
-__device__ __forceinline__ void c_sweep(const CLvl& L, const float* f, const float* src, float* dst, float omega) {
+__device__ __forceinline__ void c_sweep(const CLvl& L, const float* dg, const float* f, const float* src, float* dst,
+                                        float omega) {
   C_FOR(L, {
     dst[L.off + c] = fmaf(1.f - omega, src[L.off + c],
-                          __fdividef(omega * (f[L.off + c] + c_nsum(L, src, j, i)), c_diag(L, j, i)));
+                          __fdividef(omega * (f[L.off + c] + c_nsum(L, src, j, i)), dg[L.off + c]));
   })
   __syncthreads();
 }
 
-// The coarse V-cycle of instance M by the whole NT-thread CTA; sm: 3 x (its
+// The coarse V-cycle of instance M by the whole NT-thread CTA; sm: 4 x (its
 // levels' cells) floats of shared memory.
 template <int NT>
 __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, float* sm) {
@@ -920,24 +924,30 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
   float* rh = sm;            // right-hand side of every level (level 0: the entry level's f)
   float* e = sm + tot;       // pre-smoothed iterate on the way down; the bottom solution
   float* w = sm + 2 * tot;   // residual on the way down; each level's result on the way up
+  float* dg = sm + 3 * tot;  // every cell's diagonal, formed once
   C_FOR(L[0], { rh[c] = __ldcg(C.f + (long)j * C.ld + i); })
+  for (int l = 0; l < nl; ++l) {
+    const CLvl& Lv = L[l];
+    C_FOR(Lv, { dg[Lv.off + c] = c_diag(Lv, j, i); })
+  }
   __syncthreads();
   for (int l = 0; l + 1 < nl; ++l) {
     const CLvl& Lv = L[l];
     const float* r = rh + Lv.off;
     // e = S(S(0)); the first sweep from zero is pointwise (w1 rh / d) and is folded into the second
     C_FOR(Lv, {
-      auto s1 = [&](int jj, int ii) { return __fdividef(sw.w1 * r[jj * Lv.nx + ii], c_diag(Lv, jj, ii)); };
+      const float* dl = dg + Lv.off;
+      auto s1 = [&](int jj, int ii) { return __fdividef(sw.w1 * r[jj * Lv.nx + ii], dl[jj * Lv.nx + ii]); };
       float ns = 0.f;
       if (i > 0) ns = fmaf(Lv.cx, s1(j, i - 1), ns);
       if (i < Lv.nx - 1) ns = fmaf(Lv.cx, s1(j, i + 1), ns);
       if (j > 0) ns = fmaf(Lv.cy, s1(j - 1, i), ns);
       if (j < Lv.ny - 1) ns = fmaf(Lv.cy, s1(j + 1, i), ns);
-      e[Lv.off + c] = fmaf(1.f - sw.w2, s1(j, i), __fdividef(sw.w2 * (r[c] + ns), c_diag(Lv, j, i)));
+      e[Lv.off + c] = fmaf(1.f - sw.w2, s1(j, i), __fdividef(sw.w2 * (r[c] + ns), dl[c]));
     })
     __syncthreads();
     // residual rh - A e of this level into w, then rh_{l+1} = P^T w
-    C_FOR(Lv, { w[Lv.off + c] = r[c] - (c_diag(Lv, j, i) * e[Lv.off + c] - c_nsum(Lv, e, j, i)); })
+    C_FOR(Lv, { w[Lv.off + c] = r[c] - (dg[Lv.off + c] * e[Lv.off + c] - c_nsum(Lv, e, j, i)); })
     __syncthreads();
     const CLvl& Cv = L[l + 1];
     C_FOR(Cv, { rh[Cv.off + c] = restrict_val(w + Lv.off, Lv.nx, 0, 0, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i); })
@@ -980,7 +990,7 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
     } else {
       C_FOR(Lv, { e[Lv.off + c] = 0.f; })
       __syncthreads();
-      for (int q = 0; q < bottom_sweeps; ++q) c_sweep<NT>(Lv, rh, (q & 1) ? w : e, (q & 1) ? e : w, sw.wb);
+      for (int q = 0; q < bottom_sweeps; ++q) c_sweep<NT>(Lv, dg, rh, (q & 1) ? w : e, (q & 1) ? e : w, sw.wb);
       if (bottom_sweeps & 1) {
         C_FOR(Lv, { e[Lv.off + c] = w[Lv.off + c]; })
         __syncthreads();
@@ -999,8 +1009,8 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
       w[Lv.off + c] = e[Lv.off + c] + prolong_val(catc, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i);
     })
     __syncthreads();
-    c_sweep<NT>(Lv, rh, w, e, sw.w2);
-    c_sweep<NT>(Lv, rh, e, w, sw.w1);
+    c_sweep<NT>(Lv, dg, rh, w, e, sw.w2);
+    c_sweep<NT>(Lv, dg, rh, e, w, sw.w1);
   }
   const float* z = (nl == 1) ? e : w;
   C_FOR(L[0], { C.u[(long)j * C.ld + i] = z[c]; })
@@ -1455,7 +1465,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
       return set_error(PFGB_EINVAL, "mixed solver: the coarse multigrid level would exceed 4096 cells "
                                     "(nx and ny need enough factors of two)");
     }
-    smem = std::max(smem, (size_t)3 * plan[k].cta_tot * sizeof(float));
+    smem = std::max(smem, (size_t)4 * plan[k].cta_tot * sizeof(float));
     const PlanLvl& bot = plan[k].cta.back();
     if (bot.nx * bot.ny <= BMAX) bytes += up((size_t)bot.nx * bot.ny * bot.nx * bot.ny * sizeof(float));
     B->maxlev = std::max(B->maxlev, (int)plan[k].global.size());
