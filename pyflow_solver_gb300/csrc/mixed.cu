@@ -45,6 +45,8 @@ namespace pfgb {
 namespace mixed {
 
 constexpr int MT = 256;
+constexpr double REACH_REL = 3e-7;           // the first pass's deepest relative aim
+constexpr int REACH_WAIT = 8;                // steps before aiming again after a miss
 constexpr int BX = 32, BY = 32;              // a tile: 32 x 32 cells, each thread a column of 4
 constexpr int RPT = BY / (MT / 32);
 
@@ -554,13 +556,22 @@ __device__ __forceinline__ void ph_init(const X& x, const MixDesc& M, const MTil
 // r~ = float(r64) with r~_0 = -sum_{k != 0} r64_k; e = 0; ||r~||^2; starts an inner solve.
 // The first pass of a cold-marked solve takes r64 = b and resets x = 0 instead.
 // The inner solve stops at ||r_in|| <= max(tol_in ||r~||, tol_abs_out / 4): a
-// quarter of the outer target is as far as this pass needs to go.
+// quarter of the outer target is as far as this pass needs to go.  When the outer
+// target is within REACH_REL ||r~|| -- about as deep as binary32 corrections still
+// improve the binary64 residual -- the first pass of a solve may instead aim there
+// (or at the quarter, if higher): on a warm start that often finishes the solve in
+// one pass.  Whether it did is seen
+// at the end of the pass (ph_resid); an instance whose first pass aimed at the
+// target and missed it goes back to tol_in for REACH_WAIT steps, then tries
+// again, so grids too large for binary32 to get there lose at most an occasional
+// iteration.
 template <class X>
 __device__ __forceinline__ void ph_prep(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml, RedSmem& rsm) {
   const Geo G = M.G;
   const Lvl L0 = M.lev[0];
   MixCtrl* ctrl = M.ctrl;
-  const bool restart = cget(&ctrl->cold) != 0 && cget(&ctrl->outer) == 0;
+  const bool first = cget(&ctrl->outer) == 0;
+  const bool restart = cget(&ctrl->cold) != 0 && first;
   const double* rsrc = restart ? M.b : M.r64;
   const int i = tl.i0 + (x.tid() & 31);
   FF v[1] = {{0.f, 0.f}};
@@ -579,7 +590,10 @@ __device__ __forceinline__ void ph_prep(const X& x, const MixDesc& M, const MTil
   if (X_RED_FF(1, v, out) && x.tid() == 0) {
     const double rt = sqrt(out[0]);
     ctrl->rt_norm = rt;
-    ctrl->tol_abs_in = fmax(cget(&ctrl->tol_in) * rt, 0.25 * cget(&ctrl->tol_abs_out));
+    const double target = cget(&ctrl->tol_abs_out), quarter = 0.25 * target;
+    const bool reach = first && cget(&ctrl->reach) != 0 && REACH_REL * rt <= target;
+    ctrl->reach_tried = reach ? 1 : 0;
+    ctrl->tol_abs_in = reach ? fmax(REACH_REL * rt, quarter) : fmax(cget(&ctrl->tol_in) * rt, quarter);
     ctrl->inner = 0;
     ctrl->inner_done = rt > 0.0 ? 0 : 1;
     if (rt > 0.0) atomicAdd(&ml->inner_active, 1);
@@ -828,6 +842,19 @@ __device__ __forceinline__ void ph_resid(const X& x, const MixDesc& M, const MTi
     ctrl->outer = outer;
     const bool conv = !(sqrt(rr) > cget(&ctrl->tol_abs_out));
     ctrl->converged = conv ? 1 : 0;
+    if (outer == 1) {
+      // the first pass's outcome steers the next solves' first passes (ph_prep)
+      if (cget(&ctrl->reach_tried)) {
+        if (!conv) {
+          ctrl->reach = 0;
+          ctrl->reach_wait = REACH_WAIT;
+        }
+      } else if (!cget(&ctrl->reach)) {
+        const int w = cget(&ctrl->reach_wait) - 1;
+        ctrl->reach_wait = w;
+        if (w <= 0) ctrl->reach = 1;
+      }
+    }
     if (conv || outer >= cget(&ctrl->max_outer)) {
       ctrl->outer_done = 1;
       if (atomicSub(&ml->outer_active, 1) == 1 && use_cond) cudaGraphSetConditional(cond_outer, 0u);
@@ -881,20 +908,28 @@ __device__ __forceinline__ float c_nsum(const CLvl& L, const float* a, int j, in
       __VA_ARGS__                                                    \
     }
 
-// one weighted-Jacobi sweep src -> dst on level L (all threads; ends with a barrier);
-// dg holds every cell's diagonal
+// a cell's diagonal: from the table dg when the CTA keeps one (NT == CT), else formed
+template <int NT>
+__device__ __forceinline__ float c_dg(const CLvl& L, const float* dg, int c, int j, int i) {
+  if constexpr (NT == CT) return dg[L.off + c];
+  else return c_diag(L, j, i);
+}
+
+// one weighted-Jacobi sweep src -> dst on level L (all threads; ends with a barrier)
 template <int NT>
 __device__ __forceinline__ void c_sweep(const CLvl& L, const float* dg, const float* f, const float* src, float* dst,
                                         float omega) {
   C_FOR(L, {
     dst[L.off + c] = fmaf(1.f - omega, src[L.off + c],
-                          __fdividef(omega * (f[L.off + c] + c_nsum(L, src, j, i)), dg[L.off + c]));
+                          __fdividef(omega * (f[L.off + c] + c_nsum(L, src, j, i)), c_dg<NT>(L, dg, c, j, i)));
   })
   __syncthreads();
 }
 
 // The coarse V-cycle of instance M by the whole NT-thread CTA; sm: 4 x (its
-// levels' cells) floats of shared memory.
+// levels' cells) floats of shared memory for 1024 threads (with a table of the cells'
+// diagonals), 3 x for 512 (two CTAs to an SM; the diagonals formed where used, the
+// same values).
 template <int NT>
 __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, float* sm) {
   Lvl C = M.lev[M.nlev - 1];
@@ -924,11 +959,13 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
   float* rh = sm;            // right-hand side of every level (level 0: the entry level's f)
   float* e = sm + tot;       // pre-smoothed iterate on the way down; the bottom solution
   float* w = sm + 2 * tot;   // residual on the way down; each level's result on the way up
-  float* dg = sm + 3 * tot;  // every cell's diagonal, formed once
+  float* dg = sm + 3 * tot;  // every cell's diagonal, formed once (1024-thread CTAs)
   C_FOR(L[0], { rh[c] = __ldcg(C.f + (long)j * C.ld + i); })
-  for (int l = 0; l < nl; ++l) {
-    const CLvl& Lv = L[l];
-    C_FOR(Lv, { dg[Lv.off + c] = c_diag(Lv, j, i); })
+  if constexpr (NT == CT) {
+    for (int l = 0; l < nl; ++l) {
+      const CLvl& Lv = L[l];
+      C_FOR(Lv, { dg[Lv.off + c] = c_diag(Lv, j, i); })
+    }
   }
   __syncthreads();
   for (int l = 0; l + 1 < nl; ++l) {
@@ -936,18 +973,19 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
     const float* r = rh + Lv.off;
     // e = S(S(0)); the first sweep from zero is pointwise (w1 rh / d) and is folded into the second
     C_FOR(Lv, {
-      const float* dl = dg + Lv.off;
-      auto s1 = [&](int jj, int ii) { return __fdividef(sw.w1 * r[jj * Lv.nx + ii], dl[jj * Lv.nx + ii]); };
+      auto s1 = [&](int jj, int ii) {
+        return __fdividef(sw.w1 * r[jj * Lv.nx + ii], c_dg<NT>(Lv, dg, jj * Lv.nx + ii, jj, ii));
+      };
       float ns = 0.f;
       if (i > 0) ns = fmaf(Lv.cx, s1(j, i - 1), ns);
       if (i < Lv.nx - 1) ns = fmaf(Lv.cx, s1(j, i + 1), ns);
       if (j > 0) ns = fmaf(Lv.cy, s1(j - 1, i), ns);
       if (j < Lv.ny - 1) ns = fmaf(Lv.cy, s1(j + 1, i), ns);
-      e[Lv.off + c] = fmaf(1.f - sw.w2, s1(j, i), __fdividef(sw.w2 * (r[c] + ns), dl[c]));
+      e[Lv.off + c] = fmaf(1.f - sw.w2, s1(j, i), __fdividef(sw.w2 * (r[c] + ns), c_dg<NT>(Lv, dg, c, j, i)));
     })
     __syncthreads();
     // residual rh - A e of this level into w, then rh_{l+1} = P^T w
-    C_FOR(Lv, { w[Lv.off + c] = r[c] - (dg[Lv.off + c] * e[Lv.off + c] - c_nsum(Lv, e, j, i)); })
+    C_FOR(Lv, { w[Lv.off + c] = r[c] - (c_dg<NT>(Lv, dg, c, j, i) * e[Lv.off + c] - c_nsum(Lv, e, j, i)); })
     __syncthreads();
     const CLvl& Cv = L[l + 1];
     C_FOR(Cv, { rh[Cv.off + c] = restrict_val(w + Lv.off, Lv.nx, 0, 0, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i); })
@@ -1456,7 +1494,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   size_t bytes = 0;
   std::vector<Plan> plan(n);
-  size_t smem = 0;
+  size_t smem = 0, smem2 = 0;
   for (int k = 0; k < n; ++k) {
     plan[k] = make_plan(prm[k].nx, prm[k].ny, prm[k].dx, prm[k].dy);
     const PlanLvl& last = plan[k].global.back();
@@ -1466,6 +1504,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
                                     "(nx and ny need enough factors of two)");
     }
     smem = std::max(smem, (size_t)4 * plan[k].cta_tot * sizeof(float));
+    smem2 = std::max(smem2, (size_t)3 * plan[k].cta_tot * sizeof(float));
     const PlanLvl& bot = plan[k].cta.back();
     if (bot.nx * bot.ny <= BMAX) bytes += up((size_t)bot.nx * bot.ny * bot.nx * bot.ny * sizeof(float));
     B->maxlev = std::max(B->maxlev, (int)plan[k].global.size());
@@ -1572,6 +1611,8 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     hc.max_outer = prm[k].max_outer;
     hc.max_inner = prm[k].max_inner;
     hc.warm = prm[k].warm ? 1 : 0;
+    hc.reach = 1;
+    hc.reach_wait = 0;
     hc.inner_done = 1;
     hc.outer_done = 1;
     cudaMemcpy(M.ctrl, &hc, sizeof(MixCtrl), cudaMemcpyHostToDevice);
@@ -1600,15 +1641,26 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_mg_coarse<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_mg_coarse<CT2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k_mg_coarse<CT2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+  if (e == cudaSuccess) {
+    // two CTAs to an SM need most of its shared memory: ask for the largest carveout
+    if (cudaFuncSetAttribute(k_mg_coarse<CT2>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+      cudaGetLastError();
+  }
   if (e == cudaSuccess) {
     // more coarse CTAs than one wave of 1024-thread CTAs holds: 512-thread CTAs, two to an SM
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (n > sms && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mg_coarse<CT2>, CT2, smem) == cudaSuccess &&
-        occ >= 2)
+    if (n > sms && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mg_coarse<CT2>, CT2, smem2) == cudaSuccess &&
+        occ >= 2) {
       B->coarse_nt = CT2;
+      B->coarse_smem = smem2;
+    }
+    if (std::getenv("PFGB_GRAPH_DEBUG"))
+      std::fprintf(stderr, "pfgb mixed batch: %d instances, coarse CTA %d threads (%zu B shared, %d per SM at 512)\n", n,
+                   B->coarse_nt, B->coarse_smem, occ);
     cudaGetLastError();
   }
   if (e == cudaSuccess) {
@@ -1646,6 +1698,8 @@ int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer
   head.max_outer = max_outer;
   head.max_inner = max_inner;
   head.warm = warm ? 1 : 0;
+  head.reach = 1;
+  head.reach_wait = 0;
   // the leading fields up to bnorm; the rest of the control block is rewritten by every solve
   cudaError_t e = cudaMemcpy(B->hd[k].ctrl, &head, offsetof(MixCtrl, bnorm), cudaMemcpyHostToDevice);
   B->hd[k].maxiter_report = maxiter_report;

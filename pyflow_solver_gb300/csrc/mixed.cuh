@@ -51,12 +51,15 @@ struct MixCtrl {
   double tol_out, tol_in;
   int max_outer, max_inner;
   int warm;                    // start from the previous pressure (else from zero)
+  int reach;                   // the first pass aims at the outer target (see ph_prep)
+  int reach_wait;              // steps until that is tried again after a miss
   double bnorm, tol_abs_out, rr64, sum64;
   double rt_norm, tol_abs_in;
   double rho, beta, pq, alpha, rr_in;
   int outer, inner, inner_total, converged;
   int inner_done, outer_done;
   int cold;                    // this solve's first pass starts from zero (the warm guess was worse)
+  int reach_tried;             // this solve's first pass aimed at the outer target
 };
 
 // One tile of work of a mixed batch: instance and the tile's first cell.
