@@ -182,8 +182,14 @@ def launches_per_step(precision, cg_iters, passes, nlev, persistent=True):
         return 11 + 3 * cg_iters
     if persistent:                    # prologue 3, RHS, loop reset, the solve, correction, diagnostics, gather
         return 9
-    v = 2 * nlev - 1                  # down-sweeps, the coarse CTA, up-sweeps
-    return 11 + passes * (6 + v) + cg_iters * (3 + v)
+    v = 2 * nlev - 1                  # a V-cycle: down-sweeps, the coarse CTA, up-sweeps
+    # an iteration: the V-cycle after level 0's down-sweep (which the update before it
+    # fuses), the matvec and the update; a pass: loop reset, prep, level 0's first
+    # down-sweep, loop arm, correction, residual (the loop guards run in the last CTA
+    # of the update and of the residual kernels)
+    per_iter = (v - 1 if nlev >= 2 else v) + 2
+    per_pass = 5 + (1 if nlev >= 2 else 0)
+    return 11 + passes * per_pass + cg_iters * per_iter
 
 
 # ---- CPU arm -----------------------------------------------------------------
@@ -358,8 +364,9 @@ def kernel_roofline(lib, cfg, st, tr, it, cells, precision, workload=None):
             "algorithmic_bytes_per_launch": nbytes, "bytes_model": model}
 
 
-def e2e_cavity(cfg, n, steps):
-    """Through the public step() on a State whose fields are host NumPy arrays."""
+def e2e_cavity(cfg, n, steps, warmup=2):
+    """Through the public step() on a State whose fields are host NumPy arrays: `warmup`
+    untimed steps, then `steps` timed ones (the same step range as the device-timed run)."""
     import numpy as np
 
     from pyflow_solver_gb300 import ResidualManager
@@ -369,10 +376,10 @@ def e2e_cavity(cfg, n, steps):
         return None
     host = State(n, n, {k: np.zeros((n + 2, n + 2)) for k in "uvp"})
     tr = ResidualManager()
-    step(cfg, host, tr, 0)
-    step(cfg, host, tr, 1)
+    for it in range(warmup):
+        step(cfg, host, tr, it)
     t0 = time.perf_counter()
-    for it in range(2, 2 + steps):
+    for it in range(warmup, warmup + steps):
         step(cfg, host, tr, it)
     dt = time.perf_counter() - t0
     nbytes = 3 * (n + 2) ** 2 * 8
@@ -422,7 +429,8 @@ def bench_cavity(args, dist, world, rank, local):
         extra["plain_fp64"] = {"value": pval, "unit": "cell-updates/s", "ms_per_step": ptot / args.plain_steps,
                                "steps": args.plain_steps, "cg_iterations_per_step": [d["cg_iterations"] for d in pd]}
         extra["speedup_vs_plain_fp64"] = value / pval
-    e2e = e2e_cavity(cfg, n, args.e2e_steps) if args.e2e_steps > 0 else None
+    e2e_steps = args.steps if args.e2e_steps is None else args.e2e_steps
+    e2e = e2e_cavity(cfg, n, e2e_steps, args.warmup) if e2e_steps > 0 else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         steps = 6 if wl == "cavity512" else 1
@@ -482,7 +490,7 @@ def bench_batched(args, dist, world, rank, local):
     # end to end: the fields of all instances copied in (pinned host -> device) and out every step
     host = torch.empty(arena.numel(), dtype=torch.float64, pin_memory=True)
     host.copy_(arena)
-    e2e_steps = max(1, args.e2e_steps)
+    e2e_steps = max(1, args.steps if args.e2e_steps is None else args.e2e_steps)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -559,7 +567,8 @@ def main():
     ap.add_argument("--no-roofline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain binary64 comparison run")
     ap.add_argument("--plain-steps", type=int, default=3)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=None,
+                    help="timed steps of the end-to-end run (default: --steps; 0 skips it)")
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--no-graph", action="store_true", help="individual launches instead of one graph per step")
     ap.add_argument("--persistent", action="store_true",

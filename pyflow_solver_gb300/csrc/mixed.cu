@@ -1145,19 +1145,6 @@ __global__ void k_ml_arm(MixLoop* ml, int which, cudaGraphConditionalHandle cond
   if (use_cond) cudaGraphSetConditional(cond, a > 0 ? 1u : 0u);
 }
 
-// last node of a loop body: stops the loop after its trip bound whatever the instances report
-__global__ void k_ml_guard(MixLoop* ml, int which, cudaGraphConditionalHandle cond, int use_cond) {
-  pdl_enter();
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const int g = which == 0 ? ++ml->guard_o : ++ml->guard_i;
-  const int gmax = which == 0 ? ml->gmax_o : ml->gmax_i;
-  const int a = which == 0 ? ml->outer_active : ml->inner_active;
-  if (g >= gmax && a > 0) {
-    ml->tripped = 1;
-    if (use_cond) cudaGraphSetConditional(cond, 0u);
-  }
-}
-
 __global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                  MixLoop* ml) {
   pdl_enter();
@@ -1173,13 +1160,41 @@ __global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD
   ph_matvec(x, M, tl, sm);
 }
 
+// The guard of a loop body, run by the last CTA of the body's last kernel to
+// finish (an arrival ticket over the launch): it counts the body's trips and stops
+// the loop at its trip bound whatever the instances report (the host then reports
+// an error instead of waiting on a loop that does not end).  Every CTA of the
+// launch arrives, whether or not its instance was live.
+__device__ __forceinline__ void loop_guard(MixLoop* ml, int which, cudaGraphConditionalHandle cond) {
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned* t = which == 0 ? &ml->ticket_o : &ml->ticket_i;
+    __threadfence();
+    s_last = (atomicAdd(t, 1u) == gridDim.x - 1) ? 1 : 0;
+    if (s_last) {
+      __threadfence();
+      atomicExch(t, 0u);
+      const int g = which == 0 ? ++ml->guard_o : ++ml->guard_i;
+      const int gmax = which == 0 ? ml->gmax_o : ml->gmax_i;
+      const int a = atomicAdd(which == 0 ? &ml->outer_active : &ml->inner_active, 0);
+      if (g >= gmax && a > 0) {
+        ml->tripped = 1;
+        cudaGraphSetConditional(cond, 0u);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(MT, 5) k_mx_update_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                         MixLoop* ml, cudaGraphConditionalHandle cond_inner, int use_cond,
                                                         Smooth sw) {
   pdl_enter();
-  CTA_TILE(1)
+  const MTile tl = TL[blockIdx.x];
+  const MixDesc& M = MD[tl.inst];
   __shared__ UpdDownSmem sm;
-  ph_update_down(x, M, tl, ml, cond_inner, use_cond, sw, sm);
+  if (mx_live(M, 1)) ph_update_down(CtaCtx{}, M, tl, ml, cond_inner, use_cond, sw, sm);
+  if (use_cond) loop_guard(ml, 1, cond_inner);
 }
 
 __global__ void __launch_bounds__(MT) k_mx_correct(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
@@ -1191,9 +1206,11 @@ __global__ void __launch_bounds__(MT) k_mx_correct(const MixDesc* __restrict__ M
 __global__ void __launch_bounds__(MT) k_mx_resid(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                   MixLoop* ml, cudaGraphConditionalHandle cond_outer, int use_cond) {
   pdl_enter();
-  CTA_TILE(0)
+  const MTile tl = TL[blockIdx.x];
+  const MixDesc& M = MD[tl.inst];
   __shared__ RedSmem rsm;
-  ph_resid(x, M, tl, ml, cond_outer, use_cond, rsm);
+  if (mx_live(M, 0)) ph_resid(CtaCtx{}, M, tl, ml, cond_outer, use_cond, rsm);
+  if (use_cond) loop_guard(ml, 0, cond_outer);
 }
 
 // summary of the mixed solve for the step record
@@ -1631,10 +1648,19 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   B->dd = (MixDesc*)take(n * sizeof(MixDesc));
   B->loop = (MixLoop*)take(sizeof(MixLoop));
   B->pad = (float*)take(sizeof(float));
+  // PFGB_TEST_LOOP_BOUND lowers both loops' trip bounds (a test of the guards: the
+  // instances then need more trips than the guards allow)
+  if (const char* tb = std::getenv("PFGB_TEST_LOOP_BOUND")) {
+    const int b = std::atoi(tb);
+    if (b > 0) {
+      gmax_o = std::min(gmax_o, b);
+      gmax_i = std::min(gmax_i, b);
+    }
+  }
   B->gmax_o = gmax_o;
   B->gmax_i = gmax_i;
   B->sw = make_smoother();
-  MixLoop ml0 = {0, 0, 0, 0, gmax_o, gmax_i, 0, {0u, 0u, 0, 0}};
+  MixLoop ml0 = {0, 0, 0, 0, gmax_o, gmax_i, 0, 0u, 0u, {0u, 0u, 0, 0}};
   cudaMemcpy(B->loop, &ml0, sizeof(MixLoop), cudaMemcpyHostToDevice);
   cudaError_t e = cudaMemcpy(B->dd, B->hd.data(), n * sizeof(MixDesc), cudaMemcpyHostToDevice);
   B->coarse_smem = smem;
@@ -1784,10 +1810,8 @@ int append_solve(GraphChain& c, Batch* B) {
   add_vcycle(inner, B, 1, sw, 1);
   inner.kernel(k_mx_matvec, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   inner.kernel(k_mx_update_down, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_inner, 1, sw);
-  inner.kernel(k_ml_guard, dim3(1), dim3(32), B->loop, 1, cond_inner, 1);
   outer.kernel(k_mx_correct, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   outer.kernel(k_mx_resid, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_outer, 1);
-  outer.kernel(k_ml_guard, dim3(1), dim3(32), B->loop, 0, cond_outer, 1);
   c.kernel(k_mx_finish, dim3((B->n + 31) / 32), dim3(32), dd, B->n);
   if (std::getenv("PFGB_GRAPH_DEBUG"))
     std::fprintf(stderr, "pfgb mixed graph: programmatic edges outer %d inner %d; last refusal: %s\n", outer.n_prog_,

@@ -103,6 +103,7 @@ struct MixLoop {
   int guard_o, guard_i;
   int gmax_o, gmax_i;
   int tripped;
+  unsigned ticket_o, ticket_i;   // CTAs done in the current launch of a loop's last kernel
   GridBar gb;     // barrier of the persistent solve
 };
 

@@ -877,7 +877,7 @@ __global__ void __launch_bounds__(NT) k_post_diag_m(const InstDesc* __restrict__
 }
 
 // one StepOut64 record per instance
-__global__ void k_gather(const InstDesc* __restrict__ ID, int n) {
+__global__ void k_gather(const InstDesc* __restrict__ ID, int n, const int* trip, const int* gb_err) {
   pdl_enter();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
@@ -907,10 +907,12 @@ __global__ void k_gather(const InstDesc* __restrict__ ID, int n) {
   for (int s = 0; s < S_COUNT; ++s) f |= slots[s].result_flags;
   out->flags_or = f;
   out->refine_passes = ctrl->refine_passes;
+  out->loop_status = (*trip ? 1 : 0) | ((gb_err && *gb_err) ? 2 : 0);
 }
 
 // ---------------------------------------------------------------------------
 // Host driver of one instance.
+
 
 static long round_up(long a, long m) { return (a + m - 1) / m * m; }
 
@@ -982,6 +984,10 @@ struct Instance64 {
   std::vector<cudaEvent_t> ev;
   int ev_used = 0;
 };
+
+// where the step's loop guards and the persistent solve's barrier report
+static const int* loop_trip(const Instance64* I) { return I->mix ? &I->mix->loop->tripped : &I->lc->tripped; }
+static const int* loop_gb_err(const Instance64* I) { return I->mix ? &I->mix->loop->gb.err : nullptr; }
 
 static int validate_params(const pfgb_params* prm) {
   if (prm->nx < 2 || prm->ny < 2) return set_error(PFGB_EINVAL, "nx and ny must be >= 2 (the reference's central divergence indexes two columns and rows)");
@@ -1235,7 +1241,7 @@ static void enqueue_projection(Instance64* I, cudaStream_t s) {
   k_post_resid<0><<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
   k_pin_correct<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
   k_post_diag<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-  k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
+  k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n, loop_trip(I), loop_gb_err(I));
 }
 
 static void enqueue_prologue(Instance64* I, cudaStream_t s) {
@@ -1296,7 +1302,7 @@ static int build_graph(Instance64* I, int mode) {
     c.kernel(k_pin_correct, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
     c.kernel(k_post_diag, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   }
-  c.kernel(k_gather, g1, dim3(32), (const InstDesc*)I->dd, I->n);
+  c.kernel(k_gather, g1, dim3(32), (const InstDesc*)I->dd, I->n, loop_trip(I), loop_gb_err(I));
   if (c.status() != cudaSuccess || (!I->mix && body.status() != cudaSuccess)) {
     cudaError_t be = c.status() != cudaSuccess ? c.status() : body.status();
     return set_error(PFGB_ECUDA, std::string("building the step graph: ") + cudaGetErrorString(be));
@@ -1337,19 +1343,13 @@ static int read_out(Instance64* I, cudaStream_t s, pfgb_step_out* out) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("step failed: ") + cudaGetErrorString(e));
   if (I->use_graph && !I->profiling) {
-    int tripped = 0;
-    if (I->mix) {
-      mixed::MixLoop ml;
-      e = cudaMemcpy(&ml, I->mix->loop, sizeof(ml), cudaMemcpyDeviceToHost);
-      if (e == cudaSuccess && ml.gb.err)
-        return set_error(PFGB_ESTATE, "the persistent solve's grid barrier timed out (its CTAs were not co-resident)");
-      tripped = (e == cudaSuccess) ? ml.tripped : 0;
-    } else {
-      LoopCtl lc;
-      e = cudaMemcpy(&lc, I->lc, sizeof(LoopCtl), cudaMemcpyDeviceToHost);
-      tripped = (e == cudaSuccess) ? lc.tripped : 0;
-    }
-    if (tripped) return set_error(PFGB_ESTATE, "a loop guard stopped the step (an instance did not report completion)");
+    // the loop status rides in the records (every active instance's carries the same word)
+    int st = 0;
+    for (int k = 0; k < I->n; ++k)
+      if (I->hd[k].active) st |= I->out_h[k].loop_status;
+    if (st & 2)
+      return set_error(PFGB_ESTATE, "the persistent solve's grid barrier timed out (its CTAs were not co-resident)");
+    if (st & 1) return set_error(PFGB_ESTATE, "a loop guard stopped the step (an instance did not report completion)");
   }
   for (int k = 0; k < I->n; ++k)
     if (I->hd[k].active) copy_out(I->out_h[k], &out[k]);
@@ -1374,7 +1374,7 @@ static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
     if (int rc = mixed::run_direct(I->mix, s)) return rc;
     k_pin_correct_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
     k_post_diag_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
-    k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
+    k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n, loop_trip(I), loop_gb_err(I));
   } else {
     enqueue_projection(I, s);
   }

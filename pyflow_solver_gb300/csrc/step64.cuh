@@ -60,6 +60,7 @@ struct StepOut64 {
   double divstar2, bnrm2, res2, ru2, rv2, divafter2, linres2, cont2;
   unsigned flags_or;    // OR of the result flags of all slots (inexact / overflow diagnostics)
   int refine_passes;
+  int loop_status;      // bit 0: a loop guard stopped the step; bit 1: the persistent solve's barrier timed out
 };
 
 struct Geo64 {

@@ -157,6 +157,25 @@ def test_interior_tile_forms_same_bits(nx, ny, Re, monkeypatch):
     assert runs[0][1] == runs[1][1]
 
 
+def test_loop_guard_stops_the_inner_loop_at_its_bound(monkeypatch):
+    """The guard run by the last CTA of each loop body's last kernel stops a loop at its trip
+    bound and the step reports it.  The bound is set below what the solve needs on the host
+    (a test setting); nothing faults on the device, and a new instance steps normally."""
+    from pyflow_solver_gb300 import ResidualManager, _capi, allocate_state, step
+    cfg = cavity(64, 64, 400.0, 1.0, precision="mixed")
+    monkeypatch.setenv("PFGB_TEST_LOOP_BOUND", "2")
+    st = allocate_state(64, 64)
+    tr = ResidualManager()
+    step(cfg, st, tr, 0)                        # zero right-hand side: no loop runs
+    with pytest.raises(_capi.PFGBError, match="loop guard"):
+        step(cfg, st, tr, 1)
+    monkeypatch.delenv("PFGB_TEST_LOOP_BOUND")
+    st2 = allocate_state(64, 64)
+    tr2 = ResidualManager()
+    diags = [step(cfg, st2, tr2, it)[2] for it in range(3)]
+    assert all(d["Rp_converged"] for d in diags[1:])
+
+
 def test_mixed_graph_and_direct_launches_agree():
     """The graph (device-side loop control) and the host-driven direct form give the same bits."""
     from pyflow_solver_gb300 import ResidualManager, SimulationDriver, allocate_state, interior_view
