@@ -180,8 +180,8 @@ def launches_per_step(precision, cg_iters, passes, nlev, persistent=True):
     """Kernel launches of one step from its loop trip counts."""
     if precision == "fp64":
         return 11 + 3 * cg_iters
-    if persistent:                    # prologue 3, RHS, loop reset, the solve, correction, diagnostics, gather
-        return 9
+    if persistent:                    # prestep, predictor, RHS, loop reset, the solve, correction, diagnostics
+        return 7
     v = 2 * nlev - 1                  # a V-cycle: down-sweeps, the coarse CTA, up-sweeps
     # an iteration: the V-cycle after level 0's down-sweep (which the update before it
     # fuses), the matvec and the update; a pass: loop reset, prep, level 0's first
@@ -189,7 +189,9 @@ def launches_per_step(precision, cg_iters, passes, nlev, persistent=True):
     # of the update and of the residual kernels)
     per_iter = (v - 1 if nlev >= 2 else v) + 2
     per_pass = 5 + (1 if nlev >= 2 else 0)
-    return 11 + passes * per_pass + cg_iters * per_iter
+    # a step: prestep (with dt), predictor, RHS, loop reset, init, loop arm, correction,
+    # diagnostics (with the solve summary and the step record)
+    return 8 + passes * per_pass + cg_iters * per_iter
 
 
 # ---- CPU arm -----------------------------------------------------------------

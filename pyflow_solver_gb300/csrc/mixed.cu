@@ -960,16 +960,18 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
   float* e = sm + tot;       // pre-smoothed iterate on the way down; the bottom solution
   float* w = sm + 2 * tot;   // residual on the way down; each level's result on the way up
   float* dg = sm + 3 * tot;  // every cell's diagonal, formed once (1024-thread CTAs)
-  C_FOR(L[0], { rh[c] = __ldcg(C.f + (long)j * C.ld + i); })
+  const CLvl Le = L[0];   // register copies of the level descriptors (the level arrays are written
+                          // through pointers the compiler cannot tell from the shared table)
+  C_FOR(Le, { rh[c] = __ldcg(C.f + (long)j * C.ld + i); })
   if constexpr (NT == CT) {
     for (int l = 0; l < nl; ++l) {
-      const CLvl& Lv = L[l];
+      const CLvl Lv = L[l];
       C_FOR(Lv, { dg[Lv.off + c] = c_diag(Lv, j, i); })
     }
   }
   __syncthreads();
   for (int l = 0; l + 1 < nl; ++l) {
-    const CLvl& Lv = L[l];
+    const CLvl Lv = L[l];
     const float* r = rh + Lv.off;
     // e = S(S(0)); the first sweep from zero is pointwise (w1 rh / d) and is folded into the second
     C_FOR(Lv, {
@@ -987,12 +989,12 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
     // residual rh - A e of this level into w, then rh_{l+1} = P^T w
     C_FOR(Lv, { w[Lv.off + c] = r[c] - (c_dg<NT>(Lv, dg, c, j, i) * e[Lv.off + c] - c_nsum(Lv, e, j, i)); })
     __syncthreads();
-    const CLvl& Cv = L[l + 1];
+    const CLvl Cv = L[l + 1];
     C_FOR(Cv, { rh[Cv.off + c] = restrict_val(w + Lv.off, Lv.nx, 0, 0, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i); })
     __syncthreads();
   }
   {
-    const CLvl& Lv = L[nl - 1];
+    const CLvl Lv = L[nl - 1];
     const int nb = Lv.nx * Lv.ny;
     if (M.binv) {
       // exact bottom solve: e = A+ rh (at most BMAX cells).  A+ is exactly symmetric, so
@@ -1037,8 +1039,8 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
   }
   // up: w_l = S(S(e_l + P result_{l+1})); the bottom's result is in e, every other level's in w
   for (int l = nl - 2; l >= 0; --l) {
-    const CLvl& Lv = L[l];
-    const CLvl& Cv = L[l + 1];
+    const CLvl Lv = L[l];
+    const CLvl Cv = L[l + 1];
     const float* ec = (l + 1 == nl - 1) ? e : w;
     const float* ecl = ec + Cv.off;
     const int cnx = Cv.nx;
@@ -1051,12 +1053,12 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
     c_sweep<NT>(Lv, dg, rh, e, w, sw.w1);
   }
   const float* z = (nl == 1) ? e : w;
-  C_FOR(L[0], { C.u[(long)j * C.ld + i] = z[c]; })
+  C_FOR(Le, { C.u[(long)j * C.ld + i] = z[c]; })
   if (M.nlev == 1) {
     // the V-cycle ran entirely here: rho = r.z over level 0, summed as the tile phases do,
     // as 1024 lanes (row j to lane-row j mod 32) whatever NT is
     __shared__ double wsum[CT / 32];
-    const CLvl& L0 = L[0];
+    const CLvl L0 = L[0];
 #pragma unroll
     for (int m = 0; m < CT / NT; ++m) {
       const int vw = (threadIdx.x >> 5) + m * (NT / 32);
@@ -1214,25 +1216,6 @@ __global__ void __launch_bounds__(MT) k_mx_resid(const MixDesc* __restrict__ MD,
 }
 
 // summary of the mixed solve for the step record
-__device__ __forceinline__ void mx_finish_one(const MixDesc& M) {
-  if (!*M.active) return;
-  const MixCtrl* m = M.ctrl;
-  Ctrl64* c = M.ctrl64;
-  c->iter = cget(&m->inner_total);
-  c->refine_passes = cget(&m->outer);
-  c->info = cget(&m->converged) ? 0 : M.maxiter_report;
-  const double bn = cget(&m->bnorm);
-  c->zero_rhs = (bn == 0.0) ? 1 : 0;
-  c->bnrm2 = bn;
-  *M.res_out = cget(&m->rr64);      // ||b - A x||^2 of the final x (the refinement's own residual)
-}
-
-__global__ void k_mx_finish(const MixDesc* __restrict__ MD, int n) {
-  pdl_enter();
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) mx_finish_one(MD[k]);
-}
-
 // ---- the persistent solve ------------------------------------------------------
 //
 // The whole refinement of every instance in one cooperative launch: one
@@ -1812,7 +1795,6 @@ int append_solve(GraphChain& c, Batch* B) {
   inner.kernel(k_mx_update_down, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_inner, 1, sw);
   outer.kernel(k_mx_correct, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   outer.kernel(k_mx_resid, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_outer, 1);
-  c.kernel(k_mx_finish, dim3((B->n + 31) / 32), dim3(32), dd, B->n);
   if (std::getenv("PFGB_GRAPH_DEBUG"))
     std::fprintf(stderr, "pfgb mixed graph: programmatic edges outer %d inner %d; last refusal: %s\n", outer.n_prog_,
                  inner.n_prog_, cudaGetErrorString(inner.last_prog_err_));
@@ -1888,7 +1870,6 @@ int run_direct(Batch* B, cudaStream_t s) {
     k_mx_resid<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0);
     if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
   }
-  k_mx_finish<<<(B->n + 31) / 32, 32, 0, s>>>(B->dd, B->n);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("mixed solve launch: ") + cudaGetErrorString(e));
   return PFGB_OK;

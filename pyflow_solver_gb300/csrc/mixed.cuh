@@ -153,6 +153,21 @@ struct MixParams {
   int maxiter_report;
 };
 
+// The summary of instance M's solve for the step record (iterations, passes,
+// convergence, ||b||, the final ||b - A x||^2); run once the solve has ended.
+__device__ __forceinline__ void mx_finish_one(const MixDesc& M) {
+  if (!*M.active) return;
+  const MixCtrl* m = M.ctrl;
+  Ctrl64* c = M.ctrl64;
+  c->iter = __ldcg(&m->inner_total);
+  c->refine_passes = __ldcg(&m->outer);
+  c->info = __ldcg(&m->converged) ? 0 : M.maxiter_report;
+  const double bn = __ldcg(&m->bnorm);
+  c->zero_rhs = (bn == 0.0) ? 1 : 0;
+  c->bnrm2 = bn;
+  *M.res_out = __ldcg(&m->rr64);      // ||b - A x||^2 of the final x (the refinement's own residual)
+}
+
 int batch_create(const MixParams* prm, int n, Batch** out);
 void batch_destroy(Batch* B);
 // Append the refinement of every instance (x = A^{-1} b) to a graph chain.

@@ -122,12 +122,7 @@ __global__ void __launch_bounds__(NT) k_prestep(const InstDesc* __restrict__ ID,
 }
 
 // dt selection, exactly the Python float sequence of solver.py:25-62 (one thread per instance)
-__global__ void k_dt(const InstDesc* __restrict__ ID, int n) {
-  pdl_enter();
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const InstDesc& Dd = ID[k];
-  if (!Dd.active) return;
+__device__ __forceinline__ void dt_one(const InstDesc& Dd) {
   const DtArgs a = Dd.D;
   const StepIn in = *Dd.in;
   Ctrl64* ctrl = Dd.ctrl;
@@ -157,6 +152,15 @@ __global__ void k_dt(const InstDesc* __restrict__ ID, int n) {
   ctrl->cfl = py_max(DIV(MUL(umax, dt), a.dx), DIV(MUL(vmax, dt), a.dy));
   ctrl->dtm = py_max(dt, 1e-14);
   ctrl->rdtm = 1.0 / ctrl->dtm;
+}
+
+__global__ void k_dt(const InstDesc* __restrict__ ID, int n) {
+  pdl_enter();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const InstDesc& Dd = ID[k];
+  if (!Dd.active) return;
+  dt_one(Dd);
 }
 
 // dt given by the caller of a stand-alone projection (instance 0)
@@ -665,6 +669,7 @@ __global__ void __launch_bounds__(NT) k_prestep_m(const InstDesc* __restrict__ I
     ctrl->vmax_bits = 0ull;
     D.slots[S_DIVC_BEFORE].result = out[0];
     ctrl->div_before = sqrt(out[0]);
+    dt_one(D);     // the instance's dt, CFL and safeguard (k_dt of the binary64 form)
   }
 }
 
@@ -849,40 +854,8 @@ __global__ void __launch_bounds__(NT) k_pin_correct_m(const InstDesc* __restrict
   }
 }
 
-// ||div_c(u*, v*)||^2 after the correction, ||A p - b||^2, ||div_central(u, v; 1, 1)||^2
-__global__ void __launch_bounds__(NT) k_post_diag_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
-  TILE_PROLOGUE
-  __shared__ StepRed rsm;
-  const RecipGrid rg = recips(G);
-  const int i = tl.i0 + (threadIdx.x & 31);
-  View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
-  View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds};
-  double v[2] = {0.0, 0.0}, out[2];
-  M_ROWS({
-    if (i < G.nx && j < G.ny) {
-      const double d = div_c_r(US, VS, j, i, rg);
-      const double c = div_central_unit(U, V, j, i, G.nx, G.ny);
-      v[0] += d * d;
-      v[1] += c * c;
-    }
-  })
-  if (STEP_RED(2, v, out) && threadIdx.x == 0) {
-    D.slots[S_DIVAFTER].result = out[0];
-    // ||A p - b||^2: p is the refinement's x exactly (x[0] stays 0), so this is the
-    // refinement's final binary64 residual, which the solve has already formed
-    D.slots[S_LINRES].result = D.slots[S_RES].result;
-    D.slots[S_CONT].result = out[1];
-  }
-}
-
-// one StepOut64 record per instance
-__global__ void k_gather(const InstDesc* __restrict__ ID, int n, const int* trip, const int* gb_err) {
-  pdl_enter();
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const InstDesc& Dd = ID[k];
-  if (!Dd.active) return;
+// one StepOut64 record of instance Dd for the host
+__device__ __forceinline__ void gather_one(const InstDesc& Dd, const int* trip, const int* gb_err) {
   const XASlot* slots = Dd.slots;
   const Ctrl64* ctrl = Dd.ctrl;
   StepOut64* out = Dd.out;
@@ -908,6 +881,49 @@ __global__ void k_gather(const InstDesc* __restrict__ ID, int n, const int* trip
   out->flags_or = f;
   out->refine_passes = ctrl->refine_passes;
   out->loop_status = (*trip ? 1 : 0) | ((gb_err && *gb_err) ? 2 : 0);
+}
+
+// ||div_c(u*, v*)||^2 after the correction, ||A p - b||^2, ||div_central(u, v; 1, 1)||^2
+__global__ void __launch_bounds__(NT) k_post_diag_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
+                                                     const mixed::MixDesc* __restrict__ MD, const int* trip,
+                                                     const int* gb_err) {
+  pdl_enter();
+  TILE_PROLOGUE
+  __shared__ StepRed rsm;
+  const RecipGrid rg = recips(G);
+  const int i = tl.i0 + (threadIdx.x & 31);
+  View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
+  View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds};
+  double v[2] = {0.0, 0.0}, out[2];
+  M_ROWS({
+    if (i < G.nx && j < G.ny) {
+      const double d = div_c_r(US, VS, j, i, rg);
+      const double c = div_central_unit(U, V, j, i, G.nx, G.ny);
+      v[0] += d * d;
+      v[1] += c * c;
+    }
+  })
+  if (STEP_RED(2, v, out) && threadIdx.x == 0) {
+    // the instance's last tile: the solve's summary, these norms, then its step record
+    mixed::mx_finish_one(MD[tl.inst]);
+    D.slots[S_DIVAFTER].result = out[0];
+    // ||A p - b||^2: p is the refinement's x exactly (x[0] stays 0), so this is the
+    // refinement's final binary64 residual, which the solve has already formed
+    D.slots[S_LINRES].result = D.slots[S_RES].result;
+    D.slots[S_CONT].result = out[1];
+    __threadfence();
+    gather_one(D, trip, gb_err);
+  }
+}
+
+// one StepOut64 record per instance
+__global__ void k_gather(const InstDesc* __restrict__ ID, int n, const int* trip, const int* gb_err) {
+  pdl_enter();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const InstDesc& Dd = ID[k];
+  if (!Dd.active) return;
+  gather_one(Dd, trip, gb_err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1247,7 +1263,7 @@ static void enqueue_projection(Instance64* I, cudaStream_t s) {
 static void enqueue_prologue(Instance64* I, cudaStream_t s) {
   if (I->mix) k_prestep_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
   else k_prestep<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-  k_dt<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
+  if (!I->mix) k_dt<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
   if (I->mix) k_predict_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
   else k_predict<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
 }
@@ -1269,7 +1285,7 @@ static int build_graph(Instance64* I, int mode) {
   if (mode == 0) {
     if (I->mix) c.kernel(k_prestep_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
     else c.kernel(k_prestep, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
-    c.kernel(k_dt, g1, dim3(32), (const InstDesc*)I->dd, I->n);
+    if (!I->mix) c.kernel(k_dt, g1, dim3(32), (const InstDesc*)I->dd, I->n);
     if (I->mix) c.kernel(k_predict_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
     else c.kernel(k_predict, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   }
@@ -1297,12 +1313,13 @@ static int build_graph(Instance64* I, int mode) {
   if (!I->mix) c.kernel(k_post_resid<0>, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   if (I->mix) {
     c.kernel(k_pin_correct_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
-    c.kernel(k_post_diag_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
+    c.kernel(k_post_diag_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm, (const mixed::MixDesc*)I->mix->dd,
+             loop_trip(I), loop_gb_err(I));
   } else {
     c.kernel(k_pin_correct, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
     c.kernel(k_post_diag, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   }
-  c.kernel(k_gather, g1, dim3(32), (const InstDesc*)I->dd, I->n, loop_trip(I), loop_gb_err(I));
+  if (!I->mix) c.kernel(k_gather, g1, dim3(32), (const InstDesc*)I->dd, I->n, loop_trip(I), loop_gb_err(I));
   if (c.status() != cudaSuccess || (!I->mix && body.status() != cudaSuccess)) {
     cudaError_t be = c.status() != cudaSuccess ? c.status() : body.status();
     return set_error(PFGB_ECUDA, std::string("building the step graph: ") + cudaGetErrorString(be));
@@ -1373,8 +1390,7 @@ static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
     k_rhs_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
     if (int rc = mixed::run_direct(I->mix, s)) return rc;
     k_pin_correct_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
-    k_post_diag_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
-    k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n, loop_trip(I), loop_gb_err(I));
+    k_post_diag_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm, I->mix->dd, loop_trip(I), loop_gb_err(I));
   } else {
     enqueue_projection(I, s);
   }

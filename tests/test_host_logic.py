@@ -90,10 +90,10 @@ def test_bench_accounting_helpers():
     # elongated cells coarsen the strongly coupled axis only: 256 x 64 -> 128 x 64 -> 64 x 64
     assert bench.mg_levels(128, 32) == 1 and bench.mg_levels(256, 64) == 3
     assert bench.launches_per_step("fp64", 300, 0, 1) == 11 + 900
-    assert bench.launches_per_step("mixed", 10, 2, 4, persistent=True) == 9
+    assert bench.launches_per_step("mixed", 10, 2, 4, persistent=True) == 7
     # 4 levels: an iteration is 2 down-sweeps, the coarse CTA, 3 up-sweeps, matvec, update
-    assert bench.launches_per_step("mixed", 10, 2, 4, persistent=False) == 11 + 2 * 6 + 10 * 8
+    assert bench.launches_per_step("mixed", 10, 2, 4, persistent=False) == 8 + 2 * 6 + 10 * 8
     # one level (the whole V-cycle in the coarse CTA): coarse, matvec, update; no level-0 down-sweep
-    assert bench.launches_per_step("mixed", 10, 2, 1, persistent=False) == 11 + 2 * 5 + 10 * 3
+    assert bench.launches_per_step("mixed", 10, 2, 1, persistent=False) == 8 + 2 * 5 + 10 * 3
     assert bench.mixed_solve_bytes(100, 10, 2) == 100 * (32 + 178 + 690)
     assert bench.pct([3.0, 1.0, 2.0]) == {"p50": 2.0, "p95": 3.0, "p99": 3.0}
