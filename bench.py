@@ -23,15 +23,16 @@ synthetic draws stand in for any dataset):
 
 Line contents:
 * ``value``: cell-updates/s with the state resident in HBM, K steps timed
-  with CUDA events on the launching stream; L2 (129 MB) is flushed by a
-  256 MiB write between timed steps, outside the timed intervals.
+  with CUDA events on the launching stream after W warm-up steps (K defaults
+  to the workload's own step count: 2000 for the 512^2 cavity, 1000 for
+  2048^2, 500 for the batch); L2 (129 MB) is flushed by a 256 MiB write
+  between timed steps, outside the timed intervals.
 * ``e2e``: the same metric through the public API with the fields in host
   memory: every step copies u, v, p host->device and back inside the timed
   (wall-clock) region.
-* ``roofline``: the dominant kernel, timed with CUDA events during one more
-  step: in the mixed form the persistent pressure solve (one cooperative
-  launch; algorithmic bytes from ``mixed_solve_bytes``), in the binary64 form
-  the CG matvec (4 words per cell: read r, p_old; write p_new, q).
+* ``roofline``: the pressure matvec (``k_mx_matvec`` in the mixed form,
+  ``k_cg_matvec`` in the binary64 form), timed per launch with CUDA events
+  during one more step (4 words per cell: read z or r, p_old; write p_new, q).
 * ``cpu_baseline``: the oracle port (NumPy restatement of the reference with
   its own reductions and CG sequence) on a bounded sample of the workload.
 * ``--impl reference``: that CPU port timed as the reference arm.
@@ -54,13 +55,16 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 CAVITIES = {
-    "cavity512": dict(n=512, Re=1000.0, lid=1.0, maxiter=300),
-    "cavity2048": dict(n=2048, Re=3200.0, lid=1.0, maxiter=300),
+    "cavity512": dict(n=512, Re=1000.0, lid=1.0, maxiter=300, steps=2000),
+    "cavity2048": dict(n=2048, Re=3200.0, lid=1.0, maxiter=300, steps=1000),
 }
+BATCH_STEPS = 500                 # steps of each batched instance
 L2_FLUSH_BYTES = 256 * 1024 * 1024
 PRECISION_NOTE = {
-    "mixed": "binary32 multigrid-PCG inner solves (rel tol 1e-5) inside binary64 refinement to rel 1e-8; "
-             "predictor, correction, pressure residual and all norms binary64",
+    "mixed": "binary32 multigrid-PCG inner solves (rel tol 1e-5; every pass also stops a quarter below the outer "
+             "target, and the first pass of an instance whose first passes have been reaching the outer target "
+             "aims there, down to rel 3e-7) inside binary64 refinement to rel 1e-8, warm-started from the previous "
+             "pressure; predictor, correction, pressure residual and all norms binary64",
     "fp64": "binary64 plain path (the reference's Jacobi-PCG, lin_maxiter 300, exactly rounded reductions)",
 }
 
@@ -174,6 +178,13 @@ def mg_levels(nx, ny, dx=None, dy=None):
         cx, cy = cx * py / px, cy * px / py
         n += 1
     return n
+
+
+def series_summary(xs):
+    """A per-step series as its mean, range and first and last ten entries."""
+    if not xs:
+        return {}
+    return {"mean": sum(xs) / len(xs), "min": min(xs), "max": max(xs), "first": list(xs[:10]), "last": list(xs[-10:])}
 
 
 def launches_per_step(precision, cg_iters, passes, nlev, persistent=True):
@@ -449,7 +460,9 @@ def bench_cavity(args, dist, world, rank, local):
                    "precision": PRECISION_NOTE[args.precision],
                    "l2": "flushed between timed steps (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "cg_iterations_per_step": cg, "refine_passes_per_step": passes},
+                   "timed_steps": f"steps {args.warmup}..{args.warmup + args.steps - 1} of a run from zero fields",
+                   "cg_iterations_per_step": series_summary(cg), "refine_passes_per_step": series_summary(passes),
+                   "steps_not_converged": sum(1 for d in diags if not d.get("Rp_converged", True))},
         **extra,
         "step_latency_ms": pct(ms),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
@@ -513,7 +526,8 @@ def bench_batched(args, dist, world, rank, local):
                                "[100,5000], lid uniform [0.5,2]; one graph launch per step for all instances",
                    "instances": len(inst), "cells_per_step": cells, "precision": PRECISION_NOTE[args.precision],
                    "l2": "flushed between timed steps (256 MiB write)",
-                   "max_cg_iterations_per_step": maxit, "max_refine_passes_per_step": maxpass,
+                   "max_cg_iterations_per_step": series_summary(maxit),
+                   "max_refine_passes_per_step": series_summary(maxpass),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "step_latency_ms": pct(ms),
         "roofline": None, "cpu_baseline": None, "e2e": e2e, "gpu_launches": launches,
@@ -560,7 +574,8 @@ def bench_serving(args, dist, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: the workload's own step count, 2000 / 1000 / 500)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="cavity512", choices=["cavity512", "cavity2048", "batched256", "serving"])
@@ -576,6 +591,8 @@ def main():
     ap.add_argument("--persistent", action="store_true",
                     help="mixed form: the pressure solve as one persistent cooperative launch, not a kernel graph")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = CAVITIES[args.workload]["steps"] if args.workload in CAVITIES else BATCH_STEPS
     if args.impl == "reference":
         run_reference_arm(args)
         return
