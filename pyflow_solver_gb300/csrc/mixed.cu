@@ -320,16 +320,29 @@ __device__ __forceinline__ void ph_down_t(const X& x, const MixDesc& M, const MT
   const int i0 = tl.i0, j0 = tl.j0;
   const float din = mg_diag_in(L);
   auto inside = [&](int gj, int gi) { return IN || (gj >= 0 && gj < L.ny && gi >= 0 && gi < L.nx); };
-  for (int idx = x.tid(); idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
-    const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
-    const int gj = j0 + jj, gi = i0 + ii;
-    float f = 0.f, v = 0.f;
-    if (inside(gj, gi)) {
-      f = x.ld(L.f + (long)gj * L.ld + gi);
-      v = __fdividef(sw.w1 * f, lv_diag<IN>(L, din, gj, gi));
+  {
+    // every load of the halo first, then the stores
+    constexpr int HW = BX + 2 * H3, HN = (BY + 2 * H3) * HW, NI = (HN + MT - 1) / MT;
+    float fv[NI];
+#pragma unroll
+    for (int t = 0; t < NI; ++t) {
+      const int idx = x.tid() + t * MT;
+      const int gj = j0 + idx / HW - H3, gi = i0 + idx % HW - H3;
+      fv[t] = 0.f;
+      if ((t < NI - 1 || idx < HN) && inside(gj, gi)) fv[t] = x.ld(L.f + (long)gj * L.ld + gi);
     }
-    sm.sf[jj + H3][ii + H3] = f;
-    sm.s1[jj + H3][ii + H3] = v;
+#pragma unroll
+    for (int t = 0; t < NI; ++t) {
+      const int idx = x.tid() + t * MT;
+      if (t < NI - 1 || idx < HN) {
+        const int jj = idx / HW - H3, ii = idx % HW - H3;
+        const int gj = j0 + jj, gi = i0 + ii;
+        float v = 0.f;
+        if (inside(gj, gi)) v = __fdividef(sw.w1 * fv[t], lv_diag<IN>(L, din, gj, gi));
+        sm.sf[jj + H3][ii + H3] = fv[t];
+        sm.s1[jj + H3][ii + H3] = v;
+      }
+    }
   }
   x.sync();
   for (int idx = x.tid(); idx < (BY + 4) * (BX + 4); idx += MT) {
@@ -392,21 +405,56 @@ __device__ __forceinline__ void ph_post_t(const X& x, const MixDesc& M, const MT
   const int Ilo = max(0, max(0, i0 - 2) / F.kx - 1), Ihi = min(C.nx - 1, (i0 + BX + 1) / F.kx + 1);
   const int Jlo = max(0, max(0, j0 - 2) / F.ky - 1), Jhi = min(C.ny - 1, (j0 + BY + 1) / F.ky + 1);
   const int cw = Ihi - Ilo + 1, ch = Jhi - Jlo + 1;
-  for (int idx = x.tid(); idx < (BY + 4) * (BX + 4); idx += MT) {
-    const int jj = idx / (BX + 4) - 2, ii = idx % (BX + 4) - 2;
-    const int gj = j0 + jj, gi = i0 + ii;
-    float v = 0.f, f = 0.f;
-    if (IN || (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx)) {
-      const long o = (long)gj * F.ld + gi;
-      v = x.ld(F.t + o);
-      if (jj >= -1 && jj <= BY && ii >= -1 && ii <= BX) f = x.ld(F.f + o);
+  {
+    // all of these loads are issued before the first store
+    constexpr int HW = BX + 4, HN = (BY + 4) * HW, NI = (HN + MT - 1) / MT;
+    // the coarse patch: one axis coarsened at least, so at most 38 x 20 parents
+    constexpr int NC = ((BY + 6) * (BX / 2 + 4) + MT - 1) / MT;
+    const int cn = cw * ch;
+    float tv[NI], fv[NI], cv[NC];
+#pragma unroll
+    for (int t = 0; t < NI; ++t) {
+      const int idx = x.tid() + t * MT;
+      const int jj = idx / HW - 2, ii = idx % HW - 2;
+      const int gj = j0 + jj, gi = i0 + ii;
+      tv[t] = 0.f;
+      fv[t] = 0.f;
+      if ((t < NI - 1 || idx < HN) && (IN || (gj >= 0 && gj < F.ny && gi >= 0 && gi < F.nx))) {
+        const long o = (long)gj * F.ld + gi;
+        tv[t] = x.ld(F.t + o);
+        if (jj >= -1 && jj <= BY && ii >= -1 && ii <= BX) fv[t] = x.ld(F.f + o);
+      }
     }
-    sm.w0[jj + 2][ii + 2] = v;
-    if (jj >= -1 && jj <= BY && ii >= -1 && ii <= BX) sm.sf[jj + 1][ii + 1] = f;
-  }
-  for (int idx = x.tid(); idx < cw * ch; idx += MT) {
-    const int r = idx / cw, c = idx - r * cw;
-    sm.cs[r][c] = x.ld(C.u + (long)(Jlo + r) * C.ld + Ilo + c);
+#pragma unroll
+    for (int t = 0; t < NC; ++t) {
+      const int idx = x.tid() + t * MT;
+      cv[t] = 0.f;
+      if (idx < cn) {
+        const int r = idx / cw, c = idx - r * cw;
+        cv[t] = x.ld(C.u + (long)(Jlo + r) * C.ld + Ilo + c);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < NI; ++t) {
+      const int idx = x.tid() + t * MT;
+      if (t < NI - 1 || idx < HN) {
+        const int jj = idx / HW - 2, ii = idx % HW - 2;
+        sm.w0[jj + 2][ii + 2] = tv[t];
+        if (jj >= -1 && jj <= BY && ii >= -1 && ii <= BX) sm.sf[jj + 1][ii + 1] = fv[t];
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < NC; ++t) {
+      const int idx = x.tid() + t * MT;
+      if (idx < cn) {
+        const int r = idx / cw, c = idx - r * cw;
+        sm.cs[r][c] = cv[t];
+      }
+    }
+    for (int idx = x.tid() + NC * MT; idx < cn; idx += MT) {
+      const int r = idx / cw, c = idx - r * cw;
+      sm.cs[r][c] = x.ld(C.u + (long)(Jlo + r) * C.ld + Ilo + c);
+    }
   }
   x.sync();
   auto cat = [&sm, Ilo, Jlo](int J, int I) { return sm.cs[J - Jlo][I - Ilo]; };
@@ -613,15 +661,31 @@ __device__ __forceinline__ void ph_matvec_t(const X& x, const MixDesc& M, const 
   const float beta = (float)cget(&ctrl->beta);
   const int i0 = tl.i0, j0 = tl.j0;
   const float din = mg_diag_in(L0);
-  for (int idx = x.tid(); idx < (BY + 2) * (BX + 2); idx += MT) {
-    const int jj = idx / (BX + 2) - 1, ii = idx % (BX + 2) - 1;
-    const int gj = j0 + jj, gi = i0 + ii;
-    float v = 0.f;
-    if (IN || (gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx)) {
+  // every load of the halo first (all in flight together), then the stores
+  constexpr int HW = BX + 2, HN = (BY + 2) * HW, NI = (HN + MT - 1) / MT;
+  auto inside = [&](int gj, int gi) { return IN || (gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx); };
+  float zv[NI], pv0[NI];
+#pragma unroll
+  for (int t = 0; t < NI; ++t) {
+    const int idx = x.tid() + t * MT;
+    const int gj = j0 + idx / HW - 1, gi = i0 + idx % HW - 1;
+    zv[t] = 0.f;
+    pv0[t] = 0.f;
+    if ((t < NI - 1 || idx < HN) && inside(gj, gi)) {
       const long o = (long)gj * L0.ld + gi;
-      v = (k == 0) ? x.ld(z + o) : fmaf(beta, x.ld(pold + o), x.ld(z + o));
+      zv[t] = x.ld(z + o);
+      if (k != 0) pv0[t] = x.ld(pold + o);
     }
-    sm.pn[jj + 1][ii + 1] = v;
+  }
+#pragma unroll
+  for (int t = 0; t < NI; ++t) {
+    const int idx = x.tid() + t * MT;
+    if (t < NI - 1 || idx < HN) {
+      const int jj = idx / HW - 1, ii = idx % HW - 1;
+      float v = 0.f;
+      if (inside(j0 + jj, i0 + ii)) v = (k == 0) ? zv[t] : fmaf(beta, pv0[t], zv[t]);
+      sm.pn[jj + 1][ii + 1] = v;
+    }
   }
   x.sync();
   const int tx = x.tid() & 31;
@@ -712,19 +776,38 @@ __device__ __forceinline__ void ph_update_down_t(const X& x, const MixDesc& M, c
     }
   }
   if (M.nlev < 2) return;
-  // the new residual on the tile and a 3-cell halo, then the down-sweep as ph_down
+  // the new residual on the tile and a 3-cell halo (every load first, then the
+  // stores), then the down-sweep as ph_down
   const int i0 = tl.i0, j0 = tl.j0;
   const float din = mg_diag_in(L0);
   auto inside = [&](int gj, int gi) { return IN || (gj >= 0 && gj < L0.ny && gi >= 0 && gi < L0.nx); };
-  for (int idx = x.tid(); idx < (BY + 2 * H3) * (BX + 2 * H3); idx += MT) {
-    const int jj = idx / (BX + 2 * H3) - H3, ii = idx % (BX + 2 * H3) - H3;
-    const int gj = j0 + jj, gi = i0 + ii;
-    float r = 0.f;
-    if (inside(gj, gi)) {
-      const long o = (long)gj * L0.ld + gi;
-      r = fmaf(-alpha, x.ld(M.q + o), x.ld(fo + o));
+  // (in two batches of loads: the kernel's register budget holds half the halo)
+  constexpr int HW = BX + 2 * H3, HN = (BY + 2 * H3) * HW, NI = (HN + MT - 1) / MT, NB = (NI + 1) / 2;
+#pragma unroll
+  for (int b = 0; b < NI; b += NB) {
+    float hq[NB], hf[NB];
+#pragma unroll
+    for (int t = 0; t < NB; ++t) {
+      const int idx = x.tid() + (b + t) * MT;
+      const int gj = j0 + idx / HW - H3, gi = i0 + idx % HW - H3;
+      hq[t] = 0.f;
+      hf[t] = 0.f;
+      if (b + t < NI && (b + t < NI - 1 || idx < HN) && inside(gj, gi)) {
+        const long o = (long)gj * L0.ld + gi;
+        hq[t] = x.ld(M.q + o);
+        hf[t] = x.ld(fo + o);
+      }
     }
-    sm.sf[jj + H3][ii + H3] = r;
+#pragma unroll
+    for (int t = 0; t < NB; ++t) {
+      const int idx = x.tid() + (b + t) * MT;
+      if (b + t < NI && (b + t < NI - 1 || idx < HN)) {
+        const int jj = idx / HW - H3, ii = idx % HW - H3;
+        float r = 0.f;
+        if (inside(j0 + jj, i0 + ii)) r = fmaf(-alpha, hq[t], hf[t]);
+        sm.sf[jj + H3][ii + H3] = r;
+      }
+    }
   }
   x.sync();
   const Lvl C = M.lev[1];
@@ -1086,7 +1169,7 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
   if (!mx_live(M, gate)) return;                \
   const CtaCtx x{};
 
-__global__ void __launch_bounds__(MT) k_mg_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
+__global__ void __launch_bounds__(MT, 6) k_mg_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
                                                  int gate, Smooth sw) {
   pdl_enter();
   CTA_TILE(gate)
@@ -1094,7 +1177,7 @@ __global__ void __launch_bounds__(MT) k_mg_down(const MixDesc* __restrict__ MD, 
   ph_down(x, M, tl, l, sw, sm);
 }
 
-__global__ void __launch_bounds__(MT) k_mg_post(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
+__global__ void __launch_bounds__(MT, 5) k_mg_post(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
                                                  int gate, Smooth sw) {
   pdl_enter();
   CTA_TILE(gate)
@@ -1155,7 +1238,7 @@ __global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, 
   ph_prep(x, M, tl, ml, rsm);
 }
 
-__global__ void __launch_bounds__(MT) k_mx_matvec(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
+__global__ void __launch_bounds__(MT, 6) k_mx_matvec(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
   pdl_enter();
   CTA_TILE(1)
   __shared__ MatvecSmem sm;
