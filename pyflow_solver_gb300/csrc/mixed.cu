@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdint>
 #include <cstdlib>
 #include <cstdio>
 #include <string>
@@ -716,6 +717,138 @@ __device__ __forceinline__ void ph_matvec(const X& x, const MixDesc& M, const MT
   else ph_matvec_t<false>(x, M, tl, sm);
 }
 
+// ---- the matvec with halos copied by the tensor memory accelerator ---------
+// The kernel graph's form of ph_matvec.  Each CTA takes the level-0 tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... and has TMA copy the halo of its next
+// tile (z and p_old) into one of two shared-memory stages while it computes the
+// current one.  A copy is a 40 x 34 box of binary32 from column i0 - 4 and row
+// j0 - 1: the tile's 34 x 34 halo, widened so that the copy starts on a 16-byte
+// boundary (i0 is a multiple of 32); cells outside the grid read as zero.  The
+// per-cell arithmetic (p = z or z + beta p_old, q = A p), the tile sums and
+// their order are those of ph_matvec, so both forms give the same bits.
+constexpr int MV_W = BX + 8, MV_H = BY + 2;
+constexpr int MV_X0 = 4;                       // column of cell i0 in a stage row
+constexpr unsigned MV_BYTES = MV_W * MV_H * sizeof(float);
+constexpr int MV_SPIN_LIMIT = 1 << 20;         // polls of a stage's barrier before the kernel gives up
+struct alignas(128) MvStage {
+  float v[MV_H][MV_W];
+};
+struct MvSmem {
+  MvStage z[2], p[2];
+  unsigned long long bar[2];
+  RedSmem rsm;
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(b)), "r"(parity)
+      : "memory");
+  return ok != 0u;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity) {
+  for (int i = 0; i < MV_SPIN_LIMIT; ++i)
+    if (mbar_try_wait(b, parity)) return true;
+  return false;
+}
+
+// box at (x, y) of the tensor `map` (a tensor map in global memory) into dst; x * 4 bytes
+// is a multiple of 16
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_addr(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_addr(b))
+      : "memory");
+}
+
+// thread 0: the copies of tile tl's halo into stage s (p_old only after the first iteration)
+__device__ __forceinline__ void mv_issue(const MixDesc& M, const MTile& tl, MvSmem& sm, int s) {
+  const int k = cget(&M.ctrl->inner);
+  const int xs = tl.i0 - MV_X0, ys = tl.j0 - 1;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the stage's earlier reads come first
+  mbar_expect_tx(&sm.bar[s], k == 0 ? MV_BYTES : 2u * MV_BYTES);
+  tma_load_2d(&sm.z[s], M.tmap + 0, xs, ys, &sm.bar[s]);
+  if (k != 0) tma_load_2d(&sm.p[s], M.tmap + ((k & 1) ? 2 : 1), xs, ys, &sm.bar[s]);   // p_old: p1 if k odd
+}
+
+template <bool IN>
+__device__ __forceinline__ void mv_tile_t(const CtaCtx& x, const MixDesc& M, const MTile& tl, const MvStage& zs,
+                                          const MvStage& ps, RedSmem& rsm) {
+  const Lvl L0 = M.lev[0];
+  MixCtrl* ctrl = M.ctrl;
+  const int k = cget(&ctrl->inner);
+  float* pnew = (k & 1) ? M.p0 : M.p1;
+  const float beta = (float)cget(&ctrl->beta);
+  const int i0 = tl.i0, j0 = tl.j0;
+  const float din = mg_diag_in(L0);
+  // p at halo cell (j, i): formed where it is read, with ph_matvec's operation
+  auto at = [&](int j, int i) {
+    const int r = j - j0 + 1, c = i - i0 + MV_X0;
+    const float zv = zs.v[r][c];
+    return k == 0 ? zv : fmaf(beta, ps.v[r][c], zv);
+  };
+  const int tx = x.tid() & 31;
+  const int gi = i0 + tx;
+  FF v[1] = {{0.f, 0.f}};
+  MX_ROWS_X({
+    const int gj = j0 + ty;
+    if (IN || (gi < L0.nx && gj < L0.ny)) {
+      const float pv = at(gj, gi);
+      const float qv = lv_diag<IN>(L0, din, gj, gi) * pv - lv_nsum<IN>(L0, gj, gi, at);
+      const long o = (long)gj * L0.ld + gi;
+      pnew[o] = pv;
+      M.q[o] = qv;
+      ff_add_prod(v[0], pv, qv);
+    }
+  })
+  // the tile's partial of p.q, formed as dred_sum_ff forms it and stored without a
+  // fence: the CTA publishes its tiles of an instance together (mv_publish)
+  const FF a = ff_warp_sum(v[0]);
+  if ((x.tid() & 31) == 0) rsm.w[0][x.tid() >> 5] = (double)a.hi + (double)a.lo;
+  double d[1] = {0.0};
+  dred_warps<1, MT>(x, d, rsm);
+  if (x.tid() == 0) M.part[tl.loc] = d[0];
+}
+
+// Publish cnt tile partials of instance M (one fence and one arrival for all of
+// them); the CTA whose arrival completes the instance's tiles adds the partials in
+// tile order exactly as dred_finish does and forms alpha.
+__device__ __forceinline__ void mv_publish(const CtaCtx& x, const MixDesc& M, int cnt, RedSmem& rsm) {
+  if (x.tid() == 0) {
+    __threadfence();
+    const unsigned before = atomicAdd(M.ticket, (unsigned)cnt);
+    rsm.last = (before + (unsigned)cnt == (unsigned)M.nt0) ? 1 : 0;
+  }
+  x.sync();
+  if (!rsm.last) return;
+  __threadfence();
+  double sum[1] = {0.0};
+  for (int k = x.tid(); k < M.nt0; k += MT) sum[0] += __ldcg(&M.part[k]);
+  dred_block<1, MT>(x, sum, rsm);
+  if (x.tid() == 0) {
+    atomicExch(M.ticket, 0u);
+    MixCtrl* ctrl = M.ctrl;
+    ctrl->pq = sum[0];
+    ctrl->alpha = cget(&ctrl->rho) / sum[0];
+  }
+}
+
 // e += alpha p; r -= alpha q (from residual buffer k & 1 into buffer (k + 1) & 1);
 // ||r||^2 and the inner stopping test; then, for an instance with a level below,
 // the fused down-sweep of level 0 on the new residual (its 3-cell halo formed
@@ -1245,6 +1378,67 @@ __global__ void __launch_bounds__(MT, 6) k_mx_matvec(const MixDesc* __restrict__
   ph_matvec(x, M, tl, sm);
 }
 
+// The TMA form (see mv_tile_t).  A stage's barrier that is not complete after
+// MV_SPIN_LIMIT polls stops the kernel: the CTA records it in the loop control's
+// error flag (the step then reports a failed solve), waits -- again bounded --
+// for the copy it has in flight into the other stage, and returns.
+__global__ void __launch_bounds__(MT, 6) k_mx_matvec_tma(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
+                                                          int ntiles, MixLoop* ml) {
+  pdl_enter();
+  __shared__ MvSmem sm;
+  const CtaCtx x{};
+  if (x.tid() == 0) {
+    mbar_init(&sm.bar[0], 1u);
+    mbar_init(&sm.bar[1], 1u);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int t = blockIdx.x;
+  if (t < ntiles && x.tid() == 0) {
+    const MTile tl = TL[t];
+    if (mx_live(MD[tl.inst], 1)) mv_issue(MD[tl.inst], tl, sm, 0);
+  }
+  unsigned phase = 0u;
+  int cur = -1, cnt = 0;   // the instance of the partials not yet published, and their number
+  for (int n = 0; t < ntiles; ++n, t += gridDim.x) {
+    const int s = n & 1;
+    const MTile tl = TL[t];
+    const MixDesc& M = MD[tl.inst];
+    // the next tile's copies go into the other stage, whose last reader (the tile before)
+    // finished with the barriers of its reduction
+    const int tn = t + gridDim.x;
+    bool next = false;
+    if (tn < ntiles && x.tid() == 0) {
+      const MTile tln = TL[tn];
+      if (mx_live(MD[tln.inst], 1)) {
+        mv_issue(MD[tln.inst], tln, sm, s ^ 1);
+        next = true;
+      }
+    }
+    if (!mx_live(M, 1)) continue;
+    if (tl.inst != cur) {
+      if (cnt) mv_publish(x, MD[cur], cnt, sm.rsm);
+      cur = tl.inst;
+      cnt = 0;
+    }
+    const bool ok = mbar_wait_bounded(&sm.bar[s], (phase >> s) & 1u);
+    phase ^= 1u << s;
+    if (__syncthreads_or(!ok)) {
+      if (x.tid() == 0) {
+        atomicExch(&ml->gb.err, 1);
+        if (next) mbar_wait_bounded(&sm.bar[s ^ 1], (phase >> (s ^ 1)) & 1u);
+      }
+      return;
+    }
+    if (M.interior && tile_interior(tl, M.lev[0].nx, M.lev[0].ny, 1))
+      mv_tile_t<true>(x, M, tl, sm.z[s], sm.p[s], sm.rsm);
+    else
+      mv_tile_t<false>(x, M, tl, sm.z[s], sm.p[s], sm.rsm);
+    ++cnt;
+  }
+  if (cnt) mv_publish(x, MD[cur], cnt, sm.rsm);
+}
+
 // The guard of a loop body, run by the last CTA of the body's last kernel to
 // finish (an arrival ticket over the launch): it counts the body's trips and stops
 // the loop at its trip bound whatever the instances report (the host then reports
@@ -1564,6 +1758,41 @@ static Smooth make_smoother() {
   return s;
 }
 
+// cuTensorMapEncodeTiled, fetched once through the runtime (the library does not
+// link the driver API); null where the driver does not provide it
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static const EncodeTiledFn fn = []() -> EncodeTiledFn {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// The halo box of the TMA matvec over a level-0 binary32 array of nx x ny cells with
+// a pitch of ld floats: 40 x 34 floats, no swizzle, zero fill outside the array.
+// The encoder checks the base (16-byte aligned), the pitch (a multiple of 16 bytes)
+// and the box's row (160 bytes).
+static bool encode_halo_map(CUtensorMap* m, const float* base, int nx, int ny, long ld) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn || (reinterpret_cast<uintptr_t>(base) & 15u) != 0 || (ld * sizeof(float)) % 16 != 0) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)MV_W, (cuuint32_t)MV_H};
+  const cuuint32_t es[2] = {1u, 1u};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 static void add_mtiles(std::vector<MTile>& v, int k, int nx, int ny) {
   int loc = 0;
   for (int j0 = 0; j0 < ny; j0 += BY)
@@ -1609,7 +1838,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   }
   for (int l = 0; l < B->maxlev; ++l)
     bytes += up(tl[l].size() * sizeof(MTile)) + up(tpre[l].size() * sizeof(MTile));
-  bytes += up(n * sizeof(MixDesc)) + up(sizeof(MixLoop)) + up(sizeof(float));
+  bytes += up(n * sizeof(MixDesc)) + up(sizeof(MixLoop)) + up(sizeof(float)) + up(3 * n * sizeof(CUtensorMap));
   if (cudaMalloc(&B->ws, bytes) != cudaSuccess) {
     delete B;
     return set_error(PFGB_ENOMEM, "cudaMalloc of the mixed-solver workspace failed");
@@ -1714,6 +1943,28 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   B->dd = (MixDesc*)take(n * sizeof(MixDesc));
   B->loop = (MixLoop*)take(sizeof(MixLoop));
   B->pad = (float*)take(sizeof(float));
+  {
+    // tensor maps of the TMA matvec: z, p0, p1 of every instance.  PFGB_MATVEC_TMA=1
+    // selects that form; the default is the one-tile-per-CTA matvec, which measured
+    // faster on GB300 (2048^2: 48.5 against 51.2 us a launch; the 256-instance batch:
+    // 1.589 against 1.621 ms a step).  Both give the same bits.
+    CUtensorMap* tm = (CUtensorMap*)take(3 * n * sizeof(CUtensorMap));
+    const char* tv = std::getenv("PFGB_MATVEC_TMA");
+    bool ok = tv && std::string(tv) == "1";
+    std::vector<CUtensorMap> hm(ok ? 3 * n : 0);
+    for (int k = 0; ok && k < n; ++k) {
+      const MixDesc& M = B->hd[k];
+      const float* src[3] = {M.lev[0].u, M.p0, M.p1};
+      for (int a = 0; ok && a < 3; ++a) ok = encode_halo_map(&hm[3 * k + a], src[a], M.lev[0].nx, M.lev[0].ny, M.lev[0].ld);
+    }
+    if (!ok && std::getenv("PFGB_GRAPH_DEBUG"))
+      std::fprintf(stderr, "pfgb mixed batch: TMA matvec maps %s\n",
+                   !(tv && std::string(tv) == "1") ? "not wanted" : (encode_tiled() ? "refused by the encoder" : "without an encoder"));
+    if (ok && cudaMemcpy(tm, hm.data(), hm.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice) != cudaSuccess) ok = false;
+    for (int k = 0; k < n; ++k) B->hd[k].tmap = ok ? tm + 3 * k : nullptr;
+    B->mv_tma = ok ? 1 : 0;
+    cudaGetLastError();
+  }
   // PFGB_TEST_LOOP_BOUND lowers both loops' trip bounds (a test of the guards: the
   // instances then need more trips than the guards allow)
   if (const char* tb = std::getenv("PFGB_TEST_LOOP_BOUND")) {
@@ -1755,6 +2006,19 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
                    B->coarse_nt, B->coarse_smem, occ);
     cudaGetLastError();
   }
+  if (e == cudaSuccess && B->mv_tma) {
+    // the TMA matvec: as many CTAs as fit on the device at once, at most one per tile
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mx_matvec_tma, MT, 0) == cudaSuccess && occ >= 1)
+      B->mv_grid = std::min(B->ntl[0], sms * occ);
+    else
+      B->mv_tma = 0;
+    cudaGetLastError();
+  }
+  if (std::getenv("PFGB_GRAPH_DEBUG"))
+    std::fprintf(stderr, "pfgb mixed batch: TMA matvec %s, %d CTAs\n", B->mv_tma ? "on" : "off", B->mv_grid);
   if (e == cudaSuccess) {
     // the persistent solve: one 1024-thread CTA per SM, if the device co-schedules them
     const size_t psmem = std::max(4 * sizeof(TileSmem), smem);
@@ -1874,7 +2138,10 @@ int append_solve(GraphChain& c, Batch* B) {
   // level-0 down-sweep of r_{k+1}; no V-cycle runs after the last test
   GraphChain inner = outer.while_loop_with(cond_inner);
   add_vcycle(inner, B, 1, sw, 1);
-  inner.kernel(k_mx_matvec, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
+  if (B->mv_tma)
+    inner.kernel(k_mx_matvec_tma, dim3(B->mv_grid), dim3(MT), dd, (const MTile*)B->tl[0], B->ntl[0], B->loop);
+  else
+    inner.kernel(k_mx_matvec, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   inner.kernel(k_mx_update_down, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_inner, 1, sw);
   outer.kernel(k_mx_correct, g0, dim3(MT), dd, (const MTile*)B->tl[0]);
   outer.kernel(k_mx_resid, g0, dim3(MT), dd, (const MTile*)B->tl[0], B->loop, cond_outer, 1);
@@ -1941,7 +2208,10 @@ int run_direct(Batch* B, cudaStream_t s) {
       // the events bracket the matvec alone: the V-cycle queued before keeps the stream busy
       const bool timed = B->ev && 2 * timed_launches + 1 < B->nev;
       if (timed) cudaEventRecord(B->ev[2 * timed_launches], s);
-      k_mx_matvec<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
+      if (B->mv_tma)
+        k_mx_matvec_tma<<<B->mv_grid, MT, 0, s>>>(B->dd, B->tl[0], B->ntl[0], B->loop);
+      else
+        k_mx_matvec<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
       if (timed) {
         cudaEventRecord(B->ev[2 * timed_launches + 1], s);
         *B->ev_used = ++timed_launches;

@@ -1,6 +1,7 @@
 // Mixed-precision pressure solve (FP64 refinement around FP32 multigrid-PCG):
 // device structures and the host interface used by the step graph.
 #pragma once
+#include <cuda.h>           // CUtensorMap (the encoder is fetched through the runtime; no libcuda link)
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -95,6 +96,7 @@ struct MixDesc {
   int maxiter_report;
   int nt0;                     // tiles of level 0 (= tiles of the binary64 grid)
   int interior;                // tiles away from the walls take the interior forms of the phases
+  const CUtensorMap* tmap;     // level-0 halo copies of z (= lev[0].u), p0, p1 (null: no TMA form)
 };
 
 // Batch-wide control of the two WHILE loops.
@@ -131,6 +133,9 @@ struct Batch {
   int persist = 0;                             // in use
   int pgrid = 0;
   size_t psmem = 0;
+  // the matvec of the kernel graph with TMA-copied halos (persistent over the level-0 tiles)
+  int mv_tma = 0;                              // in use (every instance has its tensor maps)
+  int mv_grid = 0;                             // its CTAs
   char* ws = nullptr;
   size_t ws_bytes = 0;
 };

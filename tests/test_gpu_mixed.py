@@ -157,6 +157,30 @@ def test_interior_tile_forms_same_bits(nx, ny, Re, monkeypatch):
     assert runs[0][1] == runs[1][1]
 
 
+@pytest.mark.parametrize("nx,ny,Re", [(512, 512, 1000.0), (200, 136, 400.0)])
+def test_tma_matvec_same_bits(nx, ny, Re, monkeypatch, capfd):
+    """The TMA form of the kernel graph's matvec (PFGB_MATVEC_TMA=1: persistent over the
+    tiles, each tile's halo copied by TMA in a box widened to start on a 16-byte boundary,
+    zeros outside the grid) gives the bits of the default one-tile-per-CTA matvec, on a
+    grid whose edge tiles are ragged as well."""
+    from pyflow_solver_gb300 import ResidualManager, allocate_state, interior_view, step
+    cfg = cavity(nx, ny, Re, 1.0, precision="mixed")
+    monkeypatch.setenv("PFGB_GRAPH_DEBUG", "1")
+    runs = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("PFGB_MATVEC_TMA", flag)
+        st = allocate_state(nx, ny)
+        tr = ResidualManager()
+        diags = [step(cfg, st, tr, it)[2] for it in range(4)]
+        runs.append(([interior_view(st.fields[k]).cpu().numpy() for k in "uvp"], diags))
+    err = capfd.readouterr().err
+    assert err.index("TMA matvec on") < err.index("TMA matvec off"), err
+    assert all(d["Rp_converged"] for d in runs[0][1][1:])
+    for a, b in zip(runs[0][0], runs[1][0]):
+        np.testing.assert_array_equal(a, b)
+    assert runs[0][1] == runs[1][1]
+
+
 def test_loop_guard_stops_the_inner_loop_at_its_bound(monkeypatch):
     """The guard run by the last CTA of each loop body's last kernel stops a loop at its trip
     bound and the step reports it.  The bound is set below what the solve needs on the host
