@@ -327,6 +327,7 @@ def max_over_ranks(x, dist):
 TRAFFIC = {
     ("cavity512", "mixed::k_mx_matvec"): 1.60e6,      # profiles/roofline_traffic.md
     ("cavity2048", "mixed::k_mx_matvec"): 34.11e6,
+    ("cavity2048", "mixed::k_mx_matvec_tma"): 33.74e6,  # profiles/k_mx_matvec_tma_2048.md
     ("cavity2048", "pfgb::k_cg_matvec"): 94.64e6,
     ("cavity512", "pfgb::k_cg_matvec"): 4.27e6,       # profiles/k_cg_matvec_fp64_512.md
 }
@@ -366,7 +367,10 @@ def kernel_roofline(lib, cfg, st, tr, it, cells, precision, workload=None):
         kern, model = "mixed::k_mx_persist", "mixed_solve_bytes (bench.py)"
     elif precision == "mixed":
         nbytes = 4 * 4 * cells
-        kern, model = "mixed::k_mx_matvec", "4 binary32 words per cell"
+        tma = ctypes.c_int()
+        _capi.check(lib.pfgb_matvec_form(inst.handle, ctypes.byref(tma)), "matvec_form")
+        kern = "mixed::k_mx_matvec_tma" if tma.value else "mixed::k_mx_matvec"
+        model = "4 binary32 words per cell"
     else:
         nbytes = 4 * 8 * cells
         kern, model = "pfgb::k_cg_matvec", "4 binary64 words per cell"

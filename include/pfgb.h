@@ -260,6 +260,13 @@ PFGB_API int pfgb_host_unregister(void* ptr);
  * default).  Both give the same bits.  No reference counterpart. */
 PFGB_API int pfgb_set_persistent(pfgb_handle* handle, int on);
 
+/* With precision 1: *tma = 1 when the kernel graph's PCG matvec is the TMA form
+ * (persistent over the level-0 tiles, halos copied by the tensor memory
+ * accelerator; chosen for instances of at least 64 tiles and at least 2 tiles per
+ * CTA, or forced by PFGB_MATVEC_TMA=1 / 0 when the instance is created), 0 when it
+ * is one tile per CTA.  Both give the same bits.  No reference counterpart. */
+PFGB_API int pfgb_matvec_form(pfgb_handle* handle, int* tma);
+
 /* ---- tile autotuner ---------------------------------------------------------- */
 
 /* Time the three tile shapes of the binary64 CG kernel pair (32 x 8, 32 x 16,

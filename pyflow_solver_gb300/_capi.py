@@ -91,6 +91,7 @@ SIGNATURES = {
     "pfgb_cg_solve_noalloc": (_I, [_I, _P, _P, _I, _I, _D, _D, _I, _D, _D, _I, _P, ctypes.POINTER(SolveOut)]),
     "pfgb_set_graph": (_I, [_P, _I]),
     "pfgb_set_persistent": (_I, [_P, _I]),
+    "pfgb_matvec_form": (_I, [_P, ctypes.POINTER(_I)]),
     "pfgb_host_register": (_I, [_P, ctypes.c_size_t]),
     "pfgb_host_unregister": (_I, [_P]),
     "pfgb_autotune": (_I, [_P, _P, ctypes.POINTER(_I), c_double_p]),

@@ -146,6 +146,11 @@ extern "C" int pfgb_set_persistent(pfgb_handle* handle, int on) {
   return instance64_set_persistent(handle->inst, on);
 }
 
+extern "C" int pfgb_matvec_form(pfgb_handle* handle, int* tma) {
+  if (!handle || !tma) return set_error(PFGB_EINVAL, "null argument");
+  return instance64_matvec_form(handle->inst, tma);
+}
+
 extern "C" int pfgb_set_graph(pfgb_handle* handle, int on) {
   if (!handle) return set_error(PFGB_EINVAL, "null handle");
   return instance64_set_graph(handle->inst, on);

@@ -777,9 +777,9 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// thread 0: the copies of tile tl's halo into stage s (p_old only after the first iteration)
-__device__ __forceinline__ void mv_issue(const MixDesc& M, const MTile& tl, MvSmem& sm, int s) {
-  const int k = cget(&M.ctrl->inner);
+// thread 0: the copies of tile tl's halo into stage s (p_old only after the first
+// iteration; k is the instance's inner iteration)
+__device__ __forceinline__ void mv_issue(const MixDesc& M, const MTile& tl, int k, MvSmem& sm, int s) {
   const int xs = tl.i0 - MV_X0, ys = tl.j0 - 1;
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the stage's earlier reads come first
   mbar_expect_tx(&sm.bar[s], k == 0 ? MV_BYTES : 2u * MV_BYTES);
@@ -788,13 +788,10 @@ __device__ __forceinline__ void mv_issue(const MixDesc& M, const MTile& tl, MvSm
 }
 
 template <bool IN>
-__device__ __forceinline__ void mv_tile_t(const CtaCtx& x, const MixDesc& M, const MTile& tl, const MvStage& zs,
-                                          const MvStage& ps, RedSmem& rsm) {
+__device__ __forceinline__ void mv_tile_t(const CtaCtx& x, const MixDesc& M, const MTile& tl, int k, float beta,
+                                          const MvStage& zs, const MvStage& ps, RedSmem& rsm) {
   const Lvl L0 = M.lev[0];
-  MixCtrl* ctrl = M.ctrl;
-  const int k = cget(&ctrl->inner);
   float* pnew = (k & 1) ? M.p0 : M.p1;
-  const float beta = (float)cget(&ctrl->beta);
   const int i0 = tl.i0, j0 = tl.j0;
   const float din = mg_diag_in(L0);
   // p at halo cell (j, i): formed where it is read, with ph_matvec's operation
@@ -1382,7 +1379,7 @@ __global__ void __launch_bounds__(MT, 6) k_mx_matvec(const MixDesc* __restrict__
 // MV_SPIN_LIMIT polls stops the kernel: the CTA records it in the loop control's
 // error flag (the step then reports a failed solve), waits -- again bounded --
 // for the copy it has in flight into the other stage, and returns.
-__global__ void __launch_bounds__(MT, 6) k_mx_matvec_tma(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
+__global__ void __launch_bounds__(MT, 4) k_mx_matvec_tma(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                           int ntiles, MixLoop* ml) {
   pdl_enter();
   __shared__ MvSmem sm;
@@ -1392,49 +1389,68 @@ __global__ void __launch_bounds__(MT, 6) k_mx_matvec_tma(const MixDesc* __restri
     mbar_init(&sm.bar[1], 1u);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  __syncthreads();
+  const int g = gridDim.x;
   int t = blockIdx.x;
-  if (t < ntiles && x.tid() == 0) {
-    const MTile tl = TL[t];
-    if (mx_live(MD[tl.inst], 1)) mv_issue(MD[tl.inst], tl, sm, 0);
-  }
+  // the tile table is read one tile ahead of its use (the next tile's entry is at hand
+  // when its copies are issued), and what a tile needs of its instance (live or not, the
+  // inner iteration, beta) is read once per run of tiles of one instance: none of it
+  // changes during the launch, so the chain of dependent loads is paid per instance
+  MTile tl = t < ntiles ? TL[t] : MTile{0, 0, 0, 0};
+  MTile tln = t + g < ntiles ? TL[t + g] : MTile{0, 0, 0, 0};
+  __syncthreads();
+  int ii = -1, ilive = 0, ik = 0;   // thread 0's instance of the copies
+  auto issue = [&](const MTile& u, int stage) -> bool {
+    if (u.inst != ii) {
+      ii = u.inst;
+      ilive = mx_live(MD[ii], 1) ? 1 : 0;
+      ik = ilive ? cget(&MD[ii].ctrl->inner) : 0;
+    }
+    if (ilive) mv_issue(MD[ii], u, ik, sm, stage);
+    return ilive != 0;
+  };
+  if (t < ntiles && x.tid() == 0) issue(tl, 0);
   unsigned phase = 0u;
-  int cur = -1, cnt = 0;   // the instance of the partials not yet published, and their number
-  for (int n = 0; t < ntiles; ++n, t += gridDim.x) {
+  int cur = -1, cnt = 0;        // the instance of the partials not yet published, and their number
+  bool live = false;
+  int k = 0;
+  float beta = 0.f;
+  for (int n = 0; t < ntiles; ++n) {
     const int s = n & 1;
-    const MTile tl = TL[t];
-    const MixDesc& M = MD[tl.inst];
+    const int tn = t + g;
+    const MTile tlnn = tn + g < ntiles ? TL[tn + g] : MTile{0, 0, 0, 0};
     // the next tile's copies go into the other stage, whose last reader (the tile before)
     // finished with the barriers of its reduction
-    const int tn = t + gridDim.x;
     bool next = false;
-    if (tn < ntiles && x.tid() == 0) {
-      const MTile tln = TL[tn];
-      if (mx_live(MD[tln.inst], 1)) {
-        mv_issue(MD[tln.inst], tln, sm, s ^ 1);
-        next = true;
-      }
-    }
-    if (!mx_live(M, 1)) continue;
+    if (tn < ntiles && x.tid() == 0) next = issue(tln, s ^ 1);
     if (tl.inst != cur) {
       if (cnt) mv_publish(x, MD[cur], cnt, sm.rsm);
       cur = tl.inst;
       cnt = 0;
+      const MixDesc& Mc = MD[cur];
+      live = mx_live(Mc, 1);
+      k = live ? cget(&Mc.ctrl->inner) : 0;
+      beta = live ? (float)cget(&Mc.ctrl->beta) : 0.f;
     }
-    const bool ok = mbar_wait_bounded(&sm.bar[s], (phase >> s) & 1u);
-    phase ^= 1u << s;
-    if (__syncthreads_or(!ok)) {
-      if (x.tid() == 0) {
-        atomicExch(&ml->gb.err, 1);
-        if (next) mbar_wait_bounded(&sm.bar[s ^ 1], (phase >> (s ^ 1)) & 1u);
+    if (live) {
+      const bool ok = mbar_wait_bounded(&sm.bar[s], (phase >> s) & 1u);
+      phase ^= 1u << s;
+      if (__syncthreads_or(!ok)) {
+        if (x.tid() == 0) {
+          atomicExch(&ml->gb.err, 1);
+          if (next) mbar_wait_bounded(&sm.bar[s ^ 1], (phase >> (s ^ 1)) & 1u);
+        }
+        return;
       }
-      return;
+      const MixDesc& M = MD[cur];
+      if (M.interior && tile_interior(tl, M.lev[0].nx, M.lev[0].ny, 1))
+        mv_tile_t<true>(x, M, tl, k, beta, sm.z[s], sm.p[s], sm.rsm);
+      else
+        mv_tile_t<false>(x, M, tl, k, beta, sm.z[s], sm.p[s], sm.rsm);
+      ++cnt;
     }
-    if (M.interior && tile_interior(tl, M.lev[0].nx, M.lev[0].ny, 1))
-      mv_tile_t<true>(x, M, tl, sm.z[s], sm.p[s], sm.rsm);
-    else
-      mv_tile_t<false>(x, M, tl, sm.z[s], sm.p[s], sm.rsm);
-    ++cnt;
+    t = tn;
+    tl = tln;
+    tln = tlnn;
   }
   if (cnt) mv_publish(x, MD[cur], cnt, sm.rsm);
 }
@@ -1944,13 +1960,19 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   B->loop = (MixLoop*)take(sizeof(MixLoop));
   B->pad = (float*)take(sizeof(float));
   {
-    // tensor maps of the TMA matvec: z, p0, p1 of every instance.  PFGB_MATVEC_TMA=1
-    // selects that form; the default is the one-tile-per-CTA matvec, which measured
-    // faster on GB300 (2048^2: 48.5 against 51.2 us a launch; the 256-instance batch:
-    // 1.589 against 1.621 ms a step).  Both give the same bits.
+    // tensor maps of the TMA matvec: z, p0, p1 of every instance.  That form pays when
+    // a CTA takes several tiles of one instance in turn (each instance's lookups once, the
+    // next tile's copies in flight during the current one): measured on GB300, 2048^2
+    // 34.8 against 48.5 us a launch; with one tile per CTA (512^2: 14.3 against 12.3 us)
+    // or many small instances (the 256-instance batch: 1.668 against 1.585 ms a step) the
+    // one-tile-per-CTA matvec is faster.  So by default the TMA form is taken for batches
+    // of at least 64 level-0 tiles per instance and at least 2 tiles per CTA (the second
+    // test below, once the grid is known); PFGB_MATVEC_TMA=1 or 0 forces it on or off.
+    // Both forms give the same bits.
     CUtensorMap* tm = (CUtensorMap*)take(3 * n * sizeof(CUtensorMap));
     const char* tv = std::getenv("PFGB_MATVEC_TMA");
-    bool ok = tv && std::string(tv) == "1";
+    B->mv_force = (tv && std::string(tv) == "1") ? 1 : ((tv && std::string(tv) == "0") ? -1 : 0);
+    bool ok = B->mv_force > 0 || (B->mv_force == 0 && n > 0 && (long)B->ntl[0] >= 64L * n);
     std::vector<CUtensorMap> hm(ok ? 3 * n : 0);
     for (int k = 0; ok && k < n; ++k) {
       const MixDesc& M = B->hd[k];
@@ -1959,7 +1981,10 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     }
     if (!ok && std::getenv("PFGB_GRAPH_DEBUG"))
       std::fprintf(stderr, "pfgb mixed batch: TMA matvec maps %s\n",
-                   !(tv && std::string(tv) == "1") ? "not wanted" : (encode_tiled() ? "refused by the encoder" : "without an encoder"));
+                   B->mv_force < 0 ? "not wanted"
+                   : hm.empty()    ? "not used (fewer than 64 level-0 tiles per instance)"
+                   : encode_tiled() ? "refused by the encoder"
+                                    : "without an encoder");
     if (ok && cudaMemcpy(tm, hm.data(), hm.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice) != cudaSuccess) ok = false;
     for (int k = 0; k < n; ++k) B->hd[k].tmap = ok ? tm + 3 * k : nullptr;
     B->mv_tma = ok ? 1 : 0;
@@ -2015,6 +2040,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
       B->mv_grid = std::min(B->ntl[0], sms * occ);
     else
       B->mv_tma = 0;
+    if (B->mv_tma && B->mv_force == 0 && B->ntl[0] < 2 * B->mv_grid) B->mv_tma = 0;   // under 2 tiles per CTA
     cudaGetLastError();
   }
   if (std::getenv("PFGB_GRAPH_DEBUG"))

@@ -135,6 +135,7 @@ struct Batch {
   size_t psmem = 0;
   // the matvec of the kernel graph with TMA-copied halos (persistent over the level-0 tiles)
   int mv_tma = 0;                              // in use (every instance has its tensor maps)
+  int mv_force = 0;                            // PFGB_MATVEC_TMA: 1 on, -1 off, 0 chosen by the batch's shape
   int mv_grid = 0;                             // its CTAs
   char* ws = nullptr;
   size_t ws_bytes = 0;
@@ -181,6 +182,8 @@ int append_solve(GraphChain& c, Batch* B);
 int run_direct(Batch* B, cudaStream_t s);
 // Use the persistent cooperative solve (on, where the device allows it) or the kernel graph.
 int set_persistent(Batch* B, int on);
+// 1 when the kernel graph's matvec is the TMA form (persistent over the level-0 tiles)
+inline int matvec_form(const Batch* B) { return B->mv_tma; }
 // New tolerances and iteration limits for instance k (limits within the loop guards).
 int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer, int max_inner, int warm,
                    int maxiter_report);

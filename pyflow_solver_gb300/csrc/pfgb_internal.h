@@ -25,6 +25,7 @@ int instance64_project(Instance64* I, double* u, double* v, double* p, long lds,
                        pfgb_step_out* out);
 int instance64_set_graph(Instance64* I, int on);
 int instance64_set_persistent(Instance64* I, int on);
+int instance64_matvec_form(const Instance64* I, int* tma);
 int instance64_autotune(Instance64* I, cudaStream_t s, int* chosen, double* us);
 int instance64_set_cg_variant(Instance64* I, int v);
 int instance64_set_params(Instance64* I, int k, const pfgb_params* prm);

@@ -1574,6 +1574,11 @@ int instance64_autotune(Instance64* I, cudaStream_t s, int* chosen, double* us) 
   return PFGB_OK;
 }
 
+int instance64_matvec_form(const Instance64* I, int* tma) {
+  *tma = I->mix ? mixed::matvec_form(I->mix) : 0;
+  return PFGB_OK;
+}
+
 int instance64_set_persistent(Instance64* I, int on) {
   if (!I->mix) return PFGB_OK;
   mixed::set_persistent(I->mix, on);

@@ -181,6 +181,24 @@ def test_tma_matvec_same_bits(nx, ny, Re, monkeypatch, capfd):
     assert runs[0][1] == runs[1][1]
 
 
+def test_tma_matvec_chosen_by_batch_shape(monkeypatch, capfd):
+    """Without PFGB_MATVEC_TMA the TMA matvec is taken where a CTA gets several tiles of one
+    instance (a 2048 x 2048 cavity: 4096 tiles) and not where it gets about one (512 x 512:
+    256 tiles)."""
+    from pyflow_solver_gb300 import ResidualManager, allocate_state, step
+    monkeypatch.delenv("PFGB_MATVEC_TMA", raising=False)
+    monkeypatch.setenv("PFGB_GRAPH_DEBUG", "1")
+    seen = {}
+    for n in (2048, 512):
+        capfd.readouterr()
+        st = allocate_state(n, n)
+        step(cavity(n, n, 1000.0, 1.0, precision="mixed"), st, ResidualManager(), 0)
+        err = capfd.readouterr().err
+        seen[n] = "TMA matvec on" in err
+        del st
+    assert seen == {2048: True, 512: False}
+
+
 def test_loop_guard_stops_the_inner_loop_at_its_bound(monkeypatch):
     """The guard run by the last CTA of each loop body's last kernel stops a loop at its trip
     bound and the step reports it.  The bound is set below what the solve needs on the host
