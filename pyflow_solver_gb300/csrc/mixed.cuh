@@ -106,7 +106,7 @@ struct MixLoop {
   int gmax_o, gmax_i;
   int tripped;
   unsigned ticket_o, ticket_i;   // CTAs done in the current launch of a loop's last kernel
-  GridBar gb;     // barrier of the persistent solve
+  GridBar gb;     // barrier of the persistent solve; its err also records a TMA matvec copy that never landed
 };
 
 struct Batch {

@@ -1001,7 +1001,8 @@ struct Instance64 {
   int ev_used = 0;
 };
 
-// where the step's loop guards and the persistent solve's barrier report
+// where the step's loop guards report, and the bounded waits (the persistent solve's
+// barrier, the TMA matvec's copies)
 static const int* loop_trip(const Instance64* I) { return I->mix ? &I->mix->loop->tripped : &I->lc->tripped; }
 static const int* loop_gb_err(const Instance64* I) { return I->mix ? &I->mix->loop->gb.err : nullptr; }
 
@@ -1365,7 +1366,8 @@ static int read_out(Instance64* I, cudaStream_t s, pfgb_step_out* out) {
     for (int k = 0; k < I->n; ++k)
       if (I->hd[k].active) st |= I->out_h[k].loop_status;
     if (st & 2)
-      return set_error(PFGB_ESTATE, "the persistent solve's grid barrier timed out (its CTAs were not co-resident)");
+      return set_error(PFGB_ESTATE, "a bounded device wait gave up: the persistent solve's grid barrier (its CTAs "
+                                    "were not co-resident) or the TMA matvec's wait for a halo copy");
     if (st & 1) return set_error(PFGB_ESTATE, "a loop guard stopped the step (an instance did not report completion)");
   }
   for (int k = 0; k < I->n; ++k)
