@@ -325,11 +325,11 @@ def max_over_ranks(x, dist):
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the roofline
 # kernel, from the ncu captures summarised in profiles/ (two launches each, averaged).
 TRAFFIC = {
-    ("cavity512", "mixed::k_mx_matvec"): 1.60e6,      # profiles/roofline_traffic.md
+    ("cavity512", "mixed::k_mx_matvec"): 1.60e6,
     ("cavity2048", "mixed::k_mx_matvec"): 34.11e6,
-    ("cavity2048", "mixed::k_mx_matvec_tma"): 33.74e6,  # profiles/k_mx_matvec_tma_2048.md
+    ("cavity2048", "mixed::k_mx_matvec_tma"): 33.74e6,
     ("cavity2048", "pfgb::k_cg_matvec"): 94.64e6,
-    ("cavity512", "pfgb::k_cg_matvec"): 4.27e6,       # profiles/k_cg_matvec_fp64_512.md
+    ("cavity512", "pfgb::k_cg_matvec"): 4.27e6,
 }
 
 
