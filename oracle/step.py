@@ -88,13 +88,29 @@ def converged_pressure(b, nx, ny, dx, dy):
     solve gives x to binary64 accuracy.  This is the converged FP64 oracle of the
     mixed-precision path (the reference's own CG stops at lin_maxiter unconverged).
     """
-    import scipy.sparse.linalg as spla
-    L = neg_laplacian_matrix(nx, ny, dx, dy).tocsc()
+    L, lu = _pinned_factor(nx, ny, float(dx), float(dy))
     x = np.zeros(nx * ny)
     x[0] = b[0]
     rhs = b[1:] - L[1:, :1].toarray().ravel() * x[0]
-    x[1:] = spla.spsolve(L[1:, 1:], rhs)
+    x[1:] = lu.solve(rhs)
     return x
+
+
+_FACTORS = {}
+
+
+def _pinned_factor(nx, ny, dx, dy):
+    """Sparse LU of -lap_c restricted to the unknowns k != 0, kept per grid and
+    spacing (the matrix is the same at every step of a cavity; at 1024 x 1024
+    the factorisation takes seconds and each solve a fraction of one)."""
+    key = (nx, ny, dx, dy)
+    if key not in _FACTORS:
+        import scipy.sparse.linalg as spla
+        L = neg_laplacian_matrix(nx, ny, dx, dy).tocsc()
+        if len(_FACTORS) >= 4:
+            _FACTORS.clear()
+        _FACTORS[key] = (L, spla.splu(L[1:, 1:].tocsc()))
+    return _FACTORS[key]
 
 
 def solve_pressure_poisson(state, dt, dx, dy, cfg, red="exact", rhs_override=None, extra=None):

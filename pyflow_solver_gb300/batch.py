@@ -112,6 +112,12 @@ class BatchedCavities:
         self._hist[k, :len(tail)] = tail
         self._hist_len[k] = len(tail)
 
+    def reload_meta(self, k=None):
+        """Read state.meta of instance k (all if None) into the array bookkeeping, after
+        the caller replaced that state's fields and meta (e.g. restored a snapshot)."""
+        for j in (range(len(self)) if k is None else [k]):
+            self._load_meta(j)
+
     def sync_meta(self, k=None):
         """Write the array bookkeeping of instance k (all if None) into state.meta."""
         for j in (range(len(self)) if k is None else [k]):

@@ -77,7 +77,8 @@ def test_mixed_step_512_matches_converged_fp64():
 
 
 def test_mixed_trajectory_stays_close():
-    """Free-running trajectories (no resynchronisation) of GPU mixed and converged oracle."""
+    """Free-running trajectories (no resynchronisation) of GPU mixed and converged oracle:
+    u, v and p after 20 steps within the 1e-6 bar."""
     from pyflow_solver_gb300 import ResidualManager, SimulationDriver, allocate_state, interior_view
     cfg = cavity(64, 64, 100.0, 1.0)
     gcfg = SimpleNamespace(**vars(cfg), precision="mixed")
@@ -88,8 +89,10 @@ def test_mixed_trajectory_stays_close():
     tw = ost.allocate_state(64, 64)
     for _ in ost.run(ocfg, tw, max_steps=20, red="exact"):
         pass
-    for k in "uv":
-        assert rel(interior_view(st.fields[k]).cpu().numpy(), ost.interior(tw.fields[k])) <= 1e-5, k
+    errs = {k: rel(interior_view(st.fields[k]).cpu().numpy(), ost.interior(tw.fields[k])) for k in "uvp"}
+    print("\nfree-running 20 steps, 64x64 Re 100, mixed vs converged binary64: "
+          + ", ".join(f"{k} {e:.2e}" for k, e in errs.items()))
+    assert max(errs.values()) <= TOL, errs
 
 
 def test_mixed_warm_start_and_fallback():
