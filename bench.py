@@ -1,41 +1,45 @@
 """Benchmark of the projection step on one GB300: cell-updates per second.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--workload cavity512|cavity2048|batched256|serving] [--precision mixed|fp64]
+                    [--workload batched256|cavity512|cavity2048|serving] [--precision mixed|fp64]
 
 Workloads (zero initial fields, unit square, CFL target 0.5 / growth 1.05,
 QUICK advection, Jacobi preconditioner, pressure tolerance 1e-8; seeded
 synthetic draws stand in for any dataset):
 
-* ``cavity512`` (default): one 512 x 512 cavity, Re 1000, lid 1.0.  A step is
-  one projection step.  Default precision ``mixed``: binary32
-  multigrid-preconditioned CG (rel tol 1e-5) inside a binary64 refinement of
-  the pressure solve to 1e-8, everything else binary64.  The same run also
-  times the plain binary64 path (the reference's algorithm, CG with
-  lin_maxiter 300) on the same cavity: ``plain_fp64`` and the ratio
-  ``speedup_vs_plain_fp64``.
-* ``cavity2048``: one 2048 x 2048 cavity, Re 3200, lid 1.0 (both precisions).
-* ``batched256``: 256 cavities from seed 0 (nx, ny in {32..128}, Re
+* ``batched256`` (default): 256 cavities from seed 0 (nx, ny in {32..128}, Re
   log-uniform in [100, 5000], lid uniform in [0.5, 2]) advanced together: a
-  step advances every instance once (one graph launch).
+  step advances every instance once (one graph launch).  Default precision
+  ``mixed``: binary32 multigrid-preconditioned CG (rel tol 1e-5) inside a
+  binary64 refinement of the pressure solve to 1e-8, everything else binary64.
+  The same run times the plain binary64 path (the reference's algorithm, CG
+  with lin_maxiter 300) on the same 256 cavities: ``plain_fp64`` and the ratio
+  ``speedup_vs_plain_fp64``.
+* ``cavity512``: one 512 x 512 cavity, Re 1000, lid 1.0 (with the same plain
+  comparison).
+* ``cavity2048``: one 2048 x 2048 cavity, Re 3200, lid 1.0 (both precisions).
 * ``serving``: the Poisson request trace (200 req/s for 60 s, seed 1) served
   by continuous batching; reports latency percentiles beside throughput.
 
 Line contents:
 * ``value``: cell-updates/s with the state resident in HBM, K steps timed
   with CUDA events on the launching stream after W warm-up steps (K defaults
-  to the workload's own step count: 2000 for the 512^2 cavity, 1000 for
-  2048^2, 500 for the batch); L2 (129 MB) is flushed by a 256 MiB write
-  between timed steps, outside the timed intervals.
+  to the workload's own step count: 500 for the batch, 2000 for the 512^2
+  cavity, 1000 for 2048^2); L2 (129 MB) is flushed by a 256 MiB write between
+  timed steps, outside the timed intervals.
 * ``e2e``: the same metric through the public API with the fields in host
   memory: every step copies u, v, p host->device and back inside the timed
   (wall-clock) region.
-* ``roofline``: the pressure matvec (``k_mx_matvec`` in the mixed form,
-  ``k_cg_matvec`` in the binary64 form), timed per launch with CUDA events
-  during one more step (4 words per cell: read z or r, p_old; write p_new, q).
+* ``kernels`` / ``roofline``: one more step run kernel by kernel with CUDA
+  events around every launch: per kernel its launches, device time, share of
+  the step, algorithmic bytes per launch (per-cell words of each kernel times
+  the cells of its level) and the fraction of the measured HBM copy bandwidth
+  that implies.  ``roofline`` is the kernel with the largest share;
+  ``step_roofline`` is the whole step's algorithmic bytes over its time.
 * ``cpu_baseline``: the oracle port (NumPy restatement of the reference with
   its own reductions and CG sequence) on a bounded sample of the workload.
-* ``--impl reference``: that CPU port timed as the reference arm.
+* ``--impl reference``: that CPU port timed as the reference arm (all host
+  cores for the batch, one process per core; one thread for a single cavity).
 With torchrun (N > 1) every rank runs an independent replica (a cavity does
 not shard; replicas only): value = all cells updated / max time over ranks.
 """
@@ -67,6 +71,25 @@ PRECISION_NOTE = {
              "pressure; predictor, correction, pressure residual and all norms binary64",
     "fp64": "binary64 plain path (the reference's Jacobi-PCG, lin_maxiter 300, exactly rounded reductions)",
 }
+
+
+PRECISION_REFERENCE = ("binary64, the reference's algorithm: Jacobi-PCG with lin_maxiter 300 and the reference's "
+                       "own NumPy reductions (oracle port)")
+L2_NOTE = "GPU arm: L2 flushed between timed steps (256 MiB write)"
+
+
+def cavity_config_line(name):
+    """The `config` of a single-cavity line (the same in both arms)."""
+    c = CAVITIES[name]
+    return {"workload": describe(name), "nx": c["n"], "ny": c["n"], "Re": c["Re"], "l2": L2_NOTE}
+
+
+def batch_config():
+    """The `config` of a batched line (the same in both arms)."""
+    from pyflow_solver_gb300.workloads import batched_instances
+    inst = batched_instances(256, 0)
+    return {"workload": BATCH_WORKLOAD, "instances": len(inst), "cells_per_step": sum(nx * ny for nx, ny, _, _ in inst),
+            "l2": L2_NOTE}
 
 
 def cavity_cfg(name, precision):
@@ -159,15 +182,17 @@ class ClockSampler:
 
 # ---- kernel-launch accounting ------------------------------------------------
 
-def mg_levels(nx, ny, dx=None, dy=None):
-    """Global multigrid levels of the mixed solve (the last one is the coarse CTA's):
-    halve both axes, or only the strongly coupled one, while above 4096 cells."""
+def mg_shapes(nx, ny, dx=None, dy=None):
+    """Global multigrid levels (nx_l, ny_l) of the mixed solve (the last one is the
+    coarse CTA's finest): halve both axes, or only the strongly coupled one, while
+    above 4096 cells -- the plan the library builds."""
     import numpy as np
     dx = 1.0 / max(nx - 1, 1) if dx is None else dx
     dy = 1.0 / max(ny - 1, 1) if dy is None else dy
     cx, cy = float(np.float32(1.0 / (dx * dx))), float(np.float32(1.0 / (dy * dy)))
-    n, lx, ly = 1, nx, ny
-    while n < 16 and lx * ly > 4096:
+    lx, ly = nx, ny
+    out = [(lx, ly)]
+    while len(out) < 16 and lx * ly > 4096:
         fx, fy = lx % 2 == 0 and lx // 2 >= 8, ly % 2 == 0 and ly // 2 >= 8
         px, py = (2, 1) if cx > 2 * cy else ((1, 2) if cy > 2 * cx else (2, 2))
         if not ((px == 1 or fx) and (py == 1 or fy)):
@@ -176,8 +201,12 @@ def mg_levels(nx, ny, dx=None, dy=None):
             break
         lx, ly = lx // px, ly // py
         cx, cy = cx * py / px, cy * px / py
-        n += 1
-    return n
+        out.append((lx, ly))
+    return out
+
+
+def mg_levels(nx, ny, dx=None, dy=None):
+    return len(mg_shapes(nx, ny, dx, dy))
 
 
 def series_summary(xs):
@@ -187,7 +216,7 @@ def series_summary(xs):
     return {"mean": sum(xs) / len(xs), "min": min(xs), "max": max(xs), "first": list(xs[:10]), "last": list(xs[-10:])}
 
 
-def launches_per_step(precision, cg_iters, passes, nlev, persistent=True):
+def launches_per_step(precision, cg_iters, passes, nlev, persistent=False):
     """Kernel launches of one step from its loop trip counts."""
     if precision == "fp64":
         return 11 + 3 * cg_iters
@@ -205,48 +234,199 @@ def launches_per_step(precision, cg_iters, passes, nlev, persistent=True):
     return 8 + passes * per_pass + cg_iters * per_iter
 
 
+# Compulsory DRAM bytes per cell of each kernel at the level it works on (binary64
+# words 8 B, binary32 words 4 B): what it must read and write once.
+KERNEL_BYTES = {
+    # binary64 plain path
+    "k_prestep": 16,        # u, v
+    "k_predict": 32,        # u, v -> u*, v*
+    "k_rhs": 24,            # u*, v* -> b
+    "k_cg_init": 32,        # b -> b, r, x
+    "k_cg_matvec": 32,      # z (from r), p_old -> p, q
+    "k_cg_update": 48,      # x, p, r, q -> x, r
+    "k_post_resid": 16,     # b, x
+    "k_pin_correct": 80,    # x, u*, v*, u, v -> u*, v*, u, v, p
+    "k_post_diag": 48,      # u*, v*, p, b, u, v
+    # mixed form: binary64 stages
+    "k_prestep_m": 16,
+    "k_predict_m": 32,
+    "k_rhs_m": 24,
+    "k_mx_init": 40,        # b, p_prev -> b, x, r64
+    "k_mx_prep": 16,        # r64 -> f0 (binary32), e
+    "k_mx_correct": 20,     # x, e -> x
+    "k_mx_resid": 24,       # x, b -> r64
+    "k_pin_correct_m": 80,
+    "k_post_diag_m": 32,    # u*, v*, u, v
+    # mixed form: binary32 PCG and V-cycle (per cell of the kernel's level)
+    "k_mx_matvec": 16,      # z, p_old -> p, q
+    "k_mx_matvec_tma": 16,
+    "k_mx_update_down": 33,  # e, p, r, q -> e, r (24) + level-0 down-sweep: t, coarse f (9)
+    "k_mg_down": 9,         # f -> t, coarse f (a quarter of the cells on full coarsening)
+    "k_mg_post": 13,        # t, f, coarse u -> u
+    "k_mg_coarse": 8,       # f -> u of its finest level (everything else stays in shared memory)
+}
+
+
+def level_cells(shape_lists):
+    """Cells of the levels that have a coarser global level below them (the tiles of
+    the down- and up-sweeps of level l), and of every instance's last global level
+    (where its coarse CTA starts)."""
+    pre, coarse = {}, 0
+    for shapes in shape_lists:
+        for l, (a, b) in enumerate(shapes):
+            if l + 1 < len(shapes):
+                pre[l] = pre.get(l, 0) + a * b
+        coarse += shapes[-1][0] * shapes[-1][1]
+    return pre, coarse
+
+
+def kernel_table(prof, cells, shape_lists, step_ms, hbm):
+    """Rows {kernel, launches, total_us, us_per_launch, share, bytes_per_launch,
+    gbs, frac} of a profiled step, largest share first; plus the step-level
+    figures (all kernels' algorithmic bytes over the timed step's mean)."""
+    pre, coarse = level_cells(shape_lists)
+    all_ms = sum(ms for _, _, ms in prof)
+    rows, step_bytes = [], 0.0
+    for name, n, ms in prof:
+        base, _, lvl = name.partition("@")
+        per_cell = KERNEL_BYTES.get(base)
+        if base in ("k_mg_down", "k_mg_post"):
+            c = pre.get(int(lvl), 0)
+        elif base == "k_mg_coarse":
+            c = coarse
+        elif base in ("k_dt", "k_gather", "k_mx_persist"):
+            c = 0
+        else:
+            c = cells
+        b = per_cell * c if per_cell is not None else None
+        us = 1e3 * ms / max(n, 1)
+        row = {"kernel": name, "launches": n, "total_us": 1e3 * ms, "us_per_launch": us,
+               "share": ms / all_ms if all_ms > 0 else None, "bytes_per_launch": b}
+        if b:
+            row["gbs"] = b / (us * 1e-6) / 1e9
+            row["frac"] = row["gbs"] / hbm
+            step_bytes += b * n
+        rows.append(row)
+    rows.sort(key=lambda r: -(r["share"] or 0.0))
+    step = {"bytes": step_bytes, "profiled_ms": all_ms, "timed_ms": step_ms,
+            "achieved": step_bytes / (step_ms * 1e-3) / 1e9 if step_ms else None}
+    if step["achieved"] is not None:
+        step["frac"] = step["achieved"] / hbm
+    return rows, step
+
+
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
+# captures of the same kernel and workload, with the file that records the capture.
+TRAFFIC = {
+    ("cavity512", "k_mx_matvec"): (1.60e6, "profiles/k_mx_matvec_2048.md (512^2 capture)"),
+    ("cavity2048", "k_mx_matvec"): (34.11e6, "profiles/k_mx_matvec_2048.md"),
+    ("cavity2048", "k_mx_matvec_tma"): (33.74e6, "profiles/k_mx_matvec_tma_2048.md"),
+    ("cavity2048", "k_cg_matvec"): (94.64e6, "profiles/cavity2048_fp64_launches.md"),
+    ("cavity512", "k_cg_matvec"): (4.27e6, "profiles/k_cg_matvec_fp64_512.md"),
+}
+
+
+def profile_step(handle, run_one):
+    """One more step run kernel by kernel with events around every launch."""
+    import torch
+
+    from pyflow_solver_gb300 import _capi
+    lib = _capi.load()
+    _capi.check(lib.pfgb_set_profiling(handle, 1), "set_profiling")
+    try:
+        out = run_one()
+        torch.cuda.synchronize()
+        prof = _capi.profile_kernels(handle)
+    finally:
+        _capi.check(lib.pfgb_set_profiling(handle, 0), "set_profiling")
+    return prof, out
+
+
+def roofline_of(rows, step, workload, hbm, src):
+    top = rows[0]
+    tr = TRAFFIC.get((workload, top["kernel"]))
+    return {"bound": "hbm", "achieved": top.get("gbs"), "peak": hbm, "unit": "GB/s", "frac": top.get("frac"),
+            "traffic": tr[0] if tr else None, "traffic_source": tr[1] if tr else None,
+            "kernel": top["kernel"], "share_of_step": top["share"], "per_launch_us": top["us_per_launch"],
+            "launches_timed": top["launches"], "algorithmic_bytes_per_launch": top["bytes_per_launch"],
+            "peak_source": f"{src} (copy bandwidth)",
+            "bytes_model": "KERNEL_BYTES per cell of the kernel's level (bench.py)"}
+
+
 # ---- CPU arm -----------------------------------------------------------------
 
-def cpu_port_rate(name, steps):
-    """cell-updates/s of the oracle port (reference reductions, scipy CG sequence), one thread."""
+def cpu_port_rate(name, steps, warm=1):
+    """cell-updates/s of the oracle port (reference reductions, scipy CG sequence), one thread:
+    `warm` untimed steps from zero fields (step 0 has a zero right-hand side), then `steps`."""
     from oracle import step as ost
     cfg = cavity_cfg(name, "fp64")
     n = CAVITIES[name]["n"]
     st = ost.allocate_state(n, n)
     tr = ost.ResidualManager()
-    ost.step(cfg, st, tr, 0, red="numpy")              # step 0: zero RHS, not timed
+    for it in range(warm):
+        ost.step(cfg, st, tr, it, red="numpy")
     t0 = time.perf_counter()
-    for it in range(1, steps + 1):
+    for it in range(warm, warm + steps):
         ost.step(cfg, st, tr, it, red="numpy")
     dt = time.perf_counter() - t0
     return n * n * steps / dt, dt
 
 
-def _port_instance(args):
-    nx, ny, Re, U, steps = args
+def _port_group(args):
+    """One worker's share of the batch: its instances stepped `warm` times untimed, then
+    `steps` times timed (the instances are independent: no step-by-step hand-off)."""
+    group, warm, steps = args
     from oracle import step as ost
     from pyflow_solver_gb300.workloads import cavity_config
-    cfg = cavity_config(nx, ny, Re, U, "fp64")
-    st = ost.allocate_state(nx, ny)
-    tr = ost.ResidualManager()
-    for it in range(steps):
-        ost.step(cfg, st, tr, it, red="numpy")
-    return nx * ny * steps
+    sims = []
+    for nx, ny, Re, U in group:
+        sims.append((cavity_config(nx, ny, Re, U, "fp64"), ost.allocate_state(nx, ny), ost.ResidualManager()))
+    for it in range(warm):
+        for cfg, st, tr in sims:
+            ost.step(cfg, st, tr, it, red="numpy")
+    t0 = time.perf_counter()
+    for it in range(warm, warm + steps):
+        for cfg, st, tr in sims:
+            ost.step(cfg, st, tr, it, red="numpy")
+    return time.perf_counter() - t0, sum(nx * ny for nx, ny, _, _ in group) * steps
 
 
-def cpu_port_batched_rate(n_inst, steps, procs):
-    """The oracle port over the batched instances, one process per host core."""
+BLAS_THREAD_VARS = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+
+
+def cpu_port_batched_rate(steps, warm, procs):
+    """The oracle port over all 256 batched instances, split by cells over `procs`
+    processes (one per host core): cell-updates/s = all cells x steps / slowest worker."""
     import multiprocessing as mp
 
     from pyflow_solver_gb300.workloads import batched_instances
-    work = [(nx, ny, Re, U, steps) for nx, ny, Re, U in batched_instances(256, 0)[:n_inst]]
+    inst = sorted(batched_instances(256, 0), key=lambda t: -t[0] * t[1])
+    groups, load = [[] for _ in range(procs)], [0] * procs
+    for t in inst:                                     # largest first onto the least loaded worker
+        k = load.index(min(load))
+        groups[k].append(t)
+        load[k] += t[0] * t[1]
+    groups = [g for g in groups if g]
     ctx = mp.get_context("spawn")
-    with ctx.Pool(procs) as pool:
-        pool.map(_port_instance, work[:procs])           # start-up, not timed
-        t0 = time.perf_counter()
-        cells = sum(pool.map(_port_instance, work))
-        dt = time.perf_counter() - t0
-    return cells / dt, dt
+    # one BLAS thread per worker: the workers already take every core (the children
+    # inherit this environment before they import NumPy)
+    saved = {k: os.environ.get(k) for k in BLAS_THREAD_VARS}
+    os.environ.update({k: "1" for k in BLAS_THREAD_VARS})
+    try:
+        with ctx.Pool(len(groups)) as pool:
+            res = pool.map(_port_group, [(g, warm, steps) for g in groups])
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    wall = max(r[0] for r in res)
+    cells = sum(r[1] for r in res)
+    return cells / wall, wall
+
+
+REF_CAP = {"cavity512": 20, "cavity2048": 3, "batched256": 40, "serving": 40}
 
 
 def run_reference_arm(args):
@@ -254,26 +434,33 @@ def run_reference_arm(args):
     if rank != 0:
         return
     wl = args.workload
+    # the port's steps are seconds long: K and W are capped so that the run ends in a few minutes
+    steps = max(1, min(args.steps, REF_CAP[wl]))
     if wl in CAVITIES:
-        steps = max(1, min(args.steps, 6 if wl == "cavity512" else 1))
-        v, dt = cpu_port_rate(wl, steps)
+        warm = max(1, min(args.warmup, 3))
+        v, dt = cpu_port_rate(wl, steps, warm)
         cores = 1
-        sample = (f"steps 1..{steps} after an untimed step 0 of the same {CAVITIES[wl]['n']}^2 cavity "
-                  "(oracle port: NumPy restatement with the reference's np.dot/np.mean reductions and "
-                  "scipy's CG sequence; one thread)")
-        cfg = {"workload": describe(wl)}
+        n = CAVITIES[wl]["n"]
+        sample = (f"steps {warm}..{warm + steps - 1} of the {n}^2 cavity from zero fields after {warm} untimed "
+                  "(oracle port: NumPy restatement with the reference's np.dot/np.mean reductions and scipy's CG "
+                  "sequence; one thread -- the reference steps one cavity at a time)")
+        cfg = cavity_config_line(wl)
+        ms = 1e3 * dt / steps
     else:
+        warm = max(1, min(args.warmup, 5))
         cores = os.cpu_count() or 1
-        n_inst = min(256, 4 * cores)
-        v, dt = cpu_port_batched_rate(n_inst, 5, cores)
-        sample = f"5 steps of each of the first {n_inst} batched instances, one process per core"
-        cfg = {"workload": "256 batched cavities, seed 0" if wl == "batched256" else "serving trace mix"}
+        v, dt = cpu_port_batched_rate(steps, warm, cores)
+        sample = (f"all 256 batched instances, steps {warm}..{warm + steps - 1} after {warm} untimed, split by cells "
+                  f"over {cores} processes (one per host core; oracle port, lin_maxiter 300)")
+        cfg = batch_config() if wl == "batched256" else {"workload": "serving trace mix (the batched instances "
+                                                                     "stand in on the CPU)"}
+        ms = 1e3 * dt / steps
     line = {
         "impl": "reference", "metric": "cell-updates/s", "value": v, "unit": "cell-updates/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * CAVITIES[wl]["n"] ** 2 / v if wl in CAVITIES else None,
+        "n_gpus": args.gpus, "steps": steps, "warmup": warm, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": cfg,
+        "run": {"precision": PRECISION_REFERENCE},
         "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": cores, "kind": "port", "sample": sample,
                          "seconds": dt},
         "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -322,65 +509,6 @@ def max_over_ranks(x, dist):
     return float(t.item())
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the roofline
-# kernel, from the ncu captures summarised in profiles/ (two launches each, averaged).
-TRAFFIC = {
-    ("cavity512", "mixed::k_mx_matvec"): 1.60e6,
-    ("cavity2048", "mixed::k_mx_matvec"): 34.11e6,
-    ("cavity2048", "mixed::k_mx_matvec_tma"): 33.74e6,
-    ("cavity2048", "pfgb::k_cg_matvec"): 94.64e6,
-    ("cavity512", "pfgb::k_cg_matvec"): 4.27e6,
-}
-
-
-def mixed_solve_bytes(cells, inner, passes):
-    """Compulsory bytes of one persistent mixed solve (binary32 levels, binary64 refinement):
-    per inner iteration 16 (matvec) + 24 (update) + 22 (level-0 down- and up-sweep) + 7
-    (coarser levels) bytes per cell; per refinement pass 16 (prep) + 29 (its V-cycle) + 20
-    (correction) + 24 (binary64 residual); 32 for the start (mean removal, x = 0, r = b)."""
-    return cells * (32 + 89 * passes + 69 * inner)
-
-
-def kernel_roofline(lib, cfg, st, tr, it, cells, precision, workload=None):
-    """Live CUDA-event timing of the dominant kernel during one more step: the
-    persistent solve (mixed) or the CG matvec (binary64)."""
-    import ctypes
-
-    import torch
-
-    from pyflow_solver_gb300 import _capi, step
-    from pyflow_solver_gb300.solvers._handle import instance_for
-    from pyflow_solver_gb300.solvers.solver import step_params
-    P, *_ = step_params(cfg, st.nx, st.ny)
-    inst = instance_for(st, P)
-    hbm, src = peaks()
-    _capi.check(lib.pfgb_set_profiling(inst.handle, 1), "set_profiling")
-    _, _, diag = step(cfg, st, tr, it)
-    ms, n = ctypes.c_double(), ctypes.c_int()
-    _capi.check(lib.pfgb_profile_result(inst.handle, ctypes.byref(ms), ctypes.byref(n)), "profile_result")
-    _capi.check(lib.pfgb_set_profiling(inst.handle, 0), "set_profiling")
-    torch.cuda.synchronize()
-    per_launch_s = ms.value / 1e3 / max(n.value, 1)
-    from pyflow_solver_gb300.solvers import _handle
-    if precision == "mixed" and _handle.PERSISTENT:
-        nbytes = mixed_solve_bytes(cells, diag["cg_iterations"], diag.get("refine_passes", 0))
-        kern, model = "mixed::k_mx_persist", "mixed_solve_bytes (bench.py)"
-    elif precision == "mixed":
-        nbytes = 4 * 4 * cells
-        tma = ctypes.c_int()
-        _capi.check(lib.pfgb_matvec_form(inst.handle, ctypes.byref(tma)), "matvec_form")
-        kern = "mixed::k_mx_matvec_tma" if tma.value else "mixed::k_mx_matvec"
-        model = "4 binary32 words per cell"
-    else:
-        nbytes = 4 * 8 * cells
-        kern, model = "pfgb::k_cg_matvec", "4 binary64 words per cell"
-    achieved = nbytes / per_launch_s / 1e9
-    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": TRAFFIC.get((workload, kern)), "kernel": kern, "peak_source": f"{src} (copy bandwidth)",
-            "launches_timed": n.value, "per_launch_us": per_launch_s * 1e6,
-            "algorithmic_bytes_per_launch": nbytes, "bytes_model": model}
-
-
 def e2e_cavity(cfg, n, steps, warmup=2):
     """Through the public step() on a State whose fields are host NumPy arrays: `warmup`
     untimed steps, then `steps` timed ones (the same step range as the device-timed run)."""
@@ -407,8 +535,9 @@ def e2e_cavity(cfg, n, steps, warmup=2):
 def bench_cavity(args, dist, world, rank, local):
     import torch
 
-    from pyflow_solver_gb300 import ResidualManager, _capi, allocate_state, step
-    lib = _capi.load()
+    from pyflow_solver_gb300 import ResidualManager, allocate_state, step
+    from pyflow_solver_gb300.solvers._handle import instance_for
+    from pyflow_solver_gb300.solvers.solver import step_params
     wl = args.workload
     n = CAVITIES[wl]["n"]
     stream = torch.cuda.current_stream()
@@ -427,20 +556,28 @@ def bench_cavity(args, dist, world, rank, local):
         for _ in range(warmup):
             one()
         ms, diags = timed_steps(one, steps, stream, flush, dist)
-        return cfg, st, tr, box["it"], ms, diags
+        return cfg, st, one, ms, diags
 
     with ClockSampler(local) as clocks:
-        cfg, st, tr, it, ms, diags = run(args.precision, args.steps, args.warmup)
+        cfg, st, one, ms, diags = run(args.precision, args.steps, args.warmup)
     total = max_over_ranks(sum(ms), dist)
     value = n * n * args.steps * world / (total / 1e3)
     cg = [d["cg_iterations"] for d in diags]
     passes = [d.get("refine_passes", 0) for d in diags]
-    nlev = mg_levels(n, n)
-    launches = sum(launches_per_step(args.precision, c, p, nlev, args.persistent) for c, p in zip(cg, passes))
-    roof = None if args.no_roofline else kernel_roofline(lib, cfg, st, tr, it, n * n, args.precision, wl)
+    shapes = mg_shapes(n, n)
+    launches = sum(launches_per_step(args.precision, c, p, len(shapes), args.persistent) for c, p in zip(cg, passes))
+    kernels = roof = step_roof = None
+    if not args.no_roofline:
+        hbm, src = peaks()
+        P, *_ = step_params(cfg, st.nx, st.ny)
+        prof, _ = profile_step(instance_for(st, P).handle, one)
+        rows, step_roof = kernel_table(prof, n * n, [shapes] if args.precision == "mixed" else [], total / args.steps,
+                                       hbm)
+        kernels = rows
+        roof = roofline_of(rows, step_roof, wl, hbm, src)
     extra = {}
     if args.precision == "mixed" and not args.no_plain:
-        _, _, _, _, pms, pd = run("fp64", args.plain_steps, 1)
+        _, _, _, pms, pd = run("fp64", args.plain_steps, 1)
         ptot = max_over_ranks(sum(pms), dist)
         pval = n * n * args.plain_steps * world / (ptot / 1e3)
         extra["plain_fp64"] = {"value": pval, "unit": "cell-updates/s", "ms_per_step": ptot / args.plain_steps,
@@ -449,7 +586,7 @@ def bench_cavity(args, dist, world, rank, local):
     e2e_steps = args.steps if args.e2e_steps is None else args.e2e_steps
     e2e = e2e_cavity(cfg, n, e2e_steps, args.warmup) if e2e_steps > 0 else None
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         steps = 6 if wl == "cavity512" else 1
         v, dt = cpu_port_rate(wl, steps)
         cpu = {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port", "seconds": dt,
@@ -460,30 +597,31 @@ def bench_cavity(args, dist, world, rank, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64+f32" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": describe(wl), "nx": n, "ny": n, "Re": CAVITIES[wl]["Re"],
-                   "precision": PRECISION_NOTE[args.precision],
-                   "l2": "flushed between timed steps (256 MiB write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "timed_steps": f"steps {args.warmup}..{args.warmup + args.steps - 1} of a run from zero fields",
-                   "cg_iterations_per_step": series_summary(cg), "refine_passes_per_step": series_summary(passes),
-                   "steps_not_converged": sum(1 for d in diags if not d.get("Rp_converged", True))},
+        "config": cavity_config_line(wl),
+        "run": {"precision": PRECISION_NOTE[args.precision],
+                "parallelism": "replicas" if world > 1 else "single GPU",
+                "timed_steps": f"steps {args.warmup}..{args.warmup + args.steps - 1} of a run from zero fields",
+                "cg_iterations_per_step": series_summary(cg), "refine_passes_per_step": series_summary(passes),
+                "steps_not_converged": sum(1 for d in diags if not d.get("Rp_converged", True))},
         **extra,
         "step_latency_ms": pct(ms),
-        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roof, "step_roofline": step_roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clocks.summary(),
     }
     return line
 
 
-def bench_batched(args, dist, world, rank, local):
-    import numpy as np
+BATCH_WORKLOAD = ("256 lid-driven cavities from seed 0: nx, ny in {32,48,64,96,128}, Re log-uniform [100,5000], "
+                  "lid uniform [0.5,2]; one graph launch per step for all instances")
+
+
+def make_batch(inst, precision):
+    """The 256 instances over one device arena of fields (u, v, p of every instance)."""
     import torch
 
     from pyflow_solver_gb300.batch import BatchedCavities
     from pyflow_solver_gb300.core.ghost_fields import State
-    from pyflow_solver_gb300.workloads import batched_instances, cavity_config
-    inst = batched_instances(256, 0)
-    # one device arena for all fields (and its pinned host mirror for the end-to-end run)
+    from pyflow_solver_gb300.workloads import cavity_config
     sizes = [3 * (ny + 2) * (nx + 2) for nx, ny, _, _ in inst]
     arena = torch.zeros(sum(sizes), dtype=torch.float64, device="cuda")
     states, off = [], 0
@@ -491,8 +629,16 @@ def bench_batched(args, dist, world, rank, local):
         f = arena[off:off + sz].view(3, ny + 2, nx + 2)
         states.append(State(nx, ny, {"u": f[0], "v": f[1], "p": f[2]}))
         off += sz
-    cfgs = [cavity_config(nx, ny, Re, U, args.precision) for nx, ny, Re, U in inst]
-    B = BatchedCavities(cfgs, states)
+    cfgs = [cavity_config(nx, ny, Re, U, precision) for nx, ny, Re, U in inst]
+    return BatchedCavities(cfgs, states), arena
+
+
+def bench_batched(args, dist, world, rank, local):
+    import torch
+
+    from pyflow_solver_gb300.workloads import batched_instances
+    inst = batched_instances(256, 0)
+    B, arena = make_batch(inst, args.precision)
     cells = int(B.cells.sum())
     stream = torch.cuda.current_stream()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -504,8 +650,16 @@ def bench_batched(args, dist, world, rank, local):
     value = cells * args.steps * world / (total / 1e3)
     maxit = [int(o["cg_iterations"].max()) for o in outs]
     maxpass = [int(o["refine_passes"].max()) for o in outs]
-    nlev = max(mg_levels(nx, ny) for nx, ny, _, _ in inst)
+    shapes = [mg_shapes(nx, ny) for nx, ny, _, _ in inst]
+    nlev = max(len(s) for s in shapes)
     launches = sum(launches_per_step(args.precision, c, p, nlev, args.persistent) for c, p in zip(maxit, maxpass))
+    kernels = roof = step_roof = None
+    if not args.no_roofline:
+        hbm, src = peaks()
+        prof, _ = profile_step(B._h, B.step_arrays)
+        kernels, step_roof = kernel_table(prof, cells, shapes if args.precision == "mixed" else [],
+                                          total / args.steps, hbm)
+        roof = roofline_of(kernels, step_roof, "batched256", hbm, src)
     # end to end: the fields of all instances copied in (pinned host -> device) and out every step
     host = torch.empty(arena.numel(), dtype=torch.float64, pin_memory=True)
     host.copy_(arena)
@@ -521,23 +675,47 @@ def bench_batched(args, dist, world, rank, local):
     nbytes = arena.numel() * 8
     e2e = {"value": cells * e2e_steps / dt, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
            "d2h_bytes_per_step": nbytes, "steps": e2e_steps}
+    B.close()
+    del arena
+    extra = {}
+    if args.precision == "mixed" and not args.no_plain:
+        # the same 256 cavities through the plain binary64 path (the reference's CG, lin_maxiter 300)
+        P, parena = make_batch(inst, "fp64")
+        P.step_arrays()                                # step 0: zero right-hand side
+        pms, pouts = timed_steps(P.step_arrays, args.plain_steps, stream, flush, dist)
+        ptot = max_over_ranks(sum(pms), dist)
+        pval = cells * args.plain_steps * world / (ptot / 1e3)
+        extra["plain_fp64"] = {"value": pval, "unit": "cell-updates/s", "ms_per_step": ptot / args.plain_steps,
+                               "steps": args.plain_steps, "timed_steps": f"steps 1..{args.plain_steps}",
+                               "max_cg_iterations_per_step": [int(o["cg_iterations"].max()) for o in pouts]}
+        extra["speedup_vs_plain_fp64"] = value / pval
+        P.close()
+        del parena
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        v, wall = cpu_port_batched_rate(2, 1, cores)
+        cpu = {"value": v, "unit": "cell-updates/s", "cores": cores, "kind": "port", "seconds": wall,
+               "sample": f"all 256 instances, steps 1..2 after step 0, split by cells over {cores} processes "
+                         "(oracle port: NumPy restatement with the reference's reductions and CG sequence, "
+                         "lin_maxiter 300)"}
     line = {
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64+f32" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": "256 lid-driven cavities from seed 0: nx, ny in {32,48,64,96,128}, Re log-uniform "
-                               "[100,5000], lid uniform [0.5,2]; one graph launch per step for all instances",
-                   "instances": len(inst), "cells_per_step": cells, "precision": PRECISION_NOTE[args.precision],
-                   "l2": "flushed between timed steps (256 MiB write)",
-                   "max_cg_iterations_per_step": series_summary(maxit),
-                   "max_refine_passes_per_step": series_summary(maxpass),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": batch_config(),
+        "run": {"precision": PRECISION_NOTE[args.precision],
+                "timed_steps": f"steps {args.warmup}..{args.warmup + args.steps - 1} of a run from zero fields",
+                "max_cg_iterations_per_step": series_summary(maxit),
+                "max_refine_passes_per_step": series_summary(maxpass),
+                "parallelism": "replicas" if world > 1 else "single GPU"},
+        **extra,
         "step_latency_ms": pct(ms),
-        "roofline": None, "cpu_baseline": None, "e2e": e2e, "gpu_launches": launches,
-        "gpu_launches_note": "from the largest loop trip counts of each step", "clocks": clocks.summary(),
+        "roofline": roof, "step_roofline": step_roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": launches, "gpu_launches_note": "from the largest loop trip counts of each step",
+        "clocks": clocks.summary(),
     }
-    B.close()
     return line
 
 
@@ -582,7 +760,7 @@ def main():
                     help="timed steps (default: the workload's own step count, 2000 / 1000 / 500)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="cavity512", choices=["cavity512", "cavity2048", "batched256", "serving"])
+    ap.add_argument("--workload", default="batched256", choices=["batched256", "cavity512", "cavity2048", "serving"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")

@@ -231,9 +231,11 @@ PFGB_API int pfgb_cg_solve(int op, const double* b, double* x, int nx, int ny, d
  * can synchronise the whole device), or a host application that has reserved
  * the device memory for its own pool and admits no third-party allocation.
  * The CG work vectors live in one fixed device array compiled into the library
- * (about 8.4 MiB, reserved on every device that loads the library until the
- * process exits), so nx*ny must not exceed 262,144 cells (512 x 512); larger
- * grids return PFGB_EINVAL without launching anything.
+ * (about 8.5 MiB), reserved on a device when the library's module is loaded
+ * there -- with CUDA's lazy module loading, the default, that can be this
+ * function's first call on the device -- and held until the process exits, so
+ * nx*ny must not exceed 262,144 cells (512 x 512); larger grids return
+ * PFGB_EINVAL without launching anything.
  * The first call on a device looks up that array's device address (once per
  * device, with the device current); make that first call before any stream
  * capture.  Every call reuses the same array: two calls that overlap on the GPU
@@ -284,15 +286,29 @@ PFGB_API int pfgb_set_cg_variant(pfgb_handle* handle, int variant);
 
 /* ---- measurement ----------------------------------------------------------- */
 
-/* Record CUDA events around every pressure-matvec launch (p = z + beta p;
- * q = A p; p.q) of the following steps of this handle: the binary64 CG matvec,
- * or with precision 1 the binary32 PCG matvec of the inner solves -- or, when
- * the persistent solve is on, around that one launch.  Steps then run as
- * individual launches (no graph).  No reference counterpart: benchmark
- * instrumentation. */
+/* Record CUDA events around every kernel launch of the following steps of this
+ * handle.  Steps then run as individual launches (no graph); after each host
+ * read-back inside a step a short spin kernel keeps the stream busy, so the
+ * events bracket kernel execution rather than host launch latency.  No
+ * reference counterpart: benchmark instrumentation. */
 PFGB_API int pfgb_set_profiling(pfgb_handle* handle, int on);
-/* Total device time (ms) and number of the timed launches of the last step. */
+/* Total device time (ms) and number of the pressure-matvec launches (p = z +
+ * beta p; q = A p; p.q) of the last profiled step: the binary64 CG matvec, or
+ * with precision 1 the binary32 PCG matvec of the inner solves (or the
+ * persistent solve as one launch where that form runs). */
 PFGB_API int pfgb_profile_result(pfgb_handle* handle, double* ms, int* launches);
+
+/* Device time of one kernel over the last profiled step. */
+typedef struct pfgb_kernel_time {
+  char name[48];     /* kernel name; multigrid kernels carry their level ("k_mg_down@1") */
+  int launches;
+  double total_ms;
+} pfgb_kernel_time;
+/* Per-kernel sums of the last profiled step, in order of first launch: writes up
+ * to `capacity` entries and sets *count to the number of kernels (which may
+ * exceed capacity).  Call after the step returned (its stream is synchronised).
+ * No reference counterpart: benchmark instrumentation. */
+PFGB_API int pfgb_profile_kernels(pfgb_handle* handle, pfgb_kernel_time* out, int capacity, int* count);
 /* Measured FP64 FMA issue rate of the current device, in 1e12 instructions/s.
  * No reference counterpart: the denominator of the FP64 roofline. */
 PFGB_API int pfgb_probe_fp64(void* stream, double* tops);

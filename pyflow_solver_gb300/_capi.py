@@ -60,6 +60,10 @@ class SolveOut(ctypes.Structure):
     ]
 
 
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 48), ("launches", ctypes.c_int), ("total_ms", ctypes.c_double)]
+
+
 # name -> (restype, argtypes)
 _P = ctypes.c_void_p
 _L = ctypes.c_long
@@ -98,6 +102,7 @@ SIGNATURES = {
     "pfgb_set_cg_variant": (_I, [_P, _I]),
     "pfgb_set_profiling": (_I, [_P, _I]),
     "pfgb_profile_result": (_I, [_P, c_double_p, ctypes.POINTER(_I)]),
+    "pfgb_profile_kernels": (_I, [_P, ctypes.POINTER(KernelTime), _I, ctypes.POINTER(_I)]),
     "pfgb_probe_fp64": (_I, [_P, c_double_p]),
 }
 
@@ -139,3 +144,17 @@ def last_error() -> str:
 def check(rc: int, what: str):
     if rc != 0:
         raise PFGBError(f"{what} failed ({rc}): {last_error()}")
+
+
+def profile_kernels(handle) -> list:
+    """Per-kernel device time of the last profiled step of a handle:
+    [(name, launches, total_ms)] in order of first launch."""
+    lib = load()
+    cap = 64
+    while True:
+        buf = (KernelTime * cap)()
+        n = ctypes.c_int()
+        check(lib.pfgb_profile_kernels(handle, buf, cap, ctypes.byref(n)), "pfgb_profile_kernels")
+        if n.value <= cap:
+            return [(buf[k].name.decode(), int(buf[k].launches), float(buf[k].total_ms)) for k in range(n.value)]
+        cap = n.value

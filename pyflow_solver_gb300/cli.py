@@ -102,7 +102,7 @@ def main(argv: list[str] | None = None) -> int:
     tracker = ResidualManager()
     if args.restart:
         try:
-            state, meta = load_checkpoint(args.restart)
+            state, meta = load_checkpoint(args.restart, device="cuda")
             ck_hash = meta.get("structured_config_hash")
             if ck_hash and ck_hash != cfg.config_hash and not args.allow_hash_mismatch:
                 print(f"Refusing restart: checkpoint hash {ck_hash} != current {cfg.config_hash} "

@@ -4,6 +4,7 @@
 #include <string>
 #include <vector>
 
+#include "kprof.cuh"
 #include "pfgb_internal.h"
 #include "step64.cuh"
 
@@ -96,6 +97,20 @@ extern "C" int pfgb_set_profiling(pfgb_handle* handle, int on) {
 extern "C" int pfgb_profile_result(pfgb_handle* handle, double* ms, int* launches) {
   if (!handle || !ms || !launches) return set_error(PFGB_EINVAL, "null argument");
   return instance64_profile_result(handle->inst, ms, launches);
+}
+
+extern "C" int pfgb_profile_kernels(pfgb_handle* handle, pfgb_kernel_time* out, int capacity, int* count) {
+  if (!handle || !count || (capacity > 0 && !out)) return set_error(PFGB_EINVAL, "null argument");
+  std::vector<KTime> kt;
+  if (int rc = instance64_profile_kernels(handle->inst, kt)) return rc;
+  *count = (int)kt.size();
+  for (int k = 0; k < capacity && k < (int)kt.size(); ++k) {
+    std::memset(out[k].name, 0, sizeof(out[k].name));
+    std::strncpy(out[k].name, kt[k].name.c_str(), sizeof(out[k].name) - 1);
+    out[k].launches = kt[k].launches;
+    out[k].total_ms = kt[k].ms;
+  }
+  return PFGB_OK;
 }
 
 extern "C" int pfgb_probe_fp64(void* stream, double* tops) {

@@ -761,8 +761,8 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
   return ok != 0u;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity) {
-  for (int i = 0; i < MV_SPIN_LIMIT; ++i)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity, int limit = MV_SPIN_LIMIT) {
+  for (int i = 0; i < limit; ++i)
     if (mbar_try_wait(b, parity)) return true;
   return false;
 }
@@ -1432,12 +1432,19 @@ __global__ void __launch_bounds__(MT, 4) k_mx_matvec_tma(const MixDesc* __restri
       beta = live ? (float)cget(&Mc.ctrl->beta) : 0.f;
     }
     if (live) {
-      const bool ok = mbar_wait_bounded(&sm.bar[s], (phase >> s) & 1u);
+      const unsigned par = (phase >> s) & 1u;
+      const bool ok = mbar_wait_bounded(&sm.bar[s], par);
       phase ^= 1u << s;
       if (__syncthreads_or(!ok)) {
+        // a copy did not land in time: flag the error, and before the CTA (and its
+        // shared memory) goes, wait -- longer, still bounded -- for each copy it may
+        // have in flight: this tile's (stage s) unless thread 0 saw it land, and the
+        // next tile's (stage s ^ 1) if thread 0 issued it.  A copy still outstanding
+        // after that is abandoned; the step reports the failed wait to the host.
         if (x.tid() == 0) {
           atomicExch(&ml->gb.err, 1);
-          if (next) mbar_wait_bounded(&sm.bar[s ^ 1], (phase >> (s ^ 1)) & 1u);
+          if (!ok) mbar_wait_bounded(&sm.bar[s], par, 16 * MV_SPIN_LIMIT);
+          if (next) mbar_wait_bounded(&sm.bar[s ^ 1], (phase >> (s ^ 1)) & 1u, 16 * MV_SPIN_LIMIT);
         }
         return;
       }
@@ -2181,72 +2188,69 @@ int append_solve(GraphChain& c, Batch* B) {
 
 // Host-driven form of append_solve with direct launches: the loop decisions
 // are read back from the loop control after each stopping test.  Used for
-// profiling (ncu does not profile kernels of graphs with conditional nodes).
+// profiling (ncu does not profile kernels of graphs with conditional nodes, and
+// with B->kp set every launch is timed with events).
 static void launch_vcycle(Batch* B, int gate, Smooth sw, cudaStream_t s, int l0 = 0) {
+  KProf* kp = B->kp;
   for (int l = l0; l + 1 < B->maxlev; ++l) {
-    if (B->ntpre[l]) k_mg_down<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, sw);
+    if (B->ntpre[l]) PFGB_TIMED(kp, "k_mg_down", l, s, k_mg_down<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, sw));
   }
+  // (each instance's coarse CTA starts from that instance's last global level)
   if (B->coarse_nt == CT2)
-    k_mg_coarse<CT2><<<B->n, CT2, B->coarse_smem, s>>>(B->dd, gate, 8, sw);
+    PFGB_TIMED(kp, "k_mg_coarse", -1, s, k_mg_coarse<CT2><<<B->n, CT2, B->coarse_smem, s>>>(B->dd, gate, 8, sw));
   else
-    k_mg_coarse<CT><<<B->n, CT, B->coarse_smem, s>>>(B->dd, gate, 8, sw);
+    PFGB_TIMED(kp, "k_mg_coarse", -1, s, k_mg_coarse<CT><<<B->n, CT, B->coarse_smem, s>>>(B->dd, gate, 8, sw));
   for (int l = B->maxlev - 2; l >= 0; --l)
-    if (B->ntpre[l]) k_mg_post<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, sw);
+    if (B->ntpre[l]) PFGB_TIMED(kp, "k_mg_post", l, s, k_mg_post<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, sw));
+}
+
+// A few tens of microseconds of device work ahead of the next launches (profiling only).
+static void pad_stream(Batch* B, cudaStream_t s) {
+  if (B->kp) k_pad<<<1, 32, 0, s>>>(B->pad, 20000);
 }
 
 int run_direct(Batch* B, cudaStream_t s) {
   const Smooth sw = B->sw;
+  KProf* kp = B->kp;
   if (B->persist) {
     k_ml_reset<<<1, 32, 0, s>>>(B->loop, 0);
     PersistArgs a = persist_args(B, sw);
     void* args[] = {&a};
-    const bool timed = B->ev && B->nev >= 2;
-    if (timed) {
-      k_pad<<<1, 32, 0, s>>>(B->pad, 20000);
-      cudaEventRecord(B->ev[0], s);
-    }
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_mx_persist, dim3(B->pgrid), dim3(CT), args, B->psmem, s);
+    cudaError_t e = cudaSuccess;
+    pad_stream(B, s);
+    PFGB_TIMED(kp, "k_mx_persist", -1, s,
+               e = cudaLaunchCooperativeKernel((const void*)k_mx_persist, dim3(B->pgrid), dim3(CT), args, B->psmem, s));
     if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("persistent solve launch: ") + cudaGetErrorString(e));
-    if (timed) {
-      cudaEventRecord(B->ev[1], s);
-      *B->ev_used = 1;
-    }
     return PFGB_OK;
   }
   const int g0 = B->ntl[0];
   MixLoop h;
-  int timed_launches = 0;
-  if (B->ev_used) *B->ev_used = 0;
   auto read = [&]() -> bool {
-    return cudaMemcpyAsync(&h, B->loop, sizeof(MixLoop), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
-           cudaStreamSynchronize(s) == cudaSuccess;
+    const bool ok = cudaMemcpyAsync(&h, B->loop, sizeof(MixLoop), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+                    cudaStreamSynchronize(s) == cudaSuccess;
+    pad_stream(B, s);
+    return ok;
   };
   k_ml_reset<<<1, 32, 0, s>>>(B->loop, 0);
-  k_mx_init<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop);
+  PFGB_TIMED(kp, "k_mx_init", -1, s, k_mx_init<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop));
   if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
   for (int po = 0; h.outer_active > 0 && po < h.gmax_o; ++po) {
     k_ml_reset<<<1, 32, 0, s>>>(B->loop, 1);
-    k_mx_prep<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop);
-    if (B->ntpre[0]) k_mg_down<<<B->ntpre[0], MT, 0, s>>>(B->dd, B->tpre[0], 0, 1, sw);
+    PFGB_TIMED(kp, "k_mx_prep", -1, s, k_mx_prep<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop));
+    if (B->ntpre[0]) PFGB_TIMED(kp, "k_mg_down", 0, s, k_mg_down<<<B->ntpre[0], MT, 0, s>>>(B->dd, B->tpre[0], 0, 1, sw));
     if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
     for (int pi = 0; h.inner_active > 0 && pi < h.gmax_i; ++pi) {
       launch_vcycle(B, 1, sw, s, 1);
-      // the events bracket the matvec alone: the V-cycle queued before keeps the stream busy
-      const bool timed = B->ev && 2 * timed_launches + 1 < B->nev;
-      if (timed) cudaEventRecord(B->ev[2 * timed_launches], s);
       if (B->mv_tma)
-        k_mx_matvec_tma<<<B->mv_grid, MT, 0, s>>>(B->dd, B->tl[0], B->ntl[0], B->loop);
+        PFGB_TIMED(kp, "k_mx_matvec_tma", -1, s,
+                   k_mx_matvec_tma<<<B->mv_grid, MT, 0, s>>>(B->dd, B->tl[0], B->ntl[0], B->loop));
       else
-        k_mx_matvec<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
-      if (timed) {
-        cudaEventRecord(B->ev[2 * timed_launches + 1], s);
-        *B->ev_used = ++timed_launches;
-      }
-      k_mx_update_down<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0, sw);
+        PFGB_TIMED(kp, "k_mx_matvec", -1, s, k_mx_matvec<<<g0, MT, 0, s>>>(B->dd, B->tl[0]));
+      PFGB_TIMED(kp, "k_mx_update_down", -1, s, k_mx_update_down<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0, sw));
       if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
     }
-    k_mx_correct<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
-    k_mx_resid<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0);
+    PFGB_TIMED(kp, "k_mx_correct", -1, s, k_mx_correct<<<g0, MT, 0, s>>>(B->dd, B->tl[0]));
+    PFGB_TIMED(kp, "k_mx_resid", -1, s, k_mx_resid<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0));
     if (!read()) return set_error(PFGB_ECUDA, "mixed solve: control read failed");
   }
   cudaError_t e = cudaGetLastError();

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "graph.cuh"
+#include "kprof.cuh"
 #include "persist.cuh"
 #include "stencil.cuh"
 #include "step64.cuh"
@@ -123,10 +124,8 @@ struct Batch {
   MixLoop* loop = nullptr;
   int gmax_o = 1, gmax_i = 1;                  // trip bounds of the loop guards
   Smooth sw = {0.8f, 0.8f, 0.8f};              // smoother weights
-  // profiling (direct launches): events around each PCG matvec launch
-  cudaEvent_t* ev = nullptr;
-  int nev = 0;
-  int* ev_used = nullptr;
+  // profiling (direct launches): per-kernel events, owned by the step's instance
+  KProf* kp = nullptr;
   float* pad = nullptr;                        // sink of the profiling pad kernel
   // the persistent form of the solve (one cooperative launch)
   int persist_ok = 0;                          // the device co-schedules its CTAs

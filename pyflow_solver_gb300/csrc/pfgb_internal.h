@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/pfgb.h"
 
@@ -31,6 +32,8 @@ int instance64_set_cg_variant(Instance64* I, int v);
 int instance64_set_params(Instance64* I, int k, const pfgb_params* prm);
 int instance64_set_profiling(Instance64* I, int on);
 int instance64_profile_result(Instance64* I, double* ms, int* launches);
+struct KTime;
+int instance64_profile_kernels(Instance64* I, std::vector<KTime>& out);
 int probe_fp64(cudaStream_t s, double* tops);
 int cg_solve_noalloc_run(int op, const double* b, double* x, int nx, int ny, double dx, double dy, int precond,
                          double invd, double tol, int maxiter, cudaStream_t s, pfgb_solve_out* out);

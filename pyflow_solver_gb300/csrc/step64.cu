@@ -995,10 +995,10 @@ struct Instance64 {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_mode = -1;               // 0 step, 1 projection
-  // optional per-launch timing of k_cg_matvec (benchmark roofline, single instance)
+  // per-kernel timing of the following steps (benchmark profiling; direct launches)
   int profiling = 0;
-  std::vector<cudaEvent_t> ev;
-  int ev_used = 0;
+  KProf kp;
+  KProf* prof() { return profiling ? &kp : nullptr; }
 };
 
 // where the step's loop guards report, and the bounded waits (the persistent solve's
@@ -1166,7 +1166,6 @@ int instance64_create(const pfgb_params* prm, Instance64** out) { return instanc
 void instance64_destroy(Instance64* I) {
   if (!I) return;
   if (I->mix) mixed::batch_destroy(I->mix);
-  for (cudaEvent_t e : I->ev) cudaEventDestroy(e);
   if (I->exec) cudaGraphExecDestroy(I->exec);
   if (I->graph) cudaGraphDestroy(I->graph);
   if (I->ws) cudaFree(I->ws);
@@ -1243,30 +1242,26 @@ static void launch_update(int var, int grid, cudaStream_t s, const InstDesc* dd,
 
 // Direct launches of the projection stage (host loop bound = largest maxiter).
 static void enqueue_projection(Instance64* I, cudaStream_t s) {
-  k_rhs<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-  k_cg_init<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc, nullptr);
+  KProf* kp = I->prof();
+  PFGB_TIMED(kp, "k_rhs", -1, s, k_rhs<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc));
+  PFGB_TIMED(kp, "k_cg_init", -1, s, k_cg_init<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc, nullptr));
   for (int k = 0; k < I->maxiter_max; ++k) {
-    const bool timed = I->profiling && (size_t)(2 * k + 1) < I->ev.size();
-    if (timed) cudaEventRecord(I->ev[2 * k], s);
-    launch_matvec<0>(I->cg_var, I->ntcg, s, I->dd, I->tcg);
-    if (timed) {
-      cudaEventRecord(I->ev[2 * k + 1], s);
-      I->ev_used = k + 1;
-    }
-    launch_update(I->cg_var, I->ntcg, s, I->dd, I->tcg);
+    PFGB_TIMED(kp, "k_cg_matvec", -1, s, launch_matvec<0>(I->cg_var, I->ntcg, s, I->dd, I->tcg));
+    PFGB_TIMED(kp, "k_cg_update", -1, s, launch_update(I->cg_var, I->ntcg, s, I->dd, I->tcg));
   }
-  k_post_resid<0><<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-  k_pin_correct<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-  k_post_diag<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-  k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n, loop_trip(I), loop_gb_err(I));
+  PFGB_TIMED(kp, "k_post_resid", -1, s, k_post_resid<0><<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc));
+  PFGB_TIMED(kp, "k_pin_correct", -1, s, k_pin_correct<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc));
+  PFGB_TIMED(kp, "k_post_diag", -1, s, k_post_diag<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc));
+  PFGB_TIMED(kp, "k_gather", -1, s, k_gather<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n, loop_trip(I), loop_gb_err(I)));
 }
 
 static void enqueue_prologue(Instance64* I, cudaStream_t s) {
-  if (I->mix) k_prestep_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
-  else k_prestep<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
-  if (!I->mix) k_dt<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n);
-  if (I->mix) k_predict_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
-  else k_predict<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc);
+  KProf* kp = I->prof();
+  if (I->mix) PFGB_TIMED(kp, "k_prestep_m", -1, s, k_prestep_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm));
+  else PFGB_TIMED(kp, "k_prestep", -1, s, k_prestep<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc));
+  if (!I->mix) PFGB_TIMED(kp, "k_dt", -1, s, k_dt<<<(I->n + 31) / 32, 32, 0, s>>>(I->dd, I->n));
+  if (I->mix) PFGB_TIMED(kp, "k_predict_m", -1, s, k_predict_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm));
+  else PFGB_TIMED(kp, "k_predict", -1, s, k_predict<<<I->ntpc, NT, 0, s>>>(I->dd, I->tpc));
 }
 
 // Build the step graph (mode 0: full step; mode 1: stand-alone projection).
@@ -1375,6 +1370,17 @@ static int read_out(Instance64* I, cudaStream_t s, pfgb_step_out* out) {
   return PFGB_OK;
 }
 
+// A few tens of microseconds of device work ahead of the next launches (profiling:
+// the first timed kernel then does not absorb the host's launch latency).
+__global__ void k_pad64(float* sink, int n) {
+  float x = (float)threadIdx.x;
+  for (int i = 0; i < n; ++i) x = fmaf(x, 1.0000001f, 0.5f);
+  if (x == -1.f) *sink = x;
+}
+static void pad_stream(Instance64* I, cudaStream_t s) {
+  k_pad64<<<1, 32, 0, s>>>(reinterpret_cast<float*>(I->out_d), 20000);
+}
+
 // Run one step (mode 0) or projection (mode 1) for the bound instances.
 static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
   if (int rc = upload_desc(I, s)) return rc;
@@ -1387,12 +1393,19 @@ static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
     if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("graph launch: ") + cudaGetErrorString(e));
     return read_out(I, s, out);
   }
+  KProf* kp = I->prof();
+  if (kp) {
+    kp->clear();
+    if (I->mix) I->mix->kp = kp;
+    pad_stream(I, s);
+  }
   if (mode == 0) enqueue_prologue(I, s);
   if (I->mix) {
-    k_rhs_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
+    PFGB_TIMED(kp, "k_rhs_m", -1, s, k_rhs_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm));
     if (int rc = mixed::run_direct(I->mix, s)) return rc;
-    k_pin_correct_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm);
-    k_post_diag_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm, I->mix->dd, loop_trip(I), loop_gb_err(I));
+    PFGB_TIMED(kp, "k_pin_correct_m", -1, s, k_pin_correct_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm));
+    PFGB_TIMED(kp, "k_post_diag_m", -1, s,
+               k_post_diag_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm, I->mix->dd, loop_trip(I), loop_gb_err(I)));
   } else {
     enqueue_projection(I, s);
   }
@@ -1613,37 +1626,35 @@ int instance64_set_graph(Instance64* I, int on) {
   return PFGB_OK;
 }
 
-// Per-launch timing of the (binary64 or binary32) matvec kernel in the following steps.
+// Per-kernel timing of the following steps (direct launches, events around each).
 int instance64_set_profiling(Instance64* I, int on) {
-  if (on && I->ev.empty()) {
-    int n = 2 * (I->maxiter_max > 0 ? I->maxiter_max : 1);
-    if (I->mix) n = std::max(n, 2 * I->mix->gmax_o * I->mix->gmax_i);
-    I->ev.resize(n);
-    for (int k = 0; k < n; ++k)
-      if (cudaEventCreate(&I->ev[k]) != cudaSuccess) return set_error(PFGB_ECUDA, "cudaEventCreate failed");
-  }
-  I->profiling = on;
-  I->ev_used = 0;
-  if (I->mix) {
-    I->mix->ev = on ? I->ev.data() : nullptr;
-    I->mix->nev = on ? (int)I->ev.size() : 0;
-    I->mix->ev_used = on ? &I->ev_used : nullptr;
-  }
+  I->profiling = on ? 1 : 0;
+  I->kp.clear();
+  if (I->mix) I->mix->kp = on ? &I->kp : nullptr;
   return PFGB_OK;
 }
 
-// Sum of the matvec launch durations of the last (synchronised) step.  Launches
-// that returned at once because the solve had converged are included.
+// Per-kernel sums of the last (synchronised) profiled step.
+int instance64_profile_kernels(Instance64* I, std::vector<KTime>& out) {
+  if (!I->kp.ok) return set_error(PFGB_ECUDA, "profiling events could not be created or recorded");
+  const cudaError_t e = kprof_collect(I->kp, out);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("event timing: ") + cudaGetErrorString(e));
+  return PFGB_OK;
+}
+
+// Sum of the pressure-matvec launch durations of the last (synchronised) profiled
+// step (the persistent solve as a whole where that form runs).  Launches that
+// returned at once because the solve had converged are included.
 int instance64_profile_result(Instance64* I, double* ms, int* launches) {
-  double tot = 0.0;
-  for (int k = 0; k < I->ev_used; ++k) {
-    float t = 0.f;
-    cudaError_t e = cudaEventElapsedTime(&t, I->ev[2 * k], I->ev[2 * k + 1]);
-    if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("event timing: ") + cudaGetErrorString(e));
-    tot += t;
-  }
-  *ms = tot;
-  *launches = I->ev_used;
+  std::vector<KTime> kt;
+  if (int rc = instance64_profile_kernels(I, kt)) return rc;
+  *ms = 0.0;
+  *launches = 0;
+  for (const KTime& k : kt)
+    if (k.name == "k_cg_matvec" || k.name == "k_mx_matvec" || k.name == "k_mx_matvec_tma" || k.name == "k_mx_persist") {
+      *ms += k.ms;
+      *launches += k.launches;
+    }
   return PFGB_OK;
 }
 
@@ -1792,9 +1803,10 @@ namespace pfgb {
 // synchronise the whole device), or an embedding application that reserved the
 // device memory for its own pool and admits no third-party allocation.  For them the work vectors, reduction slots and
 // control block of the CG live in one file-scope device array of fixed size,
-// reserved once when the library's module is loaded on a device and held until
+// reserved on a device when the library's module is loaded there and held until
 // the process exits.  Its limit is NOALLOC_MAX_CELLS = 262,144 cells
-// (512 x 512), about 9 MiB per device.
+// (512 x 512); the array is about 8.5 MiB per device (sizeof(Scratch), pinned
+// below by a static_assert).
 namespace noalloc {
 
 constexpr long NOALLOC_MAX_CELLS = 1L << 18;
@@ -1811,6 +1823,9 @@ struct Scratch {
   InstDesc desc;
   Tile tiles[NOALLOC_MAX_TILES];
 };
+
+static_assert(sizeof(Scratch) > 8.5 * 1024 * 1024 && sizeof(Scratch) < 8.6 * 1024 * 1024,
+              "the documented size of the allocation-free CG scratch (about 8.5 MiB)");
 
 static __device__ __align__(256) Scratch g_scratch;
 
@@ -1851,8 +1866,9 @@ int cg_solve_noalloc_run(int op, const double* b, double* x, int nx, int ny, dou
     return set_error(PFGB_EINVAL, "grid shape needs more tiles than the allocation-free CG scratch holds");
   Scratch* S = nullptr;
   if (int rc = scratch_address(&S)) return rc;
-  // the slots and the control block must start from zero on every call
-  cudaError_t e = cudaMemsetAsync(S->slots, 0, sizeof(S->slots) + sizeof(S->ctrl), s);
+  // the slots and the control block (and any padding between them) must start from
+  // zero on every call
+  cudaError_t e = cudaMemsetAsync(S->slots, 0, offsetof(Scratch, desc) - offsetof(Scratch, slots), s);
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("clearing the CG scratch: ") + cudaGetErrorString(e));
   XASlot* slots = S->slots;
   Ctrl64* ctrl = &S->ctrl;

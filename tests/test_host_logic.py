@@ -1,4 +1,5 @@
 """Host-side logic of the GPU package that needs no GPU."""
+import json
 from types import SimpleNamespace
 
 import numpy as np
@@ -54,6 +55,36 @@ def test_checkpoint_format_round_trip(tmp_path):
     assert meta["field_hashes"]["u"] == ck._hash_array(st.fields["u"])
     st3, meta3 = ck.load_checkpoint_bytes(ck.save_checkpoint_bytes(st, 3, 0.0, cfg), device=None)
     assert meta3["iteration"] == 3
+    # the reference returns NumPy fields; so does load_checkpoint by default
+    st4, _ = ck.load_checkpoint(path)
+    assert isinstance(st4.fields["u"], np.ndarray)
+    # no step bookkeeping yet: no state_meta entry, and a loaded state starts with empty meta
+    assert "state_meta" not in meta and st2.meta == {}
+    # the structured hash only for a SimulationConfig (any other object with a string
+    # config_hash attribute gets None, as in the reference)
+    assert meta["structured_config_hash"] is None
+    cfg.config_hash = "abcdef0123"
+    assert json.loads(str(np.load(ck.save_checkpoint(str(tmp_path / "d.npz"), st, 1, 0.0, cfg))["meta"]))[
+        "structured_config_hash"] is None
+    from pyflow_solver_gb300.config.model import SimulationConfig
+    sc = SimulationConfig(nx=4, ny=3)
+    m5 = json.loads(str(np.load(ck.save_checkpoint(str(tmp_path / "e.npz"), st, 1, 0.0, sc))["meta"]))
+    assert m5["structured_config_hash"] == sc.config_hash
+
+
+def test_checkpoint_keeps_step_bookkeeping(tmp_path):
+    """dt_prev and the last five divergence norms go into meta["state_meta"] and come back
+    into state.meta (a restart then continues exactly); the reference's own keys stay."""
+    from pyflow_solver_gb300.core.ghost_fields import State
+    st = State(4, 3, {k: np.zeros((5, 6)) for k in "uvp"})
+    st.meta = {"dt_prev": 0.0123, "divergence_history": [1.0, 2.0, 3.0, 4.0, 5.0, 6.0], "dx": 0.3, "nu": 0.01}
+    path = ck.save_checkpoint(str(tmp_path / "c.npz"), st, 5, 0.1, SimpleNamespace(nx=4, ny=3))
+    st2, meta = ck.load_checkpoint(path)
+    assert meta["state_meta"] == {"dt_prev": 0.0123, "divergence_history": [2.0, 3.0, 4.0, 5.0, 6.0]}
+    assert st2.meta == {"dt_prev": 0.0123, "divergence_history": [2.0, 3.0, 4.0, 5.0, 6.0]}
+    for key in ("iteration", "time", "nx", "ny", "config_hash", "structured_config_hash", "field_hashes", "seed",
+                "schema_version"):
+        assert key in meta
 
 
 def test_driver_requires_state_or_grid():
@@ -95,5 +126,30 @@ def test_bench_accounting_helpers():
     assert bench.launches_per_step("mixed", 10, 2, 4, persistent=False) == 8 + 2 * 6 + 10 * 8
     # one level (the whole V-cycle in the coarse CTA): coarse, matvec, update; no level-0 down-sweep
     assert bench.launches_per_step("mixed", 10, 2, 1, persistent=False) == 8 + 2 * 5 + 10 * 3
-    assert bench.mixed_solve_bytes(100, 10, 2) == 100 * (32 + 178 + 690)
     assert bench.pct([3.0, 1.0, 2.0]) == {"p50": 2.0, "p95": 3.0, "p99": 3.0}
+    assert bench.mg_shapes(512, 512) == [(512, 512), (256, 256), (128, 128), (64, 64)]
+
+
+def test_bench_kernel_table():
+    """Per-kernel rows of a profiled step: bytes from the per-cell table times the cells of
+    each kernel's level, shares of the profiled time, the largest share first."""
+    import bench
+    shapes = [bench.mg_shapes(512, 512)]
+    prof = [("k_mx_matvec", 6, 0.060), ("k_mg_down@1", 6, 0.030), ("k_mg_coarse", 6, 0.090),
+            ("k_mx_update_down", 6, 0.060)]
+    rows, step = bench.kernel_table(prof, 512 * 512, shapes, step_ms=0.5, hbm=1000.0)
+    assert [r["kernel"] for r in rows][0] == "k_mg_coarse"
+    by = {r["kernel"]: r for r in rows}
+    assert by["k_mx_matvec"]["bytes_per_launch"] == 16 * 512 * 512
+    assert by["k_mg_down@1"]["bytes_per_launch"] == 9 * 256 * 256
+    assert by["k_mg_coarse"]["bytes_per_launch"] == 8 * 64 * 64
+    assert abs(by["k_mx_matvec"]["us_per_launch"] - 10.0) < 1e-9
+    assert abs(by["k_mx_matvec"]["gbs"] - 16 * 512 * 512 / 10e-6 / 1e9) < 1e-6
+    assert abs(sum(r["share"] for r in rows) - 1.0) < 1e-12
+    total = sum(r["bytes_per_launch"] * r["launches"] for r in rows)
+    assert step["bytes"] == total and abs(step["achieved"] - total / 0.5e-3 / 1e9) < 1e-6
+    roof = bench.roofline_of(rows, step, "cavity512", 1000.0, "measured")
+    assert roof["kernel"] == "k_mg_coarse" and roof["share_of_step"] == rows[0]["share"]
+    # a batch: the coarse CTA of each instance starts from its own last global level
+    pre, coarse = bench.level_cells([bench.mg_shapes(128, 128), bench.mg_shapes(64, 32)])
+    assert pre == {0: 128 * 128} and coarse == 64 * 64 + 64 * 32
