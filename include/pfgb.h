@@ -103,6 +103,8 @@ typedef struct pfgb_step_out {
   double cont_sq;            /* ||div_central(u,v;1,1)||^2 after the step */
   unsigned reduction_flags;  /* bit 3: a term fell below 2^-1184, bit 4: overflow */
   int refine_passes;         /* precision 1: FP64 refinement passes of the pressure solve */
+  double steady_slope;       /* pfgb_set_steady: least-squares slope of log10(Ru) over the window (NaN if none) */
+  int steady;                /* pfgb_set_steady: the steady-state test passed at this step */
 } pfgb_step_out;
 
 typedef struct pfgb_solve_out {
@@ -268,6 +270,17 @@ PFGB_API int pfgb_set_persistent(pfgb_handle* handle, int on);
  * CTA, or forced by PFGB_MATVEC_TMA=1 / 0 when the instance is created), 0 when it
  * is one tile per CTA.  Both give the same bits.  No reference counterpart. */
 PFGB_API int pfgb_matvec_form(pfgb_handle* handle, int* tma);
+
+/* Device-side steady-state test of instance k of a handle (k = 0 for a single
+ * cavity): the residual tracker's Ru series -- seed 1.0, then the Ru of every
+ * following full step -- is kept on the device, and each step record reports
+ * the least-squares slope of log10(Ru) over the last `window` entries
+ * (steady_slope) and whether every entry was positive and |slope| < slope_tol
+ * (steady).  window 0 turns the test off; otherwise 2 <= window <= 1024.
+ * Each call restarts the series from its seed.  Replaces the host-side test of
+ * the steady driver (src/pyflow/driver/simulation_driver.py:135-149); lets a
+ * batch retire instances on it without reading their Ru series back. */
+PFGB_API int pfgb_set_steady(pfgb_handle* handle, int k, int window, double slope_tol);
 
 /* ---- tile autotuner ---------------------------------------------------------- */
 

@@ -50,6 +50,7 @@ class StepOut(ctypes.Structure):
         ("divafter_sq", ctypes.c_double), ("linres_sq", ctypes.c_double),
         ("cont_sq", ctypes.c_double),
         ("reduction_flags", ctypes.c_uint), ("refine_passes", ctypes.c_int),
+        ("steady_slope", ctypes.c_double), ("steady", ctypes.c_int),
     ]
 
 
@@ -103,6 +104,7 @@ SIGNATURES = {
     "pfgb_set_profiling": (_I, [_P, _I]),
     "pfgb_profile_result": (_I, [_P, c_double_p, ctypes.POINTER(_I)]),
     "pfgb_profile_kernels": (_I, [_P, ctypes.POINTER(KernelTime), _I, ctypes.POINTER(_I)]),
+    "pfgb_set_steady": (_I, [_P, _I, _I, _D]),
     "pfgb_probe_fp64": (_I, [_P, c_double_p]),
 }
 

@@ -21,8 +21,11 @@ Two host paths share the same launch:
 The state arrays must stay the same CUDA tensors (they are updated in place);
 ``rebind(k)`` re-reads instance k's arrays after they were replaced.
 ``set_params(k, config)`` gives slot k new physical parameters (continuous
-batching reuses slots for new requests).  ``graph=False`` launches the kernels
-one by one instead of one CUDA graph per step (for kernel profilers).
+batching reuses slots for new requests).  ``set_steady(k, window, tol)`` arms
+the device-side steady-state test of instance k (the steady driver's slope test
+on its Ru series); the step records then carry ``steady`` and
+``steady_slope``.  ``graph=False`` launches the kernels one by one instead of
+one CUDA graph per step (for kernel profilers).
 """
 from __future__ import annotations
 
@@ -81,6 +84,8 @@ class BatchedCavities:
         _capi.check(_capi.load().pfgb_set_graph(h, int(graph)), "pfgb_set_graph")
         from .solvers import _handle
         _capi.check(_capi.load().pfgb_set_persistent(h, 1 if _handle.PERSISTENT else 0), "pfgb_set_persistent")
+        self._steady = {}
+        self.last_out = None
         self.cg_variant = None
         if _handle.AUTOTUNE and params[0].precision == 0:
             key = ("batch",) + tuple(sorted((int(s.nx), int(s.ny)) for s in self.states))
@@ -138,6 +143,17 @@ class BatchedCavities:
                 raise ValueError(f"instance {k}: field {name!r} must be a contiguous float64 CUDA tensor of shape {shape}")
             self._ptr[r, k] = a.data_ptr()
 
+    def set_steady(self, k, window, tol=2e-3):
+        """Arm (window >= 2) or disarm (window 0) the device-side steady-state test of
+        instance k: least-squares slope of log10(Ru) over the last `window` entries of
+        its Ru series (seed 1.0, then every step), passed when |slope| < tol.  The
+        series restarts from its seed."""
+        _capi.check(_capi.load().pfgb_set_steady(self._h, int(k), int(window), float(tol)), "pfgb_set_steady")
+        if window:
+            self._steady[int(k)] = (int(window), float(tol))
+        else:
+            self._steady.pop(int(k), None)
+
     def set_params(self, k, config, reset=True):
         """New physical parameters for slot k (same grid, spacing and precision).
 
@@ -158,6 +174,8 @@ class BatchedCavities:
             self.trackers[k] = ResidualManager()
             self.iterations[k] = 0
             self._load_meta(k)
+            if k in self._steady:
+                self.set_steady(k, *self._steady[k])
 
     # ---- stepping ----------------------------------------------------------
     def step_arrays(self, active=None):
@@ -179,6 +197,7 @@ class BatchedCavities:
             self._h, ptr[0].ctypes.data_as(_VP), ptr[1].ctypes.data_as(_VP), ptr[2].ctypes.data_as(_VP),
             self._ins, stream_handle(), self._outs), "pfgb_batch_step")
         out = self._out_np.copy()
+        self.last_out = out
         idx = np.nonzero(act)[0]
         self._dt_prev[idx] = out["dt"][idx]
         full = idx[self._hist_len[idx] >= 5]

@@ -207,3 +207,8 @@ extern "C" int pfgb_batch_set_params(pfgb_handle* handle, int k, const pfgb_para
   if (!handle || !params) return set_error(PFGB_EINVAL, "null argument");
   return instance64_set_params(handle->inst, k, params);
 }
+
+extern "C" int pfgb_set_steady(pfgb_handle* handle, int k, int window, double slope_tol) {
+  if (!handle) return set_error(PFGB_EINVAL, "null handle");
+  return instance64_set_steady(handle->inst, k, window, slope_tol);
+}

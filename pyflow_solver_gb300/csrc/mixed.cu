@@ -1080,140 +1080,149 @@ __device__ __forceinline__ void ph_resid(const X& x, const MixDesc& M, const MTi
 // prolongation as the global levels; the bottom level, at most 64 cells, by its
 // pseudo-inverse, else eight Jacobi sweeps) forms the coarse "solve" -- a fixed
 // linear, symmetric operator, as PCG requires.  The CTA has NT threads (1024, or
-// 512 for batches of more instances than SMs, two CTAs to an SM); every sum is
-// taken in an order that does not depend on NT, so both give the same bits.
+// 512 for batches of more instances than SMs, two CTAs to an SM); every cell is
+// computed with the same operations whatever NT is, and every sum is taken in an
+// order that does not depend on NT, so both give the same bits.
 constexpr int CT = 1024;                     // threads of the coarse CTA (and of the persistent CTAs)
 constexpr int CT2 = 512;                     // the batch form
 constexpr int CMAX = 4096;                   // cells of its finest level
 constexpr int BMAX = 64;                     // bottom levels up to this size are solved exactly
 
-struct CLvl {                                // a shared-memory level
-  int nx, ny, off;                           // off: offset into the level arrays
+// A shared-memory level, stored with a one-cell ring around it: interior cell
+// (j, i) at off + (j + 1) * pw + i + 1, pw = nx + 2.  The ring makes every
+// stencil branch-free.  It holds zeros while the array is the source of a
+// smoothing sweep or of a residual (a Neumann level has no neighbour across a
+// wall; the diagonal counts only the faces that exist), and the mirror image of
+// the edge cells while the array is read by the restriction or the prolongation
+// (a wall cell then takes all of its parent's weight, 3/4 + 1/4 of the same value,
+// as the global levels' wall rules give it).
+struct CLvl {
+  int nx, ny, off, pw;
   float cx, cy;
   int kx, ky;                                // coarsening factors to the next level
 };
 
-__device__ __forceinline__ float c_diag(const CLvl& L, int j, int i) {
-  float d = 0.f;
-  if (i > 0) d += L.cx;
-  if (i < L.nx - 1) d += L.cx;
-  if (j > 0) d += L.cy;
-  if (j < L.ny - 1) d += L.cy;
-  return d;
+// index 3 fx + fy of a cell's diagonal in its level's tables: fx, fy = the faces it has in x, in y
+__device__ __forceinline__ int c_dk(const CLvl& L, int j, int i) {
+  return 3 * ((i > 0) + (i < L.nx - 1)) + ((j > 0) + (j < L.ny - 1));
 }
 
-__device__ __forceinline__ float c_nsum(const CLvl& L, const float* a, int j, int i) {
-  const float* b = a + L.off;
-  float s = 0.f;
-  if (i > 0) s = fmaf(L.cx, b[j * L.nx + i - 1], s);
-  if (i < L.nx - 1) s = fmaf(L.cx, b[j * L.nx + i + 1], s);
-  if (j > 0) s = fmaf(L.cy, b[(j - 1) * L.nx + i], s);
-  if (j < L.ny - 1) s = fmaf(L.cy, b[(j + 1) * L.nx + i], s);
-  return s;
+// cx (a_W + a_E) + cy (a_S + a_N) at padded index c (the ring supplies the walls' zeros)
+__device__ __forceinline__ float c_nsum(const CLvl& L, const float* a, int c) {
+  return fmaf(L.cy, a[c + L.pw], fmaf(L.cy, a[c - L.pw], fmaf(L.cx, a[c + 1], L.cx * a[c - 1])));
+}
+
+// v into the ring cells next to edge cell (j, i) at padded index c (corners included)
+__device__ __forceinline__ void c_ring(float* a, const CLvl& L, int c, int j, int i, float v) {
+  const bool w0 = i == 0, w1 = i == L.nx - 1;
+  if (w0) a[c - 1] = v;
+  if (w1) a[c + 1] = v;
+  if (j == 0) {
+    a[c - L.pw] = v;
+    if (w0) a[c - L.pw - 1] = v;
+    if (w1) a[c - L.pw + 1] = v;
+  }
+  if (j == L.ny - 1) {
+    a[c + L.pw] = v;
+    if (w0) a[c + L.pw - 1] = v;
+    if (w1) a[c + L.pw + 1] = v;
+  }
 }
 
 // Cells of a shared-memory level, visited by the CTA's NT / 32 warps, a row of 32
-// cells to a warp (no integer division on the index).
+// cells to a warp; c is the padded index of cell (j, i).
 #define C_FOR(Lv, ...)                                               \
   for (int j = threadIdx.x >> 5; j < (Lv).ny; j += NT / 32)          \
     for (int i = threadIdx.x & 31; i < (Lv).nx; i += 32) {           \
-      const int c = j * (Lv).nx + i;                                 \
+      const int c = (Lv).off + (j + 1) * (Lv).pw + i + 1;            \
       __VA_ARGS__                                                    \
     }
 
-// a cell's diagonal: from the table dg when the CTA keeps one (NT == CT), else formed
+// one weighted-Jacobi sweep src -> dst on level L (zero ring on src); rd: the level's
+// reciprocal diagonals; all threads, ends with a barrier
 template <int NT>
-__device__ __forceinline__ float c_dg(const CLvl& L, const float* dg, int c, int j, int i) {
-  if constexpr (NT == CT) return dg[L.off + c];
-  else return c_diag(L, j, i);
-}
-
-// one weighted-Jacobi sweep src -> dst on level L (all threads; ends with a barrier)
-template <int NT>
-__device__ __forceinline__ void c_sweep(const CLvl& L, const float* dg, const float* f, const float* src, float* dst,
+__device__ __forceinline__ void c_sweep(const CLvl& L, const float* rd, const float* f, const float* src, float* dst,
                                         float omega) {
-  C_FOR(L, {
-    dst[L.off + c] = fmaf(1.f - omega, src[L.off + c],
-                          __fdividef(omega * (f[L.off + c] + c_nsum(L, src, j, i)), c_dg<NT>(L, dg, c, j, i)));
-  })
+  C_FOR(L, { dst[c] = fmaf(1.f - omega, src[c], omega * (f[c] + c_nsum(L, src, c)) * rd[c_dk(L, j, i)]); })
   __syncthreads();
 }
 
-// The coarse V-cycle of instance M by the whole NT-thread CTA; sm: 4 x (its
-// levels' cells) floats of shared memory for 1024 threads (with a table of the cells'
-// diagonals), 3 x for 512 (two CTAs to an SM; the diagonals formed where used, the
-// same values).
+// The coarse V-cycle of instance M by the whole NT-thread CTA; sm: 3 x (its
+// levels' padded cells) floats of shared memory.
 template <int NT>
 __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, float* sm) {
   Lvl C = M.lev[M.nlev - 1];
   if (M.nlev == 1) C.f = f_cur(M);
   const int nl = M.coarse_levels;
-  // the level table in shared memory (a local array indexed by the level would live in local memory)
+  // the level table and each level's nine diagonals and their reciprocals, in shared memory
   __shared__ CLvl L[8];
+  __shared__ float s_d[8][9], s_rd[8][9];
   __shared__ int s_tot;
   if (threadIdx.x == 0) {
     int nx = C.nx, ny = C.ny, t = 0;
     for (int l = 0; l < nl; ++l) {
-      L[l].nx = nx;
-      L[l].ny = ny;
-      L[l].off = t;
-      L[l].cx = M.ccx[l];
-      L[l].cy = M.ccy[l];
-      L[l].kx = M.ckx[l];
-      L[l].ky = M.cky[l];
-      t += nx * ny;
-      nx /= L[l].kx;
-      ny /= L[l].ky;
+      L[l] = CLvl{nx, ny, t, nx + 2, M.ccx[l], M.ccy[l], M.ckx[l], M.cky[l]};
+      t += (nx + 2) * (ny + 2);
+      nx /= M.ckx[l];
+      ny /= M.cky[l];
     }
     s_tot = t;
+  }
+  if (threadIdx.x < 8 * 9) {
+    const int l = threadIdx.x / 9, k = threadIdx.x - 9 * l, fx = k / 3, fy = k - 3 * fx;
+    if (l < nl) {
+      float d = 0.f;
+      if (fx >= 1) d += M.ccx[l];
+      if (fx == 2) d += M.ccx[l];
+      if (fy >= 1) d += M.ccy[l];
+      if (fy == 2) d += M.ccy[l];
+      s_d[l][k] = d;
+      s_rd[l][k] = d > 0.f ? 1.f / d : 0.f;
+    }
   }
   __syncthreads();
   const int tot = s_tot;
   float* rh = sm;            // right-hand side of every level (level 0: the entry level's f)
   float* e = sm + tot;       // pre-smoothed iterate on the way down; the bottom solution
   float* w = sm + 2 * tot;   // residual on the way down; each level's result on the way up
-  float* dg = sm + 3 * tot;  // every cell's diagonal, formed once (1024-thread CTAs)
+  for (int k = threadIdx.x; k < 2 * tot; k += NT) e[k] = 0.f;   // e and w with their rings
   const CLvl Le = L[0];   // register copies of the level descriptors (the level arrays are written
                           // through pointers the compiler cannot tell from the shared table)
   C_FOR(Le, { rh[c] = __ldcg(C.f + (long)j * C.ld + i); })
-  if constexpr (NT == CT) {
-    for (int l = 0; l < nl; ++l) {
-      const CLvl Lv = L[l];
-      C_FOR(Lv, { dg[Lv.off + c] = c_diag(Lv, j, i); })
-    }
-  }
   __syncthreads();
   for (int l = 0; l + 1 < nl; ++l) {
     const CLvl Lv = L[l];
-    const float* r = rh + Lv.off;
-    // e = S(S(0)); the first sweep from zero is pointwise (w1 rh / d) and is folded into the second
+    const float* d = s_d[l];
+    const float* rd = s_rd[l];
+    // e = S(S(0)): the first sweep from zero is pointwise, w = w1 D^-1 rh (zero ring), then the second
+    C_FOR(Lv, { w[c] = sw.w1 * rh[c] * rd[c_dk(Lv, j, i)]; })
+    __syncthreads();
+    C_FOR(Lv, { e[c] = fmaf(1.f - sw.w2, w[c], sw.w2 * (rh[c] + c_nsum(Lv, w, c)) * rd[c_dk(Lv, j, i)]); })
+    __syncthreads();
+    // residual rh - A e into w, its ring the mirror of its edges; then rh_{l+1} = P^T w
     C_FOR(Lv, {
-      auto s1 = [&](int jj, int ii) {
-        return __fdividef(sw.w1 * r[jj * Lv.nx + ii], c_dg<NT>(Lv, dg, jj * Lv.nx + ii, jj, ii));
-      };
-      float ns = 0.f;
-      if (i > 0) ns = fmaf(Lv.cx, s1(j, i - 1), ns);
-      if (i < Lv.nx - 1) ns = fmaf(Lv.cx, s1(j, i + 1), ns);
-      if (j > 0) ns = fmaf(Lv.cy, s1(j - 1, i), ns);
-      if (j < Lv.ny - 1) ns = fmaf(Lv.cy, s1(j + 1, i), ns);
-      e[Lv.off + c] = fmaf(1.f - sw.w2, s1(j, i), __fdividef(sw.w2 * (r[c] + ns), c_dg<NT>(Lv, dg, c, j, i)));
+      const float v = rh[c] - (d[c_dk(Lv, j, i)] * e[c] - c_nsum(Lv, e, c));
+      w[c] = v;
+      c_ring(w, Lv, c, j, i, v);
     })
     __syncthreads();
-    // residual rh - A e of this level into w, then rh_{l+1} = P^T w
-    C_FOR(Lv, { w[Lv.off + c] = r[c] - (c_dg<NT>(Lv, dg, c, j, i) * e[Lv.off + c] - c_nsum(Lv, e, j, i)); })
-    __syncthreads();
     const CLvl Cv = L[l + 1];
-    C_FOR(Cv, { rh[Cv.off + c] = restrict_val(w + Lv.off, Lv.nx, 0, 0, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i); })
+    const float* wf = w + Lv.off + Lv.pw + 1;
+    C_FOR(Cv, { rh[c] = restrict_lv<true>(wf, Lv.pw, 0, 0, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i); })
     __syncthreads();
   }
   {
     const CLvl Lv = L[nl - 1];
     const int nb = Lv.nx * Lv.ny;
+    auto cell = [&Lv](int q) {            // padded index of bottom cell q (row-major)
+      const int qj = q / Lv.nx;
+      return Lv.off + (qj + 1) * Lv.pw + (q - qj * Lv.nx) + 1;
+    };
     if (M.binv) {
       // exact bottom solve: e = A+ rh (at most BMAX cells).  A+ is exactly symmetric, so
       // column q0 is read for row q0 (consecutive threads, consecutive addresses); the
       // sum over q is split into NS slices of QS terms, added in slice order through w
-      // (dead on the way down past the restrictions).
+      // (dead past the restrictions; the up-sweep rewrites it, rings included).
       constexpr int NS = 16, QS = BMAX / NS;
       if (nb == BMAX && tot >= NS * BMAX) {
         for (int v = threadIdx.x; v < NS * BMAX; v += NT) {
@@ -1222,7 +1231,7 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
 #pragma unroll
           for (int k = 0; k < QS; ++k) {
             const int q = h * QS + k;
-            acc = fmaf(__ldg(M.binv + (long)q * nb + q0), rh[Lv.off + q], acc);
+            acc = fmaf(__ldg(M.binv + (long)q * nb + q0), rh[cell(q)], acc);
           }
           w[v] = acc;
         }
@@ -1230,40 +1239,53 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
         if (threadIdx.x < BMAX) {
           float sacc = w[threadIdx.x];
           for (int k = 1; k < NS; ++k) sacc += w[k * BMAX + threadIdx.x];
-          e[Lv.off + threadIdx.x] = sacc;
+          const int q0 = threadIdx.x, qj = q0 / Lv.nx, c = cell(q0);
+          e[c] = sacc;
+          c_ring(e, Lv, c, qj, q0 - qj * Lv.nx, sacc);
         }
       } else {
         for (int q0 = threadIdx.x; q0 < nb; q0 += NT) {
           float acc = 0.f;
-          for (int q = 0; q < nb; ++q) acc = fmaf(__ldg(M.binv + (long)q * nb + q0), rh[Lv.off + q], acc);
-          e[Lv.off + q0] = acc;
+          for (int q = 0; q < nb; ++q) acc = fmaf(__ldg(M.binv + (long)q * nb + q0), rh[cell(q)], acc);
+          const int qj = q0 / Lv.nx, c = cell(q0);
+          e[c] = acc;
+          c_ring(e, Lv, c, qj, q0 - qj * Lv.nx, acc);
         }
       }
       __syncthreads();
     } else {
-      C_FOR(Lv, { e[Lv.off + c] = 0.f; })
+      // Jacobi sweeps from e = 0 between e and w (both zero, rings included), then the
+      // result into e with its mirror ring
+      for (int q = 0; q < bottom_sweeps; ++q) c_sweep<NT>(Lv, s_rd[nl - 1], rh, (q & 1) ? w : e, (q & 1) ? e : w, sw.wb);
+      const float* res = (bottom_sweeps & 1) ? w : e;
+      C_FOR(Lv, {
+        const float v = res[c];
+        e[c] = v;
+        c_ring(e, Lv, c, j, i, v);
+      })
       __syncthreads();
-      for (int q = 0; q < bottom_sweeps; ++q) c_sweep<NT>(Lv, dg, rh, (q & 1) ? w : e, (q & 1) ? e : w, sw.wb);
-      if (bottom_sweeps & 1) {
-        C_FOR(Lv, { e[Lv.off + c] = w[Lv.off + c]; })
-        __syncthreads();
-      }
     }
   }
   // up: w_l = S(S(e_l + P result_{l+1})); the bottom's result is in e, every other level's in w
   for (int l = nl - 2; l >= 0; --l) {
     const CLvl Lv = L[l];
     const CLvl Cv = L[l + 1];
-    const float* ec = (l + 1 == nl - 1) ? e : w;
-    const float* ecl = ec + Cv.off;
-    const int cnx = Cv.nx;
-    auto catc = [ecl, cnx](int J, int I) { return ecl[J * cnx + I]; };
+    const float* rd = s_rd[l];
+    const float* zc = ((l + 1 == nl - 1) ? e : w) + Cv.off + Cv.pw + 1;   // mirror ring
+    const int cpw = Cv.pw;
+    auto catc = [zc, cpw](int J, int I) { return zc[J * cpw + I]; };
     C_FOR(Lv, {
-      w[Lv.off + c] = e[Lv.off + c] + prolong_val(catc, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i);
+      w[c] = e[c] + prolong_lv<true>(catc, Cv.nx, Cv.ny, Lv.kx, Lv.ky, j, i);
+      c_ring(w, Lv, c, j, i, 0.f);         // zero ring: w is the next sweep's source
     })
     __syncthreads();
-    c_sweep<NT>(Lv, dg, rh, w, e, sw.w2);
-    c_sweep<NT>(Lv, dg, rh, e, w, sw.w1);
+    c_sweep<NT>(Lv, rd, rh, w, e, sw.w2);
+    C_FOR(Lv, {
+      const float v = fmaf(1.f - sw.w1, e[c], sw.w1 * (rh[c] + c_nsum(Lv, e, c)) * rd[c_dk(Lv, j, i)]);
+      w[c] = v;
+      if (l > 0) c_ring(w, Lv, c, j, i, v);   // mirror ring for the next prolongation
+    })
+    __syncthreads();
   }
   const float* z = (nl == 1) ? e : w;
   C_FOR(Le, { C.u[(long)j * C.ld + i] = z[c]; })
@@ -1277,7 +1299,10 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
       const int vw = (threadIdx.x >> 5) + m * (NT / 32);
       FF acc = {0.f, 0.f};
       for (int j = vw; j < L0.ny; j += CT / 32)
-        for (int i = threadIdx.x & 31; i < L0.nx; i += 32) ff_add_prod(acc, rh[j * L0.nx + i], z[j * L0.nx + i]);
+        for (int i = threadIdx.x & 31; i < L0.nx; i += 32) {
+          const int c = (j + 1) * L0.pw + i + 1;
+          ff_add_prod(acc, rh[c], z[c]);
+        }
       acc = ff_warp_sum(acc);
       if ((threadIdx.x & 31) == 0) wsum[vw] = (double)acc.hi + (double)acc.lo;
     }
@@ -1647,7 +1672,7 @@ struct PlanLvl {
 struct Plan {
   std::vector<PlanLvl> global;   // global levels (kernels over tiles); the last is the CTA's first
   std::vector<PlanLvl> cta;      // levels of the coarse CTA (cta[0] == global.back())
-  int cta_tot = 0;               // cells of all CTA levels
+  int cta_tot = 0;               // cells of all CTA levels, each with a one-cell ring
 };
 
 // Coarsening from a level: halve both axes when the coupling is balanced, or only
@@ -1701,7 +1726,7 @@ static Plan make_plan(int nx, int ny, double dx, double dy) {
     L = coarsen(L, kx, ky);
     P.cta.push_back(L);
   }
-  for (const PlanLvl& c : P.cta) P.cta_tot += c.nx * c.ny;
+  for (const PlanLvl& c : P.cta) P.cta_tot += (c.nx + 2) * (c.ny + 2);   // with their rings
   return P;
 }
 
@@ -1838,8 +1863,8 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
       return set_error(PFGB_EINVAL, "mixed solver: the coarse multigrid level would exceed 4096 cells "
                                     "(nx and ny need enough factors of two)");
     }
-    smem = std::max(smem, (size_t)4 * plan[k].cta_tot * sizeof(float));
-    smem2 = std::max(smem2, (size_t)3 * plan[k].cta_tot * sizeof(float));
+    smem = std::max(smem, (size_t)3 * plan[k].cta_tot * sizeof(float));
+    smem2 = smem;
     const PlanLvl& bot = plan[k].cta.back();
     if (bot.nx * bot.ny <= BMAX) bytes += up((size_t)bot.nx * bot.ny * bot.nx * bot.ny * sizeof(float));
     B->maxlev = std::max(B->maxlev, (int)plan[k].global.size());

@@ -30,6 +30,7 @@ int instance64_matvec_form(const Instance64* I, int* tma);
 int instance64_autotune(Instance64* I, cudaStream_t s, int* chosen, double* us);
 int instance64_set_cg_variant(Instance64* I, int v);
 int instance64_set_params(Instance64* I, int k, const pfgb_params* prm);
+int instance64_set_steady(Instance64* I, int k, int window, double tol);
 int instance64_set_profiling(Instance64* I, int on);
 int instance64_profile_result(Instance64* I, double* ms, int* launches);
 struct KTime;

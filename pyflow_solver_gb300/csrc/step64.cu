@@ -854,6 +854,37 @@ __global__ void __launch_bounds__(NT) k_pin_correct_m(const InstDesc* __restrict
   }
 }
 
+// Append this step's Ru (sqrt(sum (u - u_old)^2) / max(1, N), as the host forms it) to
+// the instance's series and run the steady-state test on the last `window` entries.
+__device__ __noinline__ void steady_update(const InstDesc& Dd, double ru2, StepOut64* out) {
+  SteadyRing* sr = Dd.steady;
+  out->steady = 0;
+  out->steady_slope = __longlong_as_double(0x7ff8000000000000LL);
+  if (!sr || Dd.mode != 0) return;
+  const int W = sr->window;
+  if (W <= 0) return;
+  const double n = fmax(1.0, Dd.A.n_cells);
+  const double ru = sqrt(ru2) / n;
+  const int k = sr->count;
+  sr->y[k % STEADY_MAX_WINDOW] = ru > 0.0 ? log10(ru) : __longlong_as_double(0x7ff8000000000000LL);
+  sr->count = k + 1;
+  if (k + 1 < W) return;
+  double sy = 0.0, sxy = 0.0;
+  bool ok = true;
+  for (int m = 0; m < W; ++m) {
+    const double v = sr->y[(k - W + 1 + m) % STEADY_MAX_WINDOW];
+    ok = ok && (v == v);
+    sy += v;
+    sxy = fma((double)m, v, sxy);
+  }
+  if (!ok) return;
+  // sum (x - xm)^2 over x = 0 .. W - 1 is W (W^2 - 1) / 12
+  const double w = (double)W, xm = 0.5 * (w - 1.0), sxx = w * (w * w - 1.0) / 12.0;
+  const double slope = (sxy - xm * sy) / sxx;
+  out->steady_slope = slope;
+  out->steady = fabs(slope) < sr->tol ? 1 : 0;
+}
+
 // one StepOut64 record of instance Dd for the host
 __device__ __forceinline__ void gather_one(const InstDesc& Dd, const int* trip, const int* gb_err) {
   const XASlot* slots = Dd.slots;
@@ -881,6 +912,7 @@ __device__ __forceinline__ void gather_one(const InstDesc& Dd, const int* trip, 
   out->flags_or = f;
   out->refine_passes = ctrl->refine_passes;
   out->loop_status = (*trip ? 1 : 0) | ((gb_err && *gb_err) ? 2 : 0);
+  steady_update(Dd, out->ru2, out);
 }
 
 // ||div_c(u*, v*)||^2 after the correction, ||A p - b||^2, ||div_central(u, v; 1, 1)||^2
@@ -1032,7 +1064,7 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
   for (int k = 0; k < n; ++k) {
     const long ld = round_up(prms[k].nx, 32);
     vec[k] = up((size_t)ld * prms[k].ny * sizeof(double));
-    bytes += 8 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64)) +
+    bytes += 8 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64)) + up(sizeof(SteadyRing)) +
              up(3 * (size_t)count_tiles(prms[k].nx, prms[k].ny, PB_Y) * sizeof(double)) + up(sizeof(unsigned));
     add_tiles(tpc, k, prms[k].nx, prms[k].ny, PB_Y);
     add_tiles(tpcm, k, prms[k].nx, prms[k].ny, TY_M);
@@ -1098,6 +1130,7 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     D.nt_cg = I->ntcg_inst[I->cg_var][k];
     D.part = (double*)take(3 * (size_t)D.nt_pc * sizeof(double));
     D.ticket = (unsigned*)take(sizeof(unsigned));
+    D.steady = (SteadyRing*)take(sizeof(SteadyRing));   // zeroed: the test is off
   }
   I->dd = (InstDesc*)take(n * sizeof(InstDesc));
   I->tpc = (Tile*)take(tpc.size() * sizeof(Tile));
@@ -1329,6 +1362,24 @@ static int build_graph(Instance64* I, int mode) {
   return PFGB_OK;
 }
 
+// Turn instance k's device-side steady-state test on (window >= 2 entries of the Ru
+// series, slope tolerance tol) or off (window 0); either way its series restarts
+// from the tracker's seed 1.0 (log10 = 0).
+int instance64_set_steady(Instance64* I, int k, int window, double tol) {
+  if (k < 0 || k >= I->n) return set_error(PFGB_EINVAL, "instance index out of range");
+  if (window != 0 && (window < 2 || window > STEADY_MAX_WINDOW))
+    return set_error(PFGB_EINVAL, "steady window must be 0 (off) or between 2 and 1024 steps");
+  if (!(tol >= 0.0)) return set_error(PFGB_EINVAL, "steady slope tolerance must be >= 0");
+  struct {
+    int window, count;
+    double tol, y0;
+  } head = {window, 1, tol, 0.0};
+  static_assert(offsetof(SteadyRing, y) == 2 * sizeof(int) + sizeof(double), "SteadyRing header layout");
+  const cudaError_t e = cudaMemcpy(I->hd[k].steady, &head, sizeof(head), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("steady set-up: ") + cudaGetErrorString(e));
+  return PFGB_OK;
+}
+
 static void copy_out(const StepOut64& o, pfgb_step_out* out) {
   out->umax = o.umax;
   out->vmax = o.vmax;
@@ -1349,6 +1400,8 @@ static void copy_out(const StepOut64& o, pfgb_step_out* out) {
   out->cont_sq = o.cont2;
   out->reduction_flags = o.flags_or;
   out->refine_passes = o.refine_passes;
+  out->steady = o.steady;
+  out->steady_slope = o.steady_slope;
 }
 
 static int read_out(Instance64* I, cudaStream_t s, pfgb_step_out* out) {

@@ -61,6 +61,21 @@ struct StepOut64 {
   unsigned flags_or;    // OR of the result flags of all slots (inexact / overflow diagnostics)
   int refine_passes;
   int loop_status;      // bit 0: a loop guard stopped the step; bit 1: the persistent solve's barrier timed out
+  int steady;           // the steady-state test passed at this step (SteadyRing)
+  double steady_slope;  // its least-squares slope of log10(Ru); NaN when not formed
+};
+
+// The steady-state test of the steady driver (src/pyflow/driver/simulation_driver.py:135-149),
+// kept per instance on the device: the residual tracker's Ru series -- its seed 1.0, then
+// each full step's Ru -- as log10 values in a ring, and after every step the least-squares
+// slope of the last `window` entries against 0 .. window - 1.  The test passes when every
+// entry of the window is positive and |slope| < tol.  window 0 turns it off.
+constexpr int STEADY_MAX_WINDOW = 1024;
+struct SteadyRing {
+  int window;
+  int count;            // entries of the series so far (the seed included)
+  double tol;
+  double y[STEADY_MAX_WINDOW];   // entry k at y[k % STEADY_MAX_WINDOW]; NaN where Ru <= 0
 };
 
 struct Geo64 {
@@ -115,6 +130,7 @@ struct InstDesc {
   int nt_m;                    // this instance's tiles in the mixed-form per-cell table (32 x 32)
   double* part;                // per-tile partial sums of the deterministic reductions (3 x nt_pc)
   unsigned* ticket;            // their arrival counter
+  SteadyRing* steady;          // the device-side steady-state test of this instance
 };
 
 // Batch-wide loop control of a WHILE node: the number of instances still

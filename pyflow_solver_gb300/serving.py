@@ -11,7 +11,11 @@ GPU join the next step and their work shares its launches.  The slot pool is
 sized to a device-memory budget before any request is taken.
 
 A request ends after its step count or, from its second step on, when its
-continuity residual falls below the tolerance.  The reference's CLI breaks on
+continuity residual falls below the tolerance -- or, with ``steady_window`` set,
+when the device-side steady-state test fires for its slot (the steady driver's
+least-squares slope of log10(Ru) over the last ``steady_window`` steps below
+``steady_slope_tol``; src/pyflow/driver/simulation_driver.py:135-149), read from
+the step records without any host-side series.  The reference's CLI breaks on
 ``continuity < threshold`` after any step (src/pyflow/cli.py:174-178); after
 step 0 of a zero initial field the continuity is exactly 0, so the test
 starts at step 1 here, or every request would end after one step.
@@ -51,7 +55,7 @@ class Served:
     start: float = math.nan
     finish: float = math.nan
     steps_done: int = 0
-    stop: str = ""                       # "steps" | "continuity"
+    stop: str = ""                       # "steps" | "continuity" | "steady"
     last_continuity: float = math.nan
     fields: dict | None = None           # final u, v, p (kept with keep_fields=True)
 
@@ -91,9 +95,12 @@ def slot_plan(sides, budget_bytes: float, probe_bytes, weights=None):
 
 class ServingEngine:
     def __init__(self, slots: dict, precision: str = "mixed", continuity_tol: float = 1e-6,
-                 memory_budget_bytes: float = 60e9, lin_tol: float = 1e-8, lin_maxiter: int = 300):
+                 memory_budget_bytes: float = 60e9, lin_tol: float = 1e-8, lin_maxiter: int = 300,
+                 steady_window: int = 0, steady_slope_tol: float = 2e-3):
         self.precision = precision
         self.tol = continuity_tol
+        self.steady_window = int(steady_window)
+        self.steady_tol = float(steady_slope_tol)
         self.lin_tol = lin_tol
         self.lin_maxiter = lin_maxiter
         self.sides = []
@@ -123,6 +130,8 @@ class ServingEngine:
 
     def _assign(self, k: int, req, now: float):
         self.batch.set_params(k, self._config(req.side, req.Re, req.U), reset=True)
+        if self.steady_window:
+            self.batch.set_steady(k, self.steady_window, self.steady_tol)
         self.owner[k] = Served(req.rid, req.side, req.arrival, req.steps, start=now)
         self.busy[k] = True
         self.target[k] = req.steps
@@ -168,6 +177,7 @@ class ServingEngine:
                 cont = B.continuity(out)
             else:
                 res_list = B.step(busy)
+                out = B.last_out
                 cont = np.array([r[0]["continuity"] if r is not None else 0.0 for r in res_list])
                 for k in np.nonzero(busy)[0]:
                     res, diag = res_list[k]
@@ -180,11 +190,12 @@ class ServingEngine:
             rep.cell_updates += int((self.side_arr[busy] ** 2).sum())
             by_steps = busy & (self.done >= self.target)
             by_cont = busy & ~by_steps & (its >= 1) & (cont < self.tol)
-            for k in np.nonzero(by_steps | by_cont)[0]:
+            by_steady = busy & ~by_steps & ~by_cont & (out["steady"] != 0)
+            for k in np.nonzero(by_steps | by_cont | by_steady)[0]:
                 s = self.owner[k]
                 s.steps_done = int(self.done[k])
                 s.last_continuity = float(cont[k])
-                s.stop = "steps" if by_steps[k] else "continuity"
+                s.stop = "steps" if by_steps[k] else ("continuity" if by_cont[k] else "steady")
                 s.finish = t_done
                 if keep_fields:
                     s.fields = {f: a.clone() for f, a in B.states[k].fields.items()}
@@ -205,8 +216,11 @@ class ServingEngine:
         self.batch.close()
 
 
-def run_alone(req, precision="mixed", continuity_tol=1e-6, lin_tol=1e-8, lin_maxiter=300):
-    """The same request by itself through the single-instance step: (state, steps run)."""
+def run_alone(req, precision="mixed", continuity_tol=1e-6, lin_tol=1e-8, lin_maxiter=300, steady_window=0,
+              steady_slope_tol=2e-3):
+    """The same request by itself through the single-instance step: (state, steps run).
+    The steady-state stop here is the reference's host-side test (NumPy polyfit on the
+    tracker's Ru series), against which the engine's device-side test is checked."""
     from .solvers.solver import step
     cfg = cavity_config(req.side, req.side, req.Re, req.U, precision, lin_tol=lin_tol, lin_maxiter=lin_maxiter)
     st = allocate_state(req.side, req.side)
@@ -217,4 +231,11 @@ def run_alone(req, precision="mixed", continuity_tol=1e-6, lin_tol=1e-8, lin_max
         n += 1
         if it >= 1 and res["continuity"] < continuity_tol:
             break
+        ru = tr.series["Ru"].values
+        if steady_window and len(ru) >= steady_window:
+            recent = np.array(ru[-steady_window:])
+            if np.all(recent > 0):
+                slope = float(np.polyfit(np.arange(recent.size), np.log10(recent), 1)[0])
+                if abs(slope) < steady_slope_tol:
+                    break
     return st, n

@@ -38,6 +38,17 @@ def test_steady_driver_detects_and_stops_like_the_oracle_series():
                 break
     assert expect is not None
     assert drv.steady_detected and drv.steady_iteration == expect
+    # the device's slope (formed in the step's last kernel) against NumPy's polyfit on the
+    # host tracker's series, at every step where the window is full
+    ru = drv.tracker.series["Ru"].values
+    for p in payloads:
+        n = p["iteration"] + 2                      # series entries after this step (seed included)
+        if n < 6:
+            assert p["steady_slope"] is None
+            continue
+        rec = np.array(ru[n - 6:n])
+        host = float(np.polyfit(np.arange(6), np.log10(rec), 1)[0])
+        assert p["steady_slope"] == pytest.approx(host, rel=1e-9, abs=1e-12)
     assert payloads[-1]["steady"] and payloads[-1]["iteration"] == expect and len(payloads) == expect + 1
     # divergence statistics of the last step: central divergence, mean and mean-free norm
     from oracle import ops as oops
@@ -53,5 +64,6 @@ def test_harness_json_shape_and_work():
     for r in res["runs"]:
         assert {"nx", "ny", "steps", "total_time_s", "avg_time_per_step_s", "avg_cg_iterations"} <= set(r)
         assert r["steps"] == 3 and r["avg_true_cg_iterations"] > 0
+        assert 0 < r["device_time_s"] <= r["total_time_s"]
     deg = benchmark([16], 2, reference_defaults=True)
     assert deg["runs"][0]["avg_true_cg_iterations"] == 0

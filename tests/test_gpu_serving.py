@@ -56,3 +56,24 @@ def test_continuity_early_stop_and_streamed_records():
     assert all(r["type"] == "step" and "continuity" in r["residuals"] for r in recs)
     assert [r["iteration"] for r in recs if r["request"] == 0] == list(range(rep.completed[0].steps_done))
     eng.close()
+
+
+def test_requests_retire_on_the_device_steady_test():
+    """With a steady window the engine ends a request when the device-side slope test fires
+    for its slot; the same request alone, stopped by the reference's host-side test (NumPy
+    polyfit of the tracker's Ru series), runs the same number of steps to the same fields."""
+    from pyflow_solver_gb300.serving import ServingEngine, run_alone
+    W, tol = 6, 0.08
+    trace = [Request(0, 0.0, 32, 100.0, 1.0, 80), Request(1, 0.0, 32, 150.0, 0.8, 80),
+             Request(2, 0.0, 32, 120.0, 1.2, 80)]
+    eng = ServingEngine({32: 2}, precision="fp64", continuity_tol=0.0, lin_maxiter=120, steady_window=W,
+                        steady_slope_tol=tol)
+    rep = eng.run(trace, realtime=False, keep_fields=True)
+    assert len(rep.completed) == 3
+    for s in rep.completed:
+        st, n = run_alone(trace[s.rid], precision="fp64", continuity_tol=0.0, lin_maxiter=120, steady_window=W,
+                          steady_slope_tol=tol)
+        assert s.stop == "steady" and s.steps_done == n < 80
+        for f in "uvp":
+            np.testing.assert_array_equal(st.fields[f].cpu().numpy(), s.fields[f].cpu().numpy())
+    eng.close()
