@@ -18,9 +18,11 @@ refinement starts from the state's previous pressure (``mixed_warm_start``,
 default True; it falls back to zero when that guess is worse than zero), so the
 same stopping test is met with fewer multigrid cycles on a slowly changing flow.
 
-Not restated (host side effects outside the array path): the ``print`` output
-of the diagnostic mode is limited to its scalar lines, and JSONL logging /
-emergency checkpoints are left to the caller.
+Host side effects as in the reference (solver.py:170-192): with
+``config.log_path`` or ``config.log_stream``, one JSON-lines step record per
+step, and on a NaN an error record and an emergency ``*_FAIL_NAN`` checkpoint
+(``logging.structured.log_step``).  The ``print`` output of the diagnostic mode
+is limited to its scalar lines.
 """
 from __future__ import annotations
 
@@ -30,6 +32,7 @@ from typing import Any
 from .. import _capi
 from .._device import ptr, require_cuda, stream_handle
 from ..linear_solvers.preconditioners import jacobi_interior
+from ..logging.structured import log_step
 from ._handle import instance_for
 from .fields import device_fields
 
@@ -159,6 +162,7 @@ def finish(config, state, tracker, iteration: int, P, geo, out):
         assert continuity <= max(1e3, divergence_norm * 10)
         p0 = float(state.fields["p"][1, 1])
         assert abs(p0) < 1e-10, "Invariant failed: reference pressure cell not ~0"
+    log_step(config, state, iteration, dt, current_cfl, Ru, Rv, continuity, rp_iters, nan_detected, diagnostics)
     return residuals, diagnostics
 
 

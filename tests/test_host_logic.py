@@ -153,3 +153,30 @@ def test_bench_kernel_table():
     # a batch: the coarse CTA of each instance starts from its own last global level
     pre, coarse = bench.level_cells([bench.mg_shapes(128, 128), bench.mg_shapes(64, 32)])
     assert pre == {0: 128 * 128} and coarse == 64 * 64 + 64 * 32
+
+
+def test_step_log_and_nan_emergency_checkpoint(tmp_path):
+    """The step's JSON-lines record (src/pyflow/solvers/solver.py:170-192) and, on a NaN,
+    the error record and the emergency *_FAIL_NAN checkpoint -- formed from a step record
+    on the host, no GPU needed."""
+    from pyflow_solver_gb300.core.ghost_fields import State
+    from pyflow_solver_gb300.residuals.manager import ResidualManager
+    from pyflow_solver_gb300.solvers.solver import finish
+    log = tmp_path / "logs" / "run.jsonl"
+    cfg = SimpleNamespace(nx=4, ny=3, lx=1.0, ly=1.0, diagnostics=False, log_path=str(log),
+                          emergency_checkpoint_path=str(tmp_path / "ck" / "state.npz"))
+    st = State(4, 3, {k: np.zeros((5, 6)) for k in "uvp"})
+    P, dx, dy, nu = step_params(cfg, 4, 3)
+    tr = ResidualManager()
+    for it, nan in ((0, 0), (1, 1)):
+        out = _capi.StepOut()
+        out.dt, out.cfl, out.ru_sq, out.rv_sq, out.cont_sq, out.nan_detected = 0.01, 0.5, 4.0, 9.0, 1.0, nan
+        finish(cfg, st, tr, it, P, (dx, dy, nu), out)
+    recs = [json.loads(x) for x in log.read_text().splitlines()]
+    assert [r["type"] for r in recs] == ["step", "step", "error", "emergency_checkpoint"]
+    assert recs[0]["it"] == 0 and recs[0]["Ru"] == 2.0 / 12 and recs[0]["nan"] is False and "ts" in recs[0]
+    assert recs[1]["nan"] is True and recs[2]["reason"] == "nan_detected"
+    assert recs[3]["path"] == str(tmp_path / "ck" / "state_FAIL_NAN.npz")
+    st2, meta = ck.load_checkpoint(recs[3]["path"])
+    assert meta["iteration"] == 1
+    cfg._logger_instance.close()
