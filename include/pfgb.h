@@ -226,6 +226,30 @@ PFGB_API int pfgb_cg_solve(int op, const double* b, double* x, int nx, int ny, d
                   int precond, double jacobi_interior, double tol, int maxiter,
                   void* stream, pfgb_solve_out* out);
 
+/* ---- operator interface: an assembled sparse matrix ------------------------- */
+
+/* y = A x for an n x n CSR matrix in device memory (row pointers int64, n + 1 of
+ * them; column indices int32; values binary64): each row's terms summed in
+ * storage order, one rounded product and one rounded addition per term, as
+ * scipy's CSR product.  Replaces `A @ x` of the reference's solve
+ * (src/pyflow/linear_solvers/interface.py:48). */
+PFGB_API int pfgb_csr_matvec(long n, const long* rowptr, const int* colind, const double* vals, const double* x,
+                             double* y, void* stream);
+/* solve(A, b, method, tol, maxiter, M) of the reference for an assembled sparse
+ * matrix (src/pyflow/linear_solvers/interface.py:23-53): method 0 runs
+ * scipy.sparse.linalg.cg, method 1 scipy.sparse.linalg.bicgstab (SciPy 1.13.1 as
+ * the reference pins it), from x0 = 0 with rtol = tol; inv_diag (may be NULL:
+ * no preconditioner) is the Jacobi preconditioner's vector of 1/diag(A)
+ * (src/pyflow/linear_solvers/preconditioners.py:8-25).  Dot products and norms
+ * are exactly rounded.  out: info (0 converged, maxiter when the loop ran out,
+ * -10 / -11 for BiCGSTAB's breakdowns), the iterations executed, ||b||, and
+ * ||b - A x||^2.  x (n doubles) is overwritten.  Allocates its work vectors
+ * stream-ordered and synchronises `stream` at every scalar the iteration
+ * tests. */
+PFGB_API int pfgb_csr_solve(int method, long n, const long* rowptr, const int* colind, const double* vals,
+                            const double* inv_diag, const double* b, double* x, double tol, int maxiter,
+                            void* stream, pfgb_solve_out* out);
+
 /* Same solve as pfgb_cg_solve, but it allocates nothing: no cudaMalloc,
  * cudaMallocAsync, cudaFree or other allocating call.  It has no counterpart in
  * the reference; it exists for callers that cannot allocate device memory when
@@ -284,18 +308,28 @@ PFGB_API int pfgb_set_steady(pfgb_handle* handle, int k, int window, double slop
 
 /* ---- tile autotuner ---------------------------------------------------------- */
 
-/* Time the three tile shapes of the binary64 CG kernel pair (32 x 8, 32 x 16,
- * 32 x 32 cells per CTA) on this handle's own instances and keep the fastest
- * for its following steps.  The exactly rounded reductions make every shape
- * give identical results.  `variant` (may be NULL) receives the choice 0..2,
- * `us_per_iteration` (may be NULL, else 3 doubles) the measured microseconds
- * per CG iteration of each shape.  Synchronises `stream`; the handle's CG work
- * vectors are overwritten (every step rewrites them).  A no-op with precision
- * 1, whose pressure solve does not use these kernels.  No reference
- * counterpart: the reference has no device kernels to tune. */
+/* Time the launch shapes of this handle's pressure solve on its own instances
+ * and keep the fastest for its following steps; every shape gives identical
+ * results.  Precision 0: the three tile shapes of the binary64 CG kernel pair
+ * (32 x 8, 32 x 16, 32 x 32 cells per CTA; the exactly rounded reductions make
+ * the shape invisible in the results), variant 0..2.  Precision 1: the four
+ * launch variants of the binary32 PCG iteration, variant = 2 * (TMA matvec:
+ * persistent over the level-0 tiles with halos copied by the tensor memory
+ * accelerator) + (512-thread coarse CTAs, two to an SM, instead of 1024),
+ * those the batch cannot run skipped; the tile shape there is fixed at 32 x 32
+ * because it fixes the summation order of the tile sums.  `variant` (may be
+ * NULL) receives the choice, `us_per_iteration` (may be NULL, else room for 4
+ * doubles) the measured microseconds per iteration of each shape (-1 where not
+ * run).  Synchronises `stream`; the handle's work vectors are overwritten
+ * (every step rewrites them) and its solver state is kept.  A no-op for the
+ * persistent form of the mixed solve.  No reference counterpart: the reference
+ * has no device kernels to tune. */
 PFGB_API int pfgb_autotune(pfgb_handle* handle, void* stream, int* variant, double* us_per_iteration);
 /* Select a CG tile shape directly (a choice cached from an earlier autotune). */
 PFGB_API int pfgb_set_cg_variant(pfgb_handle* handle, int variant);
+/* Select a launch variant of the mixed solve directly (0..3 as pfgb_autotune
+ * numbers them; PFGB_EINVAL for one the batch cannot run). */
+PFGB_API int pfgb_set_mixed_variant(pfgb_handle* handle, int variant);
 
 /* ---- measurement ----------------------------------------------------------- */
 

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libpfgb.so")
-SOURCES = ["step64.cu", "mixed.cu", "ops.cu", "capi.cu"]
+SOURCES = ["step64.cu", "mixed.cu", "ops.cu", "krylov.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden"]

@@ -94,6 +94,8 @@ SIGNATURES = {
     "pfgb_xsum": (_I, [_P, _L, c_double_p, _P]),
     "pfgb_cg_solve": (_I, [_I, _P, _P, _I, _I, _D, _D, _I, _D, _D, _I, _P, ctypes.POINTER(SolveOut)]),
     "pfgb_cg_solve_noalloc": (_I, [_I, _P, _P, _I, _I, _D, _D, _I, _D, _D, _I, _P, ctypes.POINTER(SolveOut)]),
+    "pfgb_csr_matvec": (_I, [_L, _P, _P, _P, _P, _P, _P]),
+    "pfgb_csr_solve": (_I, [_I, _L, _P, _P, _P, _P, _P, _P, _D, _I, _P, ctypes.POINTER(SolveOut)]),
     "pfgb_set_graph": (_I, [_P, _I]),
     "pfgb_set_persistent": (_I, [_P, _I]),
     "pfgb_matvec_form": (_I, [_P, ctypes.POINTER(_I)]),
@@ -101,6 +103,7 @@ SIGNATURES = {
     "pfgb_host_unregister": (_I, [_P]),
     "pfgb_autotune": (_I, [_P, _P, ctypes.POINTER(_I), c_double_p]),
     "pfgb_set_cg_variant": (_I, [_P, _I]),
+    "pfgb_set_mixed_variant": (_I, [_P, _I]),
     "pfgb_set_profiling": (_I, [_P, _I]),
     "pfgb_profile_result": (_I, [_P, c_double_p, ctypes.POINTER(_I)]),
     "pfgb_profile_kernels": (_I, [_P, ctypes.POINTER(KernelTime), _I, ctypes.POINTER(_I)]),

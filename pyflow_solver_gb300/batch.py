@@ -87,9 +87,9 @@ class BatchedCavities:
         self._steady = {}
         self.last_out = None
         self.cg_variant = None
-        if _handle.AUTOTUNE and params[0].precision == 0:
+        if _handle.AUTOTUNE and not (params[0].precision == 1 and _handle.PERSISTENT):
             key = ("batch",) + tuple(sorted((int(s.nx), int(s.ny)) for s in self.states))
-            self.cg_variant = _handle.autotune(h, key)
+            self.cg_variant = _handle.autotune(h, key, int(params[0].precision))
 
     def __len__(self):
         return len(self.configs)

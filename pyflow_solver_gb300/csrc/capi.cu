@@ -131,6 +131,11 @@ extern "C" int pfgb_autotune(pfgb_handle* handle, void* stream, int* variant, do
   return instance64_autotune(handle->inst, (cudaStream_t)stream, variant, us_per_iteration);
 }
 
+extern "C" int pfgb_set_mixed_variant(pfgb_handle* handle, int variant) {
+  if (!handle) return set_error(PFGB_EINVAL, "null handle");
+  return instance64_set_mixed_variant(handle->inst, variant);
+}
+
 extern "C" int pfgb_set_cg_variant(pfgb_handle* handle, int variant) {
   if (!handle) return set_error(PFGB_EINVAL, "null handle");
   return instance64_set_cg_variant(handle->inst, variant);
@@ -211,4 +216,17 @@ extern "C" int pfgb_batch_set_params(pfgb_handle* handle, int k, const pfgb_para
 extern "C" int pfgb_set_steady(pfgb_handle* handle, int k, int window, double slope_tol) {
   if (!handle) return set_error(PFGB_EINVAL, "null handle");
   return instance64_set_steady(handle->inst, k, window, slope_tol);
+}
+
+extern "C" int pfgb_csr_matvec(long n, const long* rowptr, const int* colind, const double* vals, const double* x,
+                               double* y, void* stream) {
+  if (n > 0 && (!rowptr || !colind || !vals || !x || !y)) return set_error(PFGB_EINVAL, "null argument");
+  return csr_matvec_run(n, rowptr, colind, vals, x, y, (cudaStream_t)stream);
+}
+
+extern "C" int pfgb_csr_solve(int method, long n, const long* rowptr, const int* colind, const double* vals,
+                              const double* inv_diag, const double* b, double* x, double tol, int maxiter, void* stream,
+                              pfgb_solve_out* out) {
+  if (!rowptr || !colind || !vals || !b || !x || !out) return set_error(PFGB_EINVAL, "null argument");
+  return csr_solve_run(method, n, rowptr, colind, vals, inv_diag, b, x, tol, maxiter, (cudaStream_t)stream, out);
 }

@@ -2004,7 +2004,10 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     CUtensorMap* tm = (CUtensorMap*)take(3 * n * sizeof(CUtensorMap));
     const char* tv = std::getenv("PFGB_MATVEC_TMA");
     B->mv_force = (tv && std::string(tv) == "1") ? 1 : ((tv && std::string(tv) == "0") ? -1 : 0);
-    bool ok = B->mv_force > 0 || (B->mv_force == 0 && n > 0 && (long)B->ntl[0] >= 64L * n);
+    // the maps are encoded for any batch (unless the form is forced off), so that the
+    // tuner can try the form; the rule above picks it by default
+    bool ok = B->mv_force >= 0 && n > 0;
+    const bool by_rule = B->mv_force > 0 || (long)B->ntl[0] >= 64L * n;
     std::vector<CUtensorMap> hm(ok ? 3 * n : 0);
     for (int k = 0; ok && k < n; ++k) {
       const MixDesc& M = B->hd[k];
@@ -2019,7 +2022,8 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
                                     : "without an encoder");
     if (ok && cudaMemcpy(tm, hm.data(), hm.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice) != cudaSuccess) ok = false;
     for (int k = 0; k < n; ++k) B->hd[k].tmap = ok ? tm + 3 * k : nullptr;
-    B->mv_tma = ok ? 1 : 0;
+    B->mv_avail = ok ? 1 : 0;
+    B->mv_tma = (ok && by_rule) ? 1 : 0;
     cudaGetLastError();
   }
   // PFGB_TEST_LOOP_BOUND lowers both loops' trip bounds (a test of the guards: the
@@ -2053,8 +2057,9 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (n > sms && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mg_coarse<CT2>, CT2, smem2) == cudaSuccess &&
-        occ >= 2) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mg_coarse<CT2>, CT2, smem2) == cudaSuccess && occ >= 2)
+      B->coarse_avail2 = 1;
+    if (n > sms && B->coarse_avail2) {
       B->coarse_nt = CT2;
       B->coarse_smem = smem2;
     }
@@ -2063,7 +2068,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
                    B->coarse_nt, B->coarse_smem, occ);
     cudaGetLastError();
   }
-  if (e == cudaSuccess && B->mv_tma) {
+  if (e == cudaSuccess && B->mv_avail) {
     // the TMA matvec: as many CTAs as fit on the device at once, at most one per tile
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
@@ -2071,7 +2076,7 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mx_matvec_tma, MT, 0) == cudaSuccess && occ >= 1)
       B->mv_grid = std::min(B->ntl[0], sms * occ);
     else
-      B->mv_tma = 0;
+      B->mv_avail = B->mv_tma = 0;
     if (B->mv_tma && B->mv_force == 0 && B->ntl[0] < 2 * B->mv_grid) B->mv_tma = 0;   // under 2 tiles per CTA
     cudaGetLastError();
   }
@@ -2280,6 +2285,125 @@ int run_direct(Batch* B, cudaStream_t s) {
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("mixed solve launch: ") + cudaGetErrorString(e));
+  return PFGB_OK;
+}
+
+// ---- launch-shape tuner --------------------------------------------------------
+
+int variant_of(const Batch* B) { return 2 * (B->mv_tma ? 1 : 0) + (B->coarse_nt == CT2 ? 1 : 0); }
+
+int set_variant(Batch* B, int variant) {
+  if (variant < 0 || variant > 3) return set_error(PFGB_EINVAL, "mixed launch variant must be 0..3");
+  const int tma = variant >> 1, narrow = variant & 1;
+  if (tma && !B->mv_avail) return set_error(PFGB_EINVAL, "this batch cannot run the TMA matvec");
+  if (narrow && !B->coarse_avail2) return set_error(PFGB_EINVAL, "two 512-thread coarse CTAs do not fit on an SM");
+  B->mv_tma = tma;
+  B->coarse_nt = narrow ? CT2 : CT;
+  return PFGB_OK;
+}
+
+// A fixed pseudo-random pattern in [-1, 1) in both level-0 residual buffers and a zero
+// correction: a PCG run from it keeps every quantity finite for the timed iterations.
+__global__ void k_tune_fill_m(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
+  const MTile tl = TL[blockIdx.x];
+  const MixDesc& M = MD[tl.inst];
+  const Lvl L0 = M.lev[0];
+  for (int c = threadIdx.x; c < BX * BY; c += blockDim.x) {
+    const int i = tl.i0 + c % BX, j = tl.j0 + c / BX;
+    if (i >= L0.nx || j >= L0.ny) continue;
+    unsigned h = (unsigned)(j * 73856093) ^ (unsigned)(i * 19349663) ^ (unsigned)(tl.inst * 83492791);
+    h ^= h >> 13;
+    h *= 0x5bd1e995u;
+    h ^= h >> 15;
+    const float v = (float)(h & 0xffffu) * (1.f / 32768.f) - 1.f;
+    const long o = (long)j * L0.ld + i;
+    L0.f[o] = v;
+    M.f0b[o] = v;
+    M.e[o] = 0.f;
+  }
+}
+
+// Every instance in the inner loop, with a stopping test that never passes.
+__global__ void k_tune_arm_m(const MixDesc* __restrict__ MD, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n || !*MD[k].active) return;
+  MixCtrl* c = MD[k].ctrl;
+  c->outer_done = 0;
+  c->inner_done = 0;
+  c->inner = 0;
+  c->inner_total = 0;
+  c->max_inner = 1 << 30;
+  c->tol_abs_in = -1.0;
+  c->rho = 1.0;
+  c->beta = 0.0;
+}
+
+int tune(Batch* B, cudaStream_t s, int* chosen, double* us) {
+  if (B->persist) {                     // one cooperative launch: no launch shapes to choose
+    if (chosen) *chosen = variant_of(B);
+    return PFGB_OK;
+  }
+  const int orig = variant_of(B);
+  std::vector<MixCtrl> ctrl(B->n);
+  MixLoop loop;
+  cudaError_t err = cudaStreamSynchronize(s);
+  for (int k = 0; k < B->n && err == cudaSuccess; ++k)
+    err = cudaMemcpy(&ctrl[k], B->hd[k].ctrl, sizeof(MixCtrl), cudaMemcpyDeviceToHost);
+  if (err == cudaSuccess) err = cudaMemcpy(&loop, B->loop, sizeof(MixLoop), cudaMemcpyDeviceToHost);
+  if (err != cudaSuccess) return set_error(PFGB_ECUDA, std::string("tune: saving the solver state: ") + cudaGetErrorString(err));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  KProf* kp = B->kp;
+  B->kp = nullptr;
+  const Smooth sw = B->sw;
+  float best = 1e30f;
+  int best_v = orig;
+  const int g0 = B->ntl[0];
+  for (int v = 0; v < 4 && err == cudaSuccess; ++v) {
+    if (us) us[v] = -1.0;
+    if (set_variant(B, v) != PFGB_OK) continue;
+    k_tune_fill_m<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
+    k_tune_arm_m<<<(B->n + 127) / 128, 128, 0, s>>>(B->dd, B->n);
+    k_ml_reset<<<1, 32, 0, s>>>(B->loop, 0);
+    k_ml_reset<<<1, 32, 0, s>>>(B->loop, 1);
+    if (B->ntpre[0]) k_mg_down<<<B->ntpre[0], MT, 0, s>>>(B->dd, B->tpre[0], 0, 1, sw);
+    constexpr int WARM = 2, REPS = 10;
+    for (int it = 0; it < WARM + REPS; ++it) {
+      if (it == WARM) cudaEventRecord(e0, s);
+      launch_vcycle(B, 1, sw, s, 1);
+      if (B->mv_tma)
+        k_mx_matvec_tma<<<B->mv_grid, MT, 0, s>>>(B->dd, B->tl[0], B->ntl[0], B->loop);
+      else
+        k_mx_matvec<<<g0, MT, 0, s>>>(B->dd, B->tl[0]);
+      k_mx_update_down<<<g0, MT, 0, s>>>(B->dd, B->tl[0], B->loop, 0ull, 0, sw);
+    }
+    cudaEventRecord(e1, s);
+    err = cudaEventSynchronize(e1);
+    if (err != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const float per = 1e3f * ms / REPS;
+    if (us) us[v] = per;
+    if (per < best) {
+      best = per;
+      best_v = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  B->kp = kp;
+  if (err == cudaSuccess) err = cudaGetLastError();
+  // the instances' solver state (the refinement's per-instance history among it) as it was
+  for (int k = 0; k < B->n && err == cudaSuccess; ++k)
+    err = cudaMemcpy(B->hd[k].ctrl, &ctrl[k], sizeof(MixCtrl), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(B->loop, &loop, sizeof(MixLoop), cudaMemcpyHostToDevice);
+  if (err != cudaSuccess) {
+    set_variant(B, orig);
+    return set_error(PFGB_ECUDA, std::string("tune: ") + cudaGetErrorString(err));
+  }
+  set_variant(B, best_v);
+  if (chosen) *chosen = best_v;
   return PFGB_OK;
 }
 

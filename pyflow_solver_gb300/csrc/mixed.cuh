@@ -134,6 +134,8 @@ struct Batch {
   size_t psmem = 0;
   // the matvec of the kernel graph with TMA-copied halos (persistent over the level-0 tiles)
   int mv_tma = 0;                              // in use (every instance has its tensor maps)
+  int mv_avail = 0;                            // the TMA form can run (maps encoded, a grid that fits)
+  int coarse_avail2 = 0;                       // two 512-thread coarse CTAs fit on an SM
   int mv_force = 0;                            // PFGB_MATVEC_TMA: 1 on, -1 off, 0 chosen by the batch's shape
   int mv_grid = 0;                             // its CTAs
   char* ws = nullptr;
@@ -183,6 +185,13 @@ int run_direct(Batch* B, cudaStream_t s);
 int set_persistent(Batch* B, int on);
 // 1 when the kernel graph's matvec is the TMA form (persistent over the level-0 tiles)
 inline int matvec_form(const Batch* B) { return B->mv_tma; }
+// Launch shapes of the solve that give the same bits: variant = 2 * (TMA matvec) + (512-thread
+// coarse CTAs).  set_variant refuses one the batch cannot run; tune times every runnable one
+// on the batch's own instances (us[4] receives microseconds per PCG iteration, -1 where not
+// runnable) and keeps the fastest.  The instances' solver state is kept across tuning.
+int variant_of(const Batch* B);
+int set_variant(Batch* B, int variant);
+int tune(Batch* B, cudaStream_t s, int* chosen, double* us);
 // New tolerances and iteration limits for instance k (limits within the loop guards).
 int set_tolerances(Batch* B, int k, double tol_out, double tol_in, int max_outer, int max_inner, int warm,
                    int maxiter_report);

@@ -149,6 +149,11 @@ static int xreduce(const double* a, const double* b, long n, int mode, double* r
   return PFGB_OK;
 }
 
+// Exactly rounded a.b (mode 0) or sum(a) (mode 1) of device vectors, to the host (synchronises s).
+int exact_reduce(const double* a, const double* b, long n, int mode, double* result, cudaStream_t s) {
+  return xreduce(a, b, n, mode, result, s);
+}
+
 static int check_grid(int nx, int ny) {
   if (nx < 2 || ny < 2) return set_error(PFGB_EINVAL, "nx and ny must be >= 2");
   return PFGB_OK;

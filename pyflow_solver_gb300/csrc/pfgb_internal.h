@@ -29,6 +29,7 @@ int instance64_set_persistent(Instance64* I, int on);
 int instance64_matvec_form(const Instance64* I, int* tma);
 int instance64_autotune(Instance64* I, cudaStream_t s, int* chosen, double* us);
 int instance64_set_cg_variant(Instance64* I, int v);
+int instance64_set_mixed_variant(Instance64* I, int variant);
 int instance64_set_params(Instance64* I, int k, const pfgb_params* prm);
 int instance64_set_steady(Instance64* I, int k, int window, double tol);
 int instance64_set_profiling(Instance64* I, int on);
@@ -36,6 +37,11 @@ int instance64_profile_result(Instance64* I, double* ms, int* launches);
 struct KTime;
 int instance64_profile_kernels(Instance64* I, std::vector<KTime>& out);
 int probe_fp64(cudaStream_t s, double* tops);
+int exact_reduce(const double* a, const double* b, long n, int mode, double* result, cudaStream_t s);
+int csr_matvec_run(long n, const long* rp, const int* ci, const double* va, const double* x, double* y,
+                   cudaStream_t s);
+int csr_solve_run(int method, long n, const long* rp, const int* ci, const double* va, const double* invd,
+                  const double* b, double* x, double tol, int maxiter, cudaStream_t s, pfgb_solve_out* out);
 int cg_solve_noalloc_run(int op, const double* b, double* x, int nx, int ny, double dx, double dy, int precond,
                          double invd, double tol, int maxiter, cudaStream_t s, pfgb_solve_out* out);
 int cg_solve_run(int op, const double* b, double* x, int nx, int ny, double dx, double dy, int precond,

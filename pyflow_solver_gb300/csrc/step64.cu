@@ -1585,9 +1585,30 @@ int instance64_set_cg_variant(Instance64* I, int v) {
   return PFGB_OK;
 }
 
+static void drop_graph(Instance64* I) {
+  if (I->exec) {
+    cudaGraphExecDestroy(I->exec);
+    I->exec = nullptr;
+  }
+  if (I->graph) {
+    cudaGraphDestroy(I->graph);
+    I->graph = nullptr;
+  }
+  I->graph_mode = -1;
+}
+
+int instance64_set_mixed_variant(Instance64* I, int variant) {
+  if (!I->mix) return set_error(PFGB_EINVAL, "launch variants of the mixed solve need precision 1");
+  if (int rc = mixed::set_variant(I->mix, variant)) return rc;
+  drop_graph(I);
+  return PFGB_OK;
+}
+
 int instance64_autotune(Instance64* I, cudaStream_t s, int* chosen, double* us) {
-  if (I->mix) {  // the binary64 CG kernels do not run in the mixed form
-    if (chosen) *chosen = I->cg_var;
+  if (I->mix) {  // the mixed solve: its launch shapes (matvec form, coarse CTA width)
+    if (int rc = upload_desc(I, s)) return rc;
+    if (int rc = mixed::tune(I->mix, s, chosen, us)) return rc;
+    drop_graph(I);
     return PFGB_OK;
   }
   std::vector<InstDesc> saved = I->hd;
@@ -1650,15 +1671,7 @@ int instance64_matvec_form(const Instance64* I, int* tma) {
 int instance64_set_persistent(Instance64* I, int on) {
   if (!I->mix) return PFGB_OK;
   mixed::set_persistent(I->mix, on);
-  if (I->exec) {
-    cudaGraphExecDestroy(I->exec);
-    I->exec = nullptr;
-  }
-  if (I->graph) {
-    cudaGraphDestroy(I->graph);
-    I->graph = nullptr;
-  }
-  I->graph_mode = -1;
+  drop_graph(I);
   return PFGB_OK;
 }
 

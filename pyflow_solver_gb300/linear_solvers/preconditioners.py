@@ -1,4 +1,4 @@
-"""Jacobi preconditioner of the pressure solve.
+"""Jacobi preconditioners of the pressure solve and of assembled matrices.
 
 Same contract as src/pyflow/linear_solvers/preconditioners.py:8-25
 (``invD = 1/diag(A)`` where the diagonal is non-zero).  The reference builds it
@@ -30,15 +30,22 @@ def jacobi_interior(dx: float, dy: float) -> float:
     return 1.0 / (2.0 / dx**2 + 2.0 / dy**2)
 
 
-def jacobi_preconditioner(A) -> JacobiPreconditioner:
-    """Jacobi of the pinned pressure operator (or of its assembled CSR matrix)."""
+def jacobi_preconditioner(A):
+    """Jacobi preconditioner (src/pyflow/linear_solvers/preconditioners.py:8-25).
+
+    For the pinned pressure operator: the diagonal of assemble_negative_laplacian,
+    applied analytically by the stencil kernels (``JacobiPreconditioner``).  For an
+    assembled matrix (SciPy sparse, dense, or ``CsrMatrix``): invD = 1/diag(A) where
+    the diagonal is non-zero, 0 elsewhere, as a device vector
+    (``DiagonalPreconditioner``) for the CSR solves."""
     from .operators import PressureOperator
     if isinstance(A, PressureOperator):
         if A.kind != "neg_laplacian_pinned":
-            raise NotImplementedError("the GPU Jacobi applies the diagonal of assemble_negative_laplacian only")
+            raise NotImplementedError("the stencil Jacobi applies the diagonal of assemble_negative_laplacian; "
+                                      "assemble the operator's matrix for another diagonal")
         return JacobiPreconditioner(A.nx, A.ny, jacobi_interior(A.dx, A.dy))
-    raise NotImplementedError("jacobi_preconditioner on the GPU takes a PressureOperator; "
-                              "assembled matrices are replaced by the analytic diagonal")
+    from .sparse import jacobi_of_matrix
+    return jacobi_of_matrix(A)
 
 
 def diag_matches_assembled(D: np.ndarray, nx: int, ny: int, dx: float, dy: float) -> bool:

@@ -10,9 +10,10 @@ rhs_override=None) -> (p, diagnostics)``.
 * manufactured mode (``rhs_override``): Dirichlet Laplacian with identity ring
   rows, CG without preconditioner, p written to the state, no correction.
 
-``assemble_negative_laplacian`` is not rebuilt: only its diagonal is used by
-the reference (through ``jacobi_preconditioner``), and the kernels apply it
-analytically.
+``assemble_negative_laplacian`` builds the reference's sparse matrix (the same
+CSR entries and values, src/pyflow/solvers/pressure_solver.py:15-40) for callers
+of the operator interface; the time step itself only needs its diagonal
+(through ``jacobi_preconditioner``), which the kernels apply analytically.
 """
 from __future__ import annotations
 
@@ -29,6 +30,29 @@ from ..linear_solvers.operators import PressureOperator
 from ..linear_solvers.preconditioners import JacobiPreconditioner, jacobi_interior
 from ._handle import instance_for
 from .fields import device_fields
+
+
+def assemble_negative_laplacian(nx: int, ny: int, dx: float, dy: float):
+    """The reference's assembled matrix (pressure_solver.py:15-40) as SciPy CSR: an
+    identity row on every boundary cell (the reference cell 0 included), and inside the
+    5-point -Laplacian (centre 2/dx**2 + 2/dy**2, neighbours -1/dx**2 and -1/dy**2),
+    columns sorted within each row as the reference's LIL-to-CSR conversion leaves them."""
+    import numpy as np
+    import scipy.sparse as sp
+    N = nx * ny
+    idx = np.arange(N).reshape(ny, nx)
+    interior = np.zeros((ny, nx), dtype=bool)
+    interior[1:-1, 1:-1] = True
+    inner = idx[interior]
+    ring = idx[~interior]
+    cx, cy, cc = -1.0 / dx**2, -1.0 / dy**2, 2.0 / dx**2 + 2.0 / dy**2
+    # per interior row the five columns in increasing order: -nx, -1, 0, +1, +nx
+    cols = np.stack([inner - nx, inner - 1, inner, inner + 1, inner + nx], axis=1)
+    vals = np.broadcast_to(np.array([cy, cx, cc, cx, cy]), cols.shape)
+    rows = np.concatenate([np.repeat(inner, 5), ring])
+    cols = np.concatenate([cols.ravel(), ring])
+    vals = np.concatenate([vals.ravel(), np.ones(ring.size)])
+    return sp.csr_matrix((vals, (rows, cols)), shape=(N, N))
 
 
 def _xnorm(t: torch.Tensor) -> float:
@@ -138,8 +162,3 @@ def _manufactured(state, dt, dx, dy, cfg, preconditioner, rhs_override):
         "cg_true_iterations": res.true_iterations,
     }
     return p.clone(), diag
-
-
-def assemble_negative_laplacian(*_args, **_kwargs):  # pragma: no cover - documented replacement
-    raise NotImplementedError("the GPU path applies the Jacobi diagonal analytically; "
-                              "no sparse matrix is assembled")

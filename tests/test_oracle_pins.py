@@ -137,3 +137,34 @@ def test_reorder_floor_is_recorded():
     diffs = [np.max(np.abs(r["fields"]["u"] - g[f"u_{i}"])) for i, r in enumerate(ex_out)]
     assert diffs[0] == 0.0          # step 0: zero RHS, no CG iteration, identical
     assert max(diffs) > 0.0         # later: summation order matters (non-SPD CG cut at maxiter)
+
+
+def _krylov_cases():
+    import scipy.sparse as sp
+
+    from pyflow_solver_gb300.solvers.pressure_solver import assemble_negative_laplacian
+    rng = np.random.default_rng(11)
+    A1 = assemble_negative_laplacian(12, 9, 1.0 / 11, 1.0 / 8)
+    n = 300
+    R = sp.random(n, n, density=0.02, random_state=5, format="csr")
+    A2 = (R + sp.diags(np.abs(R).sum(axis=1).A1 + 1.0 + rng.random(n))).tocsr()   # non-symmetric, dominant
+    return [(A1, rng.standard_normal(A1.shape[0])), (A2, rng.standard_normal(n))]
+
+
+@pytest.mark.parametrize("method", ["cg", "bicgstab"])
+@pytest.mark.parametrize("pc", [False, True])
+def test_krylov_oracle_reproduces_scipy(method, pc):
+    """The restated CG and BiCGSTAB over a CSR matrix (np.dot / np.linalg.norm
+    reductions) give scipy's own iterates bit for bit, as the reference calls them
+    (src/pyflow/linear_solvers/interface.py:17-21,43-46; x0 = 0, rtol = tol, M = Jacobi)."""
+    import scipy.sparse.linalg as spla
+
+    from oracle.krylov import jacobi_inv, solve_csr
+    for A, b in _krylov_cases():
+        inv = jacobi_inv(A.diagonal()) if pc else None
+        M = spla.LinearOperator(A.shape, lambda v, inv=inv: inv * v) if pc else None
+        fn = spla.cg if method == "cg" else spla.bicgstab
+        x_ref, info_ref = fn(A, b, x0=np.zeros_like(b), rtol=1e-9, maxiter=60, M=M)
+        x, info, _, _ = solve_csr(A.indptr, A.indices, A.data, b, method, 1e-9, 60, inv, red="numpy")
+        np.testing.assert_array_equal(x, x_ref)
+        assert info == info_ref
