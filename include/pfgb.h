@@ -356,6 +356,14 @@ typedef struct pfgb_kernel_time {
  * exceed capacity).  Call after the step returned (its stream is synchronised).
  * No reference counterpart: benchmark instrumentation. */
 PFGB_API int pfgb_profile_kernels(pfgb_handle* handle, pfgb_kernel_time* out, int capacity, int* count);
+/* Self-test of the integer-pipe number conversions the kernels use in place of
+ * the hardware ones (binary64 -> binary32 round to nearest even, binary32 ->
+ * binary64, exact halving of a binary64 value): `samples` pseudo-random bit
+ * patterns (exponents concentrated around the binary32 range and its
+ * boundaries, with ties and specials) are converted both ways on the device;
+ * mismatches[0..2] receive the number of differing results of each conversion
+ * (NaN against NaN counts as equal).  No reference counterpart. */
+PFGB_API int pfgb_selftest_conversions(long samples, void* stream, long long* mismatches);
 /* Measured FP64 FMA issue rate of the current device, in 1e12 instructions/s.
  * No reference counterpart: the denominator of the FP64 roofline. */
 PFGB_API int pfgb_probe_fp64(void* stream, double* tops);

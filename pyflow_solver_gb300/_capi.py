@@ -109,6 +109,7 @@ SIGNATURES = {
     "pfgb_profile_kernels": (_I, [_P, ctypes.POINTER(KernelTime), _I, ctypes.POINTER(_I)]),
     "pfgb_set_steady": (_I, [_P, _I, _I, _D]),
     "pfgb_probe_fp64": (_I, [_P, c_double_p]),
+    "pfgb_selftest_conversions": (_I, [_L, _P, ctypes.POINTER(ctypes.c_longlong)]),
 }
 
 SCHEME_UPWIND, SCHEME_QUICK, SCHEME_NONE = 0, 1, 2

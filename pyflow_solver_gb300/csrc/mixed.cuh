@@ -47,6 +47,7 @@ struct Geo {
   long ld;
   Grid2 g;
   double rdx, rdy;             // 1/dx, 1/dy
+  double rdx2, rdy2;           // 1/dx^2, 1/dy^2
 };
 
 struct MixCtrl {

@@ -2,6 +2,7 @@
 // operators, and exactly rounded dot products / sums (see xacc.cuh).
 #include <string>
 
+#include "icvt.cuh"
 #include "pfgb_internal.h"
 #include "stencil.cuh"
 #include "xacc.cuh"
@@ -154,6 +155,68 @@ int exact_reduce(const double* a, const double* b, long n, int mode, double* res
   return xreduce(a, b, n, mode, result, s);
 }
 
+// ---- self-test of the integer-pipe conversions (icvt.cuh) -----------------------
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
+}
+
+__device__ __forceinline__ bool same_f(float a, float b) {
+  return (a != a && b != b) || __float_as_uint(a) == __float_as_uint(b);
+}
+__device__ __forceinline__ bool same_d(double a, double b) {
+  return (a != a && b != b) || __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// sample k: a random 64-bit pattern; every fourth one has its exponent drawn near the
+// binary32 range (normal, subnormal, overflow and rounding boundaries); k < 64: specials
+__global__ void k_icvt_check(long n, unsigned long long* bad) {
+  const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  uint64_t r = mix64((uint64_t)k + 0x9e3779b97f4a7c15ull);
+  if ((k & 3) == 0) {
+    const uint64_t e = 1023 - 160 + (mix64(r) % 300);       // 2^-160 .. 2^140
+    r = (r & 0x800FFFFFFFFFFFFFull) | (e << 52);
+    if ((k & 15) == 0) r &= ~0x000000000FFFFFFFull | (mix64(r) & 0x10000000ull);   // exact halfway / ties
+  }
+  if (k < 64) {
+    const uint64_t sp[16] = {0ull, 0x8000000000000000ull, 0x7FF0000000000000ull, 0xFFF0000000000000ull,
+                             0x7FF8000000000000ull, 0x0000000000000001ull, 0x0010000000000000ull,
+                             0x0020000000000000ull, 0x47EFFFFFE0000000ull, 0x47EFFFFFF0000000ull,
+                             0x47EFFFFFEFFFFFFFull, 0x3690000000000000ull, 0x36A0000000000000ull,
+                             0x3680000000000000ull, 0x380FFFFFF0000000ull, 0x380FFFFFE0000000ull};
+    r = sp[k & 15] ^ ((k >> 4) ? (1ull << 63) : 0ull);
+  }
+  const double d = __longlong_as_double((long long)r);
+  unsigned long long miss = 0;
+  if (!same_f(d2f_rn(d), __double2float_rn(d))) miss |= 1;
+  const float f = __uint_as_float((uint32_t)r ^ (uint32_t)(r >> 32));
+  if (!same_d(f2d(f), (double)f)) miss |= 2;
+  if (!same_d(half_exact(d), __dmul_rn(d, 0.5))) miss |= 4;
+  if (miss) atomicAdd(bad + (miss & 1 ? 0 : (miss & 2 ? 1 : 2)), 1ull);
+}
+
+int icvt_selftest(long n, cudaStream_t s, long long* mismatches) {
+  unsigned long long* bad = nullptr;
+  if (cudaMallocAsync(&bad, 3 * sizeof(unsigned long long), s) != cudaSuccess)
+    return set_error(PFGB_ENOMEM, "cudaMallocAsync of the self-test counters failed");
+  cudaMemsetAsync(bad, 0, 3 * sizeof(unsigned long long), s);
+  if (n > 0) k_icvt_check<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, bad);
+  unsigned long long h[3] = {0, 0, 0};
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, bad, sizeof(h), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(bad, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_error(PFGB_ECUDA, std::string("conversion self-test: ") + cudaGetErrorString(e));
+  for (int k = 0; k < 3; ++k) mismatches[k] = (long long)h[k];
+  return PFGB_OK;
+}
+
 static int check_grid(int nx, int ny) {
   if (nx < 2 || ny < 2) return set_error(PFGB_EINVAL, "nx and ny must be >= 2");
   return PFGB_OK;
@@ -230,4 +293,9 @@ extern "C" int pfgb_div_by_constant(const double* a, double* out, long n, double
   if (blocks > 0x7fffffffL) return set_error(PFGB_EINVAL, "vector too long");
   k_div_by<<<(unsigned)blocks, OT, 0, (cudaStream_t)stream>>>(a, out, n, spacing_for(d), method);
   return launch_status("div_by_constant");
+}
+
+extern "C" int pfgb_selftest_conversions(long samples, void* stream, long long* mismatches) {
+  if (!mismatches || samples < 0 || samples > (1L << 31)) return set_error(PFGB_EINVAL, "invalid self-test arguments");
+  return icvt_selftest(samples, (cudaStream_t)stream, mismatches);
 }

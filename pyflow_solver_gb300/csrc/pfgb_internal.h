@@ -38,6 +38,7 @@ struct KTime;
 int instance64_profile_kernels(Instance64* I, std::vector<KTime>& out);
 int probe_fp64(cudaStream_t s, double* tops);
 int exact_reduce(const double* a, const double* b, long n, int mode, double* result, cudaStream_t s);
+int icvt_selftest(long n, cudaStream_t s, long long* mismatches);
 int csr_matvec_run(long n, const long* rp, const int* ci, const double* va, const double* x, double* y,
                    cudaStream_t s);
 int csr_solve_run(int method, long n, const long* rp, const int* ci, const double* va, const double* invd,

@@ -13,6 +13,7 @@
 // result, which never changes a value downstream (every consumer is a product,
 // a difference, an exactly rounded sum or a comparison), so it is written x + y.
 #pragma once
+#include "icvt.cuh"
 #include "common.cuh"
 
 namespace pfgb {
@@ -69,7 +70,9 @@ __device__ __forceinline__ double div_central_at(View2<const double> u, View2<co
 
 // The same with dx = dy = 1 (the step's continuity and safeguard norms): a
 // quotient by 1 is the dividend and a quotient by 2 equals the product with
-// 0.5 (both exact, or rounded alike when subnormal), so no division is issued.
+// 0.5 (both exact, or rounded alike when subnormal), so no division is issued;
+// the product is an exponent decrement on the integer pipe wherever the result
+// stays normal (half_exact).
 __device__ __forceinline__ double div_central_unit(View2<const double> u, View2<const double> v, int j, int i, int nx,
                                                    int ny) {
   const int L = nx - 1, T = ny - 1;
@@ -77,11 +80,11 @@ __device__ __forceinline__ double div_central_unit(View2<const double> u, View2<
   if (j == 0 && i == L) return ADD(SUB(u(0, L), u(0, L - 1)), SUB(v(1, L), v(0, L)));
   if (j == T && i == 0) return ADD(SUB(u(T, 1), u(T, 0)), SUB(v(T, 0), v(T - 1, 0)));
   if (j == T && i == L) return ADD(SUB(u(T, L), u(T, L - 1)), SUB(v(T, L), v(T - 1, L)));
-  if (j == 0) return ADD(MUL(SUB(u(0, i + 1), u(0, i - 1)), 0.5), SUB(v(1, i), v(0, i)));
-  if (j == T) return ADD(MUL(SUB(u(T, i + 1), u(T, i - 1)), 0.5), SUB(v(T, i), v(T - 1, i)));
-  if (i == 0) return ADD(SUB(u(j, 1), u(j, 0)), MUL(SUB(v(j + 1, 0), v(j - 1, 0)), 0.5));
+  if (j == 0) return ADD(half_exact(SUB(u(0, i + 1), u(0, i - 1))), SUB(v(1, i), v(0, i)));
+  if (j == T) return ADD(half_exact(SUB(u(T, i + 1), u(T, i - 1))), SUB(v(T, i), v(T - 1, i)));
+  if (i == 0) return ADD(SUB(u(j, 1), u(j, 0)), half_exact(SUB(v(j + 1, 0), v(j - 1, 0))));
   if (i == L) return 0.0;
-  return ADD(MUL(SUB(u(j, i + 1), u(j, i - 1)), 0.5), MUL(SUB(v(j + 1, i), v(j - 1, i)), 0.5));
+  return ADD(half_exact(SUB(u(j, i + 1), u(j, i - 1))), half_exact(SUB(v(j + 1, i), v(j - 1, i))));
 }
 
 // ((3/8)*a + (6/8)*b) - (1/8)*c

@@ -694,8 +694,8 @@ __global__ void __launch_bounds__(NT) k_predict_m(const InstDesc* __restrict__ I
   for (int idx = threadIdx.x; idx < (TY_M + 4) * (TX + 4); idx += NT) {
     const int jj = idx / (TX + 4) - 2, ii = idx % (TX + 4) - 2;
     const int gj = clampi(j0 + jj, 0, T), gi = clampi(i0 + ii, 0, L);
-    su[jj + 2][ii + 2] = __double2float_rn(U(gj, gi));
-    sv[jj + 2][ii + 2] = __double2float_rn(V(gj, gi));
+    su[jj + 2][ii + 2] = d2f_rn(U(gj, gi));      // the conversions on the integer pipe (icvt.cuh)
+    sv[jj + 2][ii + 2] = d2f_rn(V(gj, gi));
   }
   __syncthreads();
   const double dt = D.ctrl->dt;
@@ -743,8 +743,8 @@ __global__ void __launch_bounds__(NT) k_predict_m(const InstDesc* __restrict__ I
           cu = conv(su);
           cv = conv(sv);
         }
-        un = SUB(u0, MUL(dt, (double)cu));
-        vn = SUB(v0, MUL(dt, (double)cv));
+        un = SUB(u0, MUL(dt, f2d(cu)));
+        vn = SUB(v0, MUL(dt, f2d(cv)));
       }
       us[(long)j * D.usld + i] = un;
       vs[(long)j * D.usld + i] = vn;

@@ -125,3 +125,15 @@ def test_exact_dot_edge_cases():
     assert _xdot_gpu(t) == xsum.xsum(t)
     t = np.array([1.0, 2.0**-53])
     assert _xdot_gpu(t) == 1.0
+
+
+def test_integer_pipe_conversions_equal_the_hardware_ones():
+    """The binary64 <-> binary32 conversions and the exact halving done with integer
+    operations (icvt.cuh) give the hardware instructions' results bit for bit."""
+    import ctypes
+
+    from pyflow_solver_gb300 import _capi
+    from pyflow_solver_gb300._device import stream_handle
+    bad = (ctypes.c_longlong * 3)()
+    _capi.check(_capi.load().pfgb_selftest_conversions(1 << 24, stream_handle(), bad), "selftest_conversions")
+    assert list(bad) == [0, 0, 0]
