@@ -1348,10 +1348,10 @@ __global__ void __launch_bounds__(MT, 5) k_mg_post(const MixDesc* __restrict__ M
 
 // one CTA per instance
 template <int NT>
-__global__ void __launch_bounds__(NT, CT / NT) k_mg_coarse(const MixDesc* __restrict__ MD, int gate, int bottom_sweeps,
-                                                            Smooth sw) {
+__global__ void __launch_bounds__(NT, CT / NT) k_mg_coarse(const MixDesc* __restrict__ MD, const int* __restrict__ order,
+                                                            int gate, int bottom_sweeps, Smooth sw) {
   pdl_enter();
-  const MixDesc& M = MD[blockIdx.x];
+  const MixDesc& M = MD[order[blockIdx.x]];
   if (!mx_live(M, gate)) return;
   extern __shared__ float csm[];
   coarse_cycle<NT>(M, bottom_sweeps, sw, csm);
@@ -1892,7 +1892,8 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   }
   for (int l = 0; l < B->maxlev; ++l)
     bytes += up(tl[l].size() * sizeof(MTile)) + up(tpre[l].size() * sizeof(MTile));
-  bytes += up(n * sizeof(MixDesc)) + up(sizeof(MixLoop)) + up(sizeof(float)) + up(3 * n * sizeof(CUtensorMap));
+  bytes += up(n * sizeof(MixDesc)) + up(sizeof(MixLoop)) + up(sizeof(float)) + up(3 * n * sizeof(CUtensorMap)) +
+           up(n * sizeof(int));
   if (cudaMalloc(&B->ws, bytes) != cudaSuccess) {
     delete B;
     return set_error(PFGB_ENOMEM, "cudaMalloc of the mixed-solver workspace failed");
@@ -1999,6 +2000,24 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
   B->dd = (MixDesc*)take(n * sizeof(MixDesc));
   B->loop = (MixLoop*)take(sizeof(MixLoop));
   B->pad = (float*)take(sizeof(float));
+  {
+    // Launch order of the coarse CTAs.  CTAs are handed to SMs roughly in launch order,
+    // one to each SM before any SM gets a second, and a coarse CTA sharing its SM with a
+    // second one runs slower (both compete for the SM's issue slots); the launch is as
+    // long as its slowest SM.  So the CTAs with the most coarse work (cells of the CTA's
+    // levels) go first, one to an SM, and the rest follow in increasing order of work, so
+    // that the largest instances share their SMs with the smallest.  Every CTA computes
+    // the same values wherever it runs.
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    std::vector<int> ord(n);
+    for (int k = 0; k < n; ++k) ord[k] = k;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return plan[a].cta_tot > plan[b].cta_tot; });
+    if (n > sms) std::reverse(ord.begin() + sms, ord.end());
+    B->corder = (int*)take(n * sizeof(int));
+    cudaMemcpy(B->corder, ord.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+  }
   {
     // tensor maps of the TMA matvec: z, p0, p1 of every instance.  That form pays when
     // a CTA takes several tiles of one instance in turn (each instance's lookups once, the
@@ -2150,9 +2169,9 @@ static void add_vcycle(GraphChain& c, Batch* B, int gate, Smooth sw, int l0 = 0)
     if (B->ntpre[l]) c.kernel(k_mg_down, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, sw);
   }
   if (B->coarse_nt == CT2)
-    c.kernel_smem(k_mg_coarse<CT2>, dim3(B->n), dim3(CT2), B->coarse_smem, dd, gate, 8, sw);
+    c.kernel_smem(k_mg_coarse<CT2>, dim3(B->n), dim3(CT2), B->coarse_smem, dd, (const int*)B->corder, gate, 8, sw);
   else
-    c.kernel_smem(k_mg_coarse<CT>, dim3(B->n), dim3(CT), B->coarse_smem, dd, gate, 8, sw);
+    c.kernel_smem(k_mg_coarse<CT>, dim3(B->n), dim3(CT), B->coarse_smem, dd, (const int*)B->corder, gate, 8, sw);
   for (int l = B->maxlev - 2; l >= 0; --l)
     if (B->ntpre[l]) c.kernel(k_mg_post, dim3(B->ntpre[l]), dim3(MT), dd, (const MTile*)B->tpre[l], l, gate, sw);
 }
@@ -2235,9 +2254,9 @@ static void launch_vcycle(Batch* B, int gate, Smooth sw, cudaStream_t s, int l0 
   }
   // (each instance's coarse CTA starts from that instance's last global level)
   if (B->coarse_nt == CT2)
-    PFGB_TIMED(kp, "k_mg_coarse", -1, s, k_mg_coarse<CT2><<<B->n, CT2, B->coarse_smem, s>>>(B->dd, gate, 8, sw));
+    PFGB_TIMED(kp, "k_mg_coarse", -1, s, k_mg_coarse<CT2><<<B->n, CT2, B->coarse_smem, s>>>(B->dd, B->corder, gate, 8, sw));
   else
-    PFGB_TIMED(kp, "k_mg_coarse", -1, s, k_mg_coarse<CT><<<B->n, CT, B->coarse_smem, s>>>(B->dd, gate, 8, sw));
+    PFGB_TIMED(kp, "k_mg_coarse", -1, s, k_mg_coarse<CT><<<B->n, CT, B->coarse_smem, s>>>(B->dd, B->corder, gate, 8, sw));
   for (int l = B->maxlev - 2; l >= 0; --l)
     if (B->ntpre[l]) PFGB_TIMED(kp, "k_mg_post", l, s, k_mg_post<<<B->ntpre[l], MT, 0, s>>>(B->dd, B->tpre[l], l, gate, sw));
 }

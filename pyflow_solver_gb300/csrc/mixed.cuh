@@ -128,6 +128,7 @@ struct Batch {
   // profiling (direct launches): per-kernel events, owned by the step's instance
   KProf* kp = nullptr;
   float* pad = nullptr;                        // sink of the profiling pad kernel
+  int* corder = nullptr;                       // instance of each coarse CTA, in launch order
   // the persistent form of the solve (one cooperative launch)
   int persist_ok = 0;                          // the device co-schedules its CTAs
   int persist = 0;                             // in use

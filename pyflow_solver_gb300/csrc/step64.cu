@@ -786,9 +786,12 @@ __global__ void __launch_bounds__(NT) k_rhs_m(const InstDesc* __restrict__ ID, c
 }
 
 // p = x - x[0]; u = u* - dt gx(p), v likewise; lid; sums of (u - u_old)^2, (v - v_old)^2.
-// All loads of the thread's four rows are issued before any store (the arrays
-// are distinct, so the stores cannot feed the loads).
-__global__ void __launch_bounds__(NT) k_pin_correct_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+// The thread's four rows go in two halves of two rows: all loads of a half are issued
+// before its stores (the arrays are distinct, so the stores cannot feed the loads), and
+// holding two rows' operands instead of four keeps the kernel at three CTAs to an SM (two before).
+// The sums take the rows in the same order either way.
+constexpr int PC_H = 2;                       // rows per half
+__global__ void __launch_bounds__(NT, 3) k_pin_correct_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
   pdl_enter();
   TILE_PROLOGUE
   __shared__ StepRed rsm;
@@ -804,47 +807,50 @@ __global__ void __launch_bounds__(NT) k_pin_correct_m(const InstDesc* __restrict
   double* __restrict__ vi = D.vi;
   double* __restrict__ pi = D.pi;
   const double x0 = xs[0];
-  double xc[PB_R], xe[PB_R], xn[PB_R], u1[PB_R], v1[PB_R], u0[PB_R], v0[PB_R];
-  bool in[PB_R];
-#pragma unroll
-  for (int r = 0; r < PB_R; ++r) {
-    const int j = tl.j0 + (threadIdx.x >> 5) + r * PB_Y;
-    in[r] = i < G.nx && j < G.ny;
-    if (in[r]) {
-      const long ox = (long)j * G.ld + i, o = (long)j * D.usld + i, os = (long)j * G.lds + i;
-      xc[r] = xs[ox];
-      xe[r] = (i < G.nx - 1) ? xs[ox + 1] : 0.0;
-      xn[r] = (j < G.ny - 1) ? xs[ox + G.ld] : 0.0;
-      u1[r] = us[o];
-      v1[r] = vs[o];
-      u0[r] = ui[os];
-      v0[r] = vi[os];
-    }
-  }
   double v[2] = {0.0, 0.0}, out[2];
   int bad = 0;
+#pragma unroll 1
+  for (int h = 0; h < PB_R; h += PC_H) {
+    double xc[PC_H], xe[PC_H], xn[PC_H], u1[PC_H], v1[PC_H], u0[PC_H], v0[PC_H];
+    bool in[PC_H];
 #pragma unroll
-  for (int r = 0; r < PB_R; ++r) {
-    const int j = tl.j0 + (threadIdx.x >> 5) + r * PB_Y;
-    if (in[r]) {
-      const double pv = SUB(xc[r], x0);
-      const double gx = (i < G.nx - 1) ? MUL(SUB(SUB(xe[r], x0), pv), rg.rx) : 0.0;
-      const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(xn[r], x0), pv), rg.ry) : 0.0;
-      const long o = (long)j * D.usld + i;
-      const long os = (long)j * G.lds + i;
-      const double uc = SUB(u1[r], MUL(dt, gx));
-      const double vc = SUB(v1[r], MUL(dt, gy));
-      us[o] = uc;
-      vs[o] = vc;
-      pi[os] = pv;
-      const double uf = (L.has_lid && j == G.ny - 1) ? L.lid : uc;
-      const double du = SUB(uf, u0[r]);
-      const double dv = SUB(vc, v0[r]);
-      ui[os] = uf;
-      vi[os] = vc;
-      v[0] += du * du;
-      v[1] += dv * dv;
-      bad |= !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
+    for (int r = 0; r < PC_H; ++r) {
+      const int j = tl.j0 + (threadIdx.x >> 5) + (h + r) * PB_Y;
+      in[r] = i < G.nx && j < G.ny;
+      if (in[r]) {
+        const long ox = (long)j * G.ld + i, o = (long)j * D.usld + i, os = (long)j * G.lds + i;
+        xc[r] = xs[ox];
+        xe[r] = (i < G.nx - 1) ? xs[ox + 1] : 0.0;
+        xn[r] = (j < G.ny - 1) ? xs[ox + G.ld] : 0.0;
+        u1[r] = us[o];
+        v1[r] = vs[o];
+        u0[r] = ui[os];
+        v0[r] = vi[os];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < PC_H; ++r) {
+      const int j = tl.j0 + (threadIdx.x >> 5) + (h + r) * PB_Y;
+      if (in[r]) {
+        const double pv = SUB(xc[r], x0);
+        const double gx = (i < G.nx - 1) ? MUL(SUB(SUB(xe[r], x0), pv), rg.rx) : 0.0;
+        const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(xn[r], x0), pv), rg.ry) : 0.0;
+        const long o = (long)j * D.usld + i;
+        const long os = (long)j * G.lds + i;
+        const double uc = SUB(u1[r], MUL(dt, gx));
+        const double vc = SUB(v1[r], MUL(dt, gy));
+        us[o] = uc;
+        vs[o] = vc;
+        pi[os] = pv;
+        const double uf = (L.has_lid && j == G.ny - 1) ? L.lid : uc;
+        const double du = SUB(uf, u0[r]);
+        const double dv = SUB(vc, v0[r]);
+        ui[os] = uf;
+        vi[os] = vc;
+        v[0] += du * du;
+        v[1] += dv * dv;
+        bad |= !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
+      }
     }
   }
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->nan_flag, 1u);
