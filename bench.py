@@ -318,6 +318,11 @@ def kernel_table(prof, cells, shape_lists, step_ms, hbm):
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
 # captures of the same kernel and workload, with the file that records the capture.
 TRAFFIC = {
+    ("batched256", "k_mg_coarse"): (6.54e6, "profiles/k_mg_coarse_batched256.md"),
+    ("batched256", "k_mx_update_down"): (26.90e6, "profiles/k_mg_coarse_batched256.md (other batch kernels)"),
+    ("batched256", "k_mg_post@0"): (10.68e6, "profiles/k_mg_coarse_batched256.md (other batch kernels)"),
+    ("cavity512", "k_mg_coarse"): (7.94e4, "profiles/k_mg_coarse_512.md"),
+    ("cavity2048", "k_mx_update_down"): (80.8e6, "profiles/k_mx_update_down_2048.md"),
     ("cavity512", "k_mx_matvec"): (1.60e6, "profiles/k_mx_matvec_2048.md (512^2 capture)"),
     ("cavity2048", "k_mx_matvec"): (34.11e6, "profiles/k_mx_matvec_2048.md"),
     ("cavity2048", "k_mx_matvec_tma"): (33.74e6, "profiles/k_mx_matvec_tma_2048.md"),

@@ -2,7 +2,9 @@
 
 Run from the repository root on a machine that has the reference checkout:
 
-    python tests/golden/make_golden.py [--ref /root/reference] [--only NAME]
+    python tests/golden/make_golden.py --ref PATH_TO_REFERENCE_CHECKOUT [--only NAME]
+
+(or with the checkout's path in the environment variable PYFLOW_REFERENCE).
 
 The script imports the reference package (``src/pyflow``) read-only, runs its
 own ``SimulationDriver.run`` / ``step`` / ``solve_pressure_poisson`` and numerics
@@ -222,9 +224,12 @@ def batched_instances(n=256, seed=0):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PYFLOW_REFERENCE"),
+                    help="root of the reference checkout (default: $PYFLOW_REFERENCE)")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("the reference checkout is needed: pass --ref or set PYFLOW_REFERENCE")
     R = _import_reference(args.ref)
     meta = _meta()
 
