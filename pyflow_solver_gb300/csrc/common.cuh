@@ -18,6 +18,11 @@ __device__ __forceinline__ double SUB(double a, double b) { return __dsub_rn(a, 
 __device__ __forceinline__ double MUL(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double DIV(double a, double b) { return __ddiv_rn(a, b); }
 
+// -a (a sign flip: exact, and no binary64-pipe instruction)
+__device__ __forceinline__ double neg_exact(double a) {
+  return __hiloint2double(__double2hiint(a) ^ (int)0x80000000, __double2loint(a));
+}
+
 // Division by a grid spacing.  When the spacing is a power of two the quotient
 // equals the product with its (exact) reciprocal for every operand, so the
 // cheaper multiply is used; otherwise the integer-pipe division by an invariant

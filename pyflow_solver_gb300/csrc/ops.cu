@@ -101,28 +101,27 @@ __global__ void __launch_bounds__(OT) k_xdot(const double* a, const double* b, l
   __shared__ int ired[32];
   for (int k = threadIdx.x; k < XA_DIGITS; k += OT) sacc[k] = 0;
   long base = (long)blockIdx.x * OT * XPT;
-  XTerm t[XPT];
-  unsigned fl = 0u;
+  double va[XPT], vb[XPT];
   int top = INT_MIN;
 #pragma unroll
   for (int k = 0; k < XPT; ++k) {
     long idx = base + (long)k * OT + threadIdx.x;
-    xa_zero(t[k]);
+    va[k] = 0.0;
+    vb[k] = 1.0;                  // a plain sum is the sum of the products with 1
     if (idx < n) {
-      if (mode == 0) xa_term_prod(a[idx], b[idx], t[k], fl);
-      else xa_term_val(a[idx], t[k], fl);
+      va[k] = a[idx];
+      if (mode == 0) vb[k] = b[idx];
     }
-    top = max(top, t[k].top);
+    top = max(top, xa_prod_top(va[k], vb[k]));
   }
   top = xa_block_max(top, ired);
-  XCtx c;
-  c.clear();
-  c.flags = fl;
-  c.k0 = xa_window_digit(top);
+  const int k0 = xa_window_digit(top);
+  XAcc x;
+  x.clear();
 #pragma unroll
-  for (int k = 0; k < XPT; ++k) c.add(sacc, t[k]);
-  int anyslow = __syncthreads_or(c.slow);
-  xa_cta_commit(slot, c.pos, c.neg, c.k0, sacc, anyslow, c.flags, wred);
+  for (int k = 0; k < XPT; ++k) xa_acc_prod<false>(x, sacc, k0, va[k], vb[k]);
+  const int anyslow = __syncthreads_or(x.slow);
+  xa_acc_commit(slot, x, k0, sacc, anyslow, wred);
   XASlot* sl[1] = {slot};
   xa_finish(sl, 1, gridDim.x);
 }

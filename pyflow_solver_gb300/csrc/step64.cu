@@ -51,19 +51,54 @@ __device__ __forceinline__ double jacobi_apply(const Geo64& G, int j, int i, dou
 }
 
 // ---------------------------------------------------------------------------
-// Reduction tail shared by the kernels: one slot per call.
-__device__ __forceinline__ void reduce_terms(XASlot* slot, const XTerm* t, int nt, unsigned fl,
-                                             long long* sacc, long long* wred, int* ired) {
+// Reduction tails shared by the kernels.  A CTA's share of the exactly rounded
+// sum of a[k]*b[k], k < N (SQUARE: b is a) goes into `slot`; cells outside the
+// grid pass a = 0.  A plain sum passes b = 1.
+template <int N, bool SQUARE>
+__device__ __forceinline__ void reduce_prods(XASlot* slot, const double* a, const double* b, long long* sacc,
+                                             long long* wred, int* ired) {
   int top = INT_MIN;
-  for (int k = 0; k < nt; ++k) top = max(top, t[k].top);
+#pragma unroll
+  for (int k = 0; k < N; ++k) top = max(top, xa_prod_top(a[k], SQUARE ? a[k] : b[k]));
   top = xa_block_max(top, ired);
-  XCtx c;
-  c.clear();
-  c.flags = fl;
-  c.k0 = xa_window_digit(top);
-  for (int k = 0; k < nt; ++k) c.add(sacc, t[k]);
-  int anyslow = __syncthreads_or(c.slow);
-  xa_cta_commit(slot, c.pos, c.neg, c.k0, sacc, anyslow, c.flags, wred);
+  const int k0 = xa_window_digit(top);
+  XAcc x;
+  x.clear();
+#pragma unroll
+  for (int k = 0; k < N; ++k) xa_acc_prod<SQUARE>(x, sacc, k0, a[k], SQUARE ? a[k] : b[k]);
+  const int anyslow = __syncthreads_or(x.slow);
+  xa_acc_commit(slot, x, k0, sacc, anyslow, wred);
+}
+
+// Two such sums with one block-wide maximum and one commit barrier.  `ired`
+// holds 64 ints that no earlier code of the kernel uses; `wred` holds
+// 2 x XA_WLIMBS x (warps) long longs.
+template <int N, bool SQ0, bool SQ1>
+__device__ __forceinline__ void reduce_prods2(XASlot* s0, const double* a0, const double* b0, long long* sacc0,
+                                              XASlot* s1, const double* a1, const double* b1, long long* sacc1,
+                                              long long* wred, int* ired) {
+  __shared__ XCommit2 cs;
+  cs.zero();
+  int t0 = INT_MIN, t1 = INT_MIN;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    t0 = max(t0, xa_prod_top(a0[k], SQ0 ? a0[k] : b0[k]));
+    t1 = max(t1, xa_prod_top(a1[k], SQ1 ? a1[k] : b1[k]));
+  }
+  xa_block_max2(t0, t1, ired);
+  const int k0 = xa_window_digit(t0), k1 = xa_window_digit(t1);
+  // one window at a time: the first is folded into its warp digit sums before
+  // the second is formed, which keeps the live registers of one window
+  XAcc x;
+  x.clear();
+#pragma unroll
+  for (int k = 0; k < N; ++k) xa_acc_prod<SQ0>(x, sacc0, k0, a0[k], SQ0 ? a0[k] : b0[k]);
+  XWarpPart w0 = xa_warp_part(x);
+  x.clear();
+#pragma unroll
+  for (int k = 0; k < N; ++k) xa_acc_prod<SQ1>(x, sacc1, k1, a1[k], SQ1 ? a1[k] : b1[k]);
+  XWarpPart w1 = xa_warp_part(x);
+  xa_acc_commit2(s0, w0, k0, sacc0, s1, w1, k1, sacc1, wred, cs);
 }
 
 __device__ __forceinline__ void zero_sacc(long long* sacc) {
@@ -82,23 +117,20 @@ __global__ void __launch_bounds__(NT) k_prestep(const InstDesc* __restrict__ ID,
   pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc[XA_DIGITS];
-  __shared__ long long wred[(NT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
+  __shared__ int ired[64];
   zero_sacc(sacc);
   XASlot* slots = D.slots;
   Ctrl64* ctrl = D.ctrl;
   const int i = tl.i0 + (threadIdx.x & 31);
   const int j = tl.j0 + (threadIdx.x >> 5);
   View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds};
-  XTerm t;
-  xa_zero(t);
-  unsigned fl = 0u;
+  double d = 0.0;
   unsigned long long ub = 0ull, vb = 0ull;
   if (i < G.nx && j < G.ny) {
     ub = abs_bits(U(j, i));
     vb = abs_bits(V(j, i));
-    double d = div_central_unit(U, V, j, i, G.nx, G.ny);
-    xa_term_prod(d, d, t, fl);
+    d = div_central_unit(U, V, j, i, G.nx, G.ny);
   }
   for (int o = 16; o > 0; o >>= 1) {
     ub = max(ub, __shfl_xor_sync(0xffffffffu, ub, o));
@@ -108,7 +140,7 @@ __global__ void __launch_bounds__(NT) k_prestep(const InstDesc* __restrict__ ID,
     if (ub) atomicMax(&ctrl->umax_bits, ub);
     if (vb) atomicMax(&ctrl->vmax_bits, vb);
   }
-  reduce_terms(&slots[S_DIVC_BEFORE], &t, 1, fl, sacc, wred, ired);
+  reduce_prods<1, true>(&slots[S_DIVC_BEFORE], &d, &d, sacc, wred, ired);
   XASlot* sl[1] = {&slots[S_DIVC_BEFORE]};
   if (xa_finish(sl, 1, D.nt_pc) && threadIdx.x == 0) {
     double um = __longlong_as_double((long long)*(volatile unsigned long long*)&ctrl->umax_bits);
@@ -201,27 +233,22 @@ __global__ void __launch_bounds__(NT) k_rhs(const InstDesc* __restrict__ ID, con
   pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
-  __shared__ long long wred[(NT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
+  __shared__ int ired[64];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
   XASlot* slots = D.slots;
   const int i = tl.i0 + (threadIdx.x & 31);
   const int j = tl.j0 + (threadIdx.x >> 5);
-  XTerm t0, t1;
-  xa_zero(t0);
-  xa_zero(t1);
-  unsigned f0 = 0u, f1 = 0u;
+  double d = 0.0, bv = 0.0;
+  const double one = 1.0;
   if (i < G.nx && j < G.ny) {
     View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
-    double d = div_coherent_at(US, VS, j, i, G.g);
-    double bv = DIV(-d, D.ctrl->dtm);
+    d = div_coherent_at(US, VS, j, i, G.g);
+    bv = DIV(-d, D.ctrl->dtm);
     D.b[(long)j * G.ld + i] = bv;
-    xa_term_val(bv, t0, f0);
-    xa_term_prod(d, d, t1, f1);
   }
-  reduce_terms(&slots[S_BSUM], &t0, 1, f0, sacc0, wred, ired);
-  reduce_terms(&slots[S_DIVSTAR], &t1, 1, f1, sacc1, wred, ired);
+  reduce_prods2<1, false, true>(&slots[S_BSUM], &bv, &one, sacc0, &slots[S_DIVSTAR], &d, &d, sacc1, wred, ired);
   XASlot* sl[2] = {&slots[S_BSUM], &slots[S_DIVSTAR]};
   xa_finish(sl, 2, D.nt_pc);
 }
@@ -234,8 +261,8 @@ __global__ void __launch_bounds__(NT) k_cg_init(const InstDesc* __restrict__ ID,
   pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
-  __shared__ long long wred[(NT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
+  __shared__ int ired[64];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
   XASlot* slots = D.slots;
@@ -244,13 +271,10 @@ __global__ void __launch_bounds__(NT) k_cg_init(const InstDesc* __restrict__ ID,
   const int i = tl.i0 + (threadIdx.x & 31);
   const int j = tl.j0 + (threadIdx.x >> 5);
   const double mean = D.adjust ? DIV(slots[S_BSUM].result, A.n_cells) : 0.0;
-  XTerm t0, t1;
-  xa_zero(t0);
-  xa_zero(t1);
-  unsigned f0 = 0u, f1 = 0u;
+  double bv = 0.0, zv = 0.0;
   if (i < G.nx && j < G.ny) {
     long o = (long)j * G.ld + i;
-    double bv = D.b[o];
+    bv = D.b[o];
     if (D.adjust) {
       bv = SUB(bv, mean);
       if (i == 0 && j == 0) bv = 0.0;
@@ -258,11 +282,10 @@ __global__ void __launch_bounds__(NT) k_cg_init(const InstDesc* __restrict__ ID,
     }
     D.r[o] = bv;
     D.x[o] = 0.0;
-    xa_term_prod(bv, bv, t0, f0);
-    xa_term_prod(bv, jacobi_apply(G, j, i, bv), t1, f1);
+    zv = jacobi_apply(G, j, i, bv);
+    if (D.z) D.z[o] = zv;
   }
-  reduce_terms(&slots[S_BB], &t0, 1, f0, sacc0, wred, ired);
-  reduce_terms(&slots[S_RZ0], &t1, 1, f1, sacc1, wred, ired);
+  reduce_prods2<1, true, false>(&slots[S_BB], &bv, &bv, sacc0, &slots[S_RZ0], &bv, &zv, sacc1, wred, ired);
   XASlot* sl[2] = {&slots[S_BB], &slots[S_RZ0]};
   if (xa_finish(sl, 2, D.nt_pc) && threadIdx.x == 0) {
     double bb = slots[S_BB].result;
@@ -330,14 +353,15 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
   __shared__ double gxs[TYv][TX + 1];
   __shared__ double gys[TYv + 1][TX];
   __shared__ long long sacc[XA_DIGITS];
-  __shared__ long long wred[(NT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
+  __shared__ int ired[64];
   zero_sacc(sacc);
   XASlot* slots = D.slots;
   const int k = *(volatile int*)&ctrl->iter;
   const double* __restrict__ pold = (k & 1) ? D.p1 : D.p0;
   double* __restrict__ pnew = (k & 1) ? D.p0 : D.p1;
   const double* __restrict__ r = D.r;
+  const double* __restrict__ zs = D.z;     // M r as the last update wrote it (null: formed here)
   const int i0 = tl.i0, j0 = tl.j0;
   const double beta = (k > 0) ? ctrl->beta : 0.0;
   for (int idx = threadIdx.x; idx < (TYv + 2) * (TX + 2); idx += NT) {
@@ -347,7 +371,7 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
     double val = 0.0;
     if (!corner && gj >= 0 && gj < G.ny && gi >= 0 && gi < G.nx) {
       long o = (long)gj * G.ld + gi;
-      double z = jacobi_apply(G, gj, gi, r[o]);
+      const double z = zs ? zs[o] : jacobi_apply(G, gj, gi, r[o]);
       val = (k == 0) ? z : ADD(MUL(pold[o], beta), z);
     }
     pn[jj + 1][ii + 1] = val;
@@ -369,11 +393,11 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
   }
   __syncthreads();
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  XTerm t[R];
-  unsigned fl = 0u;
+  double pa[R], qa[R];
 #pragma unroll
   for (int rr = 0; rr < R; ++rr) {
-    xa_zero(t[rr]);
+    pa[rr] = 0.0;
+    qa[rr] = 0.0;
     int jj = ty + rr * PB_Y;
     int gj = j0 + jj, gi = i0 + tx;
     if (gj < G.ny && gi < G.nx) {
@@ -383,15 +407,16 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
       double yp = (gj >= 1) ? DIVH(SUB(gyj, gys[jj][tx]), G.g.sy) : DIVH(gyj, G.g.sy);
       double pv = pn[jj + 1][tx + 1];
       double qv;
-      if (OP == 0) qv = (gi == 0 && gj == 0) ? pv : -ADD(xp, yp);
+      if (OP == 0) qv = (gi == 0 && gj == 0) ? pv : neg_exact(ADD(xp, yp));
       else qv = (gi == 0 || gj == 0 || gi == G.nx - 1 || gj == G.ny - 1) ? pv : ADD(xp, yp);
       long o = (long)gj * G.ld + gi;
       D.q[o] = qv;
       pnew[o] = pv;
-      xa_term_prod(pv, qv, t[rr], fl);
+      pa[rr] = pv;
+      qa[rr] = qv;
     }
   }
-  reduce_terms(&slots[S_PQ], t, R, fl, sacc, wred, ired);
+  reduce_prods<R, false>(&slots[S_PQ], pa, qa, sacc, wred, ired);
   XASlot* sl[1] = {&slots[S_PQ]};
   if (xa_finish(sl, 1, D.nt_cg) && threadIdx.x == 0) {
     const double pq = slots[S_PQ].result;
@@ -403,15 +428,15 @@ __global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ I
 // x += alpha p; r -= alpha q; r.r; r.(M r).  An instance that finishes
 // leaves the loop control's active count; the last one stops the loop.
 template <int R = RPT>
-__global__ void __launch_bounds__(NT) k_cg_update(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
+__global__ void __launch_bounds__(NT, R == 1 ? 6 : 5) k_cg_update(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
                                                    LoopCtl* lc, cudaGraphConditionalHandle cond, int use_cond) {
   pdl_enter();
   TILE_PROLOGUE
   Ctrl64* ctrl = D.ctrl;
   if (*(volatile int*)&ctrl->done) return;
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
-  __shared__ long long wred[(NT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
+  __shared__ int ired[64];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
   XASlot* slots = D.slots;
@@ -421,12 +446,11 @@ __global__ void __launch_bounds__(NT) k_cg_update(const InstDesc* __restrict__ I
   const int i0 = tl.i0, j0 = tl.j0;
   const double alpha = ctrl->alpha;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  XTerm trr[R], trz[R];
-  unsigned f0 = 0u, f1 = 0u;
+  double ra[R], za[R];
 #pragma unroll
   for (int rr = 0; rr < R; ++rr) {
-    xa_zero(trr[rr]);
-    xa_zero(trz[rr]);
+    ra[rr] = 0.0;
+    za[rr] = 0.0;
     int gj = j0 + ty + rr * PB_Y, gi = i0 + tx;
     if (gj < G.ny && gi < G.nx) {
       long o = (long)gj * G.ld + gi;
@@ -434,12 +458,12 @@ __global__ void __launch_bounds__(NT) k_cg_update(const InstDesc* __restrict__ I
       double rv = SUB(D.r[o], MUL(alpha, D.q[o]));
       D.x[o] = xv;
       D.r[o] = rv;
-      xa_term_prod(rv, rv, trr[rr], f0);
-      xa_term_prod(rv, jacobi_apply(G, gj, gi, rv), trz[rr], f1);
+      ra[rr] = rv;
+      za[rr] = jacobi_apply(G, gj, gi, rv);
+      if (D.z) D.z[o] = za[rr];
     }
   }
-  reduce_terms(&slots[S_RR], trr, R, f0, sacc0, wred, ired);
-  reduce_terms(&slots[S_RZ], trz, R, f1, sacc1, wred, ired);
+  reduce_prods2<R, true, false>(&slots[S_RR], ra, ra, sacc0, &slots[S_RZ], ra, za, sacc1, wred, ired);
   XASlot* sl[2] = {&slots[S_RR], &slots[S_RZ]};
   if (xa_finish(sl, 2, D.nt_cg) && threadIdx.x == 0) {
     double rr = slots[S_RR].result;
@@ -479,21 +503,18 @@ __global__ void __launch_bounds__(NT) k_post_resid(const InstDesc* __restrict__ 
   pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc[XA_DIGITS];
-  __shared__ long long wred[(NT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
+  __shared__ int ired[64];
   zero_sacc(sacc);
   XASlot* slots = D.slots;
   const int i = tl.i0 + (threadIdx.x & 31);
   const int j = tl.j0 + (threadIdx.x >> 5);
-  XTerm t;
-  xa_zero(t);
-  unsigned fl = 0u;
+  double rv = 0.0;
   if (i < G.nx && j < G.ny) {
     View2<const double> X{D.x, G.ld};
-    double rv = SUB(D.b[(long)j * G.ld + i], apply_A<OP>(X, j, i, G.g));
-    xa_term_prod(rv, rv, t, fl);
+    rv = SUB(D.b[(long)j * G.ld + i], apply_A<OP>(X, j, i, G.g));
   }
-  reduce_terms(&slots[S_RES], &t, 1, fl, sacc, wred, ired);
+  reduce_prods<1, true>(&slots[S_RES], &rv, &rv, sacc, wred, ired);
   XASlot* sl[1] = {&slots[S_RES]};
   xa_finish(sl, 1, D.nt_pc);
 }
@@ -507,8 +528,8 @@ __global__ void __launch_bounds__(NT) k_pin_correct(const InstDesc* __restrict__
   pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
-  __shared__ long long wred[(NT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
+  __shared__ int ired[64];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
   XASlot* slots = D.slots;
@@ -516,10 +537,8 @@ __global__ void __launch_bounds__(NT) k_pin_correct(const InstDesc* __restrict__
   const LidArgs L = D.L;
   const int i = tl.i0 + (threadIdx.x & 31);
   const int j = tl.j0 + (threadIdx.x >> 5);
-  XTerm t0, t1;
-  xa_zero(t0);
-  xa_zero(t1);
-  unsigned f0 = 0u, f1 = 0u;
+  double du2 = 0.0, dv2 = 0.0;
+  const double one = 1.0;
   int bad = 0;
   if (i < G.nx && j < G.ny) {
     const double dt = ctrl->dt;
@@ -542,16 +561,15 @@ __global__ void __launch_bounds__(NT) k_pin_correct(const InstDesc* __restrict__
       const double dv = SUB(vc, D.vi[os]);
       D.ui[os] = uf;
       D.vi[os] = vc;
-      xa_term_val(MUL(du, du), t0, f0);
-      xa_term_val(MUL(dv, dv), t1, f1);
+      du2 = MUL(du, du);
+      dv2 = MUL(dv, dv);
       bad = !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
     } else {
       bad = !(isfinite_d(uc) && isfinite_d(vc) && isfinite_d(pv));
     }
   }
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->nan_flag, 1u);
-  reduce_terms(&slots[S_RU], &t0, 1, f0, sacc0, wred, ired);
-  reduce_terms(&slots[S_RV], &t1, 1, f1, sacc1, wred, ired);
+  reduce_prods2<1, false, false>(&slots[S_RU], &du2, &one, sacc0, &slots[S_RV], &dv2, &one, sacc1, wred, ired);
   XASlot* sl[2] = {&slots[S_RU], &slots[S_RV]};
   xa_finish(sl, 2, D.nt_pc);
 }
@@ -561,32 +579,24 @@ __global__ void __launch_bounds__(NT) k_post_diag(const InstDesc* __restrict__ I
   pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS], sacc2[XA_DIGITS];
-  __shared__ long long wred[(NT / 32) * XA_WLIMBS];
-  __shared__ int ired[32];
+  __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
+  __shared__ int ired[64];
   zero_sacc(sacc0);
   zero_sacc(sacc1);
   zero_sacc(sacc2);
   XASlot* slots = D.slots;
   const int i = tl.i0 + (threadIdx.x & 31);
   const int j = tl.j0 + (threadIdx.x >> 5);
-  XTerm t0, t1, t2;
-  xa_zero(t0);
-  xa_zero(t1);
-  xa_zero(t2);
-  unsigned f0 = 0u, f1 = 0u, f2 = 0u;
+  double d = 0.0, lr = 0.0, c = 0.0;
   if (i < G.nx && j < G.ny) {
     View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
     View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds}, P{D.pi, G.lds};
-    double d = div_coherent_at(US, VS, j, i, G.g);
-    xa_term_prod(d, d, t0, f0);
-    double lr = SUB(apply_A<0>(P, j, i, G.g), D.b[(long)j * G.ld + i]);
-    xa_term_prod(lr, lr, t1, f1);
-    double c = div_central_unit(U, V, j, i, G.nx, G.ny);
-    xa_term_prod(c, c, t2, f2);
+    d = div_coherent_at(US, VS, j, i, G.g);
+    lr = SUB(apply_A<0>(P, j, i, G.g), D.b[(long)j * G.ld + i]);
+    c = div_central_unit(U, V, j, i, G.nx, G.ny);
   }
-  reduce_terms(&slots[S_DIVAFTER], &t0, 1, f0, sacc0, wred, ired);
-  reduce_terms(&slots[S_LINRES], &t1, 1, f1, sacc1, wred, ired);
-  reduce_terms(&slots[S_CONT], &t2, 1, f2, sacc2, wred, ired);
+  reduce_prods2<1, true, true>(&slots[S_DIVAFTER], &d, &d, sacc0, &slots[S_LINRES], &lr, &lr, sacc1, wred, ired);
+  reduce_prods<1, true>(&slots[S_CONT], &c, &c, sacc2, wred, ired);
   XASlot* sl[3] = {&slots[S_DIVAFTER], &slots[S_LINRES], &slots[S_CONT]};
   xa_finish(sl, 3, D.nt_pc);
 }
@@ -1070,7 +1080,7 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
   for (int k = 0; k < n; ++k) {
     const long ld = round_up(prms[k].nx, 32);
     vec[k] = up((size_t)ld * prms[k].ny * sizeof(double));
-    bytes += 8 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64)) + up(sizeof(SteadyRing)) +
+    bytes += 9 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64)) + up(sizeof(SteadyRing)) +
              up(3 * (size_t)count_tiles(prms[k].nx, prms[k].ny, PB_Y) * sizeof(double)) + up(sizeof(unsigned));
     add_tiles(tpc, k, prms[k].nx, prms[k].ny, PB_Y);
     add_tiles(tpcm, k, prms[k].nx, prms[k].ny, TY_M);
@@ -1129,6 +1139,7 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     D.p0 = (double*)take(vec[k]);
     D.p1 = (double*)take(vec[k]);
     D.q = (double*)take(vec[k]);
+    D.z = (double*)take(vec[k]);
     D.slots = (XASlot*)take(S_COUNT * sizeof(XASlot));
     D.ctrl = (Ctrl64*)take(sizeof(Ctrl64));
     D.nt_pc = count_tiles(prm.nx, prm.ny, PB_Y);

@@ -122,6 +122,8 @@ struct InstDesc {
   double *us, *vs;             // u*, v* (pitch usld)
   long usld;
   double *b, *x, *r, *p0, *p1, *q;
+  double* z;                   // M r of the Jacobi-preconditioned CG, written by the kernels that form r
+                               // (null: the matvec forms M r itself)
   XASlot* slots;
   Ctrl64* ctrl;
   const StepIn* in;

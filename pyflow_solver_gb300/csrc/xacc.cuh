@@ -11,17 +11,17 @@
 // digits; digit k weighs 2^(32k + XA_LSB).  Digits are carry-save (any int64),
 // so CTAs add into them with plain atomicAdd and one finaliser normalises.
 //
-// Per CTA: every thread turns its terms (a*b products as exact 106-bit
-// integers, or plain doubles) into (mantissa, exponent) pairs, the CTA agrees on
-// the largest top bit, and each thread adds its terms into an 8-limb (256-bit)
-// two's complement window anchored just above that bit.  Terms whose low bits
-// would fall below the window take a slow path: shared-memory atomics into a
-// full-range CTA superaccumulator.  Both are flushed into the global slot with
-// int64 atomics; the last CTA to finish (atomic ticket) rounds the result to
-// double (round to nearest, ties to even) and clears the slot for reuse.
+// Per CTA: the threads agree on a bound of the largest term's top bit, and
+// each thread adds its terms (a*b products as exact 106-bit integers; a plain
+// double is the product with 1.0) into a signed 256-bit window anchored
+// XA_HEADROOM bits above that bound.  Terms whose low bits would fall below
+// the window take a slow path: shared-memory atomics into a full-range CTA
+// superaccumulator.  Both are flushed into the global slot with int64
+// atomics; the last CTA to finish (atomic ticket) rounds the result to double
+// (round to nearest, ties to even) and clears the slot for reuse.
 //
-// FP64 work on GB300 issues at ~1.6 ops/clk/SM versus ~60 integer ops/clk/SM,
-// so all of this is integer arithmetic.
+// Binary64 arithmetic on GB300 issues at ~1.6 ops/clk/SM versus ~60 integer
+// ops/clk/SM, so all of this is integer arithmetic.
 #pragma once
 #include <cstdint>
 
@@ -53,12 +53,6 @@ struct XTerm {                   // value = (-1)^neg * M * 2^e,  M = m3:m2:m1:m0
   bool neg;
 };
 
-__device__ __forceinline__ int xa_bitlen64(uint64_t x) { return x ? 64 - __clzll(x) : 0; }
-
-__device__ __forceinline__ void xa_zero(XTerm& t) {
-  t.m[0] = t.m[1] = t.m[2] = t.m[3] = 0u; t.e = 0; t.top = INT_MIN; t.neg = false;
-}
-
 // Decompose a double into (sign, 53-bit integer mantissa, exponent of its LSB).
 // Returns 0 finite, 1 NaN, 2 +inf, 3 -inf.
 __device__ __forceinline__ int xa_unpack(double a, uint64_t& m, int& e, bool& neg) {
@@ -78,78 +72,6 @@ __device__ __forceinline__ void xa_special(int kind, unsigned& flags) {
   else if (kind == 3) flags |= XA_NINF;
 }
 
-// Exact term for the product a*b.
-__device__ __forceinline__ void xa_term_prod(double a, double b, XTerm& t, unsigned& flags) {
-  uint64_t ma, mb; int ea, eb; bool sa, sb;
-  int ka = xa_unpack(a, ma, ea, sa);
-  int kb = xa_unpack(b, mb, eb, sb);
-  xa_zero(t);
-  if (ka | kb) {
-    if (ka == 1 || kb == 1) { flags |= XA_NAN; return; }
-    // at least one infinity and no NaN: inf*0 is NaN
-    bool zero_other = (ka ? (mb == 0) : (ma == 0));
-    if (zero_other) { flags |= XA_NAN; return; }
-    flags |= ((sa != sb) ? XA_NINF : XA_PINF);
-    return;
-  }
-  if (ma == 0 || mb == 0) return;
-  uint64_t lo = ma * mb;
-  uint64_t hi = __umul64hi(ma, mb);
-  t.m[0] = (uint32_t)lo; t.m[1] = (uint32_t)(lo >> 32);
-  t.m[2] = (uint32_t)hi; t.m[3] = (uint32_t)(hi >> 32);
-  t.e = ea + eb;
-  t.neg = sa != sb;
-  int bl = hi ? 64 + xa_bitlen64(hi) : xa_bitlen64(lo);
-  t.top = t.e + bl - 1;
-}
-
-// Exact term for the product of two binary32 values (48-bit significand product).
-__device__ __forceinline__ void xa_term_prod_f32(float a, float b, XTerm& t, unsigned& flags) {
-  const uint32_t ba = __float_as_uint(a), bb = __float_as_uint(b);
-  const int efa = (int)((ba >> 23) & 0xff), efb = (int)((bb >> 23) & 0xff);
-  uint32_t ma = ba & 0x7fffffu, mb = bb & 0x7fffffu;
-  const bool sa = (ba >> 31) != 0, sb = (bb >> 31) != 0;
-  xa_zero(t);
-  if (efa == 0xff || efb == 0xff) {
-    if ((efa == 0xff && ma) || (efb == 0xff && mb)) { flags |= XA_NAN; return; }
-    const bool zero_other = (efa == 0xff) ? (efb == 0 && mb == 0) : (efa == 0 && ma == 0);
-    if (zero_other) { flags |= XA_NAN; return; }
-    flags |= (sa != sb) ? XA_NINF : XA_PINF;
-    return;
-  }
-  int ea, eb;
-  if (efa == 0) { ea = 1 - 150; } else { ma |= 0x800000u; ea = efa - 150; }
-  if (efb == 0) { eb = 1 - 150; } else { mb |= 0x800000u; eb = efb - 150; }
-  if (ma == 0u || mb == 0u) return;
-  const uint64_t prod = (uint64_t)ma * (uint64_t)mb;
-  t.m[0] = (uint32_t)prod;
-  t.m[1] = (uint32_t)(prod >> 32);
-  t.e = ea + eb;
-  t.neg = sa != sb;
-  t.top = t.e + xa_bitlen64(prod) - 1;
-}
-
-// Exact term for a single double (used for sums of rounded values).
-__device__ __forceinline__ void xa_term_val(double a, XTerm& t, unsigned& flags) {
-  uint64_t ma; int ea; bool sa;
-  int ka = xa_unpack(a, ma, ea, sa);
-  xa_zero(t);
-  if (ka) { xa_special(ka, flags); return; }
-  if (ma == 0) return;
-  t.m[0] = (uint32_t)ma; t.m[1] = (uint32_t)(ma >> 32);
-  t.e = ea; t.neg = sa;
-  t.top = ea + xa_bitlen64(ma) - 1;
-}
-
-// Thread-local 256-bit windows: positive and negative terms accumulate into
-// separate unsigned windows (no sign branches); the CTA commit subtracts them.
-struct XWin { uint32_t w[XA_WLIMBS]; };
-
-__device__ __forceinline__ void xwin_clear(XWin& w) {
-#pragma unroll
-  for (int i = 0; i < XA_WLIMBS; ++i) w.w[i] = 0u;
-}
-
 // Window base digit for a CTA whose largest term top bit is `top`
 // (absolute exponent).  Window digits are [k0, k0+8).
 __device__ __forceinline__ int xa_window_digit(int top) {
@@ -165,65 +87,6 @@ __device__ __forceinline__ void xa_shift_limbs(const uint32_t m[4], int r, uint3
   sh[2] = __funnelshift_l(m[1], m[2], r);
   sh[3] = __funnelshift_l(m[2], m[3], r);
   sh[4] = (r == 0) ? 0u : (m[3] >> (32 - r));
-}
-
-// acc += sh placed at limb offset q (0..7); limbs that would land above limb 7
-// are zero because every term's top bit lies below the window top.  The carry
-// flag does not survive between asm statements, so each offset has its own chain.
-__device__ __forceinline__ void xwin_add_at(XWin& acc, const uint32_t sh[5], int q) {
-  uint32_t* a = acc.w;
-  switch (q) {
-    case 0:
-      asm("add.cc.u32 %0, %0, %8;\n\taddc.cc.u32 %1, %1, %9;\n\t"
-          "addc.cc.u32 %2, %2, %10;\n\taddc.cc.u32 %3, %3, %11;\n\t"
-          "addc.cc.u32 %4, %4, %12;\n\taddc.cc.u32 %5, %5, 0;\n\t"
-          "addc.cc.u32 %6, %6, 0;\n\taddc.u32 %7, %7, 0;"
-          : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
-          : "r"(sh[0]), "r"(sh[1]), "r"(sh[2]), "r"(sh[3]), "r"(sh[4]));
-      break;
-    case 1:
-      asm("add.cc.u32 %0, %0, %7;\n\taddc.cc.u32 %1, %1, %8;\n\t"
-          "addc.cc.u32 %2, %2, %9;\n\taddc.cc.u32 %3, %3, %10;\n\t"
-          "addc.cc.u32 %4, %4, %11;\n\taddc.cc.u32 %5, %5, 0;\n\t"
-          "addc.u32 %6, %6, 0;"
-          : "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
-          : "r"(sh[0]), "r"(sh[1]), "r"(sh[2]), "r"(sh[3]), "r"(sh[4]));
-      break;
-    case 2:
-      asm("add.cc.u32 %0, %0, %6;\n\taddc.cc.u32 %1, %1, %7;\n\t"
-          "addc.cc.u32 %2, %2, %8;\n\taddc.cc.u32 %3, %3, %9;\n\t"
-          "addc.cc.u32 %4, %4, %10;\n\taddc.u32 %5, %5, 0;"
-          : "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
-          : "r"(sh[0]), "r"(sh[1]), "r"(sh[2]), "r"(sh[3]), "r"(sh[4]));
-      break;
-    case 3:
-      asm("add.cc.u32 %0, %0, %5;\n\taddc.cc.u32 %1, %1, %6;\n\t"
-          "addc.cc.u32 %2, %2, %7;\n\taddc.cc.u32 %3, %3, %8;\n\t"
-          "addc.u32 %4, %4, %9;"
-          : "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
-          : "r"(sh[0]), "r"(sh[1]), "r"(sh[2]), "r"(sh[3]), "r"(sh[4]));
-      break;
-    case 4:  // sh[4] is zero: the term's top bit is below 256
-      asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\t"
-          "addc.cc.u32 %2, %2, %6;\n\taddc.u32 %3, %3, %7;"
-          : "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
-          : "r"(sh[0]), "r"(sh[1]), "r"(sh[2]), "r"(sh[3]));
-      break;
-    case 5:
-      asm("add.cc.u32 %0, %0, %3;\n\taddc.cc.u32 %1, %1, %4;\n\t"
-          "addc.u32 %2, %2, %5;"
-          : "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
-          : "r"(sh[0]), "r"(sh[1]), "r"(sh[2]));
-      break;
-    case 6:
-      asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;"
-          : "+r"(a[6]), "+r"(a[7])
-          : "r"(sh[0]), "r"(sh[1]));
-      break;
-    default:
-      a[7] += sh[0];
-      break;
-  }
 }
 
 // Slow path: add a term into a full-range shared-memory superaccumulator.
@@ -261,19 +124,129 @@ __device__ __forceinline__ void xa_slow_add(long long* sacc, const XTerm& t, uns
   }
 }
 
-// Add a term to the thread windows (anchored at digit k0) or the slow path.
-__device__ __forceinline__ void xa_add(XWin& pos, XWin& neg, long long* sacc, int k0,
-                                       const XTerm& t, unsigned& flags, int& slow_used) {
-  if (t.top == INT_MIN) return;
-  int s = t.e - (32 * k0 + XA_LSB);            // shift relative to the window bottom
-  if (s < 0 || k0 < 0 || k0 + XA_WLIMBS > XA_DIGITS) {
-    xa_slow_add(sacc, t, flags);
-    slow_used = 1;
+// ---- per-thread accumulation --------------------------------------------------
+//
+// A thread adds its terms into a signed 256-bit two's complement window of
+// eight 32-bit limbs; limb j is digit k0 + j of the slot.  A term a*b is the
+// exact integer product of the two 53-bit significands (four 32-bit partial
+// products), moved to its place by a funnel shift (the bit offset) and a
+// three-stage limb rotation (the limb offset, 0..4), and added with one carry
+// chain; a negative term is added as its complement with a carry-in of one.
+// Nothing branches on the term but the rare cases (a NaN or infinite operand,
+// a term whose low bits fall below the window).
+
+// Upper bound of the top bit of |a*b| (the product's LSB exponent plus 105);
+// INT_MIN when an operand is NaN or infinite (those only set flags).
+__device__ __forceinline__ int xa_prod_top(double a, double b) {
+  const int efa = (int)(((uint32_t)__double2hiint(a) >> 20) & 0x7ffu);
+  const int efb = (int)(((uint32_t)__double2hiint(b) >> 20) & 0x7ffu);
+  if (efa == 0x7ff || efb == 0x7ff) return INT_MIN;
+  return max(efa, 1) + max(efb, 1) - 2150 + 105;
+}
+
+// One thread's share of one reduction.
+struct XAcc {
+  uint32_t w[XA_WLIMBS];
+  unsigned flags;
+  int slow;       // a term went to the shared full-range accumulator
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int j = 0; j < XA_WLIMBS; ++j) w[j] = 0u;
+    flags = 0u;
+    slow = 0;
+  }
+};
+
+// NaN and infinity flags of a product with a non-finite operand (inf * 0 is NaN).
+__device__ __forceinline__ void xa_special_prod(double a, double b, unsigned& flags) {
+  uint64_t ma, mb; int ea, eb; bool sa, sb;
+  const int ka = xa_unpack(a, ma, ea, sa);
+  const int kb = xa_unpack(b, mb, eb, sb);
+  if (ka == 1 || kb == 1) { flags |= XA_NAN; return; }
+  const bool zero_other = ka ? (kb == 0 && mb == 0) : (ma == 0);
+  if (zero_other) { flags |= XA_NAN; return; }
+  flags |= (sa != sb) ? XA_NINF : XA_PINF;
+}
+
+// x += a*b (SQUARE: b is a, and the term is never negative).  k0 is the CTA's
+// window digit (xa_window_digit of the largest xa_prod_top of the CTA's terms).
+template <bool SQUARE = false>
+__device__ __forceinline__ void xa_acc_prod(XAcc& x, long long* sacc, int k0, double a, double b) {
+  const uint32_t ha = (uint32_t)__double2hiint(a), la = (uint32_t)__double2loint(a);
+  const uint32_t hb = SQUARE ? ha : (uint32_t)__double2hiint(b);
+  const uint32_t lb = SQUARE ? la : (uint32_t)__double2loint(b);
+  const int efa = (int)((ha >> 20) & 0x7ffu), efb = (int)((hb >> 20) & 0x7ffu);
+  if (efa == 0x7ff || efb == 0x7ff) {
+    xa_special_prod(a, SQUARE ? a : b, x.flags);
     return;
   }
-  uint32_t sh[5];
-  xa_shift_limbs(t.m, s & 31, sh);
-  xwin_add_at(t.neg ? neg : pos, sh, s >> 5);
+  const uint32_t a1 = (ha & 0xfffffu) | (efa ? 0x100000u : 0u);
+  const uint32_t b1 = SQUARE ? a1 : ((hb & 0xfffffu) | (efb ? 0x100000u : 0u));
+  // M = a*b significands = p00 + mid 2^32 + p11 2^64 (< 2^106)
+  const uint64_t p00 = (uint64_t)la * lb;
+  const uint64_t mid = SQUARE ? (((uint64_t)la * a1) << 1) : ((uint64_t)la * b1 + (uint64_t)a1 * lb);   // < 2^54
+  const uint64_t p11 = (uint64_t)a1 * b1;                                                             // < 2^42
+  uint32_t m1, m2, m3;
+  asm("add.cc.u32 %0, %3, %4;\n\taddc.cc.u32 %1, %5, %6;\n\taddc.u32 %2, %7, 0;"
+      : "=r"(m1), "=r"(m2), "=r"(m3)
+      : "r"((uint32_t)(p00 >> 32)), "r"((uint32_t)mid), "r"((uint32_t)(mid >> 32)), "r"((uint32_t)p11),
+        "r"((uint32_t)(p11 >> 32)));
+  const uint32_t m0 = (uint32_t)p00;
+  const int e = max(efa, 1) + max(efb, 1) - 2150;          // weight of M's LSB
+  const int s = e - (32 * k0 + XA_LSB);                      // its bit offset in the window
+  const bool neg = !SQUARE && ((ha ^ hb) >> 31);
+  if (s < 0 || k0 < 0 || k0 + XA_WLIMBS > XA_DIGITS) {
+    if ((m0 | m1 | m2 | m3) == 0u) return;
+    XTerm t;
+    t.m[0] = m0; t.m[1] = m1; t.m[2] = m2; t.m[3] = m3;
+    t.e = e;
+    t.top = e + 105;
+    t.neg = neg;
+    xa_slow_add(sacc, t, x.flags);
+    x.slow = 1;
+    return;
+  }
+  // s <= 135 here (the term lies at least XA_HEADROOM bits below the window top),
+  // so the limb offset q is at most 4 and nothing is shifted past limb 7
+  const int r = s & 31, q = s >> 5;
+  uint32_t v[XA_WLIMBS];
+  v[0] = m0 << r;
+  v[1] = __funnelshift_l(m0, m1, r);
+  v[2] = __funnelshift_l(m1, m2, r);
+  v[3] = __funnelshift_l(m2, m3, r);
+  v[4] = __funnelshift_l(m3, 0u, r);
+  v[5] = v[6] = v[7] = 0u;
+#pragma unroll
+  for (int k = 1; k <= 4; k <<= 1) {
+    const bool c = (q & k) != 0;
+#pragma unroll
+    for (int j = XA_WLIMBS - 1; j >= 0; --j) v[j] = c ? (j >= k ? v[j - k] : 0u) : v[j];
+  }
+  uint32_t* w = x.w;
+  if (SQUARE) {
+    asm("add.cc.u32 %0, %0, %8;\n\taddc.cc.u32 %1, %1, %9;\n\t"
+        "addc.cc.u32 %2, %2, %10;\n\taddc.cc.u32 %3, %3, %11;\n\t"
+        "addc.cc.u32 %4, %4, %12;\n\taddc.cc.u32 %5, %5, %13;\n\t"
+        "addc.cc.u32 %6, %6, %14;\n\taddc.u32 %7, %7, %15;"
+        : "+r"(w[0]), "+r"(w[1]), "+r"(w[2]), "+r"(w[3]), "+r"(w[4]), "+r"(w[5]), "+r"(w[6]), "+r"(w[7])
+        : "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]));
+  } else {
+    // w += (v ^ mask) + (mask & 1): the carry-in comes from mask + mask
+    const uint32_t mask = neg ? 0xffffffffu : 0u;
+    asm("{\n\t.reg .u32 t;\n\tadd.cc.u32 t, %8, %8;\n\t"
+        "addc.cc.u32 %0, %0, %9;\n\taddc.cc.u32 %1, %1, %10;\n\t"
+        "addc.cc.u32 %2, %2, %11;\n\taddc.cc.u32 %3, %3, %12;\n\t"
+        "addc.cc.u32 %4, %4, %13;\n\taddc.cc.u32 %5, %5, %14;\n\t"
+        "addc.cc.u32 %6, %6, %15;\n\taddc.u32 %7, %7, %16;\n\t}"
+        : "+r"(w[0]), "+r"(w[1]), "+r"(w[2]), "+r"(w[3]), "+r"(w[4]), "+r"(w[5]), "+r"(w[6]), "+r"(w[7])
+        : "r"(mask), "r"(v[0] ^ mask), "r"(v[1] ^ mask), "r"(v[2] ^ mask), "r"(v[3] ^ mask), "r"(v[4] ^ mask),
+          "r"(v[5] ^ mask), "r"(v[6] ^ mask), "r"(v[7] ^ mask));
+  }
+}
+
+// x += a (exactly: the product a * 1.0)
+__device__ __forceinline__ void xa_acc_val(XAcc& x, long long* sacc, int k0, double a) {
+  xa_acc_prod<false>(x, sacc, k0, a, 1.0);
 }
 
 // Block-wide max of an int (all threads get it). `red` is >= 32 ints of smem.
@@ -289,61 +262,184 @@ __device__ __forceinline__ int xa_block_max(int v, int* red) {
   return r;
 }
 
-// Reduce the per-thread windows of the CTA into digits k0..k0+7 of the global
-// slot, flush the slow-path accumulator, and OR the flags.  `wred` is smem of
-// XA_WLIMBS*32 long longs.  Must be called by all threads of the CTA.
-__device__ __forceinline__ void xa_cta_commit(XASlot* slot, const XWin& pos, const XWin& neg, int k0,
-                                              long long* sacc, int any_slow,
-                                              unsigned flags, long long* wred) {
+// Two block-wide maxima with one barrier. `red` is >= 64 ints of smem that no
+// earlier code of the kernel uses.
+__device__ __forceinline__ void xa_block_max2(int& v0, int& v1, int* red) {
+  v0 = __reduce_max_sync(0xffffffffu, v0);
+  v1 = __reduce_max_sync(0xffffffffu, v1);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) {
+    red[wid] = v0;
+    red[32 + wid] = v1;
+  }
+  __syncthreads();
+  v0 = __reduce_max_sync(0xffffffffu, (lane < nw) ? red[lane] : INT_MIN);
+  v1 = __reduce_max_sync(0xffffffffu, (lane < nw) ? red[32 + lane] : INT_MIN);
+}
+
+// Warp sum of the eight signed digits of the lanes' windows, reduce-scattered
+// (each shuffle level halves the digits a lane carries): every fourth lane
+// returns the warp sum of digit *digit.
+__device__ __forceinline__ long long xa_warp_digits(const XAcc& x, int* digit) {
+  const int lane = threadIdx.x & 31;
   long long d[XA_WLIMBS];
 #pragma unroll
-  for (int j = 0; j < XA_WLIMBS; ++j) d[j] = (long long)(uint64_t)pos.w[j] - (long long)(uint64_t)neg.w[j];
+  for (int j = 0; j < XA_WLIMBS - 1; ++j) d[j] = (long long)x.w[j];
+  d[XA_WLIMBS - 1] = (long long)(int)x.w[XA_WLIMBS - 1];   // the sign limb
+  const bool u16 = (lane & 16) != 0, u8 = (lane & 8) != 0, u4 = (lane & 4) != 0;
+  long long d4[4], d2[2], d1;
 #pragma unroll
-  for (int j = 0; j < XA_WLIMBS; ++j) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) d[j] += __shfl_xor_sync(0xffffffffu, d[j], o);
+  for (int m = 0; m < 4; ++m) {
+    const long long send = u16 ? d[m] : d[m + 4];
+    const long long keep = u16 ? d[m + 4] : d[m];
+    d4[m] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
   }
-  flags = __reduce_or_sync(0xffffffffu, flags);
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int m = 0; m < 2; ++m) {
+    const long long send = u8 ? d4[m] : d4[m + 2];
+    const long long keep = u8 ? d4[m + 2] : d4[m];
+    d2[m] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+  {
+    const long long send = u4 ? d2[0] : d2[1];
+    const long long keep = u4 ? d2[1] : d2[0];
+    d1 = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  d1 += __shfl_xor_sync(0xffffffffu, d1, 2);
+  d1 += __shfl_xor_sync(0xffffffffu, d1, 1);
+  *digit = (u16 ? 4 : 0) + (u8 ? 2 : 0) + (u4 ? 1 : 0);
+  return d1;
+}
+
+// One warp adds the CTA's window sums (wred: XA_WLIMBS per warp) into digits
+// k0..k0+7 of the slot and widens the slot's span of written digits once.
+// Returns whether this lane made an atomic update.
+__device__ __forceinline__ int xa_warp_flush(XASlot* slot, int k0, const long long* wred, int nw) {
+  const int lane = threadIdx.x & 31;
+  long long s = 0;
+  if (lane < XA_WLIMBS)
+    for (int w = 0; w < nw; ++w) s += wred[w * XA_WLIMBS + lane];
+  const int dig = k0 + lane;
+  const bool inr = dig >= 0 && dig < XA_DIGITS;
+  int did = 0;
+  if (s != 0) {
+    if (inr) atomicAdd((unsigned long long*)&slot->digit[dig], (unsigned long long)s);
+    else atomicOr(&slot->flags, XA_OVERFLOW);
+    did = 1;
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, s != 0 && inr);
+  if (lane == 0 && m) {
+    atomicMax(&slot->lo_inv, XA_DIGITS - (k0 + __ffs(m) - 1));
+    atomicMax(&slot->hi_p1, k0 + 32 - __clz(m));
+    did = 1;
+  }
+  return did;
+}
+
+// The CTA's shared-memory superaccumulator of slow-path terms into the slot.
+__device__ __forceinline__ int xa_flush_slow(XASlot* slot, const long long* sacc) {
+  int did = 0;
+  for (int k = threadIdx.x; k < XA_DIGITS; k += blockDim.x) {
+    const long long s = sacc[k];
+    if (s != 0) {
+      atomicAdd((unsigned long long*)&slot->digit[k], (unsigned long long)s);
+      atomicMax(&slot->lo_inv, XA_DIGITS - k);
+      atomicMax(&slot->hi_p1, k + 1);
+      did = 1;
+    }
+  }
+  return did;
+}
+
+// Sum the CTA's windows into digits k0..k0+7 of the global slot, flush the
+// slow-path accumulator and OR the flags.  `wred` is smem of XA_WLIMBS x
+// (warps) long longs.  Must be called by all threads of the CTA.
+__device__ __forceinline__ void xa_acc_commit(XASlot* slot, const XAcc& x, int k0, long long* sacc, int any_slow,
+                                              long long* wred) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  int my_digit;
+  const long long d1 = xa_warp_digits(x, &my_digit);
+  const unsigned flags = __reduce_or_sync(0xffffffffu, x.flags);
   __shared__ unsigned s_flags;
   if (threadIdx.x == 0) s_flags = 0u;
   __syncthreads();
+  if ((lane & 3) == 0) wred[wid * XA_WLIMBS + my_digit] = d1;
+  if (lane == 0 && flags) atomicOr(&s_flags, flags);
+  __syncthreads();
+  int did_atomic = 0;
+  if (wid == 0) did_atomic = xa_warp_flush(slot, k0, wred, nw);
+  if (any_slow) did_atomic |= xa_flush_slow(slot, sacc);
+  if (threadIdx.x == 0 && s_flags) {
+    atomicOr(&slot->flags, s_flags);
+    did_atomic = 1;
+  }
+  // make this thread's atomics visible before the CTA takes its ticket
+  if (did_atomic) __threadfence();
+}
+
+// Shared state of a two-slot commit; zero() runs before the CTA's first barrier
+// of the reduction.
+struct XCommit2 {
+  unsigned flags[2];
+  int slow;
+  __device__ __forceinline__ void zero() {
+    if (threadIdx.x == 0) {
+      flags[0] = flags[1] = 0u;
+      slow = 0;
+    }
+  }
+};
+
+// A warp's share of one window: the warp sum of digit `digit` (every fourth
+// lane), and the warp's flags and slow-path bit.
+struct XWarpPart {
+  long long sum;
+  int digit;
+  unsigned flags;
+  int slow;
+};
+
+__device__ __forceinline__ XWarpPart xa_warp_part(const XAcc& x) {
+  XWarpPart p;
+  p.sum = xa_warp_digits(x, &p.digit);
+  p.flags = __reduce_or_sync(0xffffffffu, x.flags);
+  p.slow = (int)__reduce_or_sync(0xffffffffu, (unsigned)x.slow);
+  return p;
+}
+
+// Two slots at once with one barrier: warp 0 flushes the first window, warp 1
+// the second.  `wred` holds 2 x XA_WLIMBS x (warps) long longs.  The CTA needs
+// at least two warps.
+__device__ __forceinline__ void xa_acc_commit2(XASlot* s0, const XWarpPart& p0, int k0, long long* sacc0, XASlot* s1,
+                                               const XWarpPart& p1, int k1, long long* sacc1, long long* wred,
+                                               XCommit2& cs) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  if ((lane & 3) == 0) {
+    wred[wid * XA_WLIMBS + p0.digit] = p0.sum;
+    wred[(nw + wid) * XA_WLIMBS + p1.digit] = p1.sum;
+  }
   if (lane == 0) {
-#pragma unroll
-    for (int j = 0; j < XA_WLIMBS; ++j) wred[wid * XA_WLIMBS + j] = d[j];
-    if (flags) atomicOr(&s_flags, flags);
+    if (p0.flags) atomicOr(&cs.flags[0], p0.flags);
+    if (p1.flags) atomicOr(&cs.flags[1], p1.flags);
+    const int slow = p0.slow | (p1.slow << 1);
+    if (slow) atomicOr(&cs.slow, slow);
   }
   __syncthreads();
   int did_atomic = 0;
-  if (threadIdx.x < XA_WLIMBS) {
-    long long s = 0;
-    for (int w = 0; w < nw; ++w) s += wred[w * XA_WLIMBS + threadIdx.x];
-    int dig = k0 + threadIdx.x;
-    if (s != 0) {
-      if (dig >= 0 && dig < XA_DIGITS) {
-        atomicAdd((unsigned long long*)&slot->digit[dig], (unsigned long long)s);
-        atomicMax(&slot->lo_inv, XA_DIGITS - dig);
-        atomicMax(&slot->hi_p1, dig + 1);
-      } else {
-        atomicOr(&slot->flags, XA_OVERFLOW);
-      }
-      did_atomic = 1;
-    }
+  if (wid == 0) did_atomic = xa_warp_flush(s0, k0, wred, nw);
+  else if (wid == 1) did_atomic = xa_warp_flush(s1, k1, wred + nw * XA_WLIMBS, nw);
+  const int any_slow = cs.slow;
+  if (any_slow & 1) did_atomic |= xa_flush_slow(s0, sacc0);
+  if (any_slow & 2) did_atomic |= xa_flush_slow(s1, sacc1);
+  if (threadIdx.x == 0 && cs.flags[0]) {
+    atomicOr(&s0->flags, cs.flags[0]);
+    did_atomic = 1;
   }
-  if (any_slow) {
-    for (int k = threadIdx.x; k < XA_DIGITS; k += blockDim.x) {
-      long long s = sacc[k];
-      if (s != 0) {
-        atomicAdd((unsigned long long*)&slot->digit[k], (unsigned long long)s);
-        atomicMax(&slot->lo_inv, XA_DIGITS - k);
-        atomicMax(&slot->hi_p1, k + 1);
-        did_atomic = 1;
-      }
-    }
-  }
-  if (threadIdx.x == 0 && s_flags) {
-    atomicOr(&slot->flags, s_flags);
+  if (threadIdx.x == 32 && cs.flags[1]) {
+    atomicOr(&s1->flags, cs.flags[1]);
     did_atomic = 1;
   }
   // make this thread's atomics visible before the CTA takes its ticket
@@ -413,7 +509,7 @@ static __device__ __noinline__ double xa_round(const long long* dg, int lo, int 
   return __longlong_as_double((long long)bits);
 }
 
-// Called by every CTA after its xa_cta_commit calls for `nslots` slots: the last
+// Called by every CTA after its xa_acc_commit calls for `nslots` slots: the last
 // CTA rounds and clears them.  Returns true in the (single) finalising CTA, with
 // results written into slot->result.  All threads of the CTA must call.
 __device__ __forceinline__ bool xa_finish(XASlot* const* slots, int nslots, unsigned nctas) {
@@ -446,15 +542,5 @@ __device__ __forceinline__ bool xa_finish(XASlot* const* slots, int nslots, unsi
   __threadfence();
   return true;
 }
-
-// Convenience: a per-thread accumulation context for one reduction.
-struct XCtx {
-  XWin pos, neg;
-  unsigned flags;
-  int slow;
-  int k0;
-  __device__ __forceinline__ void clear() { xwin_clear(pos); xwin_clear(neg); flags = 0u; slow = 0; k0 = 0; }
-  __device__ __forceinline__ void add(long long* sacc, const XTerm& t) { xa_add(pos, neg, sacc, k0, t, flags, slow); }
-};
 
 }  // namespace pfgb
