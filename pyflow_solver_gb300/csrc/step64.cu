@@ -343,7 +343,7 @@ __global__ void k_loop_guard(LoopCtl* lc, cudaGraphConditionalHandle cond, int u
 // ping-pong buffers: iteration k reads p[k & 1] and writes p[(k + 1) & 1].
 // R: rows per thread (the tile is 32 x 8R cells); the autotuner picks R per handle.
 template <int OP, int R = RPT>
-__global__ void __launch_bounds__(NT) k_cg_matvec(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
+__global__ void __launch_bounds__(NT, 5) k_cg_matvec(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
   pdl_enter();
   constexpr int TYv = R * PB_Y;
   TILE_PROLOGUE
