@@ -241,9 +241,9 @@ KERNEL_BYTES = {
     "k_prestep": 16,        # u, v
     "k_predict": 32,        # u, v -> u*, v*
     "k_rhs": 24,            # u*, v* -> b
-    "k_cg_init": 32,        # b -> b, r, x
-    "k_cg_matvec": 32,      # z (from r), p_old -> p, q
-    "k_cg_update": 48,      # x, p, r, q -> x, r
+    "k_cg_init": 40,        # b -> b, r, x, M r
+    "k_cg_matvec": 32,      # M r, p_old -> p, q
+    "k_cg_update": 56,      # x, p, r, q -> x, r, M r
     "k_post_resid": 16,     # b, x
     "k_pin_correct": 80,    # x, u*, v*, u, v -> u*, v*, u, v, p
     "k_post_diag": 48,      # u*, v*, p, b, u, v
@@ -326,7 +326,8 @@ TRAFFIC = {
     ("cavity512", "k_mx_matvec"): (1.60e6, "profiles/k_mx_matvec_2048.md (512^2 capture)"),
     ("cavity2048", "k_mx_matvec"): (34.11e6, "profiles/k_mx_matvec_2048.md"),
     ("cavity2048", "k_mx_matvec_tma"): (33.74e6, "profiles/k_mx_matvec_tma_2048.md"),
-    ("cavity2048", "k_cg_matvec"): (94.64e6, "profiles/cavity2048_fp64_launches.md"),
+    ("cavity2048", "k_cg_matvec"): (92.91e6, "profiles/k_cg_pair_fp64_2048.md"),
+    ("cavity2048", "k_cg_update"): (194.53e6, "profiles/k_cg_pair_fp64_2048.md"),
     ("cavity512", "k_cg_matvec"): (4.27e6, "profiles/k_cg_matvec_fp64_512.md"),
 }
 
