@@ -73,13 +73,29 @@ struct View2Cg {
   __device__ __forceinline__ T operator()(int j, int i) const { return __ldcg(p + (long)j * ld + i); }
 };
 
-// Programmatic dependent launch: let the graph's next kernel start launching
-// now, then wait until this kernel's predecessor has completed and its writes
-// are visible.  Every kernel of a step graph begins with it (a no-op for a
-// kernel that was not launched as a programmatic dependent).
+// Programmatic dependent launch, in two halves: pdl_launch lets the graph's
+// next kernel start launching; pdl_wait waits until this kernel's predecessor
+// has completed and its writes are visible.  Between the two a kernel reads only
+// what no kernel writes (tile tables and instance descriptors, which the host
+// writes before a launch), so those loads overlap the predecessor's tail.  Every
+// kernel of a step graph begins with them (no-ops for a kernel that was not
+// launched as a programmatic dependent).
+__device__ __forceinline__ void pdl_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_enter() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+  pdl_launch();
+  pdl_wait();
+}
+
+// A descriptor copied into shared memory by the CTA as 8-byte words (read-only
+// path): called between pdl_launch and pdl_wait, the caller synchronises the CTA
+// after pdl_wait.
+template <typename T>
+__device__ __forceinline__ void stage_desc(const T* src, T* dst) {
+  static_assert(sizeof(T) % 8 == 0 && alignof(T) >= 8, "descriptor copied as 8-byte words");
+  const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(dst);
+  for (int k = threadIdx.x; k < (int)(sizeof(T) / 8); k += blockDim.x) d[k] = __ldg(s + k);
 }
 
 // Ordered bit pattern of a non-negative double (NaN sorts above +inf), for

@@ -1324,15 +1324,21 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
 
 // ---- kernels: one tile per 256-thread CTA -----------------------------------
 
+// The CTA's tile; its instance's descriptor staged in shared memory before the
+// wait on the predecessor, and the liveness test after it.
 #define CTA_TILE(gate)                          \
+  pdl_launch();                                 \
+  __shared__ MixDesc smd_;                      \
   const MTile tl = TL[blockIdx.x];              \
-  const MixDesc& M = MD[tl.inst];               \
+  stage_desc(MD + tl.inst, &smd_);              \
+  pdl_wait();                                   \
+  __syncthreads();                              \
+  const MixDesc& M = smd_;                      \
   if (!mx_live(M, gate)) return;                \
   const CtaCtx x{};
 
 __global__ void __launch_bounds__(MT, 6) k_mg_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
                                                  int gate, Smooth sw) {
-  pdl_enter();
   CTA_TILE(gate)
   __shared__ DownSmem sm;
   ph_down(x, M, tl, l, sw, sm);
@@ -1340,7 +1346,6 @@ __global__ void __launch_bounds__(MT, 6) k_mg_down(const MixDesc* __restrict__ M
 
 __global__ void __launch_bounds__(MT, 5) k_mg_post(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL, int l,
                                                  int gate, Smooth sw) {
-  pdl_enter();
   CTA_TILE(gate)
   __shared__ PostSmem sm;
   ph_post(x, M, tl, l, sw, sm);
@@ -1350,8 +1355,12 @@ __global__ void __launch_bounds__(MT, 5) k_mg_post(const MixDesc* __restrict__ M
 template <int NT>
 __global__ void __launch_bounds__(NT, CT / NT) k_mg_coarse(const MixDesc* __restrict__ MD, const int* __restrict__ order,
                                                             int gate, int bottom_sweeps, Smooth sw) {
-  pdl_enter();
-  const MixDesc& M = MD[order[blockIdx.x]];
+  pdl_launch();
+  __shared__ MixDesc smd;
+  stage_desc(MD + order[blockIdx.x], &smd);
+  pdl_wait();
+  __syncthreads();
+  const MixDesc& M = smd;
   if (!mx_live(M, gate)) return;
   extern __shared__ float csm[];
   coarse_cycle<NT>(M, bottom_sweeps, sw, csm);
@@ -1359,9 +1368,13 @@ __global__ void __launch_bounds__(NT, CT / NT) k_mg_coarse(const MixDesc* __rest
 
 __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                  MixLoop* ml) {
-  pdl_enter();
+  pdl_launch();
+  __shared__ MixDesc smd;
   const MTile tl = TL[blockIdx.x];
-  const MixDesc& M = MD[tl.inst];
+  stage_desc(MD + tl.inst, &smd);
+  pdl_wait();
+  __syncthreads();
+  const MixDesc& M = smd;
   if (!*M.active) return;
   __shared__ RedSmem rsm;
   ph_init(CtaCtx{}, M, tl, ml, rsm);
@@ -1393,14 +1406,12 @@ __global__ void k_ml_arm(MixLoop* ml, int which, cudaGraphConditionalHandle cond
 
 __global__ void __launch_bounds__(MT) k_mx_prep(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                  MixLoop* ml) {
-  pdl_enter();
   CTA_TILE(0)
   __shared__ RedSmem rsm;
   ph_prep(x, M, tl, ml, rsm);
 }
 
 __global__ void __launch_bounds__(MT, 6) k_mx_matvec(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
-  pdl_enter();
   CTA_TILE(1)
   __shared__ MatvecSmem sm;
   ph_matvec(x, M, tl, sm);
@@ -1412,7 +1423,7 @@ __global__ void __launch_bounds__(MT, 6) k_mx_matvec(const MixDesc* __restrict__
 // for the copy it has in flight into the other stage, and returns.
 __global__ void __launch_bounds__(MT, 4) k_mx_matvec_tma(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                           int ntiles, MixLoop* ml) {
-  pdl_enter();
+  pdl_launch();
   __shared__ MvSmem sm;
   const CtaCtx x{};
   if (x.tid() == 0) {
@@ -1428,6 +1439,7 @@ __global__ void __launch_bounds__(MT, 4) k_mx_matvec_tma(const MixDesc* __restri
   // changes during the launch, so the chain of dependent loads is paid per instance
   MTile tl = t < ntiles ? TL[t] : MTile{0, 0, 0, 0};
   MTile tln = t + g < ntiles ? TL[t + g] : MTile{0, 0, 0, 0};
+  pdl_wait();                       // the barriers and the tile table need no predecessor
   __syncthreads();
   int ii = -1, ilive = 0, ik = 0;   // thread 0's instance of the copies
   auto issue = [&](const MTile& u, int stage) -> bool {
@@ -1522,25 +1534,32 @@ __device__ __forceinline__ void loop_guard(MixLoop* ml, int which, cudaGraphCond
 __global__ void __launch_bounds__(MT, 5) k_mx_update_down(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                         MixLoop* ml, cudaGraphConditionalHandle cond_inner, int use_cond,
                                                         Smooth sw) {
-  pdl_enter();
+  pdl_launch();
+  __shared__ MixDesc smd;
   const MTile tl = TL[blockIdx.x];
-  const MixDesc& M = MD[tl.inst];
+  stage_desc(MD + tl.inst, &smd);
+  pdl_wait();
+  __syncthreads();
+  const MixDesc& M = smd;
   __shared__ UpdDownSmem sm;
   if (mx_live(M, 1)) ph_update_down(CtaCtx{}, M, tl, ml, cond_inner, use_cond, sw, sm);
   if (use_cond) loop_guard(ml, 1, cond_inner);
 }
 
 __global__ void __launch_bounds__(MT) k_mx_correct(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL) {
-  pdl_enter();
   CTA_TILE(0)
   ph_correct(x, M, tl);
 }
 
 __global__ void __launch_bounds__(MT) k_mx_resid(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
                                                   MixLoop* ml, cudaGraphConditionalHandle cond_outer, int use_cond) {
-  pdl_enter();
+  pdl_launch();
+  __shared__ MixDesc smd;
   const MTile tl = TL[blockIdx.x];
-  const MixDesc& M = MD[tl.inst];
+  stage_desc(MD + tl.inst, &smd);
+  pdl_wait();
+  __syncthreads();
+  const MixDesc& M = smd;
   __shared__ RedSmem rsm;
   if (mx_live(M, 0)) ph_resid(CtaCtx{}, M, tl, ml, cond_outer, use_cond, rsm);
   if (use_cond) loop_guard(ml, 0, cond_outer);

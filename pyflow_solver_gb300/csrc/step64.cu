@@ -105,16 +105,22 @@ __device__ __forceinline__ void zero_sacc(long long* sacc) {
   for (int k = threadIdx.x; k < XA_DIGITS; k += blockDim.x) sacc[k] = 0;
 }
 
-// The CTA's tile and instance.  Every CTA of an inactive instance returns.
+// The CTA's tile and instance: the instance's descriptor is staged in shared
+// memory before the wait on the predecessor.  Every CTA of an inactive instance
+// returns.
 #define TILE_PROLOGUE                                             \
+  pdl_launch();                                                   \
+  __shared__ InstDesc sdesc_;                                     \
   const Tile tl = TL[blockIdx.x];                                 \
-  const InstDesc& D = ID[tl.inst];                                \
+  stage_desc(ID + tl.inst, &sdesc_);                              \
+  pdl_wait();                                                     \
+  __syncthreads();                                                \
+  const InstDesc& D = sdesc_;                                     \
   if (!D.active) return;                                          \
   const Geo64 G = D.G;
 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NT) k_prestep(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc[XA_DIGITS];
   __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
@@ -207,7 +213,6 @@ __global__ void k_set_dt(const InstDesc* __restrict__ ID, double dt) {
 
 // predictor: u* = u - dt*conv_u(u,v), v* likewise (solver.py:73-95)
 __global__ void __launch_bounds__(NT) k_predict(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   const int i = tl.i0 + (threadIdx.x & 31);
   const int j = tl.j0 + (threadIdx.x >> 5);
@@ -230,7 +235,6 @@ __global__ void __launch_bounds__(NT) k_predict(const InstDesc* __restrict__ ID,
 
 // RHS: b = -div_c(u*,v*)/max(dt,1e-14); sum(b); ||div_c(u*,v*)||^2
 __global__ void __launch_bounds__(NT) k_rhs(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
@@ -258,7 +262,6 @@ __global__ void __launch_bounds__(NT) k_rhs(const InstDesc* __restrict__ ID, con
 // Instances that start iterating are counted in the loop control.
 __global__ void __launch_bounds__(NT) k_cg_init(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
                                                  LoopCtl* lc) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
@@ -344,7 +347,6 @@ __global__ void k_loop_guard(LoopCtl* lc, cudaGraphConditionalHandle cond, int u
 // R: rows per thread (the tile is 32 x 8R cells); the autotuner picks R per handle.
 template <int OP, int R = RPT>
 __global__ void __launch_bounds__(NT, 5) k_cg_matvec(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   constexpr int TYv = R * PB_Y;
   TILE_PROLOGUE
   Ctrl64* ctrl = D.ctrl;
@@ -430,7 +432,6 @@ __global__ void __launch_bounds__(NT, 5) k_cg_matvec(const InstDesc* __restrict_
 template <int R = RPT>
 __global__ void __launch_bounds__(NT, R == 1 ? 6 : 5) k_cg_update(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
                                                    LoopCtl* lc, cudaGraphConditionalHandle cond, int use_cond) {
-  pdl_enter();
   TILE_PROLOGUE
   Ctrl64* ctrl = D.ctrl;
   if (*(volatile int*)&ctrl->done) return;
@@ -500,7 +501,6 @@ __device__ __forceinline__ double apply_A(View2<const double> X, int j, int i, c
 // ||b - A x||^2 (the true residual of interface.solve)
 template <int OP>
 __global__ void __launch_bounds__(NT) k_post_resid(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc[XA_DIGITS];
   __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
@@ -525,7 +525,6 @@ __global__ void __launch_bounds__(NT) k_post_resid(const InstDesc* __restrict__ 
 //   interior row and the sums of (u-u_old)^2 are formed.
 // mode 1 (projection only): us/vs are the state's own u/v, corrected in place.
 __global__ void __launch_bounds__(NT) k_pin_correct(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS];
   __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
@@ -576,7 +575,6 @@ __global__ void __launch_bounds__(NT) k_pin_correct(const InstDesc* __restrict__
 
 // ||div_c(u_corr)||^2, ||A p - b||^2, ||div_central(u,v;1,1)||^2
 __global__ void __launch_bounds__(NT) k_post_diag(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ long long sacc0[XA_DIGITS], sacc1[XA_DIGITS], sacc2[XA_DIGITS];
   __shared__ long long wred[2 * (NT / 32) * XA_WLIMBS];
@@ -646,7 +644,6 @@ __device__ __forceinline__ double neg_lap_pinned_r(View2<const double> p, int j,
 
 // max|u|, max|v| and ||div_central(u, v; 1, 1)||^2 (the safeguard's baseline)
 __global__ void __launch_bounds__(NT) k_prestep_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ StepRed rsm;
   Ctrl64* ctrl = D.ctrl;
@@ -694,7 +691,6 @@ __device__ __forceinline__ float q_comb(float dp, float d0, float dm, bool pos) 
 }
 
 __global__ void __launch_bounds__(NT) k_predict_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ float su[TY_M + 4][TX + 4], sv[TY_M + 4][TX + 4];
   const int i0 = tl.i0, j0 = tl.j0;
@@ -764,7 +760,6 @@ __global__ void __launch_bounds__(NT) k_predict_m(const InstDesc* __restrict__ I
 
 // b = -div_c(u*, v*) / max(dt, 1e-14); sum(b) (for the mean) and ||div_c||^2
 __global__ void __launch_bounds__(NT) k_rhs_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ StepRed rsm;
   const int i = tl.i0 + (threadIdx.x & 31);
@@ -802,7 +797,6 @@ __global__ void __launch_bounds__(NT) k_rhs_m(const InstDesc* __restrict__ ID, c
 // The sums take the rows in the same order either way.
 constexpr int PC_H = 2;                       // rows per half
 __global__ void __launch_bounds__(NT, 3) k_pin_correct_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ StepRed rsm;
   Ctrl64* ctrl = D.ctrl;
@@ -935,7 +929,6 @@ __device__ __forceinline__ void gather_one(const InstDesc& Dd, const int* trip, 
 __global__ void __launch_bounds__(NT) k_post_diag_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
                                                      const mixed::MixDesc* __restrict__ MD, const int* trip,
                                                      const int* gb_err) {
-  pdl_enter();
   TILE_PROLOGUE
   __shared__ StepRed rsm;
   const RecipGrid rg = recips(G);
