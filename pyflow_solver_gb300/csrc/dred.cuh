@@ -67,32 +67,64 @@ __device__ __forceinline__ FF ff_warp_sum(FF x) {
 }
 
 // Sum over the tile of per-warp binary64 values already in sm.w[r][warp];
-// valid in tid 0.
+// valid in tid 0.  The NT/32 values of each r are added by a fixed tree over
+// the lanes of warp 0 (lane r * NT/32 + warp), so the R sums take log2(NT/32)
+// dependent additions instead of a serial chain.
 template <int R, int NT, class X>
 __device__ __forceinline__ void dred_warps(const X& x, double (&v)[R], DRedSmem<NT>& sm) {
+  constexpr int NW = NT / 32;
+  static_assert(R * NW <= 32 && (NW & (NW - 1)) == 0, "one lane of warp 0 per value and warp");
   x.sync();
-  if (x.tid() == 0) {
+  if (x.tid() < 32) {
+    const int lane = x.tid(), r = lane / NW, w = lane % NW;
+    double a = (r < R) ? sm.w[r][w] : 0.0;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      double s = sm.w[r][0];
-      for (int k = 1; k < NT / 32; ++k) s += sm.w[r][k];
-      v[r] = s;
-    }
+    for (int o = NW / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = __shfl_sync(0xffffffffu, a, q * NW);
   }
   x.sync();
+}
+
+// Warp sums of R values per lane: a reduce-scatter for R = 2 and 4 (each of the
+// first shuffle levels halves the values a lane carries), a plain tree otherwise.
+// Returns the lane's sum and sets *r to the value it belongs to; the lanes with
+// (lane % (32 / R)) == 0 hold the warp's total of value lane / (32 / R).
+template <int R>
+__device__ __forceinline__ double dred_warp_scatter(const double (&v)[R], int lane, int* r) {
+  if constexpr (R == 2) {
+    const bool up = (lane & 16) != 0;
+    double a = (up ? v[1] : v[0]) + __shfl_xor_sync(0xffffffffu, up ? v[0] : v[1], 16);
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    *r = up ? 1 : 0;
+    return a;
+  } else if constexpr (R == 4) {
+    const bool u16 = (lane & 16) != 0, u8 = (lane & 8) != 0;
+    const double a0 = (u16 ? v[2] : v[0]) + __shfl_xor_sync(0xffffffffu, u16 ? v[0] : v[2], 16);
+    const double a1 = (u16 ? v[3] : v[1]) + __shfl_xor_sync(0xffffffffu, u16 ? v[1] : v[3], 16);
+    double a = (u8 ? a1 : a0) + __shfl_xor_sync(0xffffffffu, u8 ? a0 : a1, 8);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    *r = (u16 ? 2 : 0) + (u8 ? 1 : 0);
+    return a;
+  } else {
+    static_assert(R == 1, "warp sums of 1, 2 or 4 values");
+    double a = v[0];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    *r = 0;
+    return a;
+  }
 }
 
 // Sum of v over the tile (fixed order); valid in tid 0.
 template <int R, int NT, class X>
 __device__ __forceinline__ void dred_block(const X& x, double (&v)[R], DRedSmem<NT>& sm) {
   const int lane = x.tid() & 31, warp = x.tid() >> 5;
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    double a = v[r];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if (lane == 0) sm.w[r][warp] = a;
-  }
+  int r;
+  const double a = dred_warp_scatter<R>(v, lane, &r);
+  if ((lane & (32 / R - 1)) == 0) sm.w[r][warp] = a;
   dred_warps<R, NT>(x, v, sm);
 }
 

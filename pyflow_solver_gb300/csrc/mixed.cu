@@ -549,7 +549,11 @@ template <class X>
 __device__ __forceinline__ void ph_init(const X& x, const MixDesc& M, const MTile& tl, MixLoop* ml, RedSmem& rsm) {
   const Geo G = M.G;
   MixCtrl* ctrl = M.ctrl;
-  const double mean = __ddiv_rn(cget(M.bsum), M.n_cells);
+  // the mean, divided once for the tile (the reduction's scratch carries it)
+  if (x.tid() == 0) rsm.w[0][0] = __ddiv_rn(cget(M.bsum), M.n_cells);
+  x.sync();
+  const double mean = rsm.w[0][0];
+  x.sync();
   const bool warm = cget(&ctrl->warm) != 0;
   const double* P = warm ? *M.pprev : nullptr;
   const PrevView Pv{P, M.ldp};
