@@ -239,10 +239,12 @@ __device__ __forceinline__ float restrict_lv(const float* w, long ld, int j0, in
 // the loop the phase belongs to (gate 0: the refinement loop, 1: the inner PCG).
 
 __device__ __forceinline__ bool mx_live(const MixDesc& M, int gate) {
-  if (!*M.active) return false;
+  // the three flags are loaded together (one round trip, not a chain of three)
   const MixCtrl* c = M.ctrl;
-  if (*(volatile const int*)&c->outer_done) return false;
-  return gate == 0 || !*(volatile const int*)&c->inner_done;
+  const int act = *M.active;
+  const int od = *(volatile const int*)&c->outer_done;
+  const int id = gate ? *(volatile const int*)&c->inner_done : 0;
+  return act && !od && !id;
 }
 
 using RedSmem = DRedSmem<MT>;
