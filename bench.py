@@ -255,8 +255,7 @@ KERNEL_BYTES = {
     "k_mx_prep": 16,        # r64 -> f0 (binary32), e
     "k_mx_correct": 20,     # x, e -> x
     "k_mx_resid": 24,       # x, b -> r64
-    "k_pin_correct_m": 80,
-    "k_post_diag_m": 32,    # u*, v*, u, v
+    "k_correct_diag_m": 64,  # x, u*, v*, u, v -> u, v, p (the divergences from the same pass)
     # mixed form: binary32 PCG and V-cycle (per cell of the kernel's level)
     "k_mx_matvec": 16,      # z, p_old -> p, q
     "k_mx_matvec_tma": 16,

@@ -73,8 +73,8 @@ __device__ __forceinline__ double div_central_at(View2<const double> u, View2<co
 // 0.5 (both exact, or rounded alike when subnormal), so no division is issued;
 // the product is an exponent decrement on the integer pipe wherever the result
 // stays normal (half_exact).
-__device__ __forceinline__ double div_central_unit(View2<const double> u, View2<const double> v, int j, int i, int nx,
-                                                   int ny) {
+template <class UV, class VV>
+__device__ __forceinline__ double div_central_unit(UV u, VV v, int j, int i, int nx, int ny) {
   const int L = nx - 1, T = ny - 1;
   if (j == 0 && i == 0) return ADD(SUB(u(0, 1), u(0, 0)), SUB(v(1, 0), v(0, 0)));
   if (j == 0 && i == L) return ADD(SUB(u(0, L), u(0, L - 1)), SUB(v(1, L), v(0, L)));

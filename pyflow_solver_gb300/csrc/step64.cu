@@ -790,80 +790,6 @@ __global__ void __launch_bounds__(NT) k_rhs_m(const InstDesc* __restrict__ ID, c
   }
 }
 
-// p = x - x[0]; u = u* - dt gx(p), v likewise; lid; sums of (u - u_old)^2, (v - v_old)^2.
-// The thread's four rows go in two halves of two rows: all loads of a half are issued
-// before its stores (the arrays are distinct, so the stores cannot feed the loads), and
-// holding two rows' operands instead of four keeps the kernel at three CTAs to an SM (two before).
-// The sums take the rows in the same order either way.
-constexpr int PC_H = 2;                       // rows per half
-__global__ void __launch_bounds__(NT, 3) k_pin_correct_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL) {
-  TILE_PROLOGUE
-  __shared__ StepRed rsm;
-  Ctrl64* ctrl = D.ctrl;
-  const LidArgs L = D.L;
-  const RecipGrid rg = recips(G);
-  const int i = tl.i0 + (threadIdx.x & 31);
-  const double dt = ctrl->dt;
-  const double* __restrict__ xs = D.x;
-  double* __restrict__ us = D.us;
-  double* __restrict__ vs = D.vs;
-  double* __restrict__ ui = D.ui;
-  double* __restrict__ vi = D.vi;
-  double* __restrict__ pi = D.pi;
-  const double x0 = xs[0];
-  double v[2] = {0.0, 0.0}, out[2];
-  int bad = 0;
-#pragma unroll 1
-  for (int h = 0; h < PB_R; h += PC_H) {
-    double xc[PC_H], xe[PC_H], xn[PC_H], u1[PC_H], v1[PC_H], u0[PC_H], v0[PC_H];
-    bool in[PC_H];
-#pragma unroll
-    for (int r = 0; r < PC_H; ++r) {
-      const int j = tl.j0 + (threadIdx.x >> 5) + (h + r) * PB_Y;
-      in[r] = i < G.nx && j < G.ny;
-      if (in[r]) {
-        const long ox = (long)j * G.ld + i, o = (long)j * D.usld + i, os = (long)j * G.lds + i;
-        xc[r] = xs[ox];
-        xe[r] = (i < G.nx - 1) ? xs[ox + 1] : 0.0;
-        xn[r] = (j < G.ny - 1) ? xs[ox + G.ld] : 0.0;
-        u1[r] = us[o];
-        v1[r] = vs[o];
-        u0[r] = ui[os];
-        v0[r] = vi[os];
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < PC_H; ++r) {
-      const int j = tl.j0 + (threadIdx.x >> 5) + (h + r) * PB_Y;
-      if (in[r]) {
-        const double pv = SUB(xc[r], x0);
-        const double gx = (i < G.nx - 1) ? MUL(SUB(SUB(xe[r], x0), pv), rg.rx) : 0.0;
-        const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(xn[r], x0), pv), rg.ry) : 0.0;
-        const long o = (long)j * D.usld + i;
-        const long os = (long)j * G.lds + i;
-        const double uc = SUB(u1[r], MUL(dt, gx));
-        const double vc = SUB(v1[r], MUL(dt, gy));
-        us[o] = uc;
-        vs[o] = vc;
-        pi[os] = pv;
-        const double uf = (L.has_lid && j == G.ny - 1) ? L.lid : uc;
-        const double du = SUB(uf, u0[r]);
-        const double dv = SUB(vc, v0[r]);
-        ui[os] = uf;
-        vi[os] = vc;
-        v[0] += du * du;
-        v[1] += dv * dv;
-        bad |= !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
-      }
-    }
-  }
-  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->nan_flag, 1u);
-  if (STEP_RED(2, v, out) && threadIdx.x == 0) {
-    D.slots[S_RU].result = out[0];
-    D.slots[S_RV].result = out[1];
-  }
-}
-
 // Append this step's Ru (sqrt(sum (u - u_old)^2) / max(1, N), as the host forms it) to
 // the instance's series and run the steady-state test on the last `window` entries.
 __device__ __noinline__ void steady_update(const InstDesc& Dd, double ru2, StepOut64* out) {
@@ -925,33 +851,173 @@ __device__ __forceinline__ void gather_one(const InstDesc& Dd, const int* trip, 
   steady_update(Dd, out->ru2, out);
 }
 
-// ||div_c(u*, v*)||^2 after the correction, ||A p - b||^2, ||div_central(u, v; 1, 1)||^2
-__global__ void __launch_bounds__(NT) k_post_diag_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
-                                                     const mixed::MixDesc* __restrict__ MD, const int* trip,
-                                                     const int* gb_err) {
+// The correction and the step's closing diagnostics of the mixed form, in one pass:
+// p = x - x[0]; u* = u* - dt gx(p), v* likewise (the products with the reciprocal
+// spacings); the lid; the state u, v, p; the sums of (u - u_old)^2 and (v - v_old)^2;
+// then ||div_c(u*, v*)||^2 of the corrected u* and ||div_central(u, v; 1, 1)||^2 of the
+// new state, the solve's summary and the step record.  The divergences read the
+// corrected fields on the tile's one-cell ring too: those are formed here again from x
+// and the predictor's u*, v* with the operations of their own tile, so no second pass
+// is needed, and the corrected u* is not written back (nothing reads it after the
+// diagnostics).  Every sum is accumulated and reduced as the two passes did.
+constexpr int CD_W = TX + 3;                  // x on columns i0-1 .. i0+33
+__global__ void __launch_bounds__(NT, 3) k_correct_diag_m(const InstDesc* __restrict__ ID, const Tile* __restrict__ TL,
+                                                          const mixed::MixDesc* __restrict__ MD, const int* trip,
+                                                          const int* gb_err) {
   TILE_PROLOGUE
+  __shared__ double sx[TY_M + 3][CD_W];       // x at rows j0-1 .. j0+33, columns i0-1 .. i0+33
+  __shared__ double su[TY_M][TX + 2];         // corrected u*, rows j0 .. j0+31, columns i0-1 .. i0+32
+  __shared__ double sv[TY_M + 2][TX];         // corrected v*, rows j0-1 .. j0+32, columns i0 .. i0+31
   __shared__ StepRed rsm;
+  Ctrl64* ctrl = D.ctrl;
+  const LidArgs L = D.L;
   const RecipGrid rg = recips(G);
-  const int i = tl.i0 + (threadIdx.x & 31);
-  View2<const double> US{D.us, D.usld}, VS{D.vs, D.usld};
-  View2<const double> U{D.ui, G.lds}, V{D.vi, G.lds};
-  double v[2] = {0.0, 0.0}, out[2];
+  const int i0 = tl.i0, j0 = tl.j0;
+  const int tx = threadIdx.x & 31, i = i0 + tx;
+  const double dt = ctrl->dt;
+  const double* __restrict__ xs = D.x;
+  const double* __restrict__ us = D.us;
+  const double* __restrict__ vs = D.vs;
+  double* __restrict__ ui = D.ui;
+  double* __restrict__ vi = D.vi;
+  double* __restrict__ pi = D.pi;
+  const double x0 = xs[0];
+  for (int idx = threadIdx.x; idx < (TY_M + 3) * CD_W; idx += NT) {
+    const int jj = idx / CD_W - 1, ii = idx % CD_W - 1;
+    const int gj = j0 + jj, gi = i0 + ii;
+    sx[jj + 1][ii + 1] = (gj >= 0 && gj < G.ny && gi >= 0 && gi < G.nx) ? xs[(long)gj * G.ld + gi] : 0.0;
+  }
+  __syncthreads();
+  // the correction at (j, c) of a cell whose x is at sx[j - j0 + 1][c - i0 + 1]
+  auto ucorr = [&](int j, int c, double u1) {
+    const double pv = SUB(sx[j - j0 + 1][c - i0 + 1], x0);
+    const double gx = (c < G.nx - 1) ? MUL(SUB(SUB(sx[j - j0 + 1][c - i0 + 2], x0), pv), rg.rx) : 0.0;
+    return SUB(u1, MUL(dt, gx));
+  };
+  auto vcorr = [&](int j, int c, double v1) {
+    const double pv = SUB(sx[j - j0 + 1][c - i0 + 1], x0);
+    const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(sx[j - j0 + 2][c - i0 + 1], x0), pv), rg.ry) : 0.0;
+    return SUB(v1, MUL(dt, gy));
+  };
+  double v[2] = {0.0, 0.0};
+  int bad = 0;
+#pragma unroll 1
+  for (int h = 0; h < PB_R; h += 2) {
+    double u1[2], v1[2], u0[2], v0[2];
+    bool in[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int j = j0 + (threadIdx.x >> 5) + (h + r) * PB_Y;
+      in[r] = i < G.nx && j < G.ny;
+      if (in[r]) {
+        const long o = (long)j * D.usld + i, os = (long)j * G.lds + i;
+        u1[r] = us[o];
+        v1[r] = vs[o];
+        u0[r] = ui[os];
+        v0[r] = vi[os];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int j = j0 + (threadIdx.x >> 5) + (h + r) * PB_Y;
+      if (in[r]) {
+        const double pv = SUB(sx[j - j0 + 1][tx + 1], x0);
+        const double uc = ucorr(j, i, u1[r]);
+        const double vc = vcorr(j, i, v1[r]);
+        su[j - j0][tx + 1] = uc;
+        sv[j - j0 + 1][tx] = vc;
+        const long os = (long)j * G.lds + i;
+        pi[os] = pv;
+        const double uf = (L.has_lid && j == G.ny - 1) ? L.lid : uc;
+        const double du = SUB(uf, u0[r]);
+        const double dv = SUB(vc, v0[r]);
+        ui[os] = uf;
+        vi[os] = vc;
+        v[0] += du * du;
+        v[1] += dv * dv;
+        bad |= !(isfinite_d(uf) && isfinite_d(vc) && isfinite_d(pv));
+      }
+    }
+  }
+  // the ring: u* of columns i0-1 and i0+32, v* of rows j0-1 and j0+32 (threads 0..127)
+  if (threadIdx.x < 4 * 32) {
+    const int side = threadIdx.x >> 5, k = threadIdx.x & 31;
+    if (side < 2) {
+      const int c = side == 0 ? i0 - 1 : i0 + TX, j = j0 + k;
+      if (c >= 0 && c < G.nx && j < G.ny) su[k][side == 0 ? 0 : TX + 1] = ucorr(j, c, us[(long)j * D.usld + c]);
+    } else {
+      const int j = side == 2 ? j0 - 1 : j0 + TY_M, c = i0 + k;
+      if (j >= 0 && j < G.ny && c < G.nx) sv[side == 2 ? 0 : TY_M + 1][k] = vcorr(j, c, vs[(long)j * D.usld + c]);
+    }
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctrl->nan_flag, 1u);
+  // the divergences of the corrected fields (u* before the lid, the state after it)
+  struct SU {
+    const double (*a)[TX + 2];
+    int j0, i0;
+    __device__ double operator()(int j, int c) const { return a[j - j0][c - i0 + 1]; }
+  };
+  struct SV {
+    const double (*a)[TX];
+    int j0, i0;
+    __device__ double operator()(int j, int c) const { return a[j - j0 + 1][c - i0]; }
+  };
+  struct SUL {
+    SU s;
+    int top, lid_on;
+    double lid;
+    __device__ double operator()(int j, int c) const { return (lid_on && j == top) ? lid : s(j, c); }
+  };
+  const SU US{su, j0, i0};
+  const SV VS{sv, j0, i0};
+  const SUL U{US, G.ny - 1, L.has_lid, L.lid};
+  double w[2] = {0.0, 0.0};
   M_ROWS({
     if (i < G.nx && j < G.ny) {
-      const double d = div_c_r(US, VS, j, i, rg);
-      const double c = div_central_unit(U, V, j, i, G.nx, G.ny);
-      v[0] += d * d;
-      v[1] += c * c;
+      const double xp = (i >= 1) ? MUL(SUB(US(j, i), US(j, i - 1)), rg.rx) : MUL(US(j, 0), rg.rx);
+      const double yp = (j >= 1) ? MUL(SUB(VS(j, i), VS(j - 1, i)), rg.ry) : MUL(VS(0, i), rg.ry);
+      const double d = ADD(xp, yp);
+      const double c = div_central_unit(U, VS, j, i, G.nx, G.ny);
+      w[0] += d * d;
+      w[1] += c * c;
     }
   })
-  if (STEP_RED(2, v, out) && threadIdx.x == 0) {
-    // the instance's last tile: the solve's summary, these norms, then its step record
+  // the two pairs of sums, each formed as a two-value reduction, with one arrival
+  dred_block<2, NT>(mixed::CtaCtx{}, v, rsm);
+  dred_block<2, NT>(mixed::CtaCtx{}, w, rsm);
+  double* part = D.part;
+  const int nt = D.nt_m;
+  if (threadIdx.x == 0) {
+    part[tl.loc] = v[0];
+    part[nt + tl.loc] = v[1];
+    part[2 * nt + tl.loc] = w[0];
+    part[3 * nt + tl.loc] = w[1];
+    __threadfence();
+    rsm.last = (atomicAdd(D.ticket, 1u) == (unsigned)(nt - 1)) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!rsm.last) return;
+  __threadfence();
+  double s1[2] = {0.0, 0.0}, s2[2] = {0.0, 0.0};
+  for (int k = threadIdx.x; k < nt; k += NT) {
+    s1[0] += __ldcg(&part[k]);
+    s1[1] += __ldcg(&part[nt + k]);
+    s2[0] += __ldcg(&part[2 * nt + k]);
+    s2[1] += __ldcg(&part[3 * nt + k]);
+  }
+  dred_block<2, NT>(mixed::CtaCtx{}, s1, rsm);
+  dred_block<2, NT>(mixed::CtaCtx{}, s2, rsm);
+  if (threadIdx.x == 0) {
+    atomicExch(D.ticket, 0u);
+    // the instance's last tile: the solve's summary, the norms, then its step record
+    D.slots[S_RU].result = s1[0];
+    D.slots[S_RV].result = s1[1];
     mixed::mx_finish_one(MD[tl.inst]);
-    D.slots[S_DIVAFTER].result = out[0];
+    D.slots[S_DIVAFTER].result = s2[0];
     // ||A p - b||^2: p is the refinement's x exactly (x[0] stays 0), so this is the
     // refinement's final binary64 residual, which the solve has already formed
     D.slots[S_LINRES].result = D.slots[S_RES].result;
-    D.slots[S_CONT].result = out[1];
+    D.slots[S_CONT].result = s2[1];
     __threadfence();
     gather_one(D, trip, gb_err);
   }
@@ -983,6 +1049,12 @@ static void add_tiles(std::vector<Tile>& v, int k, int nx, int ny, int th) {
 }
 
 static int count_tiles(int nx, int ny, int th) { return ((nx + TX - 1) / TX) * ((ny + th - 1) / th); }
+
+// Per-tile partial sums of an instance: three rows over its 32 x 8 tiles (the binary64
+// stages), four rows over its 32 x 32 tiles (the mixed form's correction and diagnostics).
+static size_t part_doubles(int nx, int ny) {
+  return std::max(3 * (size_t)count_tiles(nx, ny, PB_Y), 4 * (size_t)count_tiles(nx, ny, TY_M));
+}
 
 constexpr int NVAR = 3;                          // CG tile variants: rows per thread 1, 2, 4
 constexpr int VAR_R[NVAR] = {1, 2, 4};
@@ -1074,7 +1146,7 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     const long ld = round_up(prms[k].nx, 32);
     vec[k] = up((size_t)ld * prms[k].ny * sizeof(double));
     bytes += 9 * vec[k] + up(S_COUNT * sizeof(XASlot)) + up(sizeof(Ctrl64)) + up(sizeof(SteadyRing)) +
-             up(3 * (size_t)count_tiles(prms[k].nx, prms[k].ny, PB_Y) * sizeof(double)) + up(sizeof(unsigned));
+             up(part_doubles(prms[k].nx, prms[k].ny) * sizeof(double)) + up(sizeof(unsigned));
     add_tiles(tpc, k, prms[k].nx, prms[k].ny, PB_Y);
     add_tiles(tpcm, k, prms[k].nx, prms[k].ny, TY_M);
     for (int v = 0; v < NVAR; ++v) {
@@ -1138,7 +1210,7 @@ int instance64_create_batch(const pfgb_params* prms, int n, Instance64** out) {
     D.nt_pc = count_tiles(prm.nx, prm.ny, PB_Y);
     D.nt_m = count_tiles(prm.nx, prm.ny, TY_M);
     D.nt_cg = I->ntcg_inst[I->cg_var][k];
-    D.part = (double*)take(3 * (size_t)D.nt_pc * sizeof(double));
+    D.part = (double*)take(part_doubles(prm.nx, prm.ny) * sizeof(double));
     D.ticket = (unsigned*)take(sizeof(unsigned));
     D.steady = (SteadyRing*)take(sizeof(SteadyRing));   // zeroed: the test is off
   }
@@ -1351,9 +1423,8 @@ static int build_graph(Instance64* I, int mode) {
   }
   if (!I->mix) c.kernel(k_post_resid<0>, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
   if (I->mix) {
-    c.kernel(k_pin_correct_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm);
-    c.kernel(k_post_diag_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm, (const mixed::MixDesc*)I->mix->dd,
-             loop_trip(I), loop_gb_err(I));
+    c.kernel(k_correct_diag_m, gm, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpcm,
+             (const mixed::MixDesc*)I->mix->dd, loop_trip(I), loop_gb_err(I));
   } else {
     c.kernel(k_pin_correct, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
     c.kernel(k_post_diag, gp, dim3(NT), (const InstDesc*)I->dd, (const Tile*)I->tpc);
@@ -1466,9 +1537,8 @@ static int run(Instance64* I, int mode, cudaStream_t s, pfgb_step_out* out) {
   if (I->mix) {
     PFGB_TIMED(kp, "k_rhs_m", -1, s, k_rhs_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm));
     if (int rc = mixed::run_direct(I->mix, s)) return rc;
-    PFGB_TIMED(kp, "k_pin_correct_m", -1, s, k_pin_correct_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm));
-    PFGB_TIMED(kp, "k_post_diag_m", -1, s,
-               k_post_diag_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm, I->mix->dd, loop_trip(I), loop_gb_err(I)));
+    PFGB_TIMED(kp, "k_correct_diag_m", -1, s,
+               k_correct_diag_m<<<I->ntpcm, NT, 0, s>>>(I->dd, I->tpcm, I->mix->dd, loop_trip(I), loop_gb_err(I)));
   } else {
     enqueue_projection(I, s);
   }

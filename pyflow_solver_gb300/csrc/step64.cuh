@@ -130,7 +130,7 @@ struct InstDesc {
   StepOut64* out;
   int nt_pc, nt_cg;            // this instance's tiles in the per-cell / CG tile tables
   int nt_m;                    // this instance's tiles in the mixed-form per-cell table (32 x 32)
-  double* part;                // per-tile partial sums of the deterministic reductions (3 x nt_pc)
+  double* part;                // per-tile partial sums of the deterministic reductions
   unsigned* ticket;            // their arrival counter
   SteadyRing* steady;          // the device-side steady-state test of this instance
 };
