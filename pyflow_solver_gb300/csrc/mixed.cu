@@ -880,30 +880,39 @@ __device__ __forceinline__ void ph_update_down_t(const X& x, const MixDesc& M, c
   float* fn = (k & 1) ? L0.f : M.f0b;
   const float* p = (k & 1) ? M.p0 : M.p1;
   const float alpha = (float)cget(&ctrl->alpha);
-  const int i = tl.i0 + (x.tid() & 31);
   FF v[1] = {{0.f, 0.f}};
   double out[1];
-  float pv[RPT], ev[RPT], qv[RPT], rv0[RPT];
-#pragma unroll
-  for (int r_ = 0; r_ < RPT; ++r_) {
-    const int j = tl.j0 + (x.tid() >> 5) + r_ * (MT / 32);
-    if (i < L0.nx && j < L0.ny) {
+  {
+    // four adjacent cells of one row a thread, as 16-byte accesses (rows start on 128-byte
+    // boundaries: the pitch is a multiple of 32 cells); a group that crosses the last
+    // column goes cell by cell
+    const int j = tl.j0 + (x.tid() >> 3), i = tl.i0 + ((x.tid() & 7) << 2);
+    if (j < L0.ny && i < L0.nx) {
       const long o = (long)j * L0.ld + i;
-      pv[r_] = x.ld(p + o);
-      ev[r_] = x.ld(M.e + o);
-      qv[r_] = x.ld(M.q + o);
-      rv0[r_] = x.ld(fo + o);
-    }
-  }
-#pragma unroll
-  for (int r_ = 0; r_ < RPT; ++r_) {
-    const int j = tl.j0 + (x.tid() >> 5) + r_ * (MT / 32);
-    if (i < L0.nx && j < L0.ny) {
-      const long o = (long)j * L0.ld + i;
-      M.e[o] = fmaf(alpha, pv[r_], ev[r_]);
-      const float rv = fmaf(-alpha, qv[r_], rv0[r_]);
-      fn[o] = rv;
-      ff_add_prod(v[0], rv, rv);
+      if (i + 3 < L0.nx) {
+        const float4 p4 = x.ld(reinterpret_cast<const float4*>(p + o));
+        const float4 e4 = x.ld(reinterpret_cast<const float4*>(M.e + o));
+        const float4 q4 = x.ld(reinterpret_cast<const float4*>(M.q + o));
+        const float4 r4 = x.ld(reinterpret_cast<const float4*>(fo + o));
+        const float4 en = make_float4(fmaf(alpha, p4.x, e4.x), fmaf(alpha, p4.y, e4.y), fmaf(alpha, p4.z, e4.z),
+                                      fmaf(alpha, p4.w, e4.w));
+        const float4 rn = make_float4(fmaf(-alpha, q4.x, r4.x), fmaf(-alpha, q4.y, r4.y), fmaf(-alpha, q4.z, r4.z),
+                                      fmaf(-alpha, q4.w, r4.w));
+        *reinterpret_cast<float4*>(M.e + o) = en;
+        *reinterpret_cast<float4*>(fn + o) = rn;
+        ff_add_prod(v[0], rn.x, rn.x);
+        ff_add_prod(v[0], rn.y, rn.y);
+        ff_add_prod(v[0], rn.z, rn.z);
+        ff_add_prod(v[0], rn.w, rn.w);
+      } else {
+        for (int c = 0; c < 4 && i + c < L0.nx; ++c) {
+          const float pv = x.ld(p + o + c), ev = x.ld(M.e + o + c), qv = x.ld(M.q + o + c), rv0 = x.ld(fo + o + c);
+          M.e[o + c] = fmaf(alpha, pv, ev);
+          const float rv = fmaf(-alpha, qv, rv0);
+          fn[o + c] = rv;
+          ff_add_prod(v[0], rv, rv);
+        }
+      }
     }
   }
   if (X_RED_FF(1, v, out) && x.tid() == 0) {
