@@ -1151,10 +1151,12 @@ __device__ __forceinline__ void c_ring(float* a, const CLvl& L, int c, int j, in
 }
 
 // Cells of a shared-memory level, visited by the CTA's NT / 32 warps, a row of 32
-// cells to a warp; c is the padded index of cell (j, i).
+// cells to a warp; c is the padded index of cell (j, i).  The column is the outer
+// loop, so that what depends on i alone (the x faces of the diagonal, the left and
+// right rings) is computed once for the thread's rows.
 #define C_FOR(Lv, ...)                                               \
-  for (int j = threadIdx.x >> 5; j < (Lv).ny; j += NT / 32)          \
-    for (int i = threadIdx.x & 31; i < (Lv).nx; i += 32) {           \
+  for (int i = threadIdx.x & 31; i < (Lv).nx; i += 32)               \
+    for (int j = threadIdx.x >> 5; j < (Lv).ny; j += NT / 32) {      \
       const int c = (Lv).off + (j + 1) * (Lv).pw + i + 1;            \
       __VA_ARGS__                                                    \
     }
@@ -1168,26 +1170,34 @@ __device__ __forceinline__ void c_sweep(const CLvl& L, const float* rd, const fl
   __syncthreads();
 }
 
-// The coarse V-cycle of instance M by the whole NT-thread CTA; sm: 3 x (its
-// levels' padded cells) floats of shared memory.
+// Shared tables of the coarse V-cycle: the level table and each level's nine
+// diagonals and their reciprocals.
+struct CoarseSmem {
+  CLvl L[8];
+  float d[8][9], rd[8][9];
+  int tot;
+};
+
+constexpr int NSL = 16;   // slices of the exact bottom solve's sums (held in w: at least NSL * BMAX floats)
+
+// The part of the coarse V-cycle that reads only static data: the level table and
+// diagonals and the zeros of e and w (rings included).  It may run before the wait
+// on the kernels that write the cycle's right-hand side.  sm: rh, e and w, tot
+// floats each (w at least NSL * BMAX when the bottom level is solved exactly).  No
+// closing barrier: coarse_run starts with one.
 template <int NT>
-__device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, float* sm) {
-  Lvl C = M.lev[M.nlev - 1];
-  if (M.nlev == 1) C.f = f_cur(M);
+__device__ void coarse_prep(const MixDesc& M, CoarseSmem& cs, float* sm) {
+  const Lvl& C = M.lev[M.nlev - 1];
   const int nl = M.coarse_levels;
-  // the level table and each level's nine diagonals and their reciprocals, in shared memory
-  __shared__ CLvl L[8];
-  __shared__ float s_d[8][9], s_rd[8][9];
-  __shared__ int s_tot;
   if (threadIdx.x == 0) {
     int nx = C.nx, ny = C.ny, t = 0;
     for (int l = 0; l < nl; ++l) {
-      L[l] = CLvl{nx, ny, t, nx + 2, M.ccx[l], M.ccy[l], M.ckx[l], M.cky[l]};
+      cs.L[l] = CLvl{nx, ny, t, nx + 2, M.ccx[l], M.ccy[l], M.ckx[l], M.cky[l]};
       t += (nx + 2) * (ny + 2);
       nx /= M.ckx[l];
       ny /= M.cky[l];
     }
-    s_tot = t;
+    cs.tot = t;
   }
   if (threadIdx.x < 8 * 9) {
     const int l = threadIdx.x / 9, k = threadIdx.x - 9 * l, fx = k / 3, fy = k - 3 * fx;
@@ -1197,24 +1207,67 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
       if (fx == 2) d += M.ccx[l];
       if (fy >= 1) d += M.ccy[l];
       if (fy == 2) d += M.ccy[l];
-      s_d[l][k] = d;
-      s_rd[l][k] = d > 0.f ? 1.f / d : 0.f;
+      cs.d[l][k] = d;
+      cs.rd[l][k] = d > 0.f ? 1.f / d : 0.f;
     }
   }
   __syncthreads();
-  const int tot = s_tot;
+  const int tot = cs.tot;
+  for (int k = threadIdx.x; k < 2 * tot; k += NT) sm[tot + k] = 0.f;   // e and w with their rings
+}
+
+// The coarse V-cycle of instance M by the whole NT-thread CTA, after coarse_prep.
+template <int NT>
+__device__ void coarse_run(const MixDesc& M, int bottom_sweeps, Smooth sw, const CoarseSmem& cs, float* sm) {
+  __syncthreads();
+  Lvl C = M.lev[M.nlev - 1];
+  if (M.nlev == 1) C.f = f_cur(M);
+  const int nl = M.coarse_levels;
+  const CLvl* L = cs.L;
+  const int tot = cs.tot;
   float* rh = sm;            // right-hand side of every level (level 0: the entry level's f)
   float* e = sm + tot;       // pre-smoothed iterate on the way down; the bottom solution
   float* w = sm + 2 * tot;   // residual on the way down; each level's result on the way up
-  for (int k = threadIdx.x; k < 2 * tot; k += NT) e[k] = 0.f;   // e and w with their rings
   const CLvl Le = L[0];   // register copies of the level descriptors (the level arrays are written
                           // through pointers the compiler cannot tell from the shared table)
-  C_FOR(Le, { rh[c] = __ldcg(C.f + (long)j * C.ld + i); })
+  // the loop state that the closing r.z of a single-level instance updates, read now
+  // so that its latency overlaps the cycle (only this CTA writes them meanwhile)
+  int inner0 = 0;
+  double rho0 = 0.0;
+  if (M.nlev == 1 && threadIdx.x == 0) {
+    inner0 = cget(&M.ctrl->inner);
+    rho0 = cget(&M.ctrl->rho);
+  }
+  {
+    // the entry level's right-hand side, eight loads in flight a thread: cells
+    // threadIdx.x + k NT in row-major order, (j, i) stepped by (NT / nx, NT % nx)
+    const int dj = NT / Le.nx, di = NT - dj * Le.nx;
+    int j = threadIdx.x / Le.nx, i = threadIdx.x - j * Le.nx;
+    while (j < Le.ny) {
+      float t[8];
+      int c[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const bool in = j < Le.ny;
+        t[u] = in ? __ldcg(C.f + (long)j * C.ld + i) : 0.f;
+        c[u] = in ? Le.off + (j + 1) * Le.pw + i + 1 : -1;
+        i += di;
+        j += dj;
+        if (i >= Le.nx) {
+          i -= Le.nx;
+          ++j;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (c[u] >= 0) rh[c[u]] = t[u];
+    }
+  }
   __syncthreads();
   for (int l = 0; l + 1 < nl; ++l) {
     const CLvl Lv = L[l];
-    const float* d = s_d[l];
-    const float* rd = s_rd[l];
+    const float* d = cs.d[l];
+    const float* rd = cs.rd[l];
     // e = S(S(0)): the first sweep from zero is pointwise, w = w1 D^-1 rh (zero ring), then the second
     C_FOR(Lv, { w[c] = sw.w1 * rh[c] * rd[c_dk(Lv, j, i)]; })
     __syncthreads();
@@ -1242,42 +1295,42 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
     if (M.binv) {
       // exact bottom solve: e = A+ rh (at most BMAX cells).  A+ is exactly symmetric, so
       // column q0 is read for row q0 (consecutive threads, consecutive addresses); the
-      // sum over q is split into NS slices of QS terms, added in slice order through w
-      // (dead past the restrictions; the up-sweep rewrites it, rings included).
-      constexpr int NS = 16, QS = BMAX / NS;
-      if (nb == BMAX && tot >= NS * BMAX) {
-        for (int v = threadIdx.x; v < NS * BMAX; v += NT) {
-          const int q0 = v % BMAX, h = v / BMAX;
-          float acc = 0.f;
+      // sum over q is split into NSL slices of qs <= 4 terms, added in slice order
+      // through w (dead past the restrictions; the up-sweep rewrites it, rings included).
+      const int qs = (nb + NSL - 1) / NSL;
+      for (int v = threadIdx.x; v < NSL * nb; v += NT) {
+        const int h = v / nb, q0 = v - h * nb, qa = h * qs;
+        float b[4], r[4];
+        int qj = qa / Lv.nx, qi = qa - qj * Lv.nx;   // cell qa + k, stepped along its row
 #pragma unroll
-          for (int k = 0; k < QS; ++k) {
-            const int q = h * QS + k;
-            acc = fmaf(__ldg(M.binv + (long)q * nb + q0), rh[cell(q)], acc);
+        for (int k = 0; k < 4; ++k) {
+          const bool in = k < qs && qa + k < nb;
+          b[k] = in ? __ldg(M.binv + (long)(qa + k) * nb + q0) : 0.f;
+          r[k] = in ? rh[Lv.off + (qj + 1) * Lv.pw + qi + 1] : 0.f;
+          if (++qi == Lv.nx) {
+            qi = 0;
+            ++qj;
           }
-          w[v] = acc;
         }
-        __syncthreads();
-        if (threadIdx.x < BMAX) {
-          float sacc = w[threadIdx.x];
-          for (int k = 1; k < NS; ++k) sacc += w[k * BMAX + threadIdx.x];
-          const int q0 = threadIdx.x, qj = q0 / Lv.nx, c = cell(q0);
-          e[c] = sacc;
-          c_ring(e, Lv, c, qj, q0 - qj * Lv.nx, sacc);
-        }
-      } else {
-        for (int q0 = threadIdx.x; q0 < nb; q0 += NT) {
-          float acc = 0.f;
-          for (int q = 0; q < nb; ++q) acc = fmaf(__ldg(M.binv + (long)q * nb + q0), rh[cell(q)], acc);
-          const int qj = q0 / Lv.nx, c = cell(q0);
-          e[c] = acc;
-          c_ring(e, Lv, c, qj, q0 - qj * Lv.nx, acc);
-        }
+        float acc = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (k < qs && qa + k < nb) acc = fmaf(b[k], r[k], acc);
+        w[v] = acc;
+      }
+      __syncthreads();
+      for (int q0 = threadIdx.x; q0 < nb; q0 += NT) {
+        float sacc = w[q0];
+        for (int k = 1; k < NSL; ++k) sacc += w[k * nb + q0];
+        const int qj = q0 / Lv.nx, c = cell(q0);
+        e[c] = sacc;
+        c_ring(e, Lv, c, qj, q0 - qj * Lv.nx, sacc);
       }
       __syncthreads();
     } else {
       // Jacobi sweeps from e = 0 between e and w (both zero, rings included), then the
       // result into e with its mirror ring
-      for (int q = 0; q < bottom_sweeps; ++q) c_sweep<NT>(Lv, s_rd[nl - 1], rh, (q & 1) ? w : e, (q & 1) ? e : w, sw.wb);
+      for (int q = 0; q < bottom_sweeps; ++q) c_sweep<NT>(Lv, cs.rd[nl - 1], rh, (q & 1) ? w : e, (q & 1) ? e : w, sw.wb);
       const float* res = (bottom_sweeps & 1) ? w : e;
       C_FOR(Lv, {
         const float v = res[c];
@@ -1291,7 +1344,7 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
   for (int l = nl - 2; l >= 0; --l) {
     const CLvl Lv = L[l];
     const CLvl Cv = L[l + 1];
-    const float* rd = s_rd[l];
+    const float* rd = cs.rd[l];
     const float* zc = ((l + 1 == nl - 1) ? e : w) + Cv.off + Cv.pw + 1;   // mirror ring
     const int cpw = Cv.pw;
     auto catc = [zc, cpw](int J, int I) { return zc[J * cpw + I]; };
@@ -1328,10 +1381,15 @@ __device__ void coarse_cycle(const MixDesc& M, int bottom_sweeps, Smooth sw, flo
       if ((threadIdx.x & 31) == 0) wsum[vw] = (double)acc.hi + (double)acc.lo;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double rz = wsum[0];
-      for (int k = 1; k < CT / 32; ++k) rz += wsum[k];
-      set_rho(M.ctrl, rz);
+    if (threadIdx.x < 32) {
+      // the CT / 32 row sums by a fixed shuffle tree (every lane ends with the same bits)
+      double rz = wsum[threadIdx.x];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) rz += __shfl_xor_sync(0xffffffffu, rz, o);
+      if (threadIdx.x == 0) {
+        if (inner0 > 0) M.ctrl->beta = rz / rho0;
+        M.ctrl->rho = rz;
+      }
     }
   }
   __syncthreads();
@@ -1372,13 +1430,15 @@ __global__ void __launch_bounds__(NT, CT / NT) k_mg_coarse(const MixDesc* __rest
                                                             int gate, int bottom_sweeps, Smooth sw) {
   pdl_launch();
   __shared__ MixDesc smd;
+  __shared__ CoarseSmem cs;
+  extern __shared__ float csm[];
   stage_desc(MD + order[blockIdx.x], &smd);
-  pdl_wait();
   __syncthreads();
   const MixDesc& M = smd;
+  coarse_prep<NT>(M, cs, csm);      // static data only: overlaps the predecessor
+  pdl_wait();
   if (!mx_live(M, gate)) return;
-  extern __shared__ float csm[];
-  coarse_cycle<NT>(M, bottom_sweeps, sw, csm);
+  coarse_run<NT>(M, bottom_sweeps, sw, cs, csm);
 }
 
 __global__ void __launch_bounds__(MT) k_mx_init(const MixDesc* __restrict__ MD, const MTile* __restrict__ TL,
@@ -1609,6 +1669,7 @@ struct PersistArgs {
 
 __global__ void __launch_bounds__(CT, 1) k_mx_persist(PersistArgs A) {
   extern __shared__ __align__(16) unsigned char psm[];
+  __shared__ CoarseSmem pcs;
   const GroupCtx x{(int)(threadIdx.x >> 8)};
   TileSmem& ts = reinterpret_cast<TileSmem*>(psm)[x.g];
   const int ngroups = gridDim.x * 4;
@@ -1627,7 +1688,10 @@ __global__ void __launch_bounds__(CT, 1) k_mx_persist(PersistArgs A) {
     }
     for (int k = blockIdx.x; k < A.n; k += gridDim.x) {
       const MixDesc& M = A.dd[k];
-      if (mx_live(M, 1)) coarse_cycle<CT>(M, A.bottom_sweeps, A.sw, reinterpret_cast<float*>(psm));
+      if (mx_live(M, 1)) {
+        coarse_prep<CT>(M, pcs, reinterpret_cast<float*>(psm));
+        coarse_run<CT>(M, A.bottom_sweeps, A.sw, pcs, reinterpret_cast<float*>(psm));
+      }
     }
     if (!grid_sync(gb)) return false;
     for (int l = A.maxlev - 2; l >= 0; --l) {
@@ -1903,9 +1967,11 @@ int batch_create(const MixParams* prm, int n, Batch** out) {
       return set_error(PFGB_EINVAL, "mixed solver: the coarse multigrid level would exceed 4096 cells "
                                     "(nx and ny need enough factors of two)");
     }
-    smem = std::max(smem, (size_t)3 * plan[k].cta_tot * sizeof(float));
-    smem2 = smem;
     const PlanLvl& bot = plan[k].cta.back();
+    const size_t cfl = (size_t)2 * plan[k].cta_tot +
+                       std::max((size_t)plan[k].cta_tot, (size_t)(bot.nx * bot.ny <= BMAX ? NSL * BMAX : 0));
+    smem = std::max(smem, cfl * sizeof(float));
+    smem2 = smem;
     if (bot.nx * bot.ny <= BMAX) bytes += up((size_t)bot.nx * bot.ny * bot.nx * bot.ny * sizeof(float));
     B->maxlev = std::max(B->maxlev, (int)plan[k].global.size());
     for (auto& d : plan[k].global) bytes += 3 * up((size_t)round_up(d.nx, 32) * d.ny * sizeof(float));
