@@ -865,7 +865,7 @@ __global__ void __launch_bounds__(NT, 3) k_correct_diag_m(const InstDesc* __rest
                                                           const mixed::MixDesc* __restrict__ MD, const int* trip,
                                                           const int* gb_err) {
   TILE_PROLOGUE
-  __shared__ double sx[TY_M + 3][CD_W];       // x at rows j0-1 .. j0+33, columns i0-1 .. i0+33
+  __shared__ double sx[TY_M + 3][CD_W];       // x - x[0] at rows j0-1 .. j0+33, columns i0-1 .. i0+33
   __shared__ double su[TY_M][TX + 2];         // corrected u*, rows j0 .. j0+31, columns i0-1 .. i0+32
   __shared__ double sv[TY_M + 2][TX];         // corrected v*, rows j0-1 .. j0+32, columns i0 .. i0+31
   __shared__ StepRed rsm;
@@ -885,18 +885,19 @@ __global__ void __launch_bounds__(NT, 3) k_correct_diag_m(const InstDesc* __rest
   for (int idx = threadIdx.x; idx < (TY_M + 3) * CD_W; idx += NT) {
     const int jj = idx / CD_W - 1, ii = idx % CD_W - 1;
     const int gj = j0 + jj, gi = i0 + ii;
-    sx[jj + 1][ii + 1] = (gj >= 0 && gj < G.ny && gi >= 0 && gi < G.nx) ? xs[(long)gj * G.ld + gi] : 0.0;
+    sx[jj + 1][ii + 1] = (gj >= 0 && gj < G.ny && gi >= 0 && gi < G.nx) ? SUB(xs[(long)gj * G.ld + gi], x0) : 0.0;
   }
   __syncthreads();
-  // the correction at (j, c) of a cell whose x is at sx[j - j0 + 1][c - i0 + 1]
+  // the correction at (j, c) of a cell whose x - x[0] (the pinned pressure, formed
+  // once per staged cell) is at sx[j - j0 + 1][c - i0 + 1]
   auto ucorr = [&](int j, int c, double u1) {
-    const double pv = SUB(sx[j - j0 + 1][c - i0 + 1], x0);
-    const double gx = (c < G.nx - 1) ? MUL(SUB(SUB(sx[j - j0 + 1][c - i0 + 2], x0), pv), rg.rx) : 0.0;
+    const double pv = sx[j - j0 + 1][c - i0 + 1];
+    const double gx = (c < G.nx - 1) ? MUL(SUB(sx[j - j0 + 1][c - i0 + 2], pv), rg.rx) : 0.0;
     return SUB(u1, MUL(dt, gx));
   };
   auto vcorr = [&](int j, int c, double v1) {
-    const double pv = SUB(sx[j - j0 + 1][c - i0 + 1], x0);
-    const double gy = (j < G.ny - 1) ? MUL(SUB(SUB(sx[j - j0 + 2][c - i0 + 1], x0), pv), rg.ry) : 0.0;
+    const double pv = sx[j - j0 + 1][c - i0 + 1];
+    const double gy = (j < G.ny - 1) ? MUL(SUB(sx[j - j0 + 2][c - i0 + 1], pv), rg.ry) : 0.0;
     return SUB(v1, MUL(dt, gy));
   };
   double v[2] = {0.0, 0.0};
@@ -921,7 +922,7 @@ __global__ void __launch_bounds__(NT, 3) k_correct_diag_m(const InstDesc* __rest
     for (int r = 0; r < 2; ++r) {
       const int j = j0 + (threadIdx.x >> 5) + (h + r) * PB_Y;
       if (in[r]) {
-        const double pv = SUB(sx[j - j0 + 1][tx + 1], x0);
+        const double pv = sx[j - j0 + 1][tx + 1];
         const double uc = ucorr(j, i, u1[r]);
         const double vc = vcorr(j, i, v1[r]);
         su[j - j0][tx + 1] = uc;
