@@ -1123,10 +1123,6 @@ struct CLvl {
   int kx, ky;                                // coarsening factors to the next level
 };
 
-// index 3 fx + fy of a cell's diagonal in its level's tables: fx, fy = the faces it has in x, in y
-__device__ __forceinline__ int c_dk(const CLvl& L, int j, int i) {
-  return 3 * ((i > 0) + (i < L.nx - 1)) + ((j > 0) + (j < L.ny - 1));
-}
 
 // cx (a_W + a_E) + cy (a_S + a_N) at padded index c (the ring supplies the walls' zeros)
 __device__ __forceinline__ float c_nsum(const CLvl& L, const float* a, int c) {
@@ -1161,12 +1157,26 @@ __device__ __forceinline__ void c_ring(float* a, const CLvl& L, int c, int j, in
       __VA_ARGS__                                                    \
     }
 
+// C_FOR with v = tab[3 fx + fy], the cell's entry in a level's nine-entry diagonal
+// table (fx, fy: the faces it has in x, in y).  The column's two candidates (rows
+// inside, rows on a y edge) are read once per column; the row picks one of them.
+#define C_FORD(Lv, tab, v, ...)                                                \
+  for (int i = threadIdx.x & 31; i < (Lv).nx; i += 32) {                       \
+    const int kx_ = 3 * ((i > 0) + (i < (Lv).nx - 1));                         \
+    const float vin_ = (tab)[kx_ + 2], ved_ = (tab)[kx_ + ((Lv).ny > 1)];      \
+    for (int j = threadIdx.x >> 5; j < (Lv).ny; j += NT / 32) {                \
+      const int c = (Lv).off + (j + 1) * (Lv).pw + i + 1;                      \
+      const float v = (j > 0 && j < (Lv).ny - 1) ? vin_ : ved_;                \
+      __VA_ARGS__                                                              \
+    }                                                                          \
+  }
+
 // one weighted-Jacobi sweep src -> dst on level L (zero ring on src); rd: the level's
 // reciprocal diagonals; all threads, ends with a barrier
 template <int NT>
 __device__ __forceinline__ void c_sweep(const CLvl& L, const float* rd, const float* f, const float* src, float* dst,
                                         float omega) {
-  C_FOR(L, { dst[c] = fmaf(1.f - omega, src[c], omega * (f[c] + c_nsum(L, src, c)) * rd[c_dk(L, j, i)]); })
+  C_FORD(L, rd, r, { dst[c] = fmaf(1.f - omega, src[c], omega * (f[c] + c_nsum(L, src, c)) * r); })
   __syncthreads();
 }
 
@@ -1269,13 +1279,13 @@ __device__ void coarse_run(const MixDesc& M, int bottom_sweeps, Smooth sw, const
     const float* d = cs.d[l];
     const float* rd = cs.rd[l];
     // e = S(S(0)): the first sweep from zero is pointwise, w = w1 D^-1 rh (zero ring), then the second
-    C_FOR(Lv, { w[c] = sw.w1 * rh[c] * rd[c_dk(Lv, j, i)]; })
+    C_FORD(Lv, rd, r, { w[c] = sw.w1 * rh[c] * r; })
     __syncthreads();
-    C_FOR(Lv, { e[c] = fmaf(1.f - sw.w2, w[c], sw.w2 * (rh[c] + c_nsum(Lv, w, c)) * rd[c_dk(Lv, j, i)]); })
+    C_FORD(Lv, rd, r, { e[c] = fmaf(1.f - sw.w2, w[c], sw.w2 * (rh[c] + c_nsum(Lv, w, c)) * r); })
     __syncthreads();
     // residual rh - A e into w, its ring the mirror of its edges; then rh_{l+1} = P^T w
-    C_FOR(Lv, {
-      const float v = rh[c] - (d[c_dk(Lv, j, i)] * e[c] - c_nsum(Lv, e, c));
+    C_FORD(Lv, d, dv, {
+      const float v = rh[c] - (dv * e[c] - c_nsum(Lv, e, c));
       w[c] = v;
       c_ring(w, Lv, c, j, i, v);
     })
@@ -1354,8 +1364,8 @@ __device__ void coarse_run(const MixDesc& M, int bottom_sweeps, Smooth sw, const
     })
     __syncthreads();
     c_sweep<NT>(Lv, rd, rh, w, e, sw.w2);
-    C_FOR(Lv, {
-      const float v = fmaf(1.f - sw.w1, e[c], sw.w1 * (rh[c] + c_nsum(Lv, e, c)) * rd[c_dk(Lv, j, i)]);
+    C_FORD(Lv, rd, r, {
+      const float v = fmaf(1.f - sw.w1, e[c], sw.w1 * (rh[c] + c_nsum(Lv, e, c)) * r);
       w[c] = v;
       if (l > 0) c_ring(w, Lv, c, j, i, v);   // mirror ring for the next prolongation
     })
